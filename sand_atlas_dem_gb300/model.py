@@ -1,0 +1,290 @@
+"""Host-side set-up of one periodic mesh-surface DEM specimen.
+
+Everything here runs once per engine on the host, in float64 numpy, and ends
+as the float32/uint32 arrays the device step reads.  It restates the set-up
+half of the reference ``Engine.__init__`` (``src/sand_atlas_dem/gpu.py:95-368``)
+and its timestep preflight (``gpu.py:370-413``): normalized units
+(L0 = median equivalent diameter, T0 = sqrt(rho L0 / kn), F0 = kn L0^3),
+per-grain ``body``/``invI`` rows, Verlet skin and cutoff, cell-list bins,
+capacities and the packed mesh layout.  The resulting arrays are checked
+against the reference's own ``Engine`` in the golden tests.
+"""
+
+import math
+
+import numpy as np
+
+from .packing import pack_library
+from .spec import finite_array
+
+ERRORS = {
+    2: "degenerate contact distance gradient",
+    4: "excessive penetration",
+    8: "bin capacity",
+    16: "pair capacity",
+    32: "contact capacity",
+    64: "history hash full",
+    128: "contact-list cycle",
+    256: "periodic image ambiguity",
+    512: "nonfinite state",
+    1024: "mesh traversal stack capacity",
+    2048: "nonperiodic domain escape",
+    4096: "invalid boundary box",
+    8192: "active-contact timestep bound",
+    16384: "coincident centres unsupported by experimental source-normal contacts",
+    65536: "device wait limit",
+}
+CAPACITY_FLAGS = 8 | 16 | 32 | 64
+
+# Reference ``Resources`` field order (``shaders/solver.slang:20-100``); the
+# C ABI of both the CUDA library and the CPU oracle binds buffers in it.
+RESOURCE_ORDER = (
+    "control", "cell", "position", "positionRemainder", "velocityRemainder",
+    "momentumRemainder", "rotationRemainder", "referencePositionRemainder", "cellLog",
+    "accumulatedRemainder", "velocity", "rotation", "momentum", "force", "torque",
+    "referencePosition", "referenceCell", "shapeId", "body", "invI", "grids", "sampleInfo",
+    "gridOrigin", "distance", "sample", "meshRoots", "meshHullInfo", "meshPlanes", "meshMin",
+    "meshMax", "meshLinks", "meshTriangles", "meshNormals", "meshFrontier", "meshPairMask",
+    "meshPairTransform", "meshClusterInfo", "meshClusterRanges", "meshClusterMin",
+    "meshClusterMax", "meshSampleIndices", "binCounts", "binParticles", "pairCounts",
+    "pairOffsets", "pairs", "contactCounts", "contactOffsets", "meta", "pointDepth",
+    "normalArea", "slip", "contactForce", "normalLossPower", "normalDamping", "forceVelocity",
+    "forceOmega", "oldMeta", "oldSlip", "oldNormal", "oldHash", "hash", "heads", "next",
+    "particleStress", "timestepRows", "particleDiagnostic", "diagnosticRows", "accumulated",
+    "fabricRows", "wallPlane", "wallRemainder", "wallVelocity", "wallMaterial", "wallBoxIds",
+    "wallRows", "wallAccumulated",
+)
+# Flattened ``Config`` scalars in declaration order (``solver.slang:12-19``).
+CONFIG_ORDER = (
+    "activeTimestep", "N", "shapes", "pairCapacity", "contactCapacity", "binCapacity",
+    "binCount", "bins0", "bins1", "bins2", "hashSize", "dt", "kn", "kt", "mu",
+    "normalViscosity", "skin", "drag", "maxOverlap", "historyStep", "meshGeometry",
+    "periodic", "wallCount", "wallBoxEnabled", "sourceSurfaceNormal",
+)
+
+DAMPING_STATE = ("normalDamping", "forceVelocity", "forceOmega")
+RESIDUAL_STATE = (
+    "positionRemainder", "velocityRemainder", "momentumRemainder", "rotationRemainder",
+    "accumulatedRemainder", "cellLog",
+)
+STATE_NAMES = (
+    "position", "velocity", "rotation", "momentum", "cell", "force", "torque", "accumulated",
+    *RESIDUAL_STATE,
+)
+
+
+def f4(x):
+    a = np.asarray(x, np.float32)
+    return np.pad(a, ((0, 0), (0, 4 - a.shape[1])))
+
+
+class RejectedStep(RuntimeError):
+    """A chunk raised solver flags and was rolled back (``gpu.py:51-57``)."""
+
+    def __init__(self, flags):
+        self.flags = int(flags)
+        super().__init__(
+            "GPU step rejected: " + ", ".join(v for k, v in ERRORS.items() if self.flags & k)
+        )
+
+
+class HostLayout:
+    """Units, per-grain rows, capacities and static geometry of one specimen."""
+
+    def __init__(self, library, spec, positions, cell, shape_ids, scales):
+        positions = finite_array(positions)
+        cell = finite_array(cell, (3,), positive=True)
+        if positions.ndim != 2 or positions.shape[1] != 3 or len(positions) < 1:
+            raise ValueError("At least one three-dimensional position required")
+        if not spec.periodic and (np.any(positions < 0) or np.any(positions >= cell)):
+            raise ValueError("Nonperiodic particle centres must lie in [0, cell)")
+        if spec.contact_geometry != "mesh":
+            raise ValueError("The GB300 backend implements the mesh contact geometry only")
+        if spec.planes:
+            raise ValueError("The GB300 backend implements periodic and plane-free domains only")
+        self.spec = spec
+        self.library = library
+        self.n = len(positions)
+        self.viscous = spec.viscous
+        shapes = library.shapes
+        self.length_unit = float(np.median([(6 * s.volume / np.pi) ** (1 / 3) for s in shapes]))
+        self.time_unit = math.sqrt(spec.density * self.length_unit / spec.normal_stiffness)
+        self.mass_unit = spec.density * self.length_unit**3
+        self.force_unit = spec.normal_stiffness * self.length_unit**3
+        self.stress_unit = spec.normal_stiffness * self.length_unit
+        self.energy_unit = self.force_unit * self.length_unit
+        self.ids = np.asarray(shape_ids, np.uint32)
+        self.scales = np.asarray(scales, float)
+        if len(self.ids) != self.n or len(self.scales) != self.n:
+            raise ValueError("One shape id and scale per particle required")
+        if self.ids.size and int(self.ids.max()) >= len(shapes):
+            raise ValueError("Shape id outside the library")
+        l = self.length_unit
+        self.body = np.array(
+            [
+                [
+                    s,
+                    spec.density * shapes[int(i)].volume * s**3 / self.mass_unit,
+                    shapes[int(i)].radius * s / l,
+                    (6 * shapes[int(i)].volume / np.pi) ** (1 / 3) * s / l,
+                ]
+                for i, s in zip(self.ids, self.scales)
+            ],
+            np.float32,
+        )
+        inertia = np.array(
+            [
+                np.linalg.inv(
+                    shapes[int(i)].inertia * spec.density * s**5 / (self.mass_unit * l * l)
+                )
+                for i, s in zip(self.ids, self.scales)
+            ]
+        )
+        self.invI = f4(inertia.reshape(-1, 3))
+        self.skin = float(spec.skin * 2 * self.body[:, 2].max())
+        self.cutoff = float(2 * self.body[:, 2].max() + self.skin)
+        box = np.asarray(cell, float) / l
+        if spec.periodic and self.cutoff >= 0.5 * box.min():
+            raise ValueError("Cell too small for unique periodic images")
+        self.box = box
+        self.bins = np.maximum(1, np.minimum(64, np.floor(box / self.cutoff))).astype(np.uint32)
+        self.bin_count = int(self.bins.prod())
+        self.pair_capacity = max(1, self.n * spec.pairs_per_particle)
+        self.contact_capacity = max(16, self.n * spec.contacts_per_particle)
+        self.hash_size = 1 << math.ceil(math.log2(max(32, 2 * self.contact_capacity)))
+        self.bin_capacity = spec.bin_capacity
+        self.preflight_dt()
+        self.initial_cell = np.asarray(cell, float)
+        self.normalized_position = np.asarray(positions, float) / l
+        self.geometry = self.static_geometry()
+        self.max_leaves = int(self.geometry["meshLeafInfo"][:, 1].max())
+        self.max_nodes = int(self.geometry["sampleInfo"][:, 1].max())
+
+    def preflight_dt(self):
+        """Conservative timestep bound (``gpu.py:370-413``), planes excluded."""
+        spec = self.spec
+        if spec.timestep_policy == "active-contact":
+            return
+        limit = self.timestep_limit()
+        if spec.timestep > limit:
+            raise ValueError(f"Timestep exceeds conservative estimate {limit:.6g} s")
+
+    def timestep_limit(self):
+        spec = self.spec
+        limits = []
+        for i, s in zip(self.ids, self.scales):
+            sh = self.library.shapes[int(i)]
+            mass = spec.density * sh.volume * s**3
+            stiffness = (spec.normal_stiffness + spec.tangential_stiffness) * sh.areas.sum() * s * s
+            smallest = np.linalg.eigvalsh(sh.inertia * spec.density * s**5).min()
+            elastic = math.sqrt(min(mass / stiffness, smallest / (stiffness * (sh.radius * s) ** 2)))
+            viscous = math.inf
+            viscosity = spec.normal_viscosity * sh.areas.sum() * s**2
+            if viscosity > 0:
+                viscous = min(mass / viscosity, smallest / (viscosity * (sh.radius * s) ** 2))
+            limits.append(0.1 * min(elastic, viscous))
+        return min(limits)
+
+    def static_geometry(self):
+        """Packed mesh arrays plus the per-shape node table (``gpu.py:421-488``)."""
+        data = pack_library(self.library, self.length_unit)
+        l = self.length_unit
+        info, samples, offset = [], [], 0
+        for s in self.library.shapes:
+            info.append([offset, len(s.samples), 0, 0])
+            samples.append(np.column_stack([s.samples / l, s.areas / l**2]).astype(np.float32))
+            offset += len(s.samples)
+        data["sampleInfo"] = np.asarray(info, np.uint32)
+        data["sample"] = np.concatenate(samples)
+        # The SDF grids are unused by the mesh path; one-element placeholders
+        # keep the reference buffer order.
+        data["grids"] = np.zeros((1, 4), np.uint32)
+        data["gridOrigin"] = np.zeros((1, 4), np.float32)
+        data["distance"] = np.zeros(4, np.float32)
+        return data
+
+    def config(self, *, dt, drag=0.0, history=False):
+        """Normalized ``Config`` block (``gpu.py:490-518``)."""
+        spec = self.spec
+        return {
+            "activeTimestep": int(spec.timestep_policy == "active-contact"),
+            "N": self.n,
+            "shapes": len(self.library.shapes),
+            "pairCapacity": self.pair_capacity,
+            "contactCapacity": self.contact_capacity,
+            "binCapacity": self.bin_capacity,
+            "binCount": self.bin_count,
+            "bins0": int(self.bins[0]),
+            "bins1": int(self.bins[1]),
+            "bins2": int(self.bins[2]),
+            "hashSize": self.hash_size,
+            "dt": dt / self.time_unit,
+            "kn": 1.0,
+            "kt": spec.tangential_stiffness / spec.normal_stiffness,
+            "mu": spec.friction,
+            "normalViscosity": spec.normal_viscosity / (spec.normal_stiffness * self.time_unit),
+            "skin": self.skin,
+            "drag": drag * self.time_unit,
+            "maxOverlap": spec.max_overlap_fraction,
+            "historyStep": int(history),
+            "meshGeometry": 1,
+            "sourceSurfaceNormal": int(spec.contact_normal == "source-surface-experimental"),
+            "periodic": int(spec.periodic),
+            "wallCount": 0,
+            "wallBoxEnabled": 0,
+        }
+
+    def config_values(self, config):
+        return np.array([float(config[k]) for k in CONFIG_ORDER], np.float64)
+
+    def initial_state(self):
+        """Per-grain state rows at construction (``gpu.py:193-292``)."""
+        n = self.n
+        p = self.normalized_position
+        z = lambda rows=n: np.zeros((rows, 4), np.float32)  # noqa: E731
+        state = {
+            "position": f4(p),
+            "velocity": z(),
+            "rotation": np.tile(np.array([0, 0, 0, 1], np.float32), (n, 1)),
+            "momentum": z(),
+            "force": z(),
+            "torque": z(),
+            "referencePosition": z(),
+            "particleDiagnostic": z(),
+            "timestepRows": z(),
+            "particleStress": z(3 * n),
+            "diagnosticRows": z(8 * n),
+            "accumulated": z(),
+            "referencePositionRemainder": z(),
+        }
+        for name in DAMPING_STATE:
+            state[name] = z()
+        for name in RESIDUAL_STATE:
+            residual = z(2 if name == "cellLog" else n)
+            if name == "positionRemainder":
+                residual[:, :3] = p - p.astype(np.float32).astype(float)
+            state[name] = residual
+        box = self.box
+        state["cell"] = np.array([list(box) + [0], [0, 0, 0, 0], list(box) + [0]], np.float32)
+        state["referenceCell"] = np.array([list(box) + [0], [0, 0, 0, self.cutoff]], np.float32)
+        ctrl = np.zeros(16, np.uint32)
+        ctrl[4] = 1
+        state["control"] = ctrl
+        state["shapeId"] = self.ids.copy()
+        state["body"] = self.body.copy()
+        state["invI"] = self.invI.copy()
+        return state
+
+    def estimated_bytes(self):
+        """Device working set of this backend, including its own scratch."""
+        n, p, c = self.n, self.pair_capacity, self.contact_capacity
+        geometry = sum(a.nbytes for a in self.geometry.values())
+        candidates = 2 * p * self.max_leaves
+        return int(
+            1184 * n
+            + 8 * self.bin_count * self.bin_capacity
+            + 196 * p + 2 * 8 * p * (self.max_leaves + 31) // 32
+            + 16 * candidates
+            + 2 * 96 * c + 64 * c
+            + geometry
+        )
