@@ -1,0 +1,193 @@
+// C ABI of the GB300 mesh-surface DEM step (declared in include/sand_dem_gb300.h).
+//
+// Buffers follow the reference Resources order (solver.slang:20-100, the
+// order the reference CPU backend binds in cpu_dispatch, cpu.py:189-300),
+// then this backend's extension buffers; values are the reference Config
+// scalars (solver.slang:12-19) then the extension values.  Plain pointers and
+// sizes only.  Entry points return 0 on success, nonzero on a CUDA or argument
+// error (text via sdg_last_error); solver failures are reported in control[0]
+// exactly as the reference does.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <string_view>
+#include <vector>
+#include <cuda_runtime.h>
+#include "dem_device.cuh"
+#include "launch.h"
+
+namespace sdg {
+
+static thread_local std::string g_error;
+
+static int record(cudaError_t e, const char* where) {
+    if (e == cudaSuccess) return 0;
+    g_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return 2;
+}
+
+static int unpack(void* const* buffers, const uint64_t* bytes, const double* values, uint32_t nvalues, Params& P) {
+    if (!buffers || !values || nvalues < VALUE_COUNT) {
+        g_error = "expected " + std::to_string(BUFFER_COUNT) + " buffers and " + std::to_string(VALUE_COUNT) + " values";
+        return 1;
+    }
+    static_assert(sizeof(Res) == BUFFER_COUNT * sizeof(void*), "buffer block");
+    std::memcpy(static_cast<void*>(&P.r), buffers, sizeof(Res));
+    (void)bytes;
+    Config& c = P.c;
+    const double* v = values;
+    c.activeTimestep = uint32_t(v[0]); c.N = uint32_t(v[1]); c.shapes = uint32_t(v[2]);
+    c.pairCapacity = uint32_t(v[3]); c.contactCapacity = uint32_t(v[4]); c.binCapacity = uint32_t(v[5]);
+    c.binCount = uint32_t(v[6]); c.bins[0] = uint32_t(v[7]); c.bins[1] = uint32_t(v[8]); c.bins[2] = uint32_t(v[9]);
+    c.hashSize = uint32_t(v[10]);
+    c.dt = float(v[11]); c.kn = float(v[12]); c.kt = float(v[13]); c.mu = float(v[14]);
+    c.normalViscosity = float(v[15]); c.skin = float(v[16]); c.drag = float(v[17]); c.maxOverlap = float(v[18]);
+    c.historyStep = uint32_t(v[19]); c.meshGeometry = uint32_t(v[20]); c.periodic = uint32_t(v[21]);
+    c.wallCount = uint32_t(v[22]); c.wallBoxEnabled = uint32_t(v[23]); c.sourceSurfaceNormal = uint32_t(v[24]);
+    c.leafWords = uint32_t(v[25]); c.candidateCapacity = uint32_t(v[26]); c.viscousCapture = uint32_t(v[27]);
+    if (c.N == 0 || c.meshGeometry == 0 || c.wallCount != 0) {
+        g_error = "the GB300 step needs N > 0, mesh geometry and no planes";
+        return 1;
+    }
+    if (bytes) {
+        // Capacity cross-checks against the buffer sizes the caller passed.
+        if (bytes[48] < uint64_t(c.contactCapacity) * 16 || bytes[45] < uint64_t(c.pairCapacity) * 8 ||
+            bytes[2] < uint64_t(c.N) * 16 || bytes[42] < uint64_t(c.binCount) * c.binCapacity * 4 ||
+            bytes[77 + 11] < uint64_t(c.candidateCapacity) * 8 ||
+            bytes[77 + 10] < uint64_t(2) * c.pairCapacity * c.leafWords * 4) {
+            g_error = "a buffer is smaller than its configured capacity";
+            return 1;
+        }
+    }
+    return 0;
+}
+
+void launch_forces(const Params& P, cudaStream_t s, bool captureKinematics) {
+    const Config& c = P.c;
+    if (c.normalViscosity > 0 && captureKinematics) launch_state("captureContactKinematics", P, c.N, s);
+    launch_contacts("neighbours", P, c.N, s);
+    launch_contacts("collect", P, 0, s);
+    launch_contacts("resolveContacts", P, 0, s);
+    launch_contacts("gather", P, c.N, s);
+    if (c.activeTimestep) launch_state("checkContactTimestep", P, c.N, s);
+}
+
+// One step of Engine._advance_once (gpu.py:714-724); captureContactKinematics
+// is fused into beginStep when the normal law is viscous.
+void launch_step(const Params& P, cudaStream_t s) {
+    const Config& c = P.c;
+    if (c.activeTimestep) launch_state("checkContactTimestep", P, c.N, s);
+    Params B = P;
+    B.c.viscousCapture = c.normalViscosity > 0 ? 1u : 0u;
+    launch_state("beginStep", B, c.N, s);
+    launch_state("advanceCell", P, 1, s);
+    launch_state("checkRebuild", P, c.N, s);
+    launch_forces(P, s, false);
+    launch_state("finishStep", P, c.N, s);
+}
+
+// Committed/new history sides swap every step (gpu.py:725).
+static Params swapSides(const Params& P) {
+    Params Q = P;
+    Res& r = Q.r;
+    std::swap(*reinterpret_cast<void**>(&r.meta), *reinterpret_cast<void**>(const_cast<uint4**>(&r.oldMeta)));
+    std::swap(*reinterpret_cast<void**>(&r.slip), *reinterpret_cast<void**>(const_cast<float4**>(&r.oldSlip)));
+    std::swap(*reinterpret_cast<void**>(&r.normalArea), *reinterpret_cast<void**>(const_cast<float4**>(&r.oldNormal)));
+    std::swap(*reinterpret_cast<void**>(&r.hash), *reinterpret_cast<void**>(const_cast<uint32_t**>(&r.oldHash)));
+    std::swap(*reinterpret_cast<void**>(&r.sidePairOffsets), *reinterpret_cast<void**>(const_cast<uint32_t**>(&r.oldPairOffsets)));
+    std::swap(*reinterpret_cast<void**>(&r.sidePairB), *reinterpret_cast<void**>(const_cast<uint32_t**>(&r.oldPairB)));
+    std::swap(*reinterpret_cast<void**>(&r.sideContactStart), *reinterpret_cast<void**>(const_cast<uint32_t**>(&r.oldContactStart)));
+    return Q;
+}
+
+// A captured two-step graph (one step per history side) per buffer/config set.
+struct Engine {
+    std::vector<unsigned char> key;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    uint32_t launches = 0;
+    ~Engine() { reset(); }
+    void reset() {
+        for (auto& e : exec)
+            if (e) { cudaGraphExecDestroy(e); e = nullptr; }
+        key.clear();
+    }
+};
+
+static int capture(const Params& P, cudaStream_t s, cudaGraphExec_t* out) {
+    cudaGraph_t graph = nullptr;
+    int rc = record(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (rc) return rc;
+    launch_step(P, s);
+    rc = record(cudaStreamEndCapture(s, &graph), "end capture");
+    if (rc) return rc;
+    rc = record(cudaGraphInstantiate(out, graph, 0), "instantiate");
+    cudaGraphDestroy(graph);
+    return rc;
+}
+
+}  // namespace sdg
+
+using namespace sdg;
+
+extern "C" {
+
+int sdg_abi_version(void) { return 1; }
+int sdg_buffer_count(void) { return BUFFER_COUNT; }
+int sdg_value_count(void) { return VALUE_COUNT; }
+const char* sdg_last_error(void) { return g_error.c_str(); }
+
+int sdg_dispatch(const char* kernel, uint32_t count, void* const* buffers, const uint64_t* bytes, const double* values,
+                 uint32_t nvalues, void* stream) {
+    Params P;
+    if (int rc = unpack(buffers, bytes, values, nvalues, P)) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    std::string_view k(kernel ? kernel : "");
+    if (k == "step") launch_step(P, s);
+    else if (k == "forces") launch_forces(P, s, true);
+    else if (k == "forcesNoCapture") launch_forces(P, s, false);
+    else if (launch_state(k, P, count, s) != 0 && launch_contacts(k, P, count, s) != 0) {
+        g_error = "unknown kernel " + std::string(k);
+        return 1;
+    }
+    return record(cudaGetLastError(), kernel);
+}
+
+int sdg_reduce_rows(const void* input, void* output, uint32_t n, uint32_t rows, int32_t max_row, void* stream) {
+    if (!input || !output || rows == 0) { g_error = "bad reduction arguments"; return 1; }
+    launch_reduce_rows(static_cast<const float4*>(input), static_cast<float4*>(output), n, rows, max_row,
+                       static_cast<cudaStream_t>(stream));
+    return record(cudaGetLastError(), "reduce rows");
+}
+
+void* sdg_engine_create(void) { return new (std::nothrow) Engine(); }
+void sdg_engine_destroy(void* engine) { delete static_cast<Engine*>(engine); }
+
+// Advances `steps` steps starting from the history side the buffers describe,
+// alternating sides; with use_graph, each side's step is a captured CUDA graph
+// replayed (recaptured when buffers or values change).
+int sdg_engine_advance(void* engine, void* const* buffers, const uint64_t* bytes, const double* values,
+                       uint32_t nvalues, uint32_t steps, uint32_t use_graph, void* stream) {
+    Engine* e = static_cast<Engine*>(engine);
+    if (!e) { g_error = "null engine"; return 1; }
+    Params P;
+    if (int rc = unpack(buffers, bytes, values, nvalues, P)) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Params side[2] = {P, swapSides(P)};
+    if (!use_graph) {
+        for (uint32_t k = 0; k < steps; ++k) launch_step(side[k & 1], s);
+        return record(cudaGetLastError(), "advance");
+    }
+    std::vector<unsigned char> key(sizeof(Params));
+    std::memcpy(key.data(), &P, sizeof(Params));
+    if (key != e->key) {
+        e->reset();
+        for (int k = 0; k < 2; ++k)
+            if (int rc = capture(side[k], s, &e->exec[k])) { e->reset(); return rc; }
+        e->key = key;
+    }
+    for (uint32_t k = 0; k < steps; ++k)
+        if (int rc = record(cudaGraphLaunch(e->exec[k & 1], s), "graph launch")) return rc;
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,411 @@
+// Device-side arithmetic and resource layout of the GB300 mesh-surface DEM step.
+//
+// Exactness contract: every FP32 expression that decides a pair, a contact
+// key or a history slot is evaluated in the operation order of the reference
+// CPU backend (the Slang-generated C++ of src/sand_atlas_dem/shaders/
+// solver.slang): dot = ((0 + x0*y0) + x1*y1) + x2*y2, length = sqrt(dot),
+// min/max as the ternaries a<b?a:b and a>b?a:b, float literals, no FMA
+// contraction (this translation unit is built with --fmad=false and IEEE
+// division/square root).  The minimum-image branch is FP64 as in
+// shaders/cpu_scheduling.slang:10-15, evaluated once per directed pair.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sdg {
+
+constexpr uint32_t EMPTY = 0xffffffffu;
+constexpr int RESOURCE_COUNT = 77;
+
+// Solver flags (src/sand_atlas_dem/gpu.py:11-26) plus one for bounded waits.
+enum Flag : uint32_t {
+    F_DEGENERATE = 2, F_PENETRATION = 4, F_BIN = 8, F_PAIR = 16, F_CONTACT = 32, F_HASH = 64,
+    F_CYCLE = 128, F_IMAGE = 256, F_NONFINITE = 512, F_STACK = 1024, F_ESCAPE = 2048,
+    F_TIMESTEP = 8192, F_COINCIDENT = 16384, F_WAIT = 65536
+};
+
+struct Config {
+    uint32_t activeTimestep, N, shapes, pairCapacity, contactCapacity, binCapacity, binCount;
+    uint32_t bins[3];
+    uint32_t hashSize;
+    float dt, kn, kt, mu, normalViscosity, skin, drag, maxOverlap;
+    uint32_t historyStep, meshGeometry, periodic, wallCount, wallBoxEnabled, sourceSurfaceNormal;
+    // Backend extension values.
+    uint32_t leafWords;          // 32-bit words per directed pair in the leaf mask
+    uint32_t candidateCapacity;  // (directed pair, leaf cluster) work items
+    uint32_t viscousCapture;     // fuse captureContactKinematics into beginStep
+};
+
+// Buffers: the reference Resources block (solver.slang:20-100) in declaration
+// order, then this backend's extension buffers.
+struct Res {
+    uint32_t* control; float4* cell; float4* position; float4* positionRemainder;
+    float4* velocityRemainder; float4* momentumRemainder; float4* rotationRemainder;
+    float4* referencePositionRemainder; float4* cellLog; float4* accumulatedRemainder;
+    float4* velocity; float4* rotation; float4* momentum; float4* force; float4* torque;
+    float4* referencePosition; float4* referenceCell; const uint32_t* shapeId; const float4* body;
+    const float4* invI; const uint4* grids; const uint4* sampleInfo; const float4* gridOrigin;
+    const float* distance; const float4* sample; const uint4* meshRoots; const uint4* meshHullInfo;
+    const float4* meshPlanes; const float4* meshMin; const float4* meshMax; const uint4* meshLinks;
+    const float4* meshTriangles; const float4* meshNormals; const uint4* meshFrontier;
+    uint32_t* meshPairMask; float4* meshPairTransform; const uint4* meshClusterInfo;
+    const uint4* meshClusterRanges; const float4* meshClusterMin; const float4* meshClusterMax;
+    const uint32_t* meshSampleIndices; uint32_t* binCounts; uint32_t* binParticles;
+    uint32_t* pairCounts; uint32_t* pairOffsets; uint2* pairs; uint32_t* contactCounts;
+    uint32_t* contactOffsets; uint4* meta; float4* pointDepth; float4* normalArea; float4* slip;
+    float4* contactForce; float* normalLossPower; float4* normalDamping; float4* forceVelocity;
+    float4* forceOmega; const uint4* oldMeta; const float4* oldSlip; const float4* oldNormal;
+    const uint32_t* oldHash; uint32_t* hash; uint32_t* heads; uint32_t* next;
+    float4* particleStress; float4* timestepRows; float4* particleDiagnostic;
+    float4* diagnosticRows; float4* accumulated; float4* fabricRows; float4* wallPlane;
+    float4* wallRemainder; float4* wallVelocity; float4* wallMaterial; uint32_t* wallBoxIds;
+    float4* wallRows; float4* wallAccumulated;
+    // ---- extension (index 77 onward)
+    const uint4* meshLeafInfo;        // per shape: first leaf slot, leaf count
+    const uint32_t* meshLeaves;       // leaf cluster ids, preorder
+    const uint32_t* meshSampleRank;   // per packed sample: position in meshSampleIndices
+    uint32_t* byJCounts;              // N+1
+    uint32_t* byJOffsets;             // N+1
+    uint32_t* byJCursor;              // N
+    uint32_t* byJPairs;               // pairCapacity: pair ids grouped by second grain
+    float4* dpairBranch;              // 2*pairCapacity: FP64-exact branch per directed pair
+    uint32_t* dpairLeafCount;         // 2*pairCapacity+1
+    uint32_t* dpairCandOffset;        // 2*pairCapacity+1
+    uint32_t* leafMask;               // 2*pairCapacity*leafWords
+    uint2* candidates;                // candidateCapacity: (directed pair, leaf cluster)
+    uint32_t* candHitCount;           // candidateCapacity+1
+    uint32_t* candHitOffset;          // candidateCapacity+1
+    uint2* candHitMask;               // candidateCapacity: 64-bit node hit mask
+    uint32_t* contactPair;            // contactCapacity: pair of each contact
+    uint32_t* sidePairOffsets;        // N+1   (history side being written)
+    uint32_t* sidePairB;              // pairCapacity
+    uint32_t* sideContactStart;       // pairCapacity+1
+    const uint32_t* oldPairOffsets;   // N+1   (committed history side)
+    const uint32_t* oldPairB;         // pairCapacity
+    const uint32_t* oldContactStart;  // pairCapacity+1
+    uint32_t* work;                   // 64 counters
+    uint32_t* scanPartials;           // 2*SCAN_BLOCKS
+};
+constexpr int EXTENSION_COUNT = 24;
+constexpr int BUFFER_COUNT = RESOURCE_COUNT + EXTENSION_COUNT;
+constexpr int CONFIG_VALUES = 25;
+constexpr int VALUE_COUNT = CONFIG_VALUES + 3;
+constexpr int SCAN_BLOCKS = 608;  // 4 per SM on a 152-SM GB300
+// work[] slots
+constexpr int W_CANDIDATES = 0;
+
+struct Params {
+    Config c;
+    Res r;
+};
+
+// ------------------------------------------------------------------ vectors
+struct f3 { float x, y, z; };
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ f3 xyz(float4 a) { return {a.x, a.y, a.z}; }
+__device__ __forceinline__ float4 w4(f3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y), __fmul_rn(a.z, b.z)}; }
+__device__ __forceinline__ f3 operator/(f3 a, f3 b) { return {__fdiv_rn(a.x, b.x), __fdiv_rn(a.y, b.y), __fdiv_rn(a.z, b.z)}; }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return {__fmul_rn(s, a.x), __fmul_rn(s, a.y), __fmul_rn(s, a.z)}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s)}; }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return {__fdiv_rn(a.x, s), __fdiv_rn(a.y, s), __fdiv_rn(a.z, s)}; }
+__device__ __forceinline__ f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ float4 add4(float4 a, float4 b) {
+    return make_float4(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z), __fadd_rn(a.w, b.w));
+}
+__device__ __forceinline__ float4 sub4(float4 a, float4 b) {
+    return make_float4(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z), __fsub_rn(a.w, b.w));
+}
+__device__ __forceinline__ float4 scale4(float4 a, float s) {
+    return make_float4(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s), __fmul_rn(a.w, s));
+}
+__device__ __forceinline__ float mn(float a, float b) { return a < b ? a : b; }
+__device__ __forceinline__ float mx(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ f3 mn3(f3 a, f3 b) { return {mn(a.x, b.x), mn(a.y, b.y), mn(a.z, b.z)}; }
+__device__ __forceinline__ f3 mx3(f3 a, f3 b) { return {mx(a.x, b.x), mx(a.y, b.y), mx(a.z, b.z)}; }
+__device__ __forceinline__ f3 abs3(f3 a) { return {fabsf(a.x), fabsf(a.y), fabsf(a.z)}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) {
+    float r = __fadd_rn(0.0f, __fmul_rn(a.x, b.x));
+    r = __fadd_rn(r, __fmul_rn(a.y, b.y));
+    return __fadd_rn(r, __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ float dot4(float4 a, float4 b) {
+    float r = __fadd_rn(0.0f, __fmul_rn(a.x, b.x));
+    r = __fadd_rn(r, __fmul_rn(a.y, b.y));
+    r = __fadd_rn(r, __fmul_rn(a.z, b.z));
+    return __fadd_rn(r, __fmul_rn(a.w, b.w));
+}
+__device__ __forceinline__ float length(f3 a) { return __fsqrt_rn(dot(a, a)); }
+__device__ __forceinline__ f3 cross(f3 l, f3 r) {
+    return {__fsub_rn(__fmul_rn(l.y, r.z), __fmul_rn(l.z, r.y)),
+            __fsub_rn(__fmul_rn(l.z, r.x), __fmul_rn(l.x, r.z)),
+            __fsub_rn(__fmul_rn(l.x, r.y), __fmul_rn(l.y, r.x))};
+}
+__device__ __forceinline__ float comp(f3 a, uint32_t i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+__device__ __forceinline__ bool finite3(f3 a) { return isfinite(a.x) && isfinite(a.y) && isfinite(a.z); }
+
+// Quaternions xyzw, body to world (solver.slang:104-106).
+__device__ __forceinline__ f3 qrot(float4 q, f3 v) {
+    f3 u = xyz(q);
+    return v + 2.0f * cross(u, cross(u, v) + q.w * v);
+}
+__device__ __forceinline__ f3 qinv(float4 q, f3 v) { return qrot(make_float4(-q.x, -q.y, -q.z, q.w), v); }
+__device__ __forceinline__ float4 qmul(float4 a, float4 b) {
+    f3 v = (a.w * xyz(b) + b.w * xyz(a)) + cross(xyz(a), xyz(b));
+    return w4(v, __fsub_rn(__fmul_rn(a.w, b.w), dot(xyz(a), xyz(b))));
+}
+// normalize(x) = x * (1 / sqrt(dot(x, x))).
+__device__ __forceinline__ float4 normalize4(float4 q) { return scale4(q, __fdiv_rn(1.0f, __fsqrt_rn(dot4(q, q)))); }
+
+__device__ __forceinline__ void fail(const Res& r, uint32_t bit) { atomicOr(r.control, bit); }
+
+// solver.slang:111-118
+__device__ __forceinline__ void compensated3(f3& high, f3& low, f3 inc) {
+    f3 y = inc + low;
+    f3 nx = high + y;
+    f3 moved = nx - high;
+    low = y - moved;
+    high = nx;
+}
+__device__ __forceinline__ void compensated4(float4& high, float4& low, float4 inc) {
+    float4 y = add4(inc, low);
+    float4 nx = add4(high, y);
+    float4 moved = sub4(nx, high);
+    low = sub4(y, moved);
+    high = nx;
+}
+// solver.slang:119-123
+__device__ __forceinline__ float expm1Stable(float x) {
+    if (fabsf(x) < 0.01f) {
+        float t = __fadd_rn(__fdiv_rn(1.0f, 24.0f), __fdiv_rn(x, 120.0f));
+        t = __fadd_rn(__fdiv_rn(1.0f, 6.0f), __fmul_rn(x, t));
+        t = __fadd_rn(0.5f, __fmul_rn(x, t));
+        t = __fadd_rn(1.0f, __fmul_rn(x, t));
+        return __fmul_rn(x, t);
+    }
+    return __fsub_rn(expf(x), 1.0f);
+}
+__device__ __forceinline__ f3 expm1Stable3(f3 x) { return {expm1Stable(x.x), expm1Stable(x.y), expm1Stable(x.z)}; }
+__device__ __forceinline__ f3 exp3(f3 x) { return {expf(x.x), expf(x.y), expf(x.z)}; }
+// solver.slang:124-129
+__device__ __forceinline__ float4 rotationIncrement(f3 w, float dt, float4 q) {
+    float half = __fmul_rn(__fmul_rn(0.5f, length(w)), dt);
+    float coefficient = fabsf(half) < 0.001f
+        ? __fmul_rn(__fmul_rn(0.5f, dt), __fsub_rn(1.0f, __fdiv_rn(__fmul_rn(half, half), 6.0f)))
+        : __fdiv_rn(sinf(half), length(w));
+    float s = sinf(__fmul_rn(0.5f, half));
+    float cm1 = __fmul_rn(__fmul_rn(-2.0f, s), s);
+    return qmul(w4(coefficient * w, cm1), q);
+}
+
+// Minimum-image branch j - i in FP64, cast to FP32 (cpu_scheduling.slang:10-15).
+__device__ __forceinline__ f3 centerBranch64(const Res& r, const Config& c, uint32_t i, uint32_t j) {
+    float4 pi = r.position[i], pj = r.position[j], li = r.positionRemainder[i], lj = r.positionRemainder[j];
+    float4 cell = r.cell[0];
+    double dx = __dadd_rn(__dsub_rn((double)pj.x, (double)pi.x), __dsub_rn((double)lj.x, (double)li.x));
+    double dy = __dadd_rn(__dsub_rn((double)pj.y, (double)pi.y), __dsub_rn((double)lj.y, (double)li.y));
+    double dz = __dadd_rn(__dsub_rn((double)pj.z, (double)pi.z), __dsub_rn((double)lj.z, (double)li.z));
+    if (c.periodic != 0) {
+        double bx = cell.x, by = cell.y, bz = cell.z;
+        dx = __dsub_rn(dx, __dmul_rn(floor(__dadd_rn(__ddiv_rn(dx, bx), 0.5)), bx));
+        dy = __dsub_rn(dy, __dmul_rn(floor(__dadd_rn(__ddiv_rn(dy, by), 0.5)), by));
+        dz = __dsub_rn(dz, __dmul_rn(floor(__dadd_rn(__ddiv_rn(dz, bz), 0.5)), bz));
+    }
+    return {__double2float_rn(dx), __double2float_rn(dy), __double2float_rn(dz)};
+}
+// solver.slang:154-158
+__device__ __forceinline__ f3 omega(const Res& r, uint32_t i, float4 q, f3 l) {
+    f3 b = qinv(q, l);
+    f3 w = {dot(xyz(r.invI[3 * i]), b), dot(xyz(r.invI[3 * i + 1]), b), dot(xyz(r.invI[3 * i + 2]), b)};
+    return qrot(q, w);
+}
+__device__ __forceinline__ f3 omegaOf(const Res& r, uint32_t i) {
+    return omega(r, i, r.rotation[i], xyz(r.momentum[i]) + xyz(r.momentumRemainder[i]));
+}
+
+// ------------------------------------------------------------ mesh queries
+// solver.slang:203-219
+__device__ __forceinline__ f3 closestTriangle(f3 p, f3 a, f3 b, f3 c, uint32_t& feature) {
+    f3 ab = b - a, ac = c - a, ap = p - a;
+    float d1 = dot(ab, ap), d2 = dot(ac, ap);
+    feature = 4;
+    if (d1 <= 0 && d2 <= 0) return a;
+    f3 bp = p - b;
+    float d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= 0 && d4 <= d3) { feature = 5; return b; }
+    float vc = __fsub_rn(__fmul_rn(d1, d4), __fmul_rn(d3, d2));
+    if (vc <= 0 && d1 >= 0 && d3 <= 0) { feature = 1; return a + __fdiv_rn(d1, __fsub_rn(d1, d3)) * ab; }
+    f3 cp = p - c;
+    float d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= 0 && d5 <= d6) { feature = 6; return c; }
+    float vb = __fsub_rn(__fmul_rn(d5, d2), __fmul_rn(d1, d6));
+    if (vb <= 0 && d2 >= 0 && d6 <= 0) { feature = 3; return a + __fdiv_rn(d2, __fsub_rn(d2, d6)) * ac; }
+    float va = __fsub_rn(__fmul_rn(d3, d6), __fmul_rn(d5, d4));
+    float e43 = __fsub_rn(d4, d3), e56 = __fsub_rn(d5, d6);
+    if (va <= 0 && e43 >= 0 && e56 >= 0) { feature = 2; return b + __fdiv_rn(e43, __fadd_rn(e43, e56)) * (c - b); }
+    float inv = __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(va, vb), vc));
+    feature = 0;
+    return (a + ab * __fmul_rn(vb, inv)) + ac * __fmul_rn(vc, inv);
+}
+// solver.slang:220-223
+__device__ __forceinline__ float meshBoxDistance(const Res& r, uint32_t node, f3 p) {
+    f3 d = mx3(mx3(xyz(__ldg(&r.meshMin[node])) - p, p - xyz(__ldg(&r.meshMax[node]))), mk(0.f, 0.f, 0.f));
+    return dot(d, d);
+}
+// Nearest-first BVH walk with cached pushed box distances (the reference CPU
+// variant, cpu_scheduling.slang:18-48, bit-identical to solver.slang:224-252).
+__device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 p, bool surfaceNormal) {
+    uint32_t root = __ldg(&r.meshRoots[shape].x);
+    uint32_t pending[32];
+    float pendingDistance[32];
+    uint32_t top = 1;
+    pending[0] = root;
+    pendingDistance[0] = meshBoxDistance(r, root, p);
+    float best = 1e30f;
+    f3 nearest = mk(0.f, 0.f, 0.f);
+    uint32_t nearestNormal = 0;
+    bool found = false;
+    while (top > 0) {
+        uint32_t slot = --top, node = pending[slot];
+        if (pendingDistance[slot] > best) continue;
+        uint4 link = __ldg(&r.meshLinks[node]);
+        if (link.z == 0) {
+            uint32_t a = node + 1, b = __ldg(&r.meshLinks[a].x);
+            float da = meshBoxDistance(r, a, p), db = meshBoxDistance(r, b, p);
+            if (da < db) { uint32_t s = a; a = b; b = s; float ds = da; da = db; db = ds; }
+            if (top + 2 > 32) { fail(r, F_STACK); return make_float4(0.f, 0.f, 0.f, 1e20f); }
+            if (da <= best) { pending[top] = a; pendingDistance[top++] = da; }
+            if (db <= best) { pending[top] = b; pendingDistance[top++] = db; }
+            continue;
+        }
+        for (uint32_t k = 0; k < link.z; ++k) {
+            uint32_t triangle = link.y + k, feature;
+            f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * triangle])), xyz(__ldg(&r.meshTriangles[3 * triangle + 1])),
+                                   xyz(__ldg(&r.meshTriangles[3 * triangle + 2])), feature);
+            f3 dq = p - q;
+            float distance = dot(dq, dq);
+            if (distance < best) { best = distance; nearest = q; nearestNormal = 7 * triangle + feature; found = true; }
+        }
+    }
+    f3 pseudo = found ? xyz(__ldg(&r.meshNormals[nearestNormal])) : mk(0.f, 0.f, 0.f);
+    float distance = __fsqrt_rn(best);
+    f3 off = p - nearest;
+    float side = dot(off, pseudo) < 0 ? -1.0f : 1.0f;
+    f3 normal = surfaceNormal ? pseudo : (distance > 1e-12f ? (side * off) / distance : pseudo);
+    return w4(normal, __fmul_rn(side, distance));
+}
+// solver.slang:259-272
+__device__ __forceinline__ bool meshMayContain(const Res& r, uint32_t shape, f3 p) {
+    uint32_t root = __ldg(&r.meshRoots[shape].x);
+    f3 low = xyz(__ldg(&r.meshMin[root])), high = xyz(__ldg(&r.meshMax[root]));
+    if (p.x < low.x || p.y < low.y || p.z < low.z || p.x > high.x || p.y > high.y || p.z > high.z) return false;
+    f3 direction = (p - 0.5f * (low + high)) / (high - low);
+    f3 a = abs3(direction);
+    uint32_t axis = a.x >= a.y && a.x >= a.z ? 0 : (a.y >= a.z ? 1 : 2);
+    uint32_t group = 2 * axis + (comp(direction, axis) >= 0 ? 1 : 0);
+    uint4 info = __ldg(&r.meshHullInfo[6 * shape + group]);
+    for (uint32_t i = 0; i < info.y; ++i) {
+        float4 plane = __ldg(&r.meshPlanes[info.x + i]);
+        if (__fadd_rn(dot(xyz(plane), p), plane.w) > 0) return false;
+    }
+    return true;
+}
+// solver.slang:274-288
+__device__ __forceinline__ bool meshBoxMayContact(const Res& r, uint32_t shape, f3 low, f3 high) {
+    uint32_t root = __ldg(&r.meshRoots[shape].x);
+    f3 tl = xyz(__ldg(&r.meshMin[root])), th = xyz(__ldg(&r.meshMax[root]));
+    if (high.x < tl.x || high.y < tl.y || high.z < tl.z || low.x > th.x || low.y > th.y || low.z > th.z) return false;
+    f3 center = 0.5f * (low + high), half = 0.5f * (high - low);
+    f3 direction = (center - 0.5f * (tl + th)) / (th - tl);
+    f3 a = abs3(direction);
+    uint32_t axis = a.x >= a.y && a.x >= a.z ? 0 : (a.y >= a.z ? 1 : 2);
+    uint32_t group = 2 * axis + (comp(direction, axis) >= 0 ? 1 : 0);
+    uint4 info = __ldg(&r.meshHullInfo[6 * shape + group]);
+    for (uint32_t i = 0; i < info.y; ++i) {
+        float4 plane = __ldg(&r.meshPlanes[info.x + i]);
+        if (__fsub_rn(__fadd_rn(dot(xyz(plane), center), plane.w), dot(abs3(xyz(plane)), half)) > 0) return false;
+    }
+    return true;
+}
+// solver.slang:290-305, with the directed-pair branch supplied.
+__device__ __forceinline__ bool meshClusterMayContact(const Res& r, uint32_t src, uint32_t dst, uint32_t cluster, f3 branch) {
+    f3 sl = xyz(r.meshClusterMin[cluster]), sh = xyz(r.meshClusterMax[cluster]);
+    f3 low = mk(1e30f, 1e30f, 1e30f), high = mk(-1e30f, -1e30f, -1e30f);
+    float4 qs = r.rotation[src], qd = r.rotation[dst];
+    float ss = r.body[src].x, sd = r.body[dst].x;
+    for (uint32_t corner = 0; corner < 8; ++corner) {
+        f3 p = mk((corner & 1) ? sh.x : sl.x, (corner & 2) ? sh.y : sl.y, (corner & 4) ? sh.z : sl.z);
+        p = qinv(qd, qrot(qs, p * ss) - branch) / sd;
+        low = mn3(low, p);
+        high = mx3(high, p);
+    }
+    float pad = __fmul_rn(0.00000762939453125f,
+        __fadd_rn(__fadd_rn(__fadd_rn(1.0f, mx(mx(fabsf(low.x), fabsf(low.y)), fabsf(low.z))),
+                            mx(mx(fabsf(high.x), fabsf(high.y)), fabsf(high.z))), __fdiv_rn(length(branch), sd)));
+    low = low - mk(pad, pad, pad);
+    high = high + mk(pad, pad, pad);
+    return meshBoxMayContact(r, r.shapeId[dst], low, high);
+}
+// solver.slang:404-417
+__device__ __forceinline__ void meshPairBounds(const Res& r, uint32_t direction, uint32_t cluster, f3& low, f3& high) {
+    f3 cmin = xyz(__ldg(&r.meshClusterMin[cluster])), cmax = xyz(__ldg(&r.meshClusterMax[cluster]));
+    f3 center = 0.5f * (cmin + cmax);
+    f3 half = 0.5f * (cmax - cmin);
+    float cc[3], e[3];
+#pragma unroll
+    for (uint32_t axis = 0; axis < 3; ++axis) {
+        float4 row = r.meshPairTransform[4 * direction + axis];
+        cc[axis] = __fadd_rn(dot(xyz(row), center), row.w);
+        e[axis] = dot(abs3(xyz(row)), half);
+    }
+    low = mk(cc[0], cc[1], cc[2]) - mk(e[0], e[1], e[2]);
+    high = mk(cc[0], cc[1], cc[2]) + mk(e[0], e[1], e[2]);
+    float pad = __fmul_rn(0.000030517578125f,
+        __fadd_rn(__fadd_rn(__fadd_rn(1.0f, mx(mx(fabsf(low.x), fabsf(low.y)), fabsf(low.z))),
+                            mx(mx(fabsf(high.x), fabsf(high.y)), fabsf(high.z))), r.meshPairTransform[4 * direction + 3].x));
+    low = low - mk(pad, pad, pad);
+    high = high + mk(pad, pad, pad);
+}
+// solver.slang:319-343; the directed-pair branch is precomputed (same bits).
+__device__ __forceinline__ bool nodeContact(const Res& r, const Config& c, uint32_t src, uint32_t dst, uint32_t node,
+                                            f3 branch, float4& pd, float4& na) {
+    uint32_t sid = r.shapeId[src];
+    float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[sid].x) + node]);
+    float4 qs = r.rotation[src], qd = r.rotation[dst];
+    float4 bs = r.body[src], bd = r.body[dst];
+    f3 arm = qrot(qs, xyz(sp) * bs.x);
+    f3 local = qinv(qd, arm - branch) / bd.x;
+    uint32_t targetShape = r.shapeId[dst];
+    if (!meshMayContain(r, targetShape, local)) return false;
+    float4 f = meshDistance(r, targetShape, local, false);
+    pd = w4(arm, __fmul_rn(-f.w, bd.x));
+    if (pd.w <= 0.0f) return false;
+    f3 grad = qrot(qd, xyz(f));
+    float len = length(grad);
+    if (c.sourceSurfaceNormal != 0) {
+        float4 own = meshDistance(r, sid, xyz(sp), true);
+        if (fabsf(own.w) > 0.00000999999974738f) { fail(r, F_DEGENERATE); return false; }
+        grad = -qrot(qs, xyz(own));
+        len = length(grad);
+    }
+    if (len < 1.00000001168609742e-07f || !isfinite(pd.w)) { fail(r, F_DEGENERATE); return false; }
+    na = w4(grad / len, __fmul_rn(__fmul_rn(sp.w, bs.x), bs.x));
+    if (pd.w > __fmul_rn(c.maxOverlap, mn(bs.w, bd.w))) fail(r, F_PENETRATION);
+    return true;
+}
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ uint32_t activePairs(const Res& r, const Config& c) {
+    uint32_t n = r.control[1];
+    return n < c.pairCapacity ? n : c.pairCapacity;
+}
+__device__ __forceinline__ uint32_t activeContacts(const Res& r, const Config& c) {
+    uint32_t n = r.control[2];
+    return n < c.contactCapacity ? n : c.contactCapacity;
+}
+__device__ __forceinline__ uint32_t gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ uint32_t gstride() { return gridDim.x * blockDim.x; }
+
+}  // namespace sdg

@@ -1,0 +1,708 @@
+// Neighbour build, mesh contact collection, friction-history merge, contact
+// law and the deterministic force gather.
+//
+// Contact order is canonical and equal to the reference CPU collector's
+// (cpu_scheduling.slang:53-91): pair index, then direction, then leaf cluster
+// in preorder, then node in meshSampleIndices order.  The collector keeps it
+// with no atomics on contact slots: a flat leaf cull per directed pair, an
+// exclusive scan to (directed pair, leaf) work items, one warp per item for
+// the exact node queries (two nodes per lane, ballot hit masks), an
+// exclusive scan of hit counts, and an emit pass that recomputes only the
+// hits.  The history merge and the gather then walk sorted runs instead of a
+// hash table and linked lists, so every run is reproducible bit for bit.
+#include <cuda_runtime.h>
+#include "dem_device.cuh"
+#include "launch.h"
+
+namespace sdg {
+
+constexpr uint32_t WARP = 32;
+__device__ __forceinline__ uint32_t laneId() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t warpGlobal() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ uint32_t warpStride() { return (gridDim.x * blockDim.x) >> 5; }
+__device__ __forceinline__ uint32_t lanesBelow() { return (1u << laneId()) - 1u; }
+
+// ------------------------------------------------------------------- scan
+__device__ __forceinline__ uint32_t scanCount(const ScanCount& c) {
+    if (!c.ptr) return c.constant;
+    uint32_t v = *c.ptr;
+    return (v < c.cap ? v : c.cap) * c.mul;
+}
+__device__ __forceinline__ uint32_t blockInclusive(uint32_t v, uint32_t* shared) {
+    // 256 threads: warp scans, then a scan of the 8 warp totals.
+    uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) shared[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (blockDim.x >> 5) ? shared[lane] : 0;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
+        }
+        if (lane < (blockDim.x >> 5)) shared[lane] = w;
+    }
+    __syncthreads();
+    uint32_t add = warp ? shared[warp - 1] : 0;
+    __syncthreads();
+    return v + add;
+}
+__global__ void k_scanReduce(const uint32_t* in, ScanCount count, const uint32_t* gate, uint32_t* partials) {
+    __shared__ uint32_t shared[32];
+    if (gate && *gate == 0) return;
+    uint32_t n = scanCount(count);
+    uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    uint32_t begin = blockIdx.x * chunk, end = min(n, begin + chunk);
+    uint32_t sum = 0;
+    for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) sum += in[i];
+    sum = blockInclusive(sum, shared);
+    if (threadIdx.x == blockDim.x - 1) partials[blockIdx.x] = sum;
+}
+__global__ void k_scanTop(ScanCount count, uint32_t* out, bool writeEnd, uint32_t* totalDst, const uint32_t* gate,
+                          uint32_t* partials, uint32_t blocks) {
+    __shared__ uint32_t shared[32];
+    if (gate && *gate == 0) return;
+    // blocks <= 1024: one element per thread.
+    uint32_t v = threadIdx.x < blocks ? partials[threadIdx.x] : 0;
+    uint32_t inc = blockInclusive(v, shared);
+    if (threadIdx.x < blocks) partials[blocks + threadIdx.x] = inc - v;
+    if (threadIdx.x == blockDim.x - 1) {
+        uint32_t n = scanCount(count);
+        if (writeEnd) out[n] = inc;
+        if (totalDst) *totalDst = inc;
+    }
+}
+__global__ void k_scanApply(const uint32_t* in, uint32_t* out, ScanCount count, const uint32_t* gate,
+                            const uint32_t* partials) {
+    __shared__ uint32_t shared[32];
+    __shared__ uint32_t tileTotal;
+    if (gate && *gate == 0) return;
+    uint32_t n = scanCount(count);
+    uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    uint32_t begin = blockIdx.x * chunk, end = min(n, begin + chunk);
+    uint32_t carry = partials[gridDim.x + blockIdx.x];
+    for (uint32_t base = begin; base < end; base += blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        uint32_t v = i < end ? in[i] : 0;
+        uint32_t inc = blockInclusive(v, shared);
+        if (i < end) out[i] = carry + inc - v;
+        if (threadIdx.x == blockDim.x - 1) tileTotal = inc;
+        __syncthreads();
+        carry += tileTotal;
+        __syncthreads();
+    }
+}
+
+void launch_scan(const uint32_t* in, uint32_t* out, ScanCount count, bool writeEnd, uint32_t* totalDst,
+                 const uint32_t* gate, uint32_t* partials, cudaStream_t s) {
+    k_scanReduce<<<SCAN_BLOCKS, 256, 0, s>>>(in, count, gate, partials);
+    k_scanTop<<<1, 1024, 0, s>>>(count, out, writeEnd, totalDst, gate, partials, SCAN_BLOCKS);
+    k_scanApply<<<SCAN_BLOCKS, 256, 0, s>>>(in, out, count, gate, partials);
+}
+
+// ------------------------------------------------------------ neighbours
+// solver.slang:184-186
+__device__ __forceinline__ void binIndex(const Res& r, const Config& c, uint32_t i, uint32_t b[3]) {
+    float4 p = r.position[i], box = r.cell[0];
+    float g[3] = {floorf(__fmul_rn(__fdiv_rn(p.x, box.x), float(c.bins[0]))),
+                  floorf(__fmul_rn(__fdiv_rn(p.y, box.y), float(c.bins[1]))),
+                  floorf(__fmul_rn(__fdiv_rn(p.z, box.z), float(c.bins[2])))};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        uint32_t v = uint32_t(g[k]);
+        b[k] = v < c.bins[k] - 1 ? v : c.bins[k] - 1;
+    }
+}
+__device__ __forceinline__ uint32_t binFlat(const Config& c, const uint32_t b[3]) {
+    return (b[0] * c.bins[1] + b[1]) * c.bins[2] + b[2];
+}
+__device__ __forceinline__ uint32_t modIndex(int a, uint32_t n) { return uint32_t((a % int(n) + int(n)) % int(n)); }
+
+__global__ void k_binsClear(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    if (r.control[4] == 0) return;
+    for (uint32_t b = gtid(); b < P.c.binCount; b += gstride()) r.binCounts[b] = 0;
+}
+// solver.slang:350-359
+__global__ void k_binsFill(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t id = gtid();
+    if (id >= c.N || r.control[4] == 0) return;
+    f3 p = xyz(r.position[id]), pl = xyz(r.positionRemainder[id]);
+    if (!finite3(p) || !finite3(pl)) { fail(r, F_NONFINITE); return; }
+    if (c.periodic == 0) {
+        f3 box = xyz(r.cell[0]);
+        if (__fadd_rn(p.x, pl.x) < 0 || __fadd_rn(p.y, pl.y) < 0 || __fadd_rn(p.z, pl.z) < 0 ||
+            __fadd_rn(__fsub_rn(p.x, box.x), pl.x) >= 0 || __fadd_rn(__fsub_rn(p.y, box.y), pl.y) >= 0 ||
+            __fadd_rn(__fsub_rn(p.z, box.z), pl.z) >= 0) { fail(r, F_ESCAPE); return; }
+    }
+    uint32_t b[3];
+    binIndex(r, c, id, b);
+    uint32_t bin = binFlat(c, b);
+    uint32_t slot = atomicAdd(&r.binCounts[bin], 1u);
+    if (slot < c.binCapacity) r.binParticles[bin * c.binCapacity + slot] = id;
+    else fail(r, F_BIN);
+}
+// Order each bin's slots by grain id: the serial reference fills bins in id
+// order, which fixes the pair order downstream.  Rank sort in shared memory.
+__global__ void k_binsSort(const __grid_constant__ Params P) {
+    extern __shared__ uint32_t ids[];
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[4] == 0) return;
+    uint32_t cap = c.binCapacity;
+    uint32_t* sorted = ids + cap;
+    for (uint32_t bin = blockIdx.x; bin < c.binCount; bin += gridDim.x) {
+        uint32_t occ = min(r.binCounts[bin], cap);
+        for (uint32_t k = threadIdx.x; k < occ; k += blockDim.x) ids[k] = r.binParticles[bin * cap + k];
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < occ; k += blockDim.x) {
+            uint32_t v = ids[k], rank = 0;
+            for (uint32_t t = 0; t < occ; ++t) rank += ids[t] < v;
+            sorted[rank] = v;
+        }
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < occ; k += blockDim.x) r.binParticles[bin * cap + k] = sorted[k];
+        __syncthreads();
+    }
+}
+// solver.slang:360-384.  An FP32 minimum-image estimate rejects grains that
+// are clearly beyond range before the exact FP64 branch decides.
+__device__ uint32_t findPairs(const Res& r, const Config& c, uint32_t id, bool emit) {
+    uint32_t b[3];
+    binIndex(r, c, id, b);
+    float cutoff = r.referenceCell[1].w;
+    float4 cell = r.cell[0];
+    float box[3] = {cell.x, cell.y, cell.z};
+    int reach[3], low[3];
+    uint32_t width[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        reach[k] = int(ceilf(__fmul_rn(__fdiv_rn(cutoff, box[k]), float(c.bins[k]))));
+        low[k] = max(int(b[k]) - reach[k], 0);
+        int high = min(int(b[k]) + reach[k], int(c.bins[k]) - 1);
+        uint32_t w = uint32_t(2 * reach[k] + 1);
+        width[k] = c.periodic != 0 ? min(w, c.bins[k]) : uint32_t(high - low[k] + 1);
+    }
+    float4 pi = r.position[id], li = r.positionRemainder[id];
+    float ri = r.body[id].z;
+    uint32_t count = 0, base = emit ? r.pairOffsets[id] : 0;
+    for (uint32_t x = 0; x < width[0]; ++x)
+        for (uint32_t y = 0; y < width[1]; ++y)
+            for (uint32_t z = 0; z < width[2]; ++z) {
+                uint32_t cc[3];
+                if (c.periodic != 0) {
+                    cc[0] = modIndex(int(b[0]) - reach[0] + int(x), c.bins[0]);
+                    cc[1] = modIndex(int(b[1]) - reach[1] + int(y), c.bins[1]);
+                    cc[2] = modIndex(int(b[2]) - reach[2] + int(z), c.bins[2]);
+                } else {
+                    cc[0] = uint32_t(low[0] + int(x));
+                    cc[1] = uint32_t(low[1] + int(y));
+                    cc[2] = uint32_t(low[2] + int(z));
+                }
+                uint32_t bi = binFlat(c, cc);
+                uint32_t occ = min(r.binCounts[bi], c.binCapacity);
+                for (uint32_t slot = 0; slot < occ; ++slot) {
+                    uint32_t j = r.binParticles[bi * c.binCapacity + slot];
+                    if (j <= id) continue;
+                    float range = __fadd_rn(__fadd_rn(ri, r.body[j].z), c.skin);
+                    float rr = __fmul_rn(range, range);
+                    if (c.sourceSurfaceNormal == 0) {
+                        float4 pj = r.position[j], lj = r.positionRemainder[j];
+                        float e[3] = {(pj.x - pi.x) + (lj.x - li.x), (pj.y - pi.y) + (lj.y - li.y), (pj.z - pi.z) + (lj.z - li.z)};
+                        if (c.periodic != 0) {
+#pragma unroll
+                            for (int k = 0; k < 3; ++k) e[k] -= floorf(e[k] / box[k] + 0.5f) * box[k];
+                        }
+                        float est = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+                        if (est > 1.002f * rr) continue;  // estimate error is ~1e-6 relative
+                    }
+                    f3 d = centerBranch64(r, c, id, j);
+                    float dd = dot(d, d);
+                    if (c.sourceSurfaceNormal != 0 && dd < 1e-12f) { fail(r, F_COINCIDENT); continue; }
+                    if (dd > rr) continue;
+                    if (emit) {
+                        uint32_t index = base + count;
+                        if (index < c.pairCapacity) r.pairs[index] = make_uint2(id, j);
+                        else fail(r, F_PAIR);
+                    }
+                    count++;
+                }
+            }
+    return count;
+}
+__global__ void k_pairsCount(const __grid_constant__ Params P) {
+    uint32_t id = gtid();
+    if (id < P.c.N && P.r.control[4] != 0) P.r.pairCounts[id] = findPairs(P.r, P.c, id, false);
+}
+// solver.slang:388-392 (the pair total is written by the scan)
+__global__ void k_pairsEmit(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    uint32_t id = gtid();
+    if (id >= P.c.N || r.control[4] == 0) return;
+    findPairs(r, P.c, id, true);
+    r.referencePosition[id] = r.position[id];
+    r.referencePositionRemainder[id] = r.positionRemainder[id];
+    if (id == 0) r.referenceCell[0] = r.cell[0];
+}
+// Pairs grouped by their second grain, ascending pair id per grain.
+__global__ void k_byJReset(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    if (r.control[4] == 0) return;
+    for (uint32_t g = gtid(); g <= P.c.N; g += gstride()) {
+        r.byJCounts[g] = 0;
+        if (g < P.c.N) r.byJCursor[g] = 0;
+    }
+}
+__global__ void k_byJCount(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    if (r.control[4] == 0) return;
+    uint32_t n = activePairs(r, P.c);
+    for (uint32_t p = gtid(); p < n; p += gstride()) atomicAdd(&r.byJCounts[r.pairs[p].y], 1u);
+}
+__global__ void k_byJFill(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    if (r.control[4] == 0) return;
+    uint32_t n = activePairs(r, P.c);
+    for (uint32_t p = gtid(); p < n; p += gstride()) {
+        uint32_t j = r.pairs[p].y;
+        uint32_t slot = atomicAdd(&r.byJCursor[j], 1u);
+        r.byJPairs[r.byJOffsets[j] + slot] = p;
+    }
+}
+__global__ void k_byJSort(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    uint32_t g = gtid();
+    if (g >= P.c.N || r.control[4] == 0) return;
+    uint32_t begin = r.byJOffsets[g], end = r.byJOffsets[g + 1];
+    for (uint32_t a = begin + 1; a < end; ++a) {
+        uint32_t v = r.byJPairs[a], k = a;
+        while (k > begin && r.byJPairs[k - 1] > v) { r.byJPairs[k] = r.byJPairs[k - 1]; --k; }
+        r.byJPairs[k] = v;
+    }
+}
+
+// ------------------------------------------------------------ collection
+// Per pair: FP64 branches of both directions, root cull mask and 3x4
+// source-to-target transforms (prepareMeshPairs, solver.slang:468-489), and
+// the pair table of the history side being written.
+__global__ void k_pairSetup(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = activePairs(r, c);
+    for (uint32_t p = gtid(); p < n; p += gstride()) {
+        uint2 ij = r.pairs[p];
+        f3 branch[2] = {centerBranch64(r, c, ij.x, ij.y), centerBranch64(r, c, ij.y, ij.x)};
+        r.dpairBranch[2 * p] = w4(branch[0], 0.f);
+        r.dpairBranch[2 * p + 1] = w4(branch[1], 0.f);
+        uint32_t mask = 0;
+        if (meshClusterMayContact(r, ij.x, ij.y, r.meshClusterInfo[r.shapeId[ij.x]].x, branch[0])) mask |= 1;
+        if (meshClusterMayContact(r, ij.y, ij.x, r.meshClusterInfo[r.shapeId[ij.y]].x, branch[1])) mask |= 2;
+        for (uint32_t pass = 0; pass < 2; ++pass) {
+            if ((mask & (1u << pass)) == 0) continue;
+            uint32_t i = pass == 0 ? ij.x : ij.y, j = pass == 0 ? ij.y : ij.x;
+            float4 qi = r.rotation[i], qj = r.rotation[j];
+            float sj = r.body[j].x;
+            float ratio = __fdiv_rn(r.body[i].x, sj);
+            f3 a = qinv(qj, qrot(qi, mk(ratio, 0.f, 0.f)));
+            f3 b = qinv(qj, qrot(qi, mk(0.f, ratio, 0.f)));
+            f3 cz = qinv(qj, qrot(qi, mk(0.f, 0.f, ratio)));
+            f3 offset = qinv(qj, -branch[pass]) / sj;
+            uint32_t base = 4 * (2 * p + pass);
+            r.meshPairTransform[base] = make_float4(a.x, b.x, cz.x, offset.x);
+            r.meshPairTransform[base + 1] = make_float4(a.y, b.y, cz.y, offset.y);
+            r.meshPairTransform[base + 2] = make_float4(a.z, b.z, cz.z, offset.z);
+            r.meshPairTransform[base + 3] = make_float4(__fdiv_rn(length(branch[pass]), sj), 0.f, 0.f, 0.f);
+        }
+        r.meshPairMask[p] = mask;
+        r.sidePairB[p] = ij.y;
+    }
+    uint32_t grains = c.N;
+    for (uint32_t g = gtid(); g <= grains; g += gstride())
+        r.sidePairOffsets[g] = g < grains ? min(r.pairOffsets[g], n) : n;
+}
+// resetMeshContacts (solver.slang:396-403)
+__global__ void k_resetContacts(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    if (r.control[0] != 0) return;
+    r.control[2] = 0;
+    r.control[6] = 0;
+    r.work[W_CANDIDATES] = 0;
+}
+// Flat leaf cull: one warp per directed pair; meshPairBounds (solver.slang:
+// 404-417) + meshBoxMayContact (:274-288) on every leaf, gated by the root
+// mask.  Equivalent in contacts to the reference's hierarchical walks since
+// every test is conservative and each node's decision is exact.
+__global__ void k_leafCull(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t n = 2 * activePairs(r, c);
+    bool live = r.control[0] == 0;
+    for (uint32_t d = warpGlobal(); d < n; d += warpStride()) {
+        uint32_t p = d >> 1, pass = d & 1;
+        uint2 ij = r.pairs[p];
+        uint32_t i = pass ? ij.y : ij.x, j = pass ? ij.x : ij.y;
+        uint32_t count = 0;
+        if (live && ((r.meshPairMask[p] >> pass) & 1u)) {
+            uint4 li = __ldg(&r.meshLeafInfo[r.shapeId[i]]);
+            uint32_t targetShape = r.shapeId[j];
+            for (uint32_t k0 = 0; k0 < li.y; k0 += WARP) {
+                uint32_t k = k0 + laneId();
+                bool hit = false;
+                if (k < li.y) {
+                    f3 low, high;
+                    meshPairBounds(r, d, __ldg(&r.meshLeaves[li.x + k]), low, high);
+                    hit = meshBoxMayContact(r, targetShape, low, high);
+                }
+                uint32_t m = __ballot_sync(0xffffffffu, hit);
+                if (laneId() == 0) r.leafMask[size_t(d) * c.leafWords + k0 / WARP] = m;
+                count += __popc(m);
+            }
+        }
+        if (laneId() == 0) r.dpairLeafCount[d] = count;
+    }
+}
+__global__ void k_leafEmit(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = 2 * activePairs(r, c);
+    for (uint32_t d = warpGlobal(); d < n; d += warpStride()) {
+        if (r.dpairLeafCount[d] == 0) continue;
+        uint32_t p = d >> 1, pass = d & 1;
+        uint2 ij = r.pairs[p];
+        uint32_t i = pass ? ij.y : ij.x;
+        uint4 li = __ldg(&r.meshLeafInfo[r.shapeId[i]]);
+        uint32_t base = r.dpairCandOffset[d];
+        for (uint32_t k0 = 0; k0 < li.y; k0 += WARP) {
+            uint32_t m = r.leafMask[size_t(d) * c.leafWords + k0 / WARP];
+            uint32_t k = k0 + laneId();
+            if ((m >> laneId()) & 1u) {
+                uint32_t slot = base + __popc(m & lanesBelow());
+                if (slot < c.candidateCapacity) r.candidates[slot] = make_uint2(d, __ldg(&r.meshLeaves[li.x + k]));
+            }
+            base += __popc(m);
+        }
+    }
+}
+// Exact node queries, one warp per (directed pair, leaf) item.
+__global__ void __launch_bounds__(256) k_nodeQuery(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
+    for (uint32_t item = warpGlobal(); item < n; item += warpStride()) {
+        // Leaves hold at most 64 nodes (packing splits larger sets), two per lane.
+        bool hit0 = false, hit1 = false;
+        if (r.control[0] == 0) {
+            uint2 cd = r.candidates[item];
+            uint32_t d = cd.x, p = d >> 1, pass = d & 1;
+            uint2 ij = r.pairs[p];
+            uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
+            f3 branch = xyz(r.dpairBranch[d]);
+            uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
+            float4 pd, na;
+            uint32_t k = laneId();
+            if (k < range.y) hit0 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd, na);
+            k += WARP;
+            if (k < range.y) hit1 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd, na);
+        }
+        uint32_t m0 = __ballot_sync(0xffffffffu, hit0), m1 = __ballot_sync(0xffffffffu, hit1);
+        if (laneId() == 0) {
+            r.candHitMask[item] = make_uint2(m0, m1);
+            r.candHitCount[item] = __popc(m0) + __popc(m1);
+        }
+    }
+}
+// Writes the hits of each item at its canonical offset, recomputing them.
+__global__ void __launch_bounds__(256) k_nodeEmit(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
+    for (uint32_t item = warpGlobal(); item < n; item += warpStride()) {
+        uint2 m = r.candHitMask[item];
+        if ((m.x | m.y) == 0) continue;
+        uint2 cd = r.candidates[item];
+        uint32_t d = cd.x, p = d >> 1, pass = d & 1;
+        uint2 ij = r.pairs[p];
+        uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
+        f3 branch = xyz(r.dpairBranch[d]);
+        uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
+        uint32_t base = r.candHitOffset[item];
+#pragma unroll
+        for (uint32_t half = 0; half < 2; ++half) {
+            uint32_t word = half ? m.y : m.x;
+            if (!((word >> laneId()) & 1u)) continue;
+            uint32_t slot = base + (half ? __popc(m.x) : 0) + __popc(word & lanesBelow());
+            uint32_t node = __ldg(&r.meshSampleIndices[range.x + laneId() + half * WARP]);
+            float4 pd, na;
+            if (!nodeContact(r, c, src, dst, node, branch, pd, na)) continue;
+            if (slot >= c.contactCapacity) { fail(r, F_CONTACT); continue; }
+            r.meta[slot] = make_uint4(src, dst, node, 0);
+            r.pointDepth[slot] = pd;
+            r.normalArea[slot] = na;
+            r.contactPair[slot] = p;
+        }
+    }
+}
+// Per pair: first contact of the pair on the side being written, and counts.
+__global__ void k_contactStart(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t n = activePairs(r, c);
+    uint32_t total = r.control[2];
+    if (total > c.contactCapacity) fail(r, F_CONTACT);
+    if (r.control[0] != 0) return;
+    uint32_t items = min(r.work[W_CANDIDATES], c.candidateCapacity);
+    for (uint32_t p = gtid(); p <= n; p += gstride()) {
+        uint32_t first = r.dpairCandOffset[2 * p];
+        uint32_t start = first < items ? r.candHitOffset[first] : total;
+        r.sideContactStart[p] = start;
+        if (p < n) {
+            uint32_t next = r.dpairCandOffset[2 * p + 2];
+            uint32_t end = next < items ? r.candHitOffset[next] : total;
+            r.contactCounts[p] = end - start;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- friction
+// solver.slang:691-696
+__device__ __forceinline__ f3 transported(f3 x, f3 a, f3 b, float spin) {
+    float cc = mn(mx(dot(a, b), -1.0f), 1.0f);
+    if (cc < -0.999999f) return mk(0.f, 0.f, 0.f);
+    f3 v = cross(a, b);
+    f3 out = (x + cross(v, x)) + cross(v, cross(v, x)) / __fadd_rn(1.0f, cc);
+    float cs = cosf(spin), sn = sinf(spin);
+    out = (out * cs + cross(b, out) * sn) + (b * dot(b, out)) * __fsub_rn(1.0f, cs);
+    return out - b * dot(out, b);
+}
+// normal.slang:2-11
+__device__ __forceinline__ void normalResponse(float depth, float area, float vn, float stiffness, float viscosity,
+                                               float weight, float& force, float& lossPower) {
+    force = 0.f;
+    lossPower = 0.f;
+    if (depth <= 0) return;
+    float elastic = __fmul_rn(__fmul_rn(__fmul_rn(weight, stiffness), area), depth);
+    force = viscosity == 0 ? elastic
+                           : mx(0.0f, __fsub_rn(elastic, __fmul_rn(__fmul_rn(__fmul_rn(weight, viscosity), area), vn)));
+    lossPower = mx(0.0f, __fmul_rn(__fsub_rn(elastic, force), vn));
+}
+// History key within a pair: direction (source > target) then the node's
+// position in its shape's cluster order; runs of one pair are sorted by it.
+__device__ __forceinline__ uint32_t pairKey(const Res& r, uint32_t src, uint32_t dst, uint32_t node) {
+    return (src > dst ? 0x80000000u : 0u) | __ldg(&r.meshSampleRank[__ldg(&r.sampleInfo[r.shapeId[src]].x) + node]);
+}
+// Slot of key (src, dst, node) among the committed contacts, or EMPTY.
+// The committed side stores, per grain a, the run of its pairs (a, b) with
+// b > a and, per pair, its contacts sorted by pairKey: a sorted merge done as
+// a run lookup plus a binary search.
+__device__ __forceinline__ uint32_t historySlot(const Res& r, uint32_t src, uint32_t dst, uint32_t node) {
+    uint32_t a = min(src, dst), b = max(src, dst);
+    uint32_t begin = r.oldPairOffsets[a], end = r.oldPairOffsets[a + 1];
+    uint32_t q = EMPTY;
+    for (uint32_t k = begin; k < end; ++k)
+        if (r.oldPairB[k] == b) { q = k; break; }
+    if (q == EMPTY) return EMPTY;
+    uint32_t lo = r.oldContactStart[q], hi = r.oldContactStart[q + 1];
+    uint32_t key = pairKey(r, src, dst, node);
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        uint4 m = r.oldMeta[mid];
+        uint32_t mk2 = pairKey(r, m.x, m.y, m.z);
+        if (mk2 < key) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo < r.oldContactStart[q + 1]) {
+        uint4 m = r.oldMeta[lo];
+        if (m.x == src && m.y == dst && m.z == node) return lo;
+    }
+    return EMPTY;
+}
+// solver.slang:702-749 (particle-particle contacts)
+__global__ void k_resolve(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = activeContacts(r, c);
+    for (uint32_t id = gtid(); id < n; id += gstride()) {
+        uint4 key = r.meta[id];
+        uint32_t i = key.x, j = key.y;
+        f3 nrm = xyz(r.normalArea[id]);
+        float viscosity = c.normalViscosity;
+        f3 wi = viscosity > 0 ? xyz(r.forceOmega[i]) : omegaOf(r, i);
+        f3 wj = viscosity > 0 ? xyz(r.forceOmega[j]) : omegaOf(r, j);
+        f3 elastic = mk(0.f, 0.f, 0.f);
+        if (c.historyStep != 0) {
+            uint32_t old = historySlot(r, i, j, key.z);
+            if (old != EMPTY)
+                elastic = transported(xyz(r.oldSlip[old]), xyz(r.oldNormal[old]), nrm,
+                                      __fmul_rn(__fmul_rn(0.5f, dot(wi + wj, nrm)), c.dt));
+        }
+        f3 arm = xyz(r.pointDepth[id]);
+        uint32_t p = r.contactPair[id];
+        f3 branch = xyz(r.dpairBranch[2 * p + (i > j ? 1 : 0)]);
+        f3 translation = viscosity > 0 ? xyz(r.forceVelocity[i]) - xyz(r.forceVelocity[j])
+                                       : xyz(r.velocity[i]) - xyz(r.velocity[j]);
+        f3 rv = ((translation - xyz(r.cell[1]) * branch) + cross(wi, arm)) - cross(wj, arm - branch);
+        elastic = elastic + (rv - nrm * dot(rv, nrm)) * c.dt;
+        f3 trial = elastic;
+        float area = r.normalArea[id].w, depth = r.pointDepth[id].w;
+        float fn, lossPower;
+        normalResponse(depth, area, dot(rv, nrm), c.kn, viscosity, 0.5f, fn, lossPower);
+        r.normalLossPower[id] = lossPower;
+        float ktA = __fmul_rn(__fmul_rn(-0.5f, c.kt), area);
+        f3 ft = ktA * elastic;
+        float magnitude = length(ft);
+        if (magnitude > __fmul_rn(c.mu, fn) && magnitude > 0) {
+            ft = ft * __fdiv_rn(__fmul_rn(c.mu, fn), magnitude);
+            elastic = (-ft) / __fmul_rn(__fmul_rn(0.5f, c.kt), area);
+            atomicAdd(&r.control[6], 1u);
+        }
+        r.slip[id] = w4(elastic, mx(0.0f, -dot(ft, trial - elastic)));
+        float4 cf = w4(fn * nrm + ft,
+                       __fmul_rn(__fmul_rn(0.25f, area), __fadd_rn(__fmul_rn(__fmul_rn(c.kn, depth), depth),
+                                                                   __fmul_rn(c.kt, dot(elastic, elastic)))));
+        r.contactForce[id] = cf;
+        if (!isfinite(cf.x) || !isfinite(cf.y) || !isfinite(cf.z) || !isfinite(cf.w) || !isfinite(lossPower))
+            fail(r, F_NONFINITE);
+    }
+}
+
+// -------------------------------------------------------------------- gather
+// solver.slang:760-811.  Contacts of grain g are visited in the order the
+// reference's linked lists hold them (descending contact id): pairs where g is
+// first (a contiguous run) and second (the byJ run) merged from the highest
+// pair id down, each pair's contacts from the last.
+__global__ void k_gather(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t id = gtid();
+    if (id >= c.N || r.control[0] != 0) return;
+    f3 f = mk(0.f, 0.f, 0.f), t = f, fLow = f, tLow = f, stress0 = f, stress1 = f, stress2 = f;
+    float energy = 0, denom = 0, maxDepth = 0, dissipation = 0, normalPower = 0, stiffnessRate = 0, viscousRate = 0;
+    f3 one = mk(1.f, 1.f, 1.f);
+    float inverseInertia = mx(mx(dot(abs3(xyz(r.invI[3 * id])), one), dot(abs3(xyz(r.invI[3 * id + 1])), one)),
+                              dot(abs3(xyz(r.invI[3 * id + 2])), one));
+    float m = r.body[id].y, bw = r.body[id].w;
+    uint32_t pairs = activePairs(r, c);
+    uint32_t aBegin = min(r.pairOffsets[id], pairs), aEnd = min(aBegin + r.pairCounts[id], pairs);
+    uint32_t bBegin = r.byJOffsets[id], bEnd = r.byJOffsets[id + 1];
+    uint32_t ia = aEnd, ib = bEnd;
+    while (ia > aBegin || ib > bBegin) {
+        uint32_t p;
+        if (ib == bBegin || (ia > aBegin && ia - 1 > r.byJPairs[ib - 1])) p = --ia;
+        else p = r.byJPairs[--ib];
+        uint32_t begin = r.sideContactStart[p], end = r.sideContactStart[p + 1];
+        for (uint32_t contact = end; contact-- > begin;) {
+            uint4 key = r.meta[contact];
+            bool source = key.x == id;
+            float4 cf = r.contactForce[contact];
+            f3 force = xyz(cf);
+            float4 pdv = r.pointDepth[contact];
+            f3 arm = xyz(pdv);
+            f3 branch = xyz(r.dpairBranch[2 * p + (key.x > key.y ? 1 : 0)]);
+            float area = r.normalArea[contact].w;
+            if (c.activeTimestep != 0) {
+                f3 localArm = source ? arm : arm - branch;
+                float mobility = __fadd_rn(__fdiv_rn(1.0f, m), __fmul_rn(dot(localArm, localArm), inverseInertia));
+                float half = __fmul_rn(area, 0.5f);
+                stiffnessRate = __fadd_rn(stiffnessRate,
+                    __fmul_rn(__fmul_rn(__fmul_rn(2.0f, half), __fadd_rn(__fmul_rn(c.kn, __fadd_rn(1.0f, c.mu)), c.kt)), mobility));
+                viscousRate = __fadd_rn(viscousRate,
+                    __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(2.0f, half), c.normalViscosity), __fadd_rn(1.0f, c.mu)), mobility));
+            }
+            compensated3(f, fLow, source ? force : -force);
+            compensated3(t, tLow, source ? cross(arm, force) : cross(arm - branch, -force));
+            stress0 = stress0 - __fmul_rn(0.5f, force.x) * branch;
+            stress1 = stress1 - __fmul_rn(0.5f, force.y) * branch;
+            stress2 = stress2 - __fmul_rn(0.5f, force.z) * branch;
+            energy = __fadd_rn(energy, __fmul_rn(0.5f, cf.w));
+            denom = __fadd_rn(denom, length(force));
+            uint32_t other = source ? key.y : key.x;
+            float wmin = source ? mn(bw, r.body[other].w) : mn(r.body[other].w, bw);
+            maxDepth = mx(maxDepth, __fdiv_rn(pdv.w, wmin));
+            dissipation = __fadd_rn(dissipation, __fmul_rn(0.5f, r.slip[contact].w));
+            normalPower = __fadd_rn(normalPower, __fmul_rn(0.5f, r.normalLossPower[contact]));
+        }
+    }
+    f = f + fLow;
+    t = t + tLow;
+    r.timestepRows[id] = make_float4(stiffnessRate, viscousRate, 0.f, 0.f);
+    float4 ns = r.normalDamping[id];
+    ns.z = normalPower;
+    r.normalDamping[id] = ns;
+    r.force[id] = w4(f, maxDepth);
+    r.torque[id] = w4(t, dissipation);
+    r.particleStress[3 * id] = w4(stress0, 0.f);
+    r.particleStress[3 * id + 1] = w4(stress1, 0.f);
+    r.particleStress[3 * id + 2] = w4(stress2, 0.f);
+    f3 v = xyz(r.velocity[id]);
+    float kinetic = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(m, dot(v, v)), dot(xyz(r.momentum[id]), omegaOf(r, id))));
+    r.particleDiagnostic[id] = make_float4(kinetic, energy, length(f), denom);
+    float4 high = r.accumulated[id], low = r.accumulatedRemainder[id];
+    compensated4(high, low, make_float4(dissipation, 0.f, 0.f, 0.f));
+    r.accumulated[id] = high;
+    r.accumulatedRemainder[id] = low;
+}
+
+// ---------------------------------------------------------------- launchers
+static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
+constexpr uint32_t PERSISTENT = 152 * 8;  // warps-per-item kernels: 8 CTAs of 256 per SM
+
+static void neighbours(const Params& P, cudaStream_t s) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t T = 256;
+    k_binsClear<<<blocks(c.binCount, T), T, 0, s>>>(P);
+    k_binsFill<<<blocks(c.N, T), T, 0, s>>>(P);
+    k_binsSort<<<min(c.binCount, 152u * 16u), 128, 2 * c.binCapacity * sizeof(uint32_t), s>>>(P);
+    k_pairsCount<<<blocks(c.N, 128), 128, 0, s>>>(P);
+    launch_scan(r.pairCounts, r.pairOffsets, ScanCount{nullptr, 0, 0, c.N}, false, r.control + 1, r.control + 4,
+                r.scanPartials, s);
+    k_pairsEmit<<<blocks(c.N, 128), 128, 0, s>>>(P);
+    k_byJReset<<<blocks(c.N + 1, T), T, 0, s>>>(P);
+    k_byJCount<<<PERSISTENT, T, 0, s>>>(P);
+    launch_scan(r.byJCounts, r.byJOffsets, ScanCount{nullptr, 0, 0, c.N}, true, nullptr, r.control + 4,
+                r.scanPartials, s);
+    k_byJFill<<<PERSISTENT, T, 0, s>>>(P);
+    k_byJSort<<<blocks(c.N, T), T, 0, s>>>(P);
+}
+
+static void contacts(const Params& P, cudaStream_t s) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t T = 256;
+    k_resetContacts<<<1, 1, 0, s>>>(P);
+    k_pairSetup<<<PERSISTENT, T, 0, s>>>(P);
+    k_leafCull<<<PERSISTENT, T, 0, s>>>(P);
+    launch_scan(r.dpairLeafCount, r.dpairCandOffset, ScanCount{r.control + 1, c.pairCapacity, 2, 0}, true,
+                r.work + W_CANDIDATES, nullptr, r.scanPartials, s);
+    k_leafEmit<<<PERSISTENT, T, 0, s>>>(P);
+    k_nodeQuery<<<PERSISTENT, T, 0, s>>>(P);
+    launch_scan(r.candHitCount, r.candHitOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0}, true,
+                r.control + 2, nullptr, r.scanPartials, s);
+    k_nodeEmit<<<PERSISTENT, T, 0, s>>>(P);
+    k_contactStart<<<PERSISTENT, T, 0, s>>>(P);
+}
+
+int launch_contacts(const std::string_view& name, const Params& P, uint32_t count, cudaStream_t s) {
+    const Config& c = P.c;
+    uint32_t T = 256;
+    if (name == "neighbours") neighbours(P, s);
+    else if (name == "collect") contacts(P, s);
+    else if (name == "resolveContacts") k_resolve<<<PERSISTENT, T, 0, s>>>(P);
+    else if (name == "gather") k_gather<<<blocks(c.N, 128), 128, 0, s>>>(P);
+    else return 1;
+    (void)count;
+    return 0;
+}
+
+}  // namespace sdg

@@ -1,0 +1,570 @@
+"""GB300 timestep engine: the reference ``Engine`` surface over the CUDA step.
+
+Mirrors ``src/sand_atlas_dem/gpu.py:94-1092``: constructor arguments,
+``initialize``, ``advance`` (transactional chunks with rollback and capacity
+growth), ``diagnostics``, ``state``/``restore`` in the checkpoint array schema,
+``timestep_limits``, ``check_errors``, ``profile_step``, the unit attributes
+and ``buffers[name].copy_from_numpy``.  Device buffers are torch CUDA tensors
+(memory only); every kernel runs in the sm_103a library through its C ABI,
+one CUDA stream per engine, the step replayed as a captured CUDA graph.
+"""
+
+import ctypes as ct
+import math
+import time
+import weakref
+
+import numpy as np
+
+from . import native
+from .model import (
+    CAPACITY_FLAGS,
+    DAMPING_STATE,
+    RESIDUAL_STATE,
+    RESOURCE_ORDER,
+    STATE_NAMES,
+    HostLayout,
+    RejectedStep,
+    f4,
+)
+
+EXTENSION_ORDER = (
+    "meshLeafInfo", "meshLeaves", "meshSampleRank", "byJCounts", "byJOffsets", "byJCursor",
+    "byJPairs", "dpairBranch", "dpairLeafCount", "dpairCandOffset", "leafMask", "candidates",
+    "candHitCount", "candHitOffset", "candHitMask", "contactPair", "sidePairOffsets", "sidePairB",
+    "sideContactStart", "oldPairOffsets", "oldPairB", "oldContactStart", "work", "scanPartials",
+)
+BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
+# History side fields: (name bound as the side being written, name bound as committed).
+SIDE_FIELDS = (
+    ("meta", "oldMeta"), ("slip", "oldSlip"), ("normalArea", "oldNormal"), ("hash", "oldHash"),
+    ("sidePairOffsets", "oldPairOffsets"), ("sidePairB", "oldPairB"),
+    ("sideContactStart", "oldContactStart"),
+)
+SCAN_BLOCKS = 608
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+class DeviceBuffer:
+    """One device allocation; the reference Buffer surface (``cpu.py:431-447``)."""
+
+    def __init__(self, engine, nbytes):
+        torch = _torch()
+        self._engine = weakref.ref(engine)
+        self.size = int(max(16, nbytes))
+        self.tensor = torch.zeros(self.size, dtype=torch.uint8, device=engine.device)
+
+    def ptr(self):
+        return self.tensor.data_ptr()
+
+    def copy_from_numpy(self, array):
+        torch = _torch()
+        data = np.ascontiguousarray(array).view(np.uint8).reshape(-1)
+        if data.size != self.size:
+            raise ValueError("GB300 buffer upload size mismatch")
+        engine = self._engine()
+        with torch.cuda.stream(engine.stream):
+            self.tensor.copy_(torch.from_numpy(data.copy()), non_blocking=False)
+        engine.stream.synchronize()
+
+    def write_prefix(self, array):
+        torch = _torch()
+        data = np.ascontiguousarray(array).view(np.uint8).reshape(-1)
+        if data.size > self.size:
+            raise ValueError("GB300 buffer prefix out of bounds")
+        if data.size:
+            engine = self._engine()
+            with torch.cuda.stream(engine.stream):
+                self.tensor[: data.size].copy_(torch.from_numpy(data.copy()))
+            engine.stream.synchronize()
+
+    def to_numpy(self, dtype=np.uint8, count=None):
+        engine = self._engine()
+        engine.stream.synchronize()
+        nbytes = self.size if count is None else int(count) * np.dtype(dtype).itemsize
+        return self.tensor[:nbytes].cpu().numpy().view(dtype).copy()
+
+
+class GB300Device:
+    """The adapter surface callers read through ``engine.m`` (``cpu.py:540-689``)."""
+
+    name = "gb300"
+
+    def __init__(self, engine):
+        self._engine = weakref.ref(engine)
+
+    def read(self, buffer, dtype=np.float32, shape=None):
+        array = buffer.to_numpy(dtype)
+        return array if shape is None else array[: int(np.prod(shape))].reshape(shape)
+
+    def read_prefix(self, buffer, count, dtype=np.float32, shape=None):
+        if type(count) is not int or count < 0 or count * np.dtype(dtype).itemsize > buffer.size:
+            raise ValueError("GB300 buffer prefix out of bounds")
+        array = buffer.to_numpy(dtype, count)
+        return array if shape is None else array.reshape(shape)
+
+    def write_prefix(self, buffer, array):
+        buffer.write_prefix(array)
+
+    def doctor(self):
+        torch = _torch()
+        lib = native.load()
+        props = torch.cuda.get_device_properties(self._engine().device)
+        return dict(
+            format="sand-dem-doctor/1",
+            backend="gb300",
+            fallback=False,
+            adapter=props.name,
+            compute_capability=f"{props.major}.{props.minor}",
+            multiprocessors=props.multi_processor_count,
+            library=str(native.LIBRARY),
+            abi_version=lib.sdg_abi_version(),
+            numerics="sm_103a CUDA FP32 in the reference operation order (no FMA contraction), "
+            "FP64 minimum image, compensated state, canonical contact order, deterministic gather",
+            job_parallelism="one engine per CUDA stream",
+        )
+
+
+class Engine:
+    """GPU-resident mesh-surface DEM engine (periodic, plane-free, mesh geometry)."""
+
+    def __init__(self, library, spec, positions, cell, shape_ids, scales, *, metal=None, device=None,
+                 use_graph=True):
+        torch = _torch()
+        if metal is not None:
+            raise ValueError("The GB300 engine owns its device; no adapter may be passed")
+        if not torch.cuda.is_available():
+            raise RuntimeError("The GB300 backend requires a CUDA device; there is no CPU fallback")
+        self.lib = native.load()
+        if self.lib.sdg_buffer_count() != len(BUFFER_ORDER):
+            raise RuntimeError("GB300 library buffer ABI mismatch")
+        self.layout = h = HostLayout(library, spec, positions, cell, shape_ids, scales)
+        self.spec, self.library, self.n = spec, library, h.n
+        self.viscous = spec.viscous
+        self.wall_count = 0
+        self.step = 0
+        self.history = False
+        self.active = 0
+        self.capacity_retries = []
+        self.use_graph = use_graph
+        for name in ("length_unit", "time_unit", "mass_unit", "force_unit", "stress_unit", "energy_unit",
+                     "ids", "scales", "body", "skin", "cutoff", "bins", "bin_count", "pair_capacity",
+                     "contact_capacity", "hash_size", "bin_capacity", "initial_cell"):
+            setattr(self, name, getattr(h, name))
+        self.estimated_bytes = h.estimated_bytes()
+        self.leaf_words = (h.max_leaves + 31) // 32
+        self.candidate_capacity = max(1, 2 * h.pair_capacity * h.max_leaves)
+        self.device = torch.device(device or "cuda")
+        self.stream = torch.cuda.Stream(self.device)
+        self.m = GB300Device(self)
+        self.buffers = {}
+        n, pc, cc = h.n, h.pair_capacity, h.contact_capacity
+        for name, array in h.geometry.items():
+            self._add(name, array)
+        for name, array in h.initial_state().items():
+            self._add(name, array)
+        sizes = {
+            "meshPairMask": 4 * pc, "meshPairTransform": 16 * 8 * pc, "fabricRows": 16 * 2 * pc,
+            "binCounts": 4 * h.bin_count, "binParticles": 4 * h.bin_count * h.bin_capacity,
+            "pairCounts": 4 * n, "pairOffsets": 4 * n, "pairs": 8 * pc, "contactCounts": 4 * pc,
+            "contactOffsets": 4 * pc, "pointDepth": 16 * cc, "contactForce": 16 * cc,
+            "normalLossPower": 4 * cc, "heads": 4 * n, "next": 16,
+            "wallPlane": 16, "wallRemainder": 16, "wallVelocity": 16, "wallMaterial": 16,
+            "wallBoxIds": 24, "wallRows": 16, "wallAccumulated": 16,
+            "byJCounts": 4 * (n + 1), "byJOffsets": 4 * (n + 1), "byJCursor": 4 * n, "byJPairs": 4 * pc,
+            "dpairBranch": 16 * 2 * pc, "dpairLeafCount": 4 * (2 * pc + 1),
+            "dpairCandOffset": 4 * (2 * pc + 1), "leafMask": 4 * 2 * pc * self.leaf_words,
+            "candidates": 8 * self.candidate_capacity, "candHitCount": 4 * (self.candidate_capacity + 1),
+            "candHitOffset": 4 * (self.candidate_capacity + 1), "candHitMask": 8 * self.candidate_capacity,
+            "contactPair": 4 * cc, "work": 4 * 64, "scanPartials": 4 * 2 * SCAN_BLOCKS,
+        }
+        for name, nbytes in sizes.items():
+            self.buffers[name] = DeviceBuffer(self, nbytes)
+        side_sizes = {
+            "meta": 16 * cc, "slip": 16 * cc, "normalArea": 16 * cc, "hash": 16,
+            "sidePairOffsets": 4 * (n + 1), "sidePairB": 4 * pc, "sideContactStart": 4 * (pc + 1),
+        }
+        self.sides = [{k: DeviceBuffer(self, v) for k, v in side_sizes.items()} for _ in (0, 1)]
+        for name in BUFFER_ORDER:
+            if name not in self.buffers and name not in dict(SIDE_FIELDS) and name not in dict(
+                (o, k) for k, o in SIDE_FIELDS
+            ):
+                raise RuntimeError(f"unallocated buffer {name}")
+        backup_names = (
+            "position", "velocity", "rotation", "momentum", "cell", "force", "torque", "referencePosition",
+            "referenceCell", "control", "pairs", "pairCounts", "pairOffsets", "particleStress",
+            "particleDiagnostic", "timestepRows", "accumulated", "referencePositionRemainder",
+            *RESIDUAL_STATE, *DAMPING_STATE, "contactCounts", "byJOffsets", "byJPairs",
+        )
+        self.backups = {name: DeviceBuffer(self, self.buffers[name].size) for name in backup_names}
+        self.history_backup = {k: DeviceBuffer(self, self.sides[0][k].size) for k in side_sizes}
+        self._native = self.lib.sdg_engine_create()
+        if not self._native:
+            raise MemoryError("GB300 engine allocation failed")
+        self._finalizer = weakref.finalize(self, self.lib.sdg_engine_destroy, self._native)
+        self.stream.synchronize()
+
+    # ------------------------------------------------------------ plumbing
+    def _add(self, name, array):
+        data = np.ascontiguousarray(array)
+        self.buffers[name] = DeviceBuffer(self, data.nbytes)
+        if data.nbytes:
+            self.buffers[name].copy_from_numpy(
+                data if data.nbytes >= 16 else np.pad(data.view(np.uint8).reshape(-1), (0, 16 - data.nbytes))
+            )
+
+    def _bound(self, active):
+        new, old = self.sides[active], self.sides[1 - active]
+        view = dict(self.buffers)
+        for k, o in SIDE_FIELDS:
+            view[k], view[o] = new[k], old[k]
+        return view
+
+    def _arrays(self, active):
+        view = self._bound(active)
+        ptrs = (ct.c_void_p * len(BUFFER_ORDER))(*(view[k].ptr() for k in BUFFER_ORDER))
+        sizes = (ct.c_uint64 * len(BUFFER_ORDER))(*(view[k].size for k in BUFFER_ORDER))
+        return ptrs, sizes
+
+    def config(self, dt=None, drag=0.0, history=None):
+        return self.layout.config(
+            dt=self.spec.timestep if dt is None else dt, drag=drag,
+            history=self.history if history is None else history,
+        )
+
+    def _values(self, config):
+        values = list(self.layout.config_values(config)) + [
+            float(self.leaf_words), float(self.candidate_capacity), 0.0
+        ]
+        return (ct.c_double * len(values))(*values), len(values)
+
+    def dispatch(self, name, count, config, active=None):
+        """Launch one named kernel or phase on the engine stream (test and probe entry)."""
+        ptrs, sizes = self._arrays(self.active if active is None else active)
+        values, nv = self._values(config)
+        native.check(self.lib.sdg_dispatch(name.encode(), int(count), ptrs, sizes, values, nv,
+                                           ct.c_void_p(self.stream.cuda_stream)))
+
+    def synchronize(self):
+        self.stream.synchronize()
+
+    def read(self, name, dtype=np.float32, shape=None):
+        return self.m.read(self.buffers[name], dtype, shape)
+
+    def forces(self, config, *, capture_kinematics=True):
+        """``Engine.forces`` (``gpu.py:547-565``) as one launch sequence."""
+        self.dispatch("forces" if capture_kinematics else "forcesNoCapture", self.n, config)
+
+    # --------------------------------------------------------- public API
+    def check_errors(self):
+        ctrl = self.read("control", np.uint32, (16,))
+        if ctrl[15] != 0:
+            raise RuntimeError("Arithmetic materialization mask must remain zero")
+        if ctrl[0]:
+            raise RejectedStep(ctrl[0])
+        return ctrl
+
+    def initialize(self):
+        self.forces(self.config(dt=0))
+        self.synchronize()
+        self.check_errors()
+        self.history = True
+        self.active = 1 - self.active
+
+    def timestep_limits(self):
+        if self.spec.timestep_policy != "active-contact":
+            raise ValueError("Contact limits require active-contact policy")
+        rows = self.read("timestepRows", np.float32, (self.n, 4))
+        with np.errstate(divide="ignore"):
+            elastic = 0.1 / np.sqrt(rows[:, 0].astype(float)) * self.time_unit
+            viscous = 0.1 / rows[:, 1].astype(float) * self.time_unit
+        return {"elastic_seconds": elastic, "viscous_seconds": viscous}
+
+    def advance(self, steps, *, rate=(0, 0, 0), drag=0, wall_velocities=None):
+        """Transactional chunk with capacity growth (``gpu.py:597-647``)."""
+        from dataclasses import replace
+
+        from .spec import finite_array
+
+        if type(steps) is not int or steps < 0:
+            raise ValueError("Nonnegative integer step count required")
+        rate = finite_array(rate, (3,))
+        if not self.spec.periodic and np.any(rate != 0):
+            raise ValueError("Affine cell rates require a periodic domain")
+        if not np.isfinite(drag) or drag < 0:
+            raise ValueError("Finite nonnegative drag required")
+        if wall_velocities is not None:
+            raise ValueError("Wall velocities require planes")
+        for attempt in range(5):
+            try:
+                return self._advance_once(steps, rate=rate, drag=drag)
+            except RejectedStep as exc:
+                capacity = exc.flags & CAPACITY_FLAGS
+                if not capacity or exc.flags & ~CAPACITY_FLAGS or attempt == 4:
+                    raise
+                state = self.state()
+                old = self.spec
+                settings = {}
+                if capacity & 8:
+                    settings["bin_capacity"] = old.bin_capacity * 2
+                if capacity & 16:
+                    settings["pairs_per_particle"] = old.pairs_per_particle * 2
+                if capacity & (32 | 64):
+                    settings["contacts_per_particle"] = max(
+                        old.contacts_per_particle * 2, math.ceil(2 * self.contact_capacity / self.n)
+                    )
+                log = self.capacity_retries + [
+                    {"step": self.step, "flags": exc.flags, "new_capacities": settings}
+                ]
+                replacement = Engine(
+                    self.library, replace(old, **settings), state["position"][:, :3] * self.length_unit,
+                    state["cell"][0, :3] * self.length_unit, self.ids, self.scales,
+                    device=self.device, use_graph=self.use_graph,
+                )
+                replacement.initial_cell = self.initial_cell.copy()
+                replacement.restore(state, self.step)
+                self._adopt(replacement)
+                self.capacity_retries = log
+
+    def _adopt(self, replacement):
+        """Take over a grown replacement engine's buffers (capacity retry)."""
+        self._finalizer()
+        replacement._finalizer.detach()
+        self.__dict__.update(replacement.__dict__)
+        self._finalizer = weakref.finalize(self, self.lib.sdg_engine_destroy, self._native)
+        self.m = GB300Device(self)
+        me = weakref.ref(self)
+        for group in (self.buffers, self.backups, self.history_backup, *self.sides):
+            for buffer in group.values():
+                buffer._engine = me
+
+    def _copy(self, dst, src, nbytes=None):
+        torch = _torch()
+        n = min(dst.size, src.size) if nbytes is None else int(nbytes)
+        if n:
+            with torch.cuda.stream(self.stream):
+                dst.tensor[:n].copy_(src.tensor[:n], non_blocking=True)
+
+    def _backup(self, restore=False):
+        committed = self.sides[1 - self.active]
+        count = int(self.read("control", np.uint32, (16,))[2]) if not restore else self._backup_count
+        if count < 0 or count > self.contact_capacity:
+            raise ValueError("Committed contact count is outside capacity")
+        for name, backup in self.backups.items():
+            src, dst = (backup, self.buffers[name]) if restore else (self.buffers[name], backup)
+            self._copy(dst, src)
+        for name, backup in self.history_backup.items():
+            nbytes = 16 * count if name in ("meta", "slip", "normalArea") else None
+            src, dst = (backup, committed[name]) if restore else (committed[name], backup)
+            self._copy(dst, src, nbytes)
+        self._backup_count = count
+
+    def _advance_once(self, steps, *, rate=(0, 0, 0), drag=0):
+        if getattr(self, "invalid", False):
+            raise RuntimeError("Engine is invalid; restore a checkpoint")
+        if steps < 1:
+            return
+        cell = self.read("cell", np.float32, (3, 4))
+        original_cell = cell.copy()
+        cell[1, :3] = np.asarray(rate) * self.time_unit
+        self.buffers["cell"].copy_from_numpy(cell)
+        self._backup()
+        original_active, original_history = self.active, self.history
+        done = 0
+        if not self.history:
+            # The first step after construction has no committed history.
+            self._launch_steps(1, drag)
+            self.history = True
+            done = 1
+        self._launch_steps(steps - done, drag)
+        self.synchronize()
+        try:
+            self.check_errors()
+        except RuntimeError:
+            self.active, self.history = original_active, original_history
+            self._backup(restore=True)
+            self.synchronize()
+            self.buffers["cell"].copy_from_numpy(original_cell)
+            raise
+        self.step += steps
+
+    def _launch_steps(self, steps, drag):
+        if steps <= 0:
+            return
+        ptrs, sizes = self._arrays(self.active)
+        values, nv = self._values(self.config(drag=drag))
+        native.check(self.lib.sdg_engine_advance(
+            ct.c_void_p(self._native), ptrs, sizes, values, nv, steps, int(self.use_graph),
+            ct.c_void_p(self.stream.cuda_stream)))
+        self.active ^= steps & 1
+
+    def state(self):
+        """Checkpoint arrays (``gpu.py:893-936``)."""
+        out = {}
+        for name in STATE_NAMES:
+            rows = 3 if name == "cell" else 2 if name == "cellLog" else self.n
+            out[name] = self.read(name, np.float32, (rows, 4))
+        if self.viscous:
+            for name in DAMPING_STATE:
+                out[name] = self.read(name, np.float32, (self.n, 4))
+        ctrl = self.check_errors()
+        count = int(ctrl[2])
+        side = self.sides[1 - self.active]
+        out["contacts"] = count
+        for name in ("meta", "slip", "normalArea"):
+            out[name] = self.m.read_prefix(side[name], 4 * count, np.uint32 if name == "meta" else np.float32,
+                                           shape=(count, 4))
+        return out
+
+    def _history_tables(self, meta):
+        """Committed-side pair runs for a contact list in arbitrary order.
+
+        Sorts the contacts by (first grain, second grain, direction, node rank)
+        and returns the permutation with the per-grain pair runs and per-pair
+        contact starts the device merge reads.
+        """
+        g = self.layout.geometry
+        n = self.n
+        src, dst, node = (meta[:, k].astype(np.int64) for k in range(3))
+        if len(meta) and (src.max() >= n or dst.max() >= n):
+            raise ValueError("Checkpoint contact refers to a missing grain")
+        a, b = np.minimum(src, dst), np.maximum(src, dst)
+        base = g["sampleInfo"][self.ids[src], 0].astype(np.int64)
+        rank = g["meshSampleRank"][base + node].astype(np.int64)
+        key = ((src > dst).astype(np.int64) << 31) | rank
+        order = np.lexsort((key, b, a))
+        a, b = a[order], b[order]
+        pair_start = np.flatnonzero(np.r_[True, (a[1:] != a[:-1]) | (b[1:] != b[:-1])]) if len(a) else np.zeros(0, int)
+        pair_a = a[pair_start]
+        offsets = np.searchsorted(pair_a, np.arange(n + 1)).astype(np.uint32)
+        starts = np.r_[pair_start, len(a)].astype(np.uint32)
+        return order, offsets, b[pair_start].astype(np.uint32), starts
+
+    def restore(self, state, step):
+        """Restart from checkpoint arrays (``gpu.py:1016-1092``)."""
+        for name in DAMPING_STATE:
+            value = state[name] if self.viscous else np.zeros((self.n, 4), np.float32)
+            self.buffers[name].copy_from_numpy(np.asarray(value, np.float32))
+        for name in STATE_NAMES:
+            self.buffers[name].copy_from_numpy(np.asarray(state[name], np.float32))
+        count = int(state["contacts"])
+        if count < 0 or count > self.contact_capacity:
+            raise ValueError("Checkpoint contact count is outside capacity")
+        values = {}
+        for name in ("meta", "slip", "normalArea"):
+            v = np.asarray(state[name], np.uint32 if name == "meta" else np.float32)
+            if v.shape != (count, 4):
+                raise ValueError("Checkpoint contact history shape mismatch")
+            values[name] = v
+        order, offsets, pair_b, starts = self._history_tables(values["meta"])
+        committed = self.sides[1]
+        for name in ("meta", "slip", "normalArea"):
+            committed[name].write_prefix(values[name][order])
+        committed["sidePairOffsets"].write_prefix(offsets)
+        committed["sidePairB"].write_prefix(pair_b)
+        committed["sideContactStart"].write_prefix(starts)
+        ctrl = np.zeros(16, np.uint32)
+        ctrl[2], ctrl[4] = count, 1
+        self.buffers["control"].copy_from_numpy(ctrl)
+        self.active, self.history = 0, True
+        self.forces(self.config(dt=0), capture_kinematics=False)
+        self.synchronize()
+        self.check_errors()
+        self.active = 1
+        self.step = step
+
+    def _reduce(self, name, rows, max_row):
+        """Reference 256-wide tree reduction to one row set (``diagnostic.slang:3-28``)."""
+        src = self.buffers[name]
+        n = self.n if name == "diagnosticRows" else self.pair_capacity
+        scratch = []
+        while n > 1:
+            groups = (n + 255) // 256
+            out = DeviceBuffer(self, 16 * rows * groups)
+            native.check(self.lib.sdg_reduce_rows(ct.c_void_p(src.ptr()), ct.c_void_p(out.ptr()), n, rows,
+                                                  max_row, ct.c_void_p(self.stream.cuda_stream)))
+            scratch.append(out)
+            src, n = out, groups
+        return self.m.read(src, np.float32, (rows, 4))
+
+    def diagnostics(self):
+        """Stress, energies, contact counts and fabric (``gpu.py:746-891``)."""
+        c = self.config()
+        self.dispatch("diagnosticRows", self.n, c)
+        data = self._reduce("diagnosticRows", 8, 4)
+        self.dispatch("fabricRows", self.pair_capacity, c)
+        fabric_data = self._reduce("fabricRows", 2, -1)
+        active_pairs = round(float(fabric_data[1, 2]))
+        fabric = np.array(
+            [
+                [fabric_data[0, 0], fabric_data[0, 3], fabric_data[1, 0]],
+                [fabric_data[0, 3], fabric_data[0, 1], fabric_data[1, 1]],
+                [fabric_data[1, 0], fabric_data[1, 1], fabric_data[0, 2]],
+            ]
+        ) / max(active_pairs, 1)
+        cell = self.read("cell", np.float32, (3, 4))
+        ctrl = self.check_errors()
+        box = cell[0, :3].astype(float) * self.length_unit
+        volume = float(box.prod())
+        contact = data[:3, :3].astype(float) * self.energy_unit / volume
+        kinetic = data[3:6, :3].astype(float) * self.energy_unit / volume
+        total = contact + kinetic
+        symmetric = 0.5 * (total + total.T)
+        radial = 0.5 * (symmetric[0, 0] + symmetric[1, 1])
+        solid = sum(self.library.shapes[int(i)].volume * s**3 for i, s in zip(self.ids, self.scales))
+        return {
+            "step": self.step,
+            "elapsed_time": self.step * self.spec.timestep,
+            "cell": box.tolist(),
+            "domain_cell": box.tolist(),
+            "walls": [],
+            "stress": total.tolist(),
+            "contact_stress": contact.tolist(),
+            "kinetic_stress": kinetic.tolist(),
+            "stress_antisymmetry": float(np.linalg.norm(total - total.T) / max(np.linalg.norm(total), 1e-30)),
+            "p": float(np.trace(symmetric) / 3),
+            "q": float(symmetric[2, 2] - radial),
+            "axial_strain": float(1 - box[2] / self.initial_cell[2]),
+            "volumetric_strain": float(np.sum(1 - box / self.initial_cell)),
+            "volume_ratio": float(volume / np.prod(self.initial_cell)),
+            "log_strain": (-np.log(box / self.initial_cell)).tolist(),
+            "void_ratio": float(volume / solid - 1),
+            "kinetic_energy": float(data[0, 3] * self.energy_unit),
+            "elastic_energy_proxy": float(data[1, 3] * self.energy_unit),
+            "contact_normal": self.spec.contact_normal,
+            "elastic_energy_interpretation": "proxy; source-normal forces are not its gradient"
+            if self.spec.contact_normal == "source-surface-experimental"
+            else "existing nodal spring energy proxy",
+            "unbalanced_force": float(data[2, 3] / max(data[3, 3], 1e-30)),
+            "max_overlap_fraction": float(data[4, 3]),
+            "friction_dissipation_last_step": float(data[5, 3] * self.energy_unit),
+            "candidate_pairs": int(ctrl[1]),
+            "active_surface_contacts": int(ctrl[2]),
+            "active_grain_pairs": active_pairs,
+            "coordination": 2 * active_pairs / self.n,
+            "fabric": fabric.tolist(),
+            "sliding_fraction": float(ctrl[6] / max(ctrl[2], 1)),
+            "cell_log_rate": (cell[1, :3] / self.time_unit).tolist(),
+            "friction_dissipation": float(data[6, 0] * self.energy_unit),
+            "drag_dissipation": float(data[6, 1] * self.energy_unit),
+            "cell_work": float(data[6, 2] * self.energy_unit),
+            "wall_work": float(data[6, 3] * self.energy_unit),
+            "normal_contact_dissipation": float(data[7, 0] * self.energy_unit),
+            "normal_contact_power": float(data[7, 1] * self.energy_unit / self.time_unit),
+        }
+
+    def profile_step(self):
+        """One real step, wall-clocked on the host after a device synchronize."""
+        start = time.perf_counter()
+        self.advance(1)
+        self.synchronize()
+        return {
+            "available": True,
+            "timing_source": "host wall clock around one synchronized step",
+            "seconds": {"complete_step": time.perf_counter() - start},
+        }

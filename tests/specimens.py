@@ -1,0 +1,40 @@
+"""Shared small specimens for the parity tests (seeded, seconds on the oracle)."""
+
+import numpy as np
+
+from sand_atlas_dem_gb300.shapes import ShapeLibrary, perturbed_grain
+from sand_atlas_dem_gb300.spec import Experiment
+from sand_atlas_dem_gb300.workloads import contact_lattice
+
+
+def small_library(frequency=4, count=4, seed=1000):
+    return ShapeLibrary([perturbed_grain(frequency, seed=seed + k) for k in range(count)])
+
+
+def lattice_case(side=4, *, frequency=4, friction=0.5, viscosity=0.0, policy="conservative", speed=0.02,
+                 seed=3, dt=2e-9, spacing=0.985):
+    library = small_library(frequency)
+    case = contact_lattice(library, side, spacing=spacing, seed=seed, speed=speed)
+    spec = Experiment(
+        particles=side**3, contact_geometry="mesh", timestep=dt, friction=friction,
+        normal_viscosity=viscosity, timestep_policy=policy, max_overlap_fraction=0.5,
+        contacts_per_particle=256, pairs_per_particle=32,
+    )
+    return library, spec, case
+
+
+def upload(engine, name, array):
+    buffer = engine.buffers[name]
+    if isinstance(buffer, np.ndarray):
+        buffer[...] = np.asarray(array, buffer.dtype).reshape(buffer.shape)
+    else:
+        buffer.copy_from_numpy(np.ascontiguousarray(array))
+
+
+def build(engine_cls, library, spec, case, **kwargs):
+    e = engine_cls(library, spec, case["positions"], case["cell"], case["ids"], case["scales"], **kwargs)
+    upload(e, "rotation", case["rotations"])
+    v = np.zeros((spec.particles, 4), np.float32)
+    v[:, :3] = case["velocities"] * e.time_unit / e.length_unit
+    upload(e, "velocity", v)
+    return e

@@ -1,0 +1,111 @@
+"""CUDA step against the CPU oracle on identical seeded inputs.
+
+Bit-exact gates: pair lists, contact keys (and their canonical order), contact
+geometry, history slots and, at the zero-timestep initialization, forces.
+After timesteps the integrator's transcendental functions (CUDA vs libm
+sin/cos/exp) may differ in the last place, so state is compared at 1e-5
+relative (the per-step force/torque/pose tolerance of the contract).
+"""
+
+import numpy as np
+import pytest
+
+from oracle.engine import OracleEngine
+from sand_atlas_dem_gb300.engine import Engine
+from tests.specimens import build, lattice_case
+
+pytestmark = pytest.mark.gpu
+REL = 1e-5
+
+
+def committed(e, name, dtype=np.float32):
+    count = int(e.check_errors()[2])
+    side = e.sides[1 - e.active]
+    if isinstance(side[name], np.ndarray):
+        return side[name][:count]
+    return e.m.read_prefix(side[name], 4 * count, dtype, shape=(count, 4))
+
+
+def gpu_buffer(e, name, dtype, rows, width=4):
+    return e.read(name, dtype, (rows, width))
+
+
+def assert_close(a, b, rel=REL, what=""):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = max(np.abs(b).max(), 1e-30)
+    err = np.abs(a - b).max() if a.size else 0.0
+    assert err <= rel * scale, f"{what}: max error {err:.3e} vs scale {scale:.3e}"
+
+
+@pytest.mark.parametrize("viscosity", [0.0, 4e5])
+def test_initialize_bit_exact(gpu_library, viscosity):
+    library, spec, case = lattice_case(viscosity=viscosity)
+    o = build(OracleEngine, library, spec, case)
+    g = build(Engine, library, spec, case)
+    o.initialize()
+    g.initialize()
+    oc, gc = o.check_errors(), g.check_errors()
+    assert oc[1] == gc[1] and oc[2] == gc[2] and oc[1] > 0 and oc[2] > 0
+    pairs = int(oc[1])
+    np.testing.assert_array_equal(gpu_buffer(g, "pairs", np.uint32, pairs, 2), o.buffers["pairs"][:pairs])
+    count = int(oc[2])
+    for name in ("meta", "normalArea"):
+        dtype = np.uint32 if name == "meta" else np.float32
+        assert committed(g, name, dtype).tobytes() == committed(o, name, dtype).tobytes(), name
+    for name in ("pointDepth", "contactForce"):
+        assert gpu_buffer(g, name, np.float32, count).tobytes() == o.buffers[name][:count].tobytes(), name
+    n = spec.particles
+    for name in ("force", "torque", "particleStress", "particleDiagnostic", "accumulated"):
+        rows = 3 * n if name == "particleStress" else n
+        assert gpu_buffer(g, name, np.float32, rows).tobytes() == o.buffers[name][:rows].tobytes(), name
+
+
+@pytest.mark.parametrize("policy", ["conservative", "active-contact"])
+def test_steps_match_oracle(gpu_library, policy):
+    library, spec, case = lattice_case(policy=policy, viscosity=4e5)
+    o = build(OracleEngine, library, spec, case)
+    g = build(Engine, library, spec, case)
+    o.initialize()
+    g.initialize()
+    for chunk in (1, 2, 3):
+        o.advance(chunk, rate=(-0.5, -0.5, -0.5))
+        g.advance(chunk, rate=(-0.5, -0.5, -0.5))
+        so, sg = o.state(), g.state()
+        assert so["contacts"] == sg["contacts"]
+        np.testing.assert_array_equal(sg["meta"], so["meta"])
+        for name in ("position", "velocity", "rotation", "momentum", "force", "torque", "slip",
+                     "normalArea", "accumulated"):
+            assert_close(sg[name], so[name], what=name)
+
+
+def test_restore_collects_identically(gpu_library):
+    """Per-phase gate from identical state: restore the GPU's own state into
+    both engines; pair lists, contact keys and history slots must agree."""
+    library, spec, case = lattice_case()
+    g = build(Engine, library, spec, case)
+    g.initialize()
+    g.advance(4)
+    state = g.state()
+    o = build(OracleEngine, library, spec, case)
+    g2 = build(Engine, library, spec, case)
+    o.restore(state, 4)
+    g2.restore(state, 4)
+    so, sg = o.state(), g2.state()
+    np.testing.assert_array_equal(sg["meta"], so["meta"])
+    assert sg["slip"].tobytes() == so["slip"].tobytes()
+    assert sg["force"].tobytes() == so["force"].tobytes()
+
+
+def test_graph_replay_is_bitwise_reproducible(gpu_library):
+    library, spec, case = lattice_case()
+    states = []
+    for use_graph in (True, True, False):
+        g = build(Engine, library, spec, case, use_graph=use_graph)
+        g.initialize()
+        g.advance(5, rate=(-0.5, -0.5, -0.5))
+        states.append(g.state())
+    for s in states[1:]:
+        for k, v in states[0].items():
+            if isinstance(v, np.ndarray):
+                assert v.tobytes() == s[k].tobytes(), k
