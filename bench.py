@@ -1,0 +1,385 @@
+"""Benchmark: grain-steps/s of the mesh-surface DEM step on one GB300.
+
+Workload (the 10,000-grain plain-method configuration): 64 seeded perturbed
+geodesic icospheres (1,280 triangles, 642 Sobol nodes each), grain scales
+lognormal (median 1, sigma_ln 0.2) on a 0.5 mm nominal radius, a dense
+periodic packing at solid fraction 0.58 prepared by GPU compression, then
+isotropic compression at 0.5/s with rho 2650, kn 1e12, kt 5e11, mu 0.5,
+normal viscosity for damping ratio 0.3 and dt one ulp below the reference's
+conservative bound.  Data are synthetic (seeded); the reference's Hostun
+assets are not used.
+
+``value``  : device throughput, CUDA events on the engine stream around each
+             graph-replayed step, L2 flushed (256 MiB write) before each step.
+``e2e``    : the public API a caller uses (``Engine.advance`` chunks of 10
+             steps plus ``diagnostics()``), host wall clock, including the
+             host<->device traffic of those calls.
+``--impl reference`` times the CPU oracle port of the reference CPU backend
+on the host cores (``oracle/``), same workload and metric.
+"""
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "grain-steps/s"
+WORKLOAD = dict(
+    workload="dense-periodic-10k-icosphere-f8",
+    grains=10_000,
+    triangles_per_grain=1280,
+    nodes_per_grain=642,
+    shapes=64,
+    solid_fraction=0.58,
+    strain_rate_per_s=-0.5,
+    friction=0.5,
+    damping_ratio=0.3,
+    dtype_note="FP32 state with compensated residuals; FP64 minimum image",
+)
+
+
+def log(*args):
+    print(*args, file=sys.stderr, flush=True)
+
+
+def cache_dir():
+    path = Path(os.environ.get("SAND_DEM_GB300_CACHE", "/tmp/sand-dem-gb300-cache"))
+    path.mkdir(parents=True, exist_ok=True)
+    return path
+
+
+def library():
+    from sand_atlas_dem_gb300.shapes import synthetic_library
+
+    return synthetic_library("f8", WORKLOAD["shapes"])
+
+
+def lattice_packing(lib, grains):
+    """Quick contact-rich lattice start (diagnostic workload, not the headline)."""
+    from sand_atlas_dem_gb300.engine import Engine
+    from sand_atlas_dem_gb300.workloads import contact_lattice, material_spec
+
+    side = round(grains ** (1 / 3))
+    case = contact_lattice(lib, side, spacing=0.985, scale_sigma=0.05)
+    spec = material_spec(lib, case["ids"], case["scales"], max_overlap_fraction=0.5)
+    e = Engine(lib, spec, case["positions"], case["cell"], case["ids"], case["scales"])
+    e.buffers["rotation"].copy_from_numpy(case["rotations"])
+    e.initialize()
+    return dict(state=e.state(), ids=case["ids"], scales=case["scales"], cell=case["cell"], steps=0,
+                overrides=dict(max_overlap_fraction=0.5))
+
+
+def packing(lib, grains, phi, seed=42, kind="dense"):
+    """Prepared dense packing (cached per parameter set on this machine)."""
+    from sand_atlas_dem_gb300.workloads import dense_packing
+
+    if kind == "lattice":
+        return lattice_packing(lib, grains)
+
+    path = cache_dir() / f"packing-f8-{grains}-{phi}-{seed}.npz"
+    if path.exists():
+        with np.load(path, allow_pickle=False) as z:
+            state = {k[6:]: z[k] for k in z.files if k.startswith("state_")}
+            state["contacts"] = int(z["contacts"])
+            return dict(state=state, ids=z["ids"], scales=z["scales"], cell=z["cell"],
+                        steps=int(z["steps"]))
+    t = time.perf_counter()
+    out = dense_packing(lib, grains, phi, seed=seed, log=lambda d: log("prepare", d))
+    log(f"prepared packing in {time.perf_counter() - t:.1f} s, {out['steps']} steps")
+    arrays = {f"state_{k}": v for k, v in out["state"].items() if isinstance(v, np.ndarray)}
+    np.savez(path, contacts=out["state"]["contacts"], ids=out["ids"], scales=out["scales"],
+             cell=out["cell"], steps=out["steps"], **arrays)
+    return out
+
+
+def engine_for(lib, pack, cls, **kwargs):
+    from sand_atlas_dem_gb300.workloads import material_spec
+
+    state = pack["state"]
+    spec = material_spec(lib, pack["ids"], pack["scales"], **pack.get("overrides", {}))
+    length_unit = float(np.median([(6 * s.volume / np.pi) ** (1 / 3) for s in lib.shapes]))
+    positions = (state["position"][:, :3].astype(float) + state["positionRemainder"][:, :3]) * length_unit
+    cell = state["cell"][0, :3].astype(float) * length_unit
+    e = cls(lib, spec, positions, cell, pack["ids"], pack["scales"], **kwargs)
+    e.restore(state, 0)
+    return e
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                 f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[3:7]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        data = json.loads(path.read_text())
+        return float(data["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(n, pairs, contacts, items, nodes, rebuild, library_bytes):
+    """Per-step algorithmic HBM bytes of the whole step and of the node query.
+
+    Step: 516 B/grain + 264 B/pair + 272 B/contact + 88 B/grain on rebuild
+    steps + the packed library once.  Node query (per launch): each
+    (directed pair, leaf) item reads its record, pair, branch and leaf range
+    (48 B) and writes its hit mask and count (12 B); each node reads its
+    sample index and sample (20 B); the packed library is read once.
+    """
+    step = 516 * n + 264 * pairs + 272 * contacts + 88 * n * rebuild + library_bytes
+    query = 60 * items + 20 * nodes + library_bytes
+    return step, query
+
+
+def run_gb300(args):
+    import torch
+
+    from sand_atlas_dem_gb300.engine import DeviceBuffer, Engine
+
+    lib = library()
+    pack = packing(lib, args.grains, WORKLOAD["solid_fraction"], kind=args.packing)
+    e = engine_for(lib, pack, Engine)
+    rate = (WORKLOAD["strain_rate_per_s"],) * 3
+    # Warm-up (graph capture happens in the first call).
+    e.advance(max(3, args.warmup), rate=rate)
+    cell = e.read("cell", np.float32, (3, 4))
+    cell[1, :3] = np.asarray(rate) * e.time_unit
+    e.buffers["cell"].copy_from_numpy(cell)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=e.device)
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+    ctrl0 = e.check_errors()
+    with ClockSampler() as clocks:
+        e.synchronize()
+        for k in range(args.steps):
+            with torch.cuda.stream(e.stream):
+                flush.fill_(k & 0xFF)
+                events[k][0].record(e.stream)
+            e.run_steps(1)
+            with torch.cuda.stream(e.stream):
+                events[k][1].record(e.stream)
+        e.synchronize()
+    ctrl = e.check_errors()
+    step_ms = [a.elapsed_time(b) for a, b in events]
+    device_s = sum(step_ms) / 1e3
+    value = args.grains * args.steps / device_s
+    kernels = e.lib.sdg_engine_kernels_per_step(e._native)
+    # Phase profile (cold L2 each), for the roofline of the dominant kernel.
+    phases = []
+    for _ in range(3):
+        with torch.cuda.stream(e.stream):
+            flush.fill_(1)
+        phases.append(e.profile_phases())
+    e.check_errors()
+    phase_ms = {k: float(np.median([p[k] for p in phases])) for k in phases[0]}
+    items = int(e.read("work", np.uint32, (64,))[0])
+    pairs, contacts = int(ctrl[1]), int(ctrl[2])
+    leaf_nodes = e.layout.geometry["meshClusterRanges"][:, 1]
+    cand = e.read("candidates", np.uint32, (e.candidate_capacity, 2))[:items]
+    nodes = int(leaf_nodes[cand[:, 1]].sum()) if items else 0
+    lib_bytes = sum(a.nbytes for k, a in e.layout.geometry.items() if k.startswith("mesh") or k == "sample")
+    step_bytes, query_bytes = algorithmic_bytes(args.grains, pairs, contacts, items, nodes, 0, lib_bytes)
+    hbm, peak_kind = peaks()
+    top = max(phase_ms, key=phase_ms.get)
+    query_gbs = query_bytes / (phase_ms["node_query"] / 1e3) / 1e9
+    # End to end through the public API: advance() chunks plus diagnostics().
+    chunk = 10
+    chunks = max(1, args.steps // chunk)
+    e2e_s = 0.0
+    for _ in range(chunks):
+        with torch.cuda.stream(e.stream):
+            flush.fill_(2)
+        e.synchronize()
+        t = time.perf_counter()
+        e.advance(chunk, rate=rate)
+        e.diagnostics()
+        e2e_s += time.perf_counter() - t
+    e2e = args.grains * chunk * chunks / e2e_s
+    # Host<->device bytes per step of advance()+diagnostics(): cell read and
+    # upload, control reads, diagnostic reductions read back.
+    h2d = (48 + 48) / chunk
+    d2h = (48 + 3 * 64 + 8 * 16 + 2 * 16 + 64) / chunk
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "grain-steps/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * device_s / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": dict(WORKLOAD, grains=args.grains, packing=args.packing, l2="flushed before each timed step (256 MiB write)",
+                       pairs=pairs, contacts=contacts, node_query_items=items, node_queries=nodes,
+                       timestep_s=e.spec.timestep, phase_ms=phase_ms, dominant_phase=top),
+        "e2e": {"value": e2e, "unit": "grain-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "api": f"Engine.advance({chunk}) + Engine.diagnostics() per chunk"},
+        "gpu_launches": int(kernels) * args.steps,
+        "roofline": {
+            "bound": "hbm",
+            "kernel": "k_nodeQuery (exact node queries)",
+            "achieved": query_gbs,
+            "peak": hbm,
+            "peak_source": peak_kind,
+            "unit": "GB/s",
+            "frac": query_gbs / hbm,
+            "traffic": None,
+            "algorithmic_bytes": query_bytes,
+            "step_algorithmic_bytes": step_bytes,
+            "step_achieved_gbs": step_bytes / (device_s / args.steps) / 1e9,
+        },
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(lib, pack, args)
+    if ctrl0[0] or ctrl[0]:
+        line["solver_flags"] = int(ctrl[0])
+    return line
+
+
+def cpu_baseline(lib, pack, args, steps=1):
+    """Oracle port of the reference CPU backend on this host's cores, one step."""
+    from oracle.engine import OracleEngine
+
+    e = engine_for(lib, pack, OracleEngine, threads=args.cpu_threads)
+    rate = (WORKLOAD["strain_rate_per_s"],) * 3
+    t = time.perf_counter()
+    e.advance(steps, rate=rate)
+    seconds = time.perf_counter() - t
+    return {"value": args.grains * steps / seconds, "unit": "grain-steps/s", "cores": e.threads,
+            "kind": "port", "sample": f"{steps} full step(s) of the {args.grains}-grain workload, "
+            f"{seconds:.2f} s"}
+
+
+def run_reference(args):
+    lib = library()
+    pack = packing(lib, args.grains, WORKLOAD["solid_fraction"])
+    from oracle.engine import OracleEngine
+
+    e = engine_for(lib, pack, OracleEngine, threads=args.cpu_threads)
+    rate = (WORKLOAD["strain_rate_per_s"],) * 3
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        e.advance(1, rate=rate)
+    t = time.perf_counter()
+    e.advance(args.steps, rate=rate)
+    seconds = time.perf_counter() - t
+    value = args.grains * args.steps / seconds
+    return {
+        "metric": METRIC, "value": value, "unit": "grain-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * seconds / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(WORKLOAD, grains=args.grains), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "grain-steps/s", "cores": e.threads, "kind": "port",
+                         "sample": f"{args.steps} full steps after 1 warm-up step"},
+        "e2e": {"value": value, "unit": "grain-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
+    p.add_argument("--grains", type=int, default=WORKLOAD["grains"])
+    p.add_argument("--cpu-threads", type=int, default=os.cpu_count() or 1)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--prepare-only", action="store_true")
+    p.add_argument("--packing", default="dense", choices=("dense", "lattice"))
+    args = p.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+    if args.gpus > 1 or int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        # Independent replicas: each rank runs the same workload on its GPU.
+        import torch
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        line = run_gb300(args)
+        values = torch.tensor([line["value"], line["ms_per_step"]], device="cuda")
+        gathered = [torch.zeros_like(values) for _ in range(dist.get_world_size())]
+        dist.all_gather(gathered, values)
+        if rank == 0:
+            ms = max(float(g[1]) for g in gathered)
+            line["n_gpus"] = dist.get_world_size()
+            line["ms_per_step"] = ms
+            line["value"] = args.grains * dist.get_world_size() / (ms / 1e3)
+            print(json.dumps(line), flush=True)
+        dist.destroy_process_group()
+        return
+    if args.prepare_only:
+        lib = library()
+        pack = packing(lib, args.grains, WORKLOAD["solid_fraction"])
+        print(json.dumps({"prepared": True, "steps": pack["steps"], "contacts": pack["state"]["contacts"]}))
+        return
+    print(json.dumps(run_gb300(args)), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -27,7 +27,9 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <atomic>
 #include <string_view>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -655,6 +657,70 @@ void cpuCollectMesh(R& r, uint32_t pair) {
         }
     }
 }
+// Pair-parallel collector (the reference worker bridge, shaders/
+// cpu_parallel.hpp:31-116): every pair collects with private control words
+// into private storage, then contacts are concatenated in pair order, so the
+// result equals the serial collector's; flags of all pairs are ORed.
+void collectParallel(R& r, uint32_t pairs, uint32_t threads) {
+    if (threads <= 1 || pairs <= 1 || r.control[0] != 0) {
+        for (uint32_t p = 0; p < pairs; ++p) cpuCollectMesh(r, p);
+        return;
+    }
+    std::vector<std::vector<uint4>> meta(pairs);
+    std::vector<std::vector<float4>> point(pairs), normal(pairs);
+    std::vector<uint32_t> flags(pairs, 0), counts(pairs, 0);
+    std::atomic<uint32_t> next{0};
+    auto worker = [&]() {
+        R local = r;
+        uint32_t control[16];
+        std::vector<uint4> m;
+        std::vector<float4> pd, na;
+        for (;;) {
+            uint32_t pair = next.fetch_add(1, std::memory_order_relaxed);
+            if (pair >= pairs) return;
+            uint2 ij = r.pairs[pair];
+            uint32_t capacity = r.sampleInfo[r.shapeId[ij.x]].y + r.sampleInfo[r.shapeId[ij.y]].y;
+            m.resize(capacity);
+            pd.resize(capacity);
+            na.resize(capacity);
+            std::memcpy(control, r.control, sizeof(control));
+            control[0] = 0;
+            control[2] = 0;
+            local.control = control;
+            local.c.contactCapacity = capacity;
+            local.meta = m.data();
+            local.pointDepth = pd.data();
+            local.normalArea = na.data();
+            local.contactCounts = counts.data();  // one writer per pair
+            cpuCollectMesh(local, pair);
+            flags[pair] = control[0];
+            meta[pair].assign(m.begin(), m.begin() + control[2]);
+            point[pair].assign(pd.begin(), pd.begin() + control[2]);
+            normal[pair].assign(na.begin(), na.begin() + control[2]);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (uint32_t t = 0; t < threads && t < pairs; ++t) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    uint64_t total = 0;
+    uint32_t all = 0;
+    for (uint32_t p = 0; p < pairs; ++p) { total += meta[p].size(); all |= flags[p]; }
+    r.control[2] = uint32_t(total < 0xffffffffu ? total : 0xffffffffu);
+    if (total > r.c.contactCapacity) all |= 32;
+    r.control[0] |= all;
+    if (all) return;
+    size_t offset = 0;
+    for (uint32_t p = 0; p < pairs; ++p) {
+        size_t k = meta[p].size();
+        if (k) {
+            std::memcpy(r.meta + offset, meta[p].data(), k * sizeof(uint4));
+            std::memcpy(r.pointDepth + offset, point[p].data(), k * sizeof(float4));
+            std::memcpy(r.normalArea + offset, normal[p].data(), k * sizeof(float4));
+        }
+        r.contactCounts[p] = uint32_t(k);
+        offset += k;
+    }
+}
 // Exhaustive node set: cpu_scheduling.slang:104-131 + solver.slang:566-572
 // (count, scan, total, emit); every node of both grains, no cull.
 void exhaustiveContacts(R& r) {
@@ -897,7 +963,6 @@ void fabricRows(R& r, uint32_t id) {
 extern "C" int oracle_dispatch(const char* name, uint32_t count, void** buffers, const uint64_t* bytes,
                                const double* values, uint32_t nvalues) {
     (void)bytes;
-    (void)nvalues;
     R r;
     bind(r, buffers, values);
     std::string_view k(name);
@@ -914,7 +979,7 @@ extern "C" int oracle_dispatch(const char* name, uint32_t count, void** buffers,
     else if (k == "emitPairs") each(emitPairs);
     else if (k == "resetMeshContacts") each(resetMeshContacts);
     else if (k == "prepareMeshPairs") each(prepareMeshPairs);
-    else if (k == "collectMeshFrontiers") each(cpuCollectMesh);
+    else if (k == "collectMeshFrontiers") collectParallel(r, count, nvalues > 25 ? uint32_t(r.uni[0]) : 1u);
     else if (k == "exhaustiveContacts") exhaustiveContacts(r);
     else if (k == "clearContactStorage") each(clearContactStorage);
     else if (k == "resolveContacts") each(resolveContacts);

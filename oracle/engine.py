@@ -88,7 +88,7 @@ def _zeros4(rows):
 class OracleEngine:
     """Reference-order CPU engine over the restated kernels."""
 
-    def __init__(self, library_, spec, positions, cell, shape_ids, scales, *, collector=None):
+    def __init__(self, library_, spec, positions, cell, shape_ids, scales, *, collector=None, threads=1):
         self.layout = h = HostLayout(library_, spec, positions, cell, shape_ids, scales)
         self.spec, self.library, self.n = spec, library_, h.n
         self.viscous = spec.viscous
@@ -96,6 +96,7 @@ class OracleEngine:
         self.history = False
         self.active = 0
         self.collector = collector  # None: restated collector; else ReferenceCollector
+        self.threads = max(1, int(threads))
         for name in ("length_unit", "time_unit", "mass_unit", "force_unit", "stress_unit",
                      "energy_unit", "ids", "scales", "pair_capacity", "contact_capacity",
                      "hash_size", "bin_count", "bin_capacity", "initial_cell"):
@@ -151,9 +152,11 @@ class OracleEngine:
         pointers = (ct.c_void_p * len(arrays))(*(a.ctypes.data for a in arrays))
         sizes = (ct.c_uint64 * len(arrays))(*(a.nbytes for a in arrays))
         values = list(self.layout.config_values(config)) + [float(u) for u in uniforms]
-        if name == "collectMeshFrontiers" and self.collector is not None:
-            self.collector.dispatch(count, pointers, sizes, values)
-            return
+        if name == "collectMeshFrontiers":
+            if self.collector is not None:
+                self.collector.dispatch(count, pointers, sizes, values, self.threads)
+                return
+            values.append(float(self.threads))
         vals = (ct.c_double * len(values))(*values)
         if library().oracle_dispatch(name.encode(), int(count), pointers, sizes, vals, len(values)):
             raise ValueError(f"oracle has no kernel {name}")

@@ -100,11 +100,12 @@ static Params swapSides(const Params& P) {
     return Q;
 }
 
-// A captured two-step graph (one step per history side) per buffer/config set.
+// Captured one-step graphs for the two history-side orientations of a
+// buffer/config set, keyed on the orientation-independent parameter pair.
 struct Engine {
     std::vector<unsigned char> key;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
-    uint32_t launches = 0;
+    uint32_t kernels = 0;  // kernel nodes per captured step
     ~Engine() { reset(); }
     void reset() {
         for (auto& e : exec)
@@ -113,13 +114,24 @@ struct Engine {
     }
 };
 
-static int capture(const Params& P, cudaStream_t s, cudaGraphExec_t* out) {
+static int capture(const Params& P, cudaStream_t s, cudaGraphExec_t* out, uint32_t* kernels) {
     cudaGraph_t graph = nullptr;
     int rc = record(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
     if (rc) return rc;
     launch_step(P, s);
     rc = record(cudaStreamEndCapture(s, &graph), "end capture");
     if (rc) return rc;
+    size_t count = 0;
+    cudaGraphGetNodes(graph, nullptr, &count);
+    std::vector<cudaGraphNode_t> nodes(count);
+    cudaGraphGetNodes(graph, nodes.data(), &count);
+    uint32_t k = 0;
+    for (auto n : nodes) {
+        cudaGraphNodeType t;
+        cudaGraphNodeGetType(n, &t);
+        k += t == cudaGraphNodeTypeKernel;
+    }
+    *kernels = k;
     rc = record(cudaGraphInstantiate(out, graph, 0), "instantiate");
     cudaGraphDestroy(graph);
     return rc;
@@ -152,6 +164,51 @@ int sdg_dispatch(const char* kernel, uint32_t count, void* const* buffers, const
     return record(cudaGetLastError(), kernel);
 }
 
+// Phase timing of one step (events between the launch groups of
+// launch_step; not graph-captured).  phase_ms receives SDG_PHASES values:
+// drift (checkContactTimestep, beginStep, advanceCell, checkRebuild),
+// neighbours, pair setup + leaf cull + item emit, exact node queries,
+// contact emit, friction history + contact law, force gather, final kick.
+int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes, const double* values,
+                       uint32_t nvalues, float* phase_ms, void* stream) {
+    if (!engine || !phase_ms) { g_error = "null argument"; return 1; }
+    Params P;
+    if (int rc = unpack(buffers, bytes, values, nvalues, P)) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int phases = 8;
+    cudaEvent_t ev[phases + 1];
+    for (auto& e : ev)
+        if (int rc = record(cudaEventCreate(&e), "event")) return rc;
+    const Config& c = P.c;
+    cudaEventRecord(ev[0], s);
+    if (c.activeTimestep) launch_state("checkContactTimestep", P, c.N, s);
+    Params B = P;
+    B.c.viscousCapture = c.normalViscosity > 0 ? 1u : 0u;
+    launch_state("beginStep", B, c.N, s);
+    launch_state("advanceCell", P, 1, s);
+    launch_state("checkRebuild", P, c.N, s);
+    cudaEventRecord(ev[1], s);
+    launch_contacts("neighbours", P, c.N, s);
+    cudaEventRecord(ev[2], s);
+    launch_contacts("collectCull", P, 0, s);
+    cudaEventRecord(ev[3], s);
+    launch_contacts("collectQuery", P, 0, s);
+    cudaEventRecord(ev[4], s);
+    launch_contacts("collectEmit", P, 0, s);
+    cudaEventRecord(ev[5], s);
+    launch_contacts("resolveContacts", P, 0, s);
+    cudaEventRecord(ev[6], s);
+    launch_contacts("gather", P, c.N, s);
+    if (c.activeTimestep) launch_state("checkContactTimestep", P, c.N, s);
+    cudaEventRecord(ev[7], s);
+    launch_state("finishStep", P, c.N, s);
+    cudaEventRecord(ev[8], s);
+    int rc = record(cudaEventSynchronize(ev[phases]), "profile sync");
+    for (int k = 0; k < phases && !rc; ++k) rc = record(cudaEventElapsedTime(&phase_ms[k], ev[k], ev[k + 1]), "elapsed");
+    for (auto& e : ev) cudaEventDestroy(e);
+    return rc ? rc : record(cudaGetLastError(), "profile");
+}
+
 int sdg_reduce_rows(const void* input, void* output, uint32_t n, uint32_t rows, int32_t max_row, void* stream) {
     if (!input || !output || rows == 0) { g_error = "bad reduction arguments"; return 1; }
     launch_reduce_rows(static_cast<const float4*>(input), static_cast<float4*>(output), n, rows, max_row,
@@ -177,17 +234,31 @@ int sdg_engine_advance(void* engine, void* const* buffers, const uint64_t* bytes
         for (uint32_t k = 0; k < steps; ++k) launch_step(side[k & 1], s);
         return record(cudaGetLastError(), "advance");
     }
-    std::vector<unsigned char> key(sizeof(Params));
-    std::memcpy(key.data(), &P, sizeof(Params));
+    // Orientation-independent key: the side whose buffers sort first is 0.
+    bool flipped = std::memcmp(&side[0], &side[1], sizeof(Params)) > 0;
+    const Params& first = side[flipped ? 1 : 0];
+    const Params& second = side[flipped ? 0 : 1];
+    std::vector<unsigned char> key(2 * sizeof(Params));
+    std::memcpy(key.data(), &first, sizeof(Params));
+    std::memcpy(key.data() + sizeof(Params), &second, sizeof(Params));
     if (key != e->key) {
         e->reset();
-        for (int k = 0; k < 2; ++k)
-            if (int rc = capture(side[k], s, &e->exec[k])) { e->reset(); return rc; }
+        uint32_t kernels = 0;
+        if (int rc = capture(first, s, &e->exec[0], &kernels)) { e->reset(); return rc; }
+        if (int rc = capture(second, s, &e->exec[1], &kernels)) { e->reset(); return rc; }
+        e->kernels = kernels;
         e->key = key;
     }
+    uint32_t start = flipped ? 1u : 0u;
     for (uint32_t k = 0; k < steps; ++k)
-        if (int rc = record(cudaGraphLaunch(e->exec[k & 1], s), "graph launch")) return rc;
+        if (int rc = record(cudaGraphLaunch(e->exec[(start + k) & 1], s), "graph launch")) return rc;
     return 0;
+}
+
+// Kernel launches per captured step (0 before the first graph capture).
+int sdg_engine_kernels_per_step(void* engine) {
+    Engine* e = static_cast<Engine*>(engine);
+    return e ? int(e->kernels) : -1;
 }
 
 }  // extern "C"

@@ -676,7 +676,8 @@ static void neighbours(const Params& P, cudaStream_t s) {
     k_byJSort<<<blocks(c.N, T), T, 0, s>>>(P);
 }
 
-static void contacts(const Params& P, cudaStream_t s) {
+// Pair set-up, leaf cull and the (directed pair, leaf) item list.
+static void collectCull(const Params& P, cudaStream_t s) {
     const Res& r = P.r;
     const Config& c = P.c;
     uint32_t T = 256;
@@ -686,11 +687,23 @@ static void contacts(const Params& P, cudaStream_t s) {
     launch_scan(r.dpairLeafCount, r.dpairCandOffset, ScanCount{r.control + 1, c.pairCapacity, 2, 0}, true,
                 r.work + W_CANDIDATES, nullptr, r.scanPartials, s);
     k_leafEmit<<<PERSISTENT, T, 0, s>>>(P);
-    k_nodeQuery<<<PERSISTENT, T, 0, s>>>(P);
+}
+static void collectQuery(const Params& P, cudaStream_t s) {
+    k_nodeQuery<<<PERSISTENT, 256, 0, s>>>(P);
+}
+// Canonical offsets of the hits, the contact records and per-pair starts.
+static void collectEmit(const Params& P, cudaStream_t s) {
+    const Res& r = P.r;
+    const Config& c = P.c;
     launch_scan(r.candHitCount, r.candHitOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0}, true,
                 r.control + 2, nullptr, r.scanPartials, s);
-    k_nodeEmit<<<PERSISTENT, T, 0, s>>>(P);
-    k_contactStart<<<PERSISTENT, T, 0, s>>>(P);
+    k_nodeEmit<<<PERSISTENT, 256, 0, s>>>(P);
+    k_contactStart<<<PERSISTENT, 256, 0, s>>>(P);
+}
+static void contacts(const Params& P, cudaStream_t s) {
+    collectCull(P, s);
+    collectQuery(P, s);
+    collectEmit(P, s);
 }
 
 int launch_contacts(const std::string_view& name, const Params& P, uint32_t count, cudaStream_t s) {
@@ -698,6 +711,9 @@ int launch_contacts(const std::string_view& name, const Params& P, uint32_t coun
     uint32_t T = 256;
     if (name == "neighbours") neighbours(P, s);
     else if (name == "collect") contacts(P, s);
+    else if (name == "collectCull") collectCull(P, s);
+    else if (name == "collectQuery") collectQuery(P, s);
+    else if (name == "collectEmit") collectEmit(P, s);
     else if (name == "resolveContacts") k_resolve<<<PERSISTENT, T, 0, s>>>(P);
     else if (name == "gather") k_gather<<<blocks(c.N, 128), 128, 0, s>>>(P);
     else return 1;

@@ -558,13 +558,43 @@ class Engine:
             "normal_contact_power": float(data[7, 1] * self.energy_unit / self.time_unit),
         }
 
+    def run_steps(self, steps, *, drag=0.0):
+        """Launch ``steps`` timesteps with no host synchronization, backup or
+        error check (the device-resident inner loop of :meth:`advance`)."""
+        self._launch_steps(int(steps), drag)
+        self.history = True
+        self.step += int(steps)
+
+    def profile_phases(self, *, drag=0.0):
+        """Device milliseconds per phase of one committed step (CUDA events)."""
+        ptrs, sizes = self._arrays(self.active)
+        values, nv = self._values(self.config(drag=drag))
+        out = (ct.c_float * len(native.PHASES))()
+        native.check(self.lib.sdg_engine_profile(ct.c_void_p(self._native), ptrs, sizes, values, nv, out,
+                                                 ct.c_void_p(self.stream.cuda_stream)))
+        self.active ^= 1
+        self.history = True
+        self.step += 1
+        return dict(zip(native.PHASES, map(float, out)))
+
     def profile_step(self):
-        """One real step, wall-clocked on the host after a device synchronize."""
-        start = time.perf_counter()
-        self.advance(1)
-        self.synchronize()
+        """One real step timed by subsystem (``gpu.py:938-1014``), CUDA events."""
+        if self.spec.timestep_policy == "active-contact":
+            raise ValueError("Use advance for active-contact policy: profiling has no rollback")
+        ms = self.profile_phases()
+        self.check_errors()
+        seconds = {
+            "drift": ms["drift"] / 1e3,
+            "neighbours": ms["neighbours"] / 1e3,
+            "contact_geometry": (ms["pair_cull"] + ms["node_query"] + ms["contact_emit"]) / 1e3,
+            "friction_and_history": ms["friction_and_history"] / 1e3,
+            "force_reduction": ms["force_reduction"] / 1e3,
+            "final_kick": ms["final_kick"] / 1e3,
+        }
         return {
-            "available": True,
-            "timing_source": "host wall clock around one synchronized step",
-            "seconds": {"complete_step": time.perf_counter() - start},
+            "timestamp_frequency_hz": 1e3,
+            "timing_source": "CUDA events between launch groups on the engine stream",
+            "seconds": seconds,
+            "phases_ms": ms,
+            "total_gpu_seconds": sum(seconds.values()),
         }

@@ -88,6 +88,23 @@ class RejectedStep(RuntimeError):
         )
 
 
+def conservative_timestep(library, spec, ids, scales):
+    """Smallest per-grain conservative bound 0.1 min(elastic, viscous) (``gpu.py:370-413``)."""
+    limits = []
+    for i, s in zip(np.asarray(ids), np.asarray(scales, float)):
+        sh = library.shapes[int(i)]
+        mass = spec.density * sh.volume * s**3
+        stiffness = (spec.normal_stiffness + spec.tangential_stiffness) * sh.areas.sum() * s * s
+        smallest = np.linalg.eigvalsh(sh.inertia * spec.density * s**5).min()
+        elastic = math.sqrt(min(mass / stiffness, smallest / (stiffness * (sh.radius * s) ** 2)))
+        viscous = math.inf
+        viscosity = spec.normal_viscosity * sh.areas.sum() * s**2
+        if viscosity > 0:
+            viscous = min(mass / viscosity, smallest / (viscosity * (sh.radius * s) ** 2))
+        limits.append(0.1 * min(elastic, viscous))
+    return min(limits)
+
+
 class HostLayout:
     """Units, per-grain rows, capacities and static geometry of one specimen."""
 
@@ -170,20 +187,7 @@ class HostLayout:
             raise ValueError(f"Timestep exceeds conservative estimate {limit:.6g} s")
 
     def timestep_limit(self):
-        spec = self.spec
-        limits = []
-        for i, s in zip(self.ids, self.scales):
-            sh = self.library.shapes[int(i)]
-            mass = spec.density * sh.volume * s**3
-            stiffness = (spec.normal_stiffness + spec.tangential_stiffness) * sh.areas.sum() * s * s
-            smallest = np.linalg.eigvalsh(sh.inertia * spec.density * s**5).min()
-            elastic = math.sqrt(min(mass / stiffness, smallest / (stiffness * (sh.radius * s) ** 2)))
-            viscous = math.inf
-            viscosity = spec.normal_viscosity * sh.areas.sum() * s**2
-            if viscosity > 0:
-                viscous = min(mass / viscosity, smallest / (viscosity * (sh.radius * s) ** 2))
-            limits.append(0.1 * min(elastic, viscous))
-        return min(limits)
+        return conservative_timestep(self.library, self.spec, self.ids, self.scales)
 
     def static_geometry(self):
         """Packed mesh arrays plus the per-shape node table (``gpu.py:421-488``)."""

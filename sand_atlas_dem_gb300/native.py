@@ -84,6 +84,11 @@ def load():
     lib.sdg_engine_advance.argtypes = [ct.c_void_p, P(ct.c_void_p), P(ct.c_uint64), P(ct.c_double), ct.c_uint32,
                                        ct.c_uint32, ct.c_uint32, ct.c_void_p]
     lib.sdg_engine_advance.restype = ct.c_int
+    lib.sdg_engine_profile.argtypes = [ct.c_void_p, P(ct.c_void_p), P(ct.c_uint64), P(ct.c_double), ct.c_uint32,
+                                       P(ct.c_float), ct.c_void_p]
+    lib.sdg_engine_profile.restype = ct.c_int
+    lib.sdg_engine_kernels_per_step.argtypes = [ct.c_void_p]
+    lib.sdg_engine_kernels_per_step.restype = ct.c_int
     _LIB = lib
     return lib
 
@@ -103,4 +108,8 @@ EXPORTS = (
     "sdg_engine_create",
     "sdg_engine_destroy",
     "sdg_engine_advance",
+    "sdg_engine_profile",
+    "sdg_engine_kernels_per_step",
 )
+PHASES = ("drift", "neighbours", "pair_cull", "node_query", "contact_emit", "friction_and_history",
+          "force_reduction", "final_kick")

@@ -109,3 +109,22 @@ def test_graph_replay_is_bitwise_reproducible(gpu_library):
         for k, v in states[0].items():
             if isinstance(v, np.ndarray):
                 assert v.tobytes() == s[k].tobytes(), k
+
+
+@pytest.mark.parametrize("side,spacing", [(8, 0.985), (10, 1.05)])
+def test_multibin_specimen_matches_oracle(gpu_library, side, spacing):
+    """Several bins per axis, periodic wrap across bin boundaries."""
+    library, spec, case = lattice_case(side=side, spacing=spacing, viscosity=4e5, speed=0.05)
+    o = build(OracleEngine, library, spec, case, threads=8)
+    g = build(Engine, library, spec, case)
+    assert g.bins.min() >= 3
+    o.initialize()
+    g.initialize()
+    for _ in range(3):
+        o.advance(2, rate=(-0.5, -0.5, -0.5))
+        g.advance(2, rate=(-0.5, -0.5, -0.5))
+        so, sg = o.state(), g.state()
+        assert so["contacts"] == sg["contacts"]
+        np.testing.assert_array_equal(sg["meta"], so["meta"])
+        for name in ("position", "velocity", "force", "torque", "slip"):
+            assert_close(sg[name], so[name], what=name)
