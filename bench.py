@@ -190,7 +190,7 @@ def algorithmic_bytes(n, pairs, contacts, items, nodes, rebuild, library_bytes):
     return step, query
 
 
-def run_gb300(args):
+def run_gb300(args, cpu=True):
     import torch
 
     from sand_atlas_dem_gb300.engine import DeviceBuffer, Engine
@@ -292,7 +292,7 @@ def run_gb300(args):
         },
         "clocks": clocks.summary(),
     }
-    if not args.no_cpu_baseline:
+    if cpu and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(lib, pack, args)
     if ctrl0[0] or ctrl[0]:
         line["solver_flags"] = int(ctrl[0])
@@ -355,21 +355,24 @@ def main():
             print(json.dumps(run_reference(args)), flush=True)
         return
     if args.gpus > 1 or int(os.environ.get("WORLD_SIZE", "1")) > 1:
-        # Independent replicas: each rank runs the same workload on its GPU.
+        # Independent replicas: every rank runs the same workload on its own
+        # GPU; only the timings are exchanged, after the timed region.
         import torch
         import torch.distributed as dist
 
-        dist.init_process_group("nccl")
+        from sand_atlas_dem_gb300.replicas import aggregate
+
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        line = run_gb300(args)
-        values = torch.tensor([line["value"], line["ms_per_step"]], device="cuda")
-        gathered = [torch.zeros_like(values) for _ in range(dist.get_world_size())]
-        dist.all_gather(gathered, values)
+        dist.init_process_group("nccl")
+        dist.barrier()
+        line = run_gb300(args, cpu=rank == 0)
+        job = aggregate(args.grains * args.steps, line["ms_per_step"] * args.steps / 1e3, device="cuda")
         if rank == 0:
-            ms = max(float(g[1]) for g in gathered)
-            line["n_gpus"] = dist.get_world_size()
-            line["ms_per_step"] = ms
-            line["value"] = args.grains * dist.get_world_size() / (ms / 1e3)
+            line["n_gpus"] = job["ranks"]
+            line["ms_per_step"] = 1e3 * job["seconds"] / args.steps
+            line["value"] = job["value"]
+            line["scaling"] = "weak"
+            line["config"]["parallelism"] = f"{job['ranks']} independent specimen replicas"
             print(json.dumps(line), flush=True)
         dist.destroy_process_group()
         return

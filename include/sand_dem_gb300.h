@@ -1,0 +1,115 @@
+/*
+ * C ABI of the GB300 (sm_103a) mesh-surface DEM timestep engine.
+ *
+ * Library: sand_atlas_dem_gb300/_lib/libsanddem_gb300.so (built by
+ * sand_atlas_dem_gb300.native.build()).  Plain pointers and sizes only; all
+ * buffer pointers are CUDA device pointers, `stream` is a cudaStream_t (or
+ * NULL for the legacy default stream, which graph capture does not accept).
+ *
+ * Buffer block (SDG_BUFFER_COUNT pointers, `bytes` their sizes):
+ *   [0, 77)   the reference Resources fields in declaration order
+ *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
+ *             order the reference CPU backend binds in its generated
+ *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
+ *   [77, 101) this backend's extension buffers, in the order of
+ *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
+ *             node ranks, pair-by-second-grain runs, directed-pair branches,
+ *             leaf masks, (directed pair, leaf) items and hit masks, contact
+ *             pair ids, the written and committed history pair tables, work
+ *             counters, scan partials).
+ * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
+ * declaration order (solver.slang:12-19, normalized units as
+ * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
+ * directed pair, (directed pair, leaf) item capacity, and a flag that fuses
+ * captureContactKinematics into beginStep.
+ *
+ * Return codes: 0 success; 1 argument error; 2 CUDA error.  The message of
+ * the last error on the calling thread is sdg_last_error().  Solver failures
+ * (capacity, penetration, nonfinite state, ...) are not return codes: they
+ * are the bit flags of control[0] with the reference meanings
+ * (src/sand_atlas_dem/gpu.py:11-26), read back by the host after a chunk.
+ */
+#ifndef SAND_DEM_GB300_H
+#define SAND_DEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDG_BUFFER_COUNT 101
+#define SDG_VALUE_COUNT 28
+#define SDG_PHASES 8
+
+/* ABI revision of this header. */
+int sdg_abi_version(void);
+/* SDG_BUFFER_COUNT and SDG_VALUE_COUNT as compiled into the library. */
+int sdg_buffer_count(void);
+int sdg_value_count(void);
+/* Text of the last nonzero return on this thread. */
+const char* sdg_last_error(void);
+
+/*
+ * Launches one reference-named kernel or step phase on `stream`.
+ * Replaces the reference's per-kernel `cpu_dispatch(count, buffers, bytes,
+ * values)` of src/sand_atlas_dem/cpu.py:303-428 (NativeKernel.dispatch) and
+ * the Metal adapter's `dispatch(name, n, encoder, r=bindings)` of
+ * src/sand_atlas_dem/backend.py:9-121.  Names: beginStep, advanceCell,
+ * checkRebuild, finishStep, captureContactKinematics, checkContactTimestep,
+ * diagnosticRows, fabricRows, neighbours (clearBins..emitPairs + Scan),
+ * collect (resetMeshContacts, prepareMeshPairs, collectMeshFrontiers),
+ * collectCull / collectQuery / collectEmit (its three parts),
+ * resolveContacts (friction history + contact law), gather, and the
+ * sequences forces / forcesNoCapture (Engine.forces, gpu.py:547-565) and
+ * step (Engine._advance_once body, gpu.py:714-724).  `count` is the thread
+ * count of per-element kernels (N grains, pairCapacity, ...).
+ */
+int sdg_dispatch(const char* kernel, uint32_t count, void* const* buffers, const uint64_t* bytes,
+                 const double* values, uint32_t nvalues, void* stream);
+
+/*
+ * 256-wide binary tree reduction of `rows` float4 rows per element, summing
+ * (row `max_row`, component w: maximum), one output row set per 256 inputs.
+ * Replaces the reference's reduceRows / reduceFabric
+ * (src/sand_atlas_dem/shaders/diagnostic.slang:3-28) used by
+ * Engine.diagnostics (gpu.py:746-891); `max_row` = -1 for none.
+ */
+int sdg_reduce_rows(const void* input, void* output, uint32_t n, uint32_t rows, int32_t max_row,
+                    void* stream);
+
+/*
+ * Engine handle holding the captured CUDA graphs of one step for each
+ * history-side orientation.  Replaces the per-chunk command encoder of
+ * Engine._advance_once (gpu.py:672-744): one graph launch per step.
+ */
+void* sdg_engine_create(void);
+void sdg_engine_destroy(void* engine);
+
+/*
+ * Advances `steps` timesteps starting from the history side the buffers
+ * describe (meta/slip/normalArea/... = side written first), alternating
+ * sides every step as gpu.py:725 does.  use_graph != 0 replays captured
+ * graphs (recaptured when buffers or values change).  No host
+ * synchronization; solver flags accumulate in control[0].
+ */
+int sdg_engine_advance(void* engine, void* const* buffers, const uint64_t* bytes, const double* values,
+                       uint32_t nvalues, uint32_t steps, uint32_t use_graph, void* stream);
+
+/*
+ * One committed step with CUDA events between phases; writes SDG_PHASES
+ * device milliseconds: drift, neighbours, pair cull, node queries, contact
+ * emit, friction history + contact law, force gather, final kick.
+ * Replaces Engine.profile_step's timestamp queries (gpu.py:938-1014).
+ */
+int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes, const double* values,
+                       uint32_t nvalues, float* phase_ms, void* stream);
+
+/* Kernel launches per captured step (0 before the first capture). */
+int sdg_engine_kernels_per_step(void* engine);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SAND_DEM_GB300_H */

@@ -38,3 +38,36 @@ def build(engine_cls, library, spec, case, **kwargs):
     v[:, :3] = case["velocities"] * e.time_unit / e.length_unit
     upload(e, "velocity", v)
     return e
+
+
+def engine_classes():
+    """(id, class) pairs: the CPU oracle always, the GPU engine under the gpu mark."""
+    import pytest
+
+    from oracle.engine import OracleEngine
+
+    def gpu_engine(*args, **kwargs):
+        from sand_atlas_dem_gb300.engine import Engine
+
+        return Engine(*args, **kwargs)
+
+    return [pytest.param(OracleEngine, id="oracle"), pytest.param(gpu_engine, id="gpu", marks=pytest.mark.gpu)]
+
+
+def read(e, name, rows, dtype=np.float32, width=4):
+    buffer = e.buffers[name]
+    if isinstance(buffer, np.ndarray):
+        return buffer.reshape(-1, width)[:rows].copy() if buffer.ndim > 1 else buffer[:rows].copy()
+    return e.read(name, dtype, (rows, width))
+
+
+def cube_pair(engine_cls, *, separation=9.99e-5, friction=0.5, dt=1e-9, viscosity=0.0,
+              policy="active-contact"):
+    """Two exact six-node cubes, h = 0.1 mm (``tests/test_cpu_solver.py:121-173``)."""
+    from sand_atlas_dem_gb300.shapes import ShapeLibrary, exact_cube
+
+    spec = Experiment(particles=2, periodic=True, contact_geometry="mesh", timestep=dt, timestep_policy=policy,
+                      normal_viscosity=viscosity, friction=friction, max_overlap_fraction=0.1,
+                      contacts_per_particle=128)
+    positions = [[0.005] * 3, [0.005 + separation, 0.005, 0.005]]
+    return engine_cls(ShapeLibrary([exact_cube()]), spec, positions, [0.01] * 3, [0, 0], [1, 1])
