@@ -11,12 +11,13 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 101) this backend's extension buffers, in the order of
+ *   [77, 103) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
  *             pair ids, the written and committed history pair tables, work
- *             counters, scan partials).
+ *             counters, scan partials, the per-hit scratch and the first
+ *             scratch slot of each item).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
@@ -38,7 +39,7 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 101
+#define SDG_BUFFER_COUNT 103
 #define SDG_VALUE_COUNT 28
 #define SDG_PHASES 8
 
@@ -77,6 +78,17 @@ int sdg_dispatch(const char* kernel, uint32_t count, void* const* buffers, const
  */
 int sdg_reduce_rows(const void* input, void* output, uint32_t n, uint32_t rows, int32_t max_row,
                     void* stream);
+
+/*
+ * Device-wide exclusive scan of n uint32 values: out[i] = in[0] + ... +
+ * in[i-1]; *total (device pointer, may be NULL) receives the sum.  Replaces
+ * the reference's hierarchical Scan (src/sand_atlas_dem/gpu.py:65-91,
+ * shaders/scan.slang:1-28: blockScan + addBlocks).  `partials` is caller-
+ * owned device scratch of sdg_scan_partials() uint32 words.
+ */
+int sdg_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total, uint32_t* partials,
+                       void* stream);
+int sdg_scan_partials(void);
 
 /*
  * Engine handle holding the captured CUDA graphs of one step for each

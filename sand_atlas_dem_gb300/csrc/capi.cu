@@ -216,6 +216,21 @@ int sdg_reduce_rows(const void* input, void* output, uint32_t n, uint32_t rows, 
     return record(cudaGetLastError(), "reduce rows");
 }
 
+// Exclusive scan of n uint32 values (the reference's hierarchical Scan,
+// gpu.py:65-91 / scan.slang): out[i] = sum of in[0..i); *total (device
+// pointer, optional) receives the sum.  `partials` is caller-owned device
+// scratch of SDG_SCAN_PARTIALS uint32 words.
+int sdg_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total, uint32_t* partials,
+                       void* stream) {
+    if ((!in || !out) && n) { g_error = "null scan buffer"; return 1; }
+    if (!partials) { g_error = "null scan partials"; return 1; }
+    launch_scan(in, out, ScanCount{nullptr, 0, 0, n}, false, total, nullptr, partials,
+                static_cast<cudaStream_t>(stream));
+    return record(cudaGetLastError(), "scan");
+}
+
+int sdg_scan_partials(void) { return 2 * SCAN_BLOCKS; }
+
 void* sdg_engine_create(void) { return new (std::nothrow) Engine(); }
 void sdg_engine_destroy(void* engine) { delete static_cast<Engine*>(engine); }
 

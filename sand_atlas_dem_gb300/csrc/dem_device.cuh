@@ -85,14 +85,17 @@ struct Res {
     const uint32_t* oldContactStart;  // pairCapacity+1
     uint32_t* work;                   // 64 counters
     uint32_t* scanPartials;           // 2*SCAN_BLOCKS
+    float4* hitScratch;               // 2*contactCapacity: (point/depth, normal/area) per hit
+    uint32_t* candHitBase;            // candidateCapacity: first hitScratch slot of each item
 };
-constexpr int EXTENSION_COUNT = 24;
+constexpr int EXTENSION_COUNT = 26;
 constexpr int BUFFER_COUNT = RESOURCE_COUNT + EXTENSION_COUNT;
 constexpr int CONFIG_VALUES = 25;
 constexpr int VALUE_COUNT = CONFIG_VALUES + 3;
 constexpr int SCAN_BLOCKS = 608;  // 4 per SM on a 152-SM GB300
 // work[] slots
 constexpr int W_CANDIDATES = 0;
+constexpr int W_HITS = 1;
 
 struct Params {
     Config c;

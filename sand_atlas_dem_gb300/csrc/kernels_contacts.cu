@@ -335,6 +335,7 @@ __global__ void k_resetContacts(const __grid_constant__ Params P) {
     r.control[2] = 0;
     r.control[6] = 0;
     r.work[W_CANDIDATES] = 0;
+    r.work[W_HITS] = 0;
 }
 // Flat leaf cull: one warp per directed pair; meshPairBounds (solver.slang:
 // 404-417) + meshBoxMayContact (:274-288) on every leaf, gated by the root
@@ -392,7 +393,9 @@ __global__ void k_leafEmit(const __grid_constant__ Params P) {
         }
     }
 }
-// Exact node queries, one warp per (directed pair, leaf) item.
+// Exact node queries, one warp per (directed pair, leaf) item.  Each hit's
+// point/depth and normal/area are stored once in hitScratch at a slot taken
+// with one atomic per item; the emit pass copies them to canonical order.
 __global__ void __launch_bounds__(256) k_nodeQuery(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
@@ -400,6 +403,7 @@ __global__ void __launch_bounds__(256) k_nodeQuery(const __grid_constant__ Param
     for (uint32_t item = warpGlobal(); item < n; item += warpStride()) {
         // Leaves hold at most 64 nodes (packing splits larger sets), two per lane.
         bool hit0 = false, hit1 = false;
+        float4 pd0, na0, pd1, na1;
         if (r.control[0] == 0) {
             uint2 cd = r.candidates[item];
             uint32_t d = cd.x, p = d >> 1, pass = d & 1;
@@ -407,20 +411,31 @@ __global__ void __launch_bounds__(256) k_nodeQuery(const __grid_constant__ Param
             uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
             f3 branch = xyz(r.dpairBranch[d]);
             uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
-            float4 pd, na;
             uint32_t k = laneId();
-            if (k < range.y) hit0 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd, na);
+            if (k < range.y) hit0 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd0, na0);
             k += WARP;
-            if (k < range.y) hit1 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd, na);
+            if (k < range.y) hit1 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd1, na1);
         }
         uint32_t m0 = __ballot_sync(0xffffffffu, hit0), m1 = __ballot_sync(0xffffffffu, hit1);
+        uint32_t hits = __popc(m0) + __popc(m1), base = 0;
         if (laneId() == 0) {
+            if (hits) base = atomicAdd(&r.work[W_HITS], hits);
             r.candHitMask[item] = make_uint2(m0, m1);
-            r.candHitCount[item] = __popc(m0) + __popc(m1);
+            r.candHitCount[item] = hits;
+            r.candHitBase[item] = base;
+        }
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (hit0) {
+            uint32_t slot = base + __popc(m0 & lanesBelow());
+            if (slot < c.contactCapacity) { r.hitScratch[2 * slot] = pd0; r.hitScratch[2 * slot + 1] = na0; }
+        }
+        if (hit1) {
+            uint32_t slot = base + __popc(m0) + __popc(m1 & lanesBelow());
+            if (slot < c.contactCapacity) { r.hitScratch[2 * slot] = pd1; r.hitScratch[2 * slot + 1] = na1; }
         }
     }
 }
-// Writes the hits of each item at its canonical offset, recomputing them.
+// Copies the hits of each item from hitScratch to their canonical offsets.
 __global__ void __launch_bounds__(256) k_nodeEmit(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
@@ -433,21 +448,19 @@ __global__ void __launch_bounds__(256) k_nodeEmit(const __grid_constant__ Params
         uint32_t d = cd.x, p = d >> 1, pass = d & 1;
         uint2 ij = r.pairs[p];
         uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
-        f3 branch = xyz(r.dpairBranch[d]);
         uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
-        uint32_t base = r.candHitOffset[item];
+        uint32_t out = r.candHitOffset[item], in = r.candHitBase[item];
 #pragma unroll
         for (uint32_t half = 0; half < 2; ++half) {
             uint32_t word = half ? m.y : m.x;
             if (!((word >> laneId()) & 1u)) continue;
-            uint32_t slot = base + (half ? __popc(m.x) : 0) + __popc(word & lanesBelow());
+            uint32_t rank = (half ? __popc(m.x) : 0) + __popc(word & lanesBelow());
+            uint32_t slot = out + rank, from = in + rank;
+            if (slot >= c.contactCapacity || from >= c.contactCapacity) { fail(r, F_CONTACT); continue; }
             uint32_t node = __ldg(&r.meshSampleIndices[range.x + laneId() + half * WARP]);
-            float4 pd, na;
-            if (!nodeContact(r, c, src, dst, node, branch, pd, na)) continue;
-            if (slot >= c.contactCapacity) { fail(r, F_CONTACT); continue; }
             r.meta[slot] = make_uint4(src, dst, node, 0);
-            r.pointDepth[slot] = pd;
-            r.normalArea[slot] = na;
+            r.pointDepth[slot] = r.hitScratch[2 * from];
+            r.normalArea[slot] = r.hitScratch[2 * from + 1];
             r.contactPair[slot] = p;
         }
     }
@@ -577,80 +590,116 @@ __global__ void k_resolve(const __grid_constant__ Params P) {
 }
 
 // -------------------------------------------------------------------- gather
-// solver.slang:760-811.  Contacts of grain g are visited in the order the
-// reference's linked lists hold them (descending contact id): pairs where g is
-// first (a contiguous run) and second (the byJ run) merged from the highest
-// pair id down, each pair's contacts from the last.
-__global__ void k_gather(const __grid_constant__ Params P) {
+// solver.slang:760-811, one warp per grain.  Contacts of grain g are taken in
+// the order the reference's linked lists hold them (descending contact id):
+// pairs where g is first (a contiguous run) and second (the byJ run) merged
+// from the highest pair id down, each pair's contacts from the last.  Lanes
+// load and evaluate 32 contacts at a time; every lane then replays the
+// sequential (compensated) accumulation over the shuffled per-contact terms
+// in that order, so the sums are bit-identical to the serial loop.
+struct GatherTerms {
+    f3 force, torque, s0, s1, s2;
+    float energy, denom, depth, dissipation, normalPower, stiffness, viscous;
+};
+__device__ __forceinline__ f3 shfl3(f3 v, int lane) {
+    return mk(__shfl_sync(0xffffffffu, v.x, lane), __shfl_sync(0xffffffffu, v.y, lane),
+              __shfl_sync(0xffffffffu, v.z, lane));
+}
+__global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
-    uint32_t id = gtid();
-    if (id >= c.N || r.control[0] != 0) return;
-    f3 f = mk(0.f, 0.f, 0.f), t = f, fLow = f, tLow = f, stress0 = f, stress1 = f, stress2 = f;
-    float energy = 0, denom = 0, maxDepth = 0, dissipation = 0, normalPower = 0, stiffnessRate = 0, viscousRate = 0;
-    f3 one = mk(1.f, 1.f, 1.f);
-    float inverseInertia = mx(mx(dot(abs3(xyz(r.invI[3 * id])), one), dot(abs3(xyz(r.invI[3 * id + 1])), one)),
-                              dot(abs3(xyz(r.invI[3 * id + 2])), one));
-    float m = r.body[id].y, bw = r.body[id].w;
+    if (r.control[0] != 0) return;
     uint32_t pairs = activePairs(r, c);
-    uint32_t aBegin = min(r.pairOffsets[id], pairs), aEnd = min(aBegin + r.pairCounts[id], pairs);
-    uint32_t bBegin = r.byJOffsets[id], bEnd = r.byJOffsets[id + 1];
-    uint32_t ia = aEnd, ib = bEnd;
-    while (ia > aBegin || ib > bBegin) {
-        uint32_t p;
-        if (ib == bBegin || (ia > aBegin && ia - 1 > r.byJPairs[ib - 1])) p = --ia;
-        else p = r.byJPairs[--ib];
-        uint32_t begin = r.sideContactStart[p], end = r.sideContactStart[p + 1];
-        for (uint32_t contact = end; contact-- > begin;) {
-            uint4 key = r.meta[contact];
-            bool source = key.x == id;
-            float4 cf = r.contactForce[contact];
-            f3 force = xyz(cf);
-            float4 pdv = r.pointDepth[contact];
-            f3 arm = xyz(pdv);
-            f3 branch = xyz(r.dpairBranch[2 * p + (key.x > key.y ? 1 : 0)]);
-            float area = r.normalArea[contact].w;
-            if (c.activeTimestep != 0) {
-                f3 localArm = source ? arm : arm - branch;
-                float mobility = __fadd_rn(__fdiv_rn(1.0f, m), __fmul_rn(dot(localArm, localArm), inverseInertia));
-                float half = __fmul_rn(area, 0.5f);
-                stiffnessRate = __fadd_rn(stiffnessRate,
-                    __fmul_rn(__fmul_rn(__fmul_rn(2.0f, half), __fadd_rn(__fmul_rn(c.kn, __fadd_rn(1.0f, c.mu)), c.kt)), mobility));
-                viscousRate = __fadd_rn(viscousRate,
-                    __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(2.0f, half), c.normalViscosity), __fadd_rn(1.0f, c.mu)), mobility));
+    for (uint32_t id = warpGlobal(); id < c.N; id += warpStride()) {
+        f3 f = mk(0.f, 0.f, 0.f), t = f, fLow = f, tLow = f, stress0 = f, stress1 = f, stress2 = f;
+        float energy = 0, denom = 0, maxDepth = 0, dissipation = 0, normalPower = 0, stiffnessRate = 0,
+              viscousRate = 0;
+        f3 one = mk(1.f, 1.f, 1.f);
+        float inverseInertia = mx(mx(dot(abs3(xyz(r.invI[3 * id])), one), dot(abs3(xyz(r.invI[3 * id + 1])), one)),
+                                  dot(abs3(xyz(r.invI[3 * id + 2])), one));
+        float m = r.body[id].y, bw = r.body[id].w;
+        uint32_t aBegin = min(r.pairOffsets[id], pairs), aEnd = min(aBegin + r.pairCounts[id], pairs);
+        uint32_t bBegin = r.byJOffsets[id], bEnd = r.byJOffsets[id + 1];
+        uint32_t ia = aEnd, ib = bEnd;
+        while (ia > aBegin || ib > bBegin) {
+            uint32_t p;
+            if (ib == bBegin || (ia > aBegin && ia - 1 > r.byJPairs[ib - 1])) p = --ia;
+            else p = r.byJPairs[--ib];
+            uint32_t begin = r.sideContactStart[p], end = r.sideContactStart[p + 1];
+            f3 branch0 = xyz(r.dpairBranch[2 * p]), branch1 = xyz(r.dpairBranch[2 * p + 1]);
+            for (uint32_t top = end; top > begin;) {
+                uint32_t count = min(top - begin, WARP);
+                GatherTerms g{};
+                if (laneId() < count) {
+                    uint32_t contact = top - 1 - laneId();
+                    uint4 key = r.meta[contact];
+                    bool source = key.x == id;
+                    float4 cf = r.contactForce[contact];
+                    f3 force = xyz(cf);
+                    float4 pdv = r.pointDepth[contact];
+                    f3 arm = xyz(pdv);
+                    f3 branch = key.x > key.y ? branch1 : branch0;
+                    if (c.activeTimestep != 0) {
+                        f3 localArm = source ? arm : arm - branch;
+                        float mobility = __fadd_rn(__fdiv_rn(1.0f, m), __fmul_rn(dot(localArm, localArm), inverseInertia));
+                        float half = __fmul_rn(r.normalArea[contact].w, 0.5f);
+                        g.stiffness = __fmul_rn(__fmul_rn(__fmul_rn(2.0f, half), __fadd_rn(__fmul_rn(c.kn, __fadd_rn(1.0f, c.mu)), c.kt)), mobility);
+                        g.viscous = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(2.0f, half), c.normalViscosity), __fadd_rn(1.0f, c.mu)), mobility);
+                    }
+                    g.force = source ? force : -force;
+                    g.torque = source ? cross(arm, force) : cross(arm - branch, -force);
+                    g.s0 = __fmul_rn(0.5f, force.x) * branch;
+                    g.s1 = __fmul_rn(0.5f, force.y) * branch;
+                    g.s2 = __fmul_rn(0.5f, force.z) * branch;
+                    g.energy = __fmul_rn(0.5f, cf.w);
+                    g.denom = length(force);
+                    uint32_t other = source ? key.y : key.x;
+                    float wmin = source ? mn(bw, r.body[other].w) : mn(r.body[other].w, bw);
+                    g.depth = __fdiv_rn(pdv.w, wmin);
+                    g.dissipation = __fmul_rn(0.5f, r.slip[contact].w);
+                    g.normalPower = __fmul_rn(0.5f, r.normalLossPower[contact]);
+                }
+                for (uint32_t k = 0; k < count; ++k) {
+                    int lane = int(k);
+                    if (c.activeTimestep != 0) {
+                        stiffnessRate = __fadd_rn(stiffnessRate, __shfl_sync(0xffffffffu, g.stiffness, lane));
+                        viscousRate = __fadd_rn(viscousRate, __shfl_sync(0xffffffffu, g.viscous, lane));
+                    }
+                    compensated3(f, fLow, shfl3(g.force, lane));
+                    compensated3(t, tLow, shfl3(g.torque, lane));
+                    stress0 = stress0 - shfl3(g.s0, lane);
+                    stress1 = stress1 - shfl3(g.s1, lane);
+                    stress2 = stress2 - shfl3(g.s2, lane);
+                    energy = __fadd_rn(energy, __shfl_sync(0xffffffffu, g.energy, lane));
+                    denom = __fadd_rn(denom, __shfl_sync(0xffffffffu, g.denom, lane));
+                    maxDepth = mx(maxDepth, __shfl_sync(0xffffffffu, g.depth, lane));
+                    dissipation = __fadd_rn(dissipation, __shfl_sync(0xffffffffu, g.dissipation, lane));
+                    normalPower = __fadd_rn(normalPower, __shfl_sync(0xffffffffu, g.normalPower, lane));
+                }
+                top -= count;
             }
-            compensated3(f, fLow, source ? force : -force);
-            compensated3(t, tLow, source ? cross(arm, force) : cross(arm - branch, -force));
-            stress0 = stress0 - __fmul_rn(0.5f, force.x) * branch;
-            stress1 = stress1 - __fmul_rn(0.5f, force.y) * branch;
-            stress2 = stress2 - __fmul_rn(0.5f, force.z) * branch;
-            energy = __fadd_rn(energy, __fmul_rn(0.5f, cf.w));
-            denom = __fadd_rn(denom, length(force));
-            uint32_t other = source ? key.y : key.x;
-            float wmin = source ? mn(bw, r.body[other].w) : mn(r.body[other].w, bw);
-            maxDepth = mx(maxDepth, __fdiv_rn(pdv.w, wmin));
-            dissipation = __fadd_rn(dissipation, __fmul_rn(0.5f, r.slip[contact].w));
-            normalPower = __fadd_rn(normalPower, __fmul_rn(0.5f, r.normalLossPower[contact]));
+        }
+        if (laneId() == 0) {
+            f = f + fLow;
+            t = t + tLow;
+            r.timestepRows[id] = make_float4(stiffnessRate, viscousRate, 0.f, 0.f);
+            float4 ns = r.normalDamping[id];
+            ns.z = normalPower;
+            r.normalDamping[id] = ns;
+            r.force[id] = w4(f, maxDepth);
+            r.torque[id] = w4(t, dissipation);
+            r.particleStress[3 * id] = w4(stress0, 0.f);
+            r.particleStress[3 * id + 1] = w4(stress1, 0.f);
+            r.particleStress[3 * id + 2] = w4(stress2, 0.f);
+            f3 v = xyz(r.velocity[id]);
+            float kinetic = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(m, dot(v, v)), dot(xyz(r.momentum[id]), omegaOf(r, id))));
+            r.particleDiagnostic[id] = make_float4(kinetic, energy, length(f), denom);
+            float4 high = r.accumulated[id], low = r.accumulatedRemainder[id];
+            compensated4(high, low, make_float4(dissipation, 0.f, 0.f, 0.f));
+            r.accumulated[id] = high;
+            r.accumulatedRemainder[id] = low;
         }
     }
-    f = f + fLow;
-    t = t + tLow;
-    r.timestepRows[id] = make_float4(stiffnessRate, viscousRate, 0.f, 0.f);
-    float4 ns = r.normalDamping[id];
-    ns.z = normalPower;
-    r.normalDamping[id] = ns;
-    r.force[id] = w4(f, maxDepth);
-    r.torque[id] = w4(t, dissipation);
-    r.particleStress[3 * id] = w4(stress0, 0.f);
-    r.particleStress[3 * id + 1] = w4(stress1, 0.f);
-    r.particleStress[3 * id + 2] = w4(stress2, 0.f);
-    f3 v = xyz(r.velocity[id]);
-    float kinetic = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(m, dot(v, v)), dot(xyz(r.momentum[id]), omegaOf(r, id))));
-    r.particleDiagnostic[id] = make_float4(kinetic, energy, length(f), denom);
-    float4 high = r.accumulated[id], low = r.accumulatedRemainder[id];
-    compensated4(high, low, make_float4(dissipation, 0.f, 0.f, 0.f));
-    r.accumulated[id] = high;
-    r.accumulatedRemainder[id] = low;
 }
 
 // ---------------------------------------------------------------- launchers
@@ -715,7 +764,7 @@ int launch_contacts(const std::string_view& name, const Params& P, uint32_t coun
     else if (name == "collectQuery") collectQuery(P, s);
     else if (name == "collectEmit") collectEmit(P, s);
     else if (name == "resolveContacts") k_resolve<<<PERSISTENT, T, 0, s>>>(P);
-    else if (name == "gather") k_gather<<<blocks(c.N, 128), 128, 0, s>>>(P);
+    else if (name == "gather") k_gather<<<min(blocks(c.N, 8), PERSISTENT), T, 0, s>>>(P);
     else return 1;
     (void)count;
     return 0;

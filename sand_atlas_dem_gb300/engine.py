@@ -33,6 +33,7 @@ EXTENSION_ORDER = (
     "byJPairs", "dpairBranch", "dpairLeafCount", "dpairCandOffset", "leafMask", "candidates",
     "candHitCount", "candHitOffset", "candHitMask", "contactPair", "sidePairOffsets", "sidePairB",
     "sideContactStart", "oldPairOffsets", "oldPairB", "oldContactStart", "work", "scanPartials",
+    "hitScratch", "candHitBase",
 )
 BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
 # History side fields: (name bound as the side being written, name bound as committed).
@@ -182,6 +183,7 @@ class Engine:
             "candidates": 8 * self.candidate_capacity, "candHitCount": 4 * (self.candidate_capacity + 1),
             "candHitOffset": 4 * (self.candidate_capacity + 1), "candHitMask": 8 * self.candidate_capacity,
             "contactPair": 4 * cc, "work": 4 * 64, "scanPartials": 4 * 2 * SCAN_BLOCKS,
+            "hitScratch": 32 * cc, "candHitBase": 4 * self.candidate_capacity,
         }
         for name, nbytes in sizes.items():
             self.buffers[name] = DeviceBuffer(self, nbytes)

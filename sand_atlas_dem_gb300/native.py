@@ -32,7 +32,7 @@ def nvcc():
 def build(force=False, verbose=False):
     """Compile every translation unit in parallel and link the shared library."""
     LIBDIR.mkdir(exist_ok=True)
-    headers = max(p.stat().st_mtime for p in CSRC.glob("*.h*"))
+    headers = max(p.stat().st_mtime for p in [*CSRC.glob("*.h"), *CSRC.glob("*.cuh")])
     objects = []
     jobs = []
     for name in SOURCES:
@@ -87,6 +87,10 @@ def load():
     lib.sdg_engine_profile.argtypes = [ct.c_void_p, P(ct.c_void_p), P(ct.c_uint64), P(ct.c_double), ct.c_uint32,
                                        P(ct.c_float), ct.c_void_p]
     lib.sdg_engine_profile.restype = ct.c_int
+    lib.sdg_exclusive_scan.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_uint32, ct.c_void_p, ct.c_void_p,
+                                       ct.c_void_p]
+    lib.sdg_exclusive_scan.restype = ct.c_int
+    lib.sdg_scan_partials.restype = ct.c_int
     lib.sdg_engine_kernels_per_step.argtypes = [ct.c_void_p]
     lib.sdg_engine_kernels_per_step.restype = ct.c_int
     _LIB = lib
@@ -110,6 +114,8 @@ EXPORTS = (
     "sdg_engine_advance",
     "sdg_engine_profile",
     "sdg_engine_kernels_per_step",
+    "sdg_exclusive_scan",
+    "sdg_scan_partials",
 )
 PHASES = ("drift", "neighbours", "pair_cull", "node_query", "contact_emit", "friction_and_history",
           "force_reduction", "final_kick")
