@@ -41,6 +41,7 @@ WORKLOAD = dict(
     nodes_per_grain=642,
     shapes=64,
     solid_fraction=0.58,
+    max_overlap_fraction=0.1,
     strain_rate_per_s=-0.5,
     friction=0.5,
     damping_ratio=0.3,
@@ -79,34 +80,44 @@ def lattice_packing(lib, grains):
                 overrides=dict(max_overlap_fraction=0.5))
 
 
+DATA = ROOT / "sand_atlas_dem_gb300" / "data"
+
+
 def packing(lib, grains, phi, seed=42, kind="dense"):
-    """Prepared dense packing (cached per parameter set on this machine)."""
-    from sand_atlas_dem_gb300.workloads import dense_packing
+    """The prepared dense packing (committed record, else prepared here and cached)."""
+    from sand_atlas_dem_gb300.workloads import dense_packing, load_packing, save_packing
 
     if kind == "lattice":
         return lattice_packing(lib, grains)
-
-    path = cache_dir() / f"packing-f8-{grains}-{phi}-{seed}.npz"
-    if path.exists():
-        with np.load(path, allow_pickle=False) as z:
-            state = {k[6:]: z[k] for k in z.files if k.startswith("state_")}
-            state["contacts"] = int(z["contacts"])
-            return dict(state=state, ids=z["ids"], scales=z["scales"], cell=z["cell"],
-                        steps=int(z["steps"]))
+    name = f"packing-f8-{grains}-{phi}.npz"
+    for path in (DATA / name, cache_dir() / name):
+        if path.exists():
+            return dict(load_packing(path), kind="record", path=str(path))
     t = time.perf_counter()
     out = dense_packing(lib, grains, phi, seed=seed, log=lambda d: log("prepare", d))
     log(f"prepared packing in {time.perf_counter() - t:.1f} s, {out['steps']} steps")
-    arrays = {f"state_{k}": v for k, v in out["state"].items() if isinstance(v, np.ndarray)}
-    np.savez(path, contacts=out["state"]["contacts"], ids=out["ids"], scales=out["scales"],
-             cell=out["cell"], steps=out["steps"], **arrays)
-    return out
+    save_packing(cache_dir() / name, out["engine"], out["ids"], out["scales"], dict(steps=out["steps"]))
+    return dict(load_packing(cache_dir() / name), kind="record")
 
 
 def engine_for(lib, pack, cls, **kwargs):
+    """Engine on a packing: a full checkpoint state, or a packing record
+    (centres, orientations, cell) started from rest and initialized."""
     from sand_atlas_dem_gb300.workloads import material_spec
 
+    overrides = pack.get("overrides", {"max_overlap_fraction": WORKLOAD["max_overlap_fraction"]})
+    spec = material_spec(lib, pack["ids"], pack["scales"], **overrides)
+    if pack.get("kind") == "record":
+        e = cls(lib, spec, pack["positions"], pack["cell"], pack["ids"], pack["scales"], **kwargs)
+        rotations = np.ascontiguousarray(pack["rotations"], np.float32)
+        buffer = e.buffers["rotation"]
+        if isinstance(buffer, np.ndarray):
+            buffer[...] = rotations
+        else:
+            buffer.copy_from_numpy(rotations)
+        e.initialize()
+        return e
     state = pack["state"]
-    spec = material_spec(lib, pack["ids"], pack["scales"], **pack.get("overrides", {}))
     length_unit = float(np.median([(6 * s.volume / np.pi) ** (1 / 3) for s in lib.shapes]))
     positions = (state["position"][:, :3].astype(float) + state["positionRemainder"][:, :3]) * length_unit
     cell = state["cell"][0, :3].astype(float) * length_unit
@@ -271,7 +282,7 @@ def run_gb300(args, cpu=True):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": dict(WORKLOAD, grains=args.grains, packing=args.packing, l2="flushed before each timed step (256 MiB write)",
+        "config": dict(WORKLOAD, grains=args.grains, packing=args.packing, packing_meta=pack.get("meta"), l2="flushed before each timed step (256 MiB write)",
                        pairs=pairs, contacts=contacts, node_query_items=items, node_queries=nodes,
                        timestep_s=e.spec.timestep, phase_ms=phase_ms, dominant_phase=top),
         "e2e": {"value": e2e, "unit": "grain-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -379,7 +390,7 @@ def main():
     if args.prepare_only:
         lib = library()
         pack = packing(lib, args.grains, WORKLOAD["solid_fraction"])
-        print(json.dumps({"prepared": True, "steps": pack["steps"], "contacts": pack["state"]["contacts"]}))
+        print(json.dumps({"prepared": True, "path": pack.get("path")}))
         return
     print(json.dumps(run_gb300(args)), flush=True)
 

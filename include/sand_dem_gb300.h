@@ -11,18 +11,22 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 103) this backend's extension buffers, in the order of
+ *   [77, 106) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
  *             pair ids, the written and committed history pair tables, work
- *             counters, scan partials, the per-hit scratch and the first
- *             scratch slot of each item).
+ *             counters, scan partials, the per-hit scratch, the first
+ *             scratch slot of each item, per directed pair the target
+ *             enclosure plane facing the source, the specimen of each
+ *             grain and each specimen's bin grid).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
- * directed pair, (directed pair, leaf) item capacity, and a flag that fuses
- * captureContactKinematics into beginStep.
+ * directed pair, (directed pair, leaf) item capacity, a flag that fuses
+ * captureContactKinematics into beginStep, and the number of independent
+ * periodic specimens batched in the buffers (cell rows 3 per specimen,
+ * cellLog and referenceCell rows 2 per specimen; 1 = the reference case).
  *
  * Return codes: 0 success; 1 argument error; 2 CUDA error.  The message of
  * the last error on the calling thread is sdg_last_error().  Solver failures
@@ -39,8 +43,8 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 103
-#define SDG_VALUE_COUNT 28
+#define SDG_BUFFER_COUNT 106
+#define SDG_VALUE_COUNT 29
 #define SDG_PHASES 8
 
 /* ABI revision of this header. */

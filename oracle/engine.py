@@ -140,9 +140,10 @@ class OracleEngine:
                     oldNormal=old["normalArea"], oldHash=old["hash"])
         return [view[name] for name in RESOURCE_ORDER]
 
-    def config(self, dt=None, drag=0.0):
+    def config(self, dt=None, drag=0.0, history=None):
         return self.layout.config(
-            dt=self.spec.timestep if dt is None else dt, drag=drag, history=self.history
+            dt=self.spec.timestep if dt is None else dt, drag=drag,
+            history=self.history if history is None else history,
         )
 
     def dispatch(self, name, count, config, extra=(), uniforms=()):

@@ -45,6 +45,8 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
     c.historyStep = uint32_t(v[19]); c.meshGeometry = uint32_t(v[20]); c.periodic = uint32_t(v[21]);
     c.wallCount = uint32_t(v[22]); c.wallBoxEnabled = uint32_t(v[23]); c.sourceSurfaceNormal = uint32_t(v[24]);
     c.leafWords = uint32_t(v[25]); c.candidateCapacity = uint32_t(v[26]); c.viscousCapture = uint32_t(v[27]);
+    c.specimens = uint32_t(v[28]);
+    if (c.specimens == 0) { g_error = "at least one specimen required"; return 1; }
     if (c.N == 0 || c.meshGeometry == 0 || c.wallCount != 0) {
         g_error = "the GB300 step needs N > 0, mesh geometry and no planes";
         return 1;
@@ -80,7 +82,7 @@ void launch_step(const Params& P, cudaStream_t s) {
     Params B = P;
     B.c.viscousCapture = c.normalViscosity > 0 ? 1u : 0u;
     launch_state("beginStep", B, c.N, s);
-    launch_state("advanceCell", P, 1, s);
+    launch_state("advanceCell", P, c.specimens, s);
     launch_state("checkRebuild", P, c.N, s);
     launch_forces(P, s, false);
     launch_state("finishStep", P, c.N, s);
@@ -185,7 +187,7 @@ int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes
     Params B = P;
     B.c.viscousCapture = c.normalViscosity > 0 ? 1u : 0u;
     launch_state("beginStep", B, c.N, s);
-    launch_state("advanceCell", P, 1, s);
+    launch_state("advanceCell", P, c.specimens, s);
     launch_state("checkRebuild", P, c.N, s);
     cudaEventRecord(ev[1], s);
     launch_contacts("neighbours", P, c.N, s);

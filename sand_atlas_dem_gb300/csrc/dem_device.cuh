@@ -34,6 +34,7 @@ struct Config {
     uint32_t leafWords;          // 32-bit words per directed pair in the leaf mask
     uint32_t candidateCapacity;  // (directed pair, leaf cluster) work items
     uint32_t viscousCapture;     // fuse captureContactKinematics into beginStep
+    uint32_t specimens;          // independent periodic specimens batched in one launch
 };
 
 // Buffers: the reference Resources block (solver.slang:20-100) in declaration
@@ -87,11 +88,14 @@ struct Res {
     uint32_t* scanPartials;           // 2*SCAN_BLOCKS
     float4* hitScratch;               // 2*contactCapacity: (point/depth, normal/area) per hit
     uint32_t* candHitBase;            // candidateCapacity: first hitScratch slot of each item
+    float4* dpairPlane;               // 2*pairCapacity: enclosure plane of the target facing the source
+    const uint32_t* grainSpecimen;    // N: specimen of each grain
+    const uint4* specimenBins;        // specimens: bin grid x, y, z and first bin
 };
-constexpr int EXTENSION_COUNT = 26;
+constexpr int EXTENSION_COUNT = 29;
 constexpr int BUFFER_COUNT = RESOURCE_COUNT + EXTENSION_COUNT;
 constexpr int CONFIG_VALUES = 25;
-constexpr int VALUE_COUNT = CONFIG_VALUES + 3;
+constexpr int VALUE_COUNT = CONFIG_VALUES + 4;
 constexpr int SCAN_BLOCKS = 608;  // 4 per SM on a 152-SM GB300
 // work[] slots
 constexpr int W_CANDIDATES = 0;
@@ -203,10 +207,16 @@ __device__ __forceinline__ float4 rotationIncrement(f3 w, float dt, float4 q) {
     return qmul(w4(coefficient * w, cm1), q);
 }
 
+// Batched specimens: grain i belongs to specimen s = grainSpecimen[i]; the
+// specimen's cell rows (lengths, imposed log rates, initial lengths; the
+// reference cell buffer, gpu.py:223-226) start at cell[3s], its cellLog and
+// referenceCell rows at [2s].  A single specimen is s = 0 throughout.
+__device__ __forceinline__ uint32_t specimenOf(const Res& r, uint32_t i) { return r.grainSpecimen[i]; }
+
 // Minimum-image branch j - i in FP64, cast to FP32 (cpu_scheduling.slang:10-15).
 __device__ __forceinline__ f3 centerBranch64(const Res& r, const Config& c, uint32_t i, uint32_t j) {
     float4 pi = r.position[i], pj = r.position[j], li = r.positionRemainder[i], lj = r.positionRemainder[j];
-    float4 cell = r.cell[0];
+    float4 cell = r.cell[3 * specimenOf(r, i)];
     double dx = __dadd_rn(__dsub_rn((double)pj.x, (double)pi.x), __dsub_rn((double)lj.x, (double)li.x));
     double dy = __dadd_rn(__dsub_rn((double)pj.y, (double)pi.y), __dsub_rn((double)lj.y, (double)li.y));
     double dz = __dadd_rn(__dsub_rn((double)pj.z, (double)pi.z), __dsub_rn((double)lj.z, (double)li.z));
@@ -372,8 +382,11 @@ __device__ __forceinline__ void meshPairBounds(const Res& r, uint32_t direction,
     high = high + mk(pad, pad, pad);
 }
 // solver.slang:319-343; the directed-pair branch is precomputed (same bits).
+// With `plane`, the reference CPU backend's per-directed-pair enclosure-plane
+// prefilter (cpu.py:56-76) rejects first; like the hull cull it is
+// conservative and changes no contact.
 __device__ __forceinline__ bool nodeContact(const Res& r, const Config& c, uint32_t src, uint32_t dst, uint32_t node,
-                                            f3 branch, float4& pd, float4& na) {
+                                            f3 branch, float4& pd, float4& na, const float4* plane = nullptr) {
     uint32_t sid = r.shapeId[src];
     float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[sid].x) + node]);
     float4 qs = r.rotation[src], qd = r.rotation[dst];
@@ -381,6 +394,11 @@ __device__ __forceinline__ bool nodeContact(const Res& r, const Config& c, uint3
     f3 arm = qrot(qs, xyz(sp) * bs.x);
     f3 local = qinv(qd, arm - branch) / bd.x;
     uint32_t targetShape = r.shapeId[dst];
+    if (plane) {
+        float pad = __fmul_rn(0.00000762939453125f,
+                              __fadd_rn(1.0f, mx(mx(fabsf(local.x), fabsf(local.y)), fabsf(local.z))));
+        if (__fadd_rn(dot(xyz(*plane), local), plane->w) > pad) return false;
+    }
     if (!meshMayContain(r, targetShape, local)) return false;
     float4 f = meshDistance(r, targetShape, local, false);
     pd = w4(arm, __fmul_rn(-f.w, bd.x));

@@ -107,19 +107,21 @@ void launch_scan(const uint32_t* in, uint32_t* out, ScanCount count, bool writeE
 
 // ------------------------------------------------------------ neighbours
 // solver.slang:184-186
-__device__ __forceinline__ void binIndex(const Res& r, const Config& c, uint32_t i, uint32_t b[3]) {
-    float4 p = r.position[i], box = r.cell[0];
-    float g[3] = {floorf(__fmul_rn(__fdiv_rn(p.x, box.x), float(c.bins[0]))),
-                  floorf(__fmul_rn(__fdiv_rn(p.y, box.y), float(c.bins[1]))),
-                  floorf(__fmul_rn(__fdiv_rn(p.z, box.z), float(c.bins[2])))};
+// Bin grid of a specimen: sb = (bins x, y, z, first bin of the specimen).
+__device__ __forceinline__ void binIndex(const Res& r, uint32_t i, uint4 sb, float4 box, uint32_t b[3]) {
+    float4 p = r.position[i];
+    uint32_t bins[3] = {sb.x, sb.y, sb.z};
+    float g[3] = {floorf(__fmul_rn(__fdiv_rn(p.x, box.x), float(sb.x))),
+                  floorf(__fmul_rn(__fdiv_rn(p.y, box.y), float(sb.y))),
+                  floorf(__fmul_rn(__fdiv_rn(p.z, box.z), float(sb.z)))};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         uint32_t v = uint32_t(g[k]);
-        b[k] = v < c.bins[k] - 1 ? v : c.bins[k] - 1;
+        b[k] = v < bins[k] - 1 ? v : bins[k] - 1;
     }
 }
-__device__ __forceinline__ uint32_t binFlat(const Config& c, const uint32_t b[3]) {
-    return (b[0] * c.bins[1] + b[1]) * c.bins[2] + b[2];
+__device__ __forceinline__ uint32_t binFlat(uint4 sb, const uint32_t b[3]) {
+    return sb.w + (b[0] * sb.y + b[1]) * sb.z + b[2];
 }
 __device__ __forceinline__ uint32_t modIndex(int a, uint32_t n) { return uint32_t((a % int(n) + int(n)) % int(n)); }
 
@@ -136,15 +138,18 @@ __global__ void k_binsFill(const __grid_constant__ Params P) {
     if (id >= c.N || r.control[4] == 0) return;
     f3 p = xyz(r.position[id]), pl = xyz(r.positionRemainder[id]);
     if (!finite3(p) || !finite3(pl)) { fail(r, F_NONFINITE); return; }
+    uint32_t sp = specimenOf(r, id);
+    float4 cell = r.cell[3 * sp];
     if (c.periodic == 0) {
-        f3 box = xyz(r.cell[0]);
+        f3 box = xyz(cell);
         if (__fadd_rn(p.x, pl.x) < 0 || __fadd_rn(p.y, pl.y) < 0 || __fadd_rn(p.z, pl.z) < 0 ||
             __fadd_rn(__fsub_rn(p.x, box.x), pl.x) >= 0 || __fadd_rn(__fsub_rn(p.y, box.y), pl.y) >= 0 ||
             __fadd_rn(__fsub_rn(p.z, box.z), pl.z) >= 0) { fail(r, F_ESCAPE); return; }
     }
     uint32_t b[3];
-    binIndex(r, c, id, b);
-    uint32_t bin = binFlat(c, b);
+    uint4 sb = r.specimenBins[sp];
+    binIndex(r, id, sb, cell, b);
+    uint32_t bin = binFlat(sb, b);
     uint32_t slot = atomicAdd(&r.binCounts[bin], 1u);
     if (slot < c.binCapacity) r.binParticles[bin * c.binCapacity + slot] = id;
     else fail(r, F_BIN);
@@ -175,20 +180,23 @@ __global__ void k_binsSort(const __grid_constant__ Params P) {
 // solver.slang:360-384.  An FP32 minimum-image estimate rejects grains that
 // are clearly beyond range before the exact FP64 branch decides.
 __device__ uint32_t findPairs(const Res& r, const Config& c, uint32_t id, bool emit) {
+    uint32_t sp = specimenOf(r, id);
+    uint4 sb = r.specimenBins[sp];
+    uint32_t bins[3] = {sb.x, sb.y, sb.z};
+    float4 cell = r.cell[3 * sp];
     uint32_t b[3];
-    binIndex(r, c, id, b);
-    float cutoff = r.referenceCell[1].w;
-    float4 cell = r.cell[0];
+    binIndex(r, id, sb, cell, b);
+    float cutoff = r.referenceCell[2 * sp + 1].w;
     float box[3] = {cell.x, cell.y, cell.z};
     int reach[3], low[3];
     uint32_t width[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        reach[k] = int(ceilf(__fmul_rn(__fdiv_rn(cutoff, box[k]), float(c.bins[k]))));
+        reach[k] = int(ceilf(__fmul_rn(__fdiv_rn(cutoff, box[k]), float(bins[k]))));
         low[k] = max(int(b[k]) - reach[k], 0);
-        int high = min(int(b[k]) + reach[k], int(c.bins[k]) - 1);
+        int high = min(int(b[k]) + reach[k], int(bins[k]) - 1);
         uint32_t w = uint32_t(2 * reach[k] + 1);
-        width[k] = c.periodic != 0 ? min(w, c.bins[k]) : uint32_t(high - low[k] + 1);
+        width[k] = c.periodic != 0 ? min(w, bins[k]) : uint32_t(high - low[k] + 1);
     }
     float4 pi = r.position[id], li = r.positionRemainder[id];
     float ri = r.body[id].z;
@@ -198,15 +206,15 @@ __device__ uint32_t findPairs(const Res& r, const Config& c, uint32_t id, bool e
             for (uint32_t z = 0; z < width[2]; ++z) {
                 uint32_t cc[3];
                 if (c.periodic != 0) {
-                    cc[0] = modIndex(int(b[0]) - reach[0] + int(x), c.bins[0]);
-                    cc[1] = modIndex(int(b[1]) - reach[1] + int(y), c.bins[1]);
-                    cc[2] = modIndex(int(b[2]) - reach[2] + int(z), c.bins[2]);
+                    cc[0] = modIndex(int(b[0]) - reach[0] + int(x), bins[0]);
+                    cc[1] = modIndex(int(b[1]) - reach[1] + int(y), bins[1]);
+                    cc[2] = modIndex(int(b[2]) - reach[2] + int(z), bins[2]);
                 } else {
                     cc[0] = uint32_t(low[0] + int(x));
                     cc[1] = uint32_t(low[1] + int(y));
                     cc[2] = uint32_t(low[2] + int(z));
                 }
-                uint32_t bi = binFlat(c, cc);
+                uint32_t bi = binFlat(sb, cc);
                 uint32_t occ = min(r.binCounts[bi], c.binCapacity);
                 for (uint32_t slot = 0; slot < occ; ++slot) {
                     uint32_t j = r.binParticles[bi * c.binCapacity + slot];
@@ -249,7 +257,10 @@ __global__ void k_pairsEmit(const __grid_constant__ Params P) {
     findPairs(r, P.c, id, true);
     r.referencePosition[id] = r.position[id];
     r.referencePositionRemainder[id] = r.positionRemainder[id];
-    if (id == 0) r.referenceCell[0] = r.cell[0];
+    // Every grain of a specimen stores the same row (referenceCell[0] in the
+    // reference, written by its thread 0).
+    uint32_t sp = specimenOf(r, id);
+    r.referenceCell[2 * sp] = r.cell[3 * sp];
 }
 // Pairs grouped by their second grain, ascending pair id per grain.
 __global__ void k_byJReset(const __grid_constant__ Params P) {
@@ -354,6 +365,30 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
         if (live && ((r.meshPairMask[p] >> pass) & 1u)) {
             uint4 li = __ldg(&r.meshLeafInfo[r.shapeId[i]]);
             uint32_t targetShape = r.shapeId[j];
+            // Enclosure plane of the target most violated by the source centre
+            // (cpu_scheduling.slang:58-71): warp arg-max, lowest index on ties.
+            {
+                f3 branch = xyz(r.dpairBranch[d]);
+                f3 centre = (-qinv(r.rotation[j], branch)) / r.body[j].x;
+                uint4 first = __ldg(&r.meshHullInfo[6 * targetShape]);
+                uint4 last = __ldg(&r.meshHullInfo[6 * targetShape + 5]);
+                uint32_t begin = first.x, end = last.x + last.y;
+                float best = -1e30f;
+                uint32_t bestIndex = EMPTY;
+                for (uint32_t k = begin + laneId(); k < end; k += WARP) {
+                    float4 plane = __ldg(&r.meshPlanes[k]);
+                    float violation = __fadd_rn(dot(xyz(plane), centre), plane.w);
+                    if (violation > best) { best = violation; bestIndex = k; }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    float ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    uint32_t oi = __shfl_xor_sync(0xffffffffu, bestIndex, o);
+                    if (ob > best || (ob == best && oi < bestIndex)) { best = ob; bestIndex = oi; }
+                }
+                if (laneId() == 0)
+                    r.dpairPlane[d] = bestIndex == EMPTY ? make_float4(0.f, 0.f, 0.f, 0.f) : __ldg(&r.meshPlanes[bestIndex]);
+            }
             for (uint32_t k0 = 0; k0 < li.y; k0 += WARP) {
                 uint32_t k = k0 + laneId();
                 bool hit = false;
@@ -410,11 +445,14 @@ __global__ void __launch_bounds__(256) k_nodeQuery(const __grid_constant__ Param
             uint2 ij = r.pairs[p];
             uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
             f3 branch = xyz(r.dpairBranch[d]);
+            float4 plane = r.dpairPlane[d];
             uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
             uint32_t k = laneId();
-            if (k < range.y) hit0 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd0, na0);
+            if (k < range.y)
+                hit0 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd0, na0, &plane);
             k += WARP;
-            if (k < range.y) hit1 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd1, na1);
+            if (k < range.y)
+                hit1 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd1, na1, &plane);
         }
         uint32_t m0 = __ballot_sync(0xffffffffu, hit0), m1 = __ballot_sync(0xffffffffu, hit1);
         uint32_t hits = __popc(m0) + __popc(m1), base = 0;
@@ -564,7 +602,7 @@ __global__ void k_resolve(const __grid_constant__ Params P) {
         f3 branch = xyz(r.dpairBranch[2 * p + (i > j ? 1 : 0)]);
         f3 translation = viscosity > 0 ? xyz(r.forceVelocity[i]) - xyz(r.forceVelocity[j])
                                        : xyz(r.velocity[i]) - xyz(r.velocity[j]);
-        f3 rv = ((translation - xyz(r.cell[1]) * branch) + cross(wi, arm)) - cross(wj, arm - branch);
+        f3 rv = ((translation - xyz(r.cell[3 * specimenOf(r, i) + 1]) * branch) + cross(wi, arm)) - cross(wj, arm - branch);
         elastic = elastic + (rv - nrm * dot(rv, nrm)) * c.dt;
         f3 trial = elastic;
         float area = r.normalArea[id].w, depth = r.pointDepth[id].w;

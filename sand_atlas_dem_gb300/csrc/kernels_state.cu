@@ -29,7 +29,7 @@ __device__ __forceinline__ void accumulateNormalLoss(const Res& r, uint32_t id, 
 __device__ __forceinline__ float cellPower(const Res& r, uint32_t i) {
     f3 diagonal = mk(r.particleStress[3 * i].x, r.particleStress[3 * i + 1].y, r.particleStress[3 * i + 2].z);
     f3 v = xyz(r.velocity[i]);
-    return -dot(diagonal + (r.body[i].y * v) * v, xyz(r.cell[1]));
+    return -dot(diagonal + (r.body[i].y * v) * v, xyz(r.cell[3 * specimenOf(r, i) + 1]));
 }
 // solver.slang:130-134
 __device__ __forceinline__ void accumulate(const Res& r, uint32_t id, float4 inc) {
@@ -66,7 +66,8 @@ __global__ void k_beginStep(const __grid_constant__ Params P) {
     uint32_t id = gtid();
     if (id >= c.N || r.control[0] != 0) return;
     float dt = c.dt;
-    f3 rate = xyz(r.cell[1]);
+    uint32_t sp = specimenOf(r, id);
+    f3 rate = xyz(r.cell[3 * sp + 1]);
     f3 v, vl, l, ll;
     halfKick(r, c, id, v, vl, l, ll);
     r.momentum[id] = w4(l, 0.f);
@@ -83,9 +84,9 @@ __global__ void k_beginStep(const __grid_constant__ Params P) {
     }
     r.rotation[id] = q;
     r.rotationRemainder[id] = ql;
-    f3 logarithm = xyz(r.cellLog[0]), residual = xyz(r.cellLog[1]);
+    f3 logarithm = xyz(r.cellLog[2 * sp]), residual = xyz(r.cellLog[2 * sp + 1]);
     compensated3(logarithm, residual, rate * dt);
-    f3 box = xyz(r.cell[2]) * exp3(logarithm);
+    f3 box = xyz(r.cell[3 * sp + 2]) * exp3(logarithm);
     f3 p = xyz(r.position[id]), pl = xyz(r.positionRemainder[id]);
     compensated3(p, pl, expm1Stable3(rate * dt) * (p + pl) + dt * (v + vl));
     if (!finite3(p) || !finite3(pl)) { fail(r, F_NONFINITE); return; }
@@ -117,19 +118,21 @@ __global__ void k_captureContactKinematics(const __grid_constant__ Params P) {
     r.forceOmega[id] = w4(omegaOf(r, id), 0.f);
 }
 
-// solver.slang:889-897
+// solver.slang:889-897, one thread per specimen.
 __global__ void k_advanceCell(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
-    if (r.control[0] != 0) return;
-    f3 logarithm = xyz(r.cellLog[0]), residual = xyz(r.cellLog[1]);
-    compensated3(logarithm, residual, xyz(r.cell[1]) * c.dt);
-    r.cellLog[0] = w4(logarithm, 0.f);
-    r.cellLog[1] = w4(residual, 0.f);
-    float4 cell = w4(xyz(r.cell[2]) * exp3(logarithm), 0.f);
-    r.cell[0] = cell;
-    r.control[4] = 0;
-    if (c.periodic != 0 && r.referenceCell[1].w >= __fmul_rn(0.5f, mn(cell.x, mn(cell.y, cell.z)))) fail(r, F_IMAGE);
+    uint32_t sp = gtid();
+    if (sp >= c.specimens || r.control[0] != 0) return;
+    f3 logarithm = xyz(r.cellLog[2 * sp]), residual = xyz(r.cellLog[2 * sp + 1]);
+    compensated3(logarithm, residual, xyz(r.cell[3 * sp + 1]) * c.dt);
+    r.cellLog[2 * sp] = w4(logarithm, 0.f);
+    r.cellLog[2 * sp + 1] = w4(residual, 0.f);
+    float4 cell = w4(xyz(r.cell[3 * sp + 2]) * exp3(logarithm), 0.f);
+    r.cell[3 * sp] = cell;
+    if (sp == 0) r.control[4] = 0;
+    if (c.periodic != 0 && r.referenceCell[2 * sp + 1].w >= __fmul_rn(0.5f, mn(cell.x, mn(cell.y, cell.z))))
+        fail(r, F_IMAGE);
 }
 
 // solver.slang:898-904
@@ -140,12 +143,13 @@ __global__ void k_checkRebuild(const __grid_constant__ Params P) {
     if (id >= c.N) return;
     f3 d = (xyz(r.position[id]) - xyz(r.referencePosition[id])) +
            (xyz(r.positionRemainder[id]) - xyz(r.referencePositionRemainder[id]));
+    uint32_t sp = specimenOf(r, id);
     if (c.periodic != 0) {
-        f3 box = xyz(r.cell[0]);
+        f3 box = xyz(r.cell[3 * sp]);
         d = d - mk(floorf(__fadd_rn(__fdiv_rn(d.x, box.x), 0.5f)), floorf(__fadd_rn(__fdiv_rn(d.y, box.y), 0.5f)),
                    floorf(__fadd_rn(__fdiv_rn(d.z, box.z), 0.5f))) * box;
     }
-    float deformation = length(xyz(r.cell[0]) - xyz(r.referenceCell[0]));
+    float deformation = length(xyz(r.cell[3 * sp]) - xyz(r.referenceCell[2 * sp]));
     if (__fadd_rn(length(d), deformation) > __fmul_rn(0.5f, c.skin)) atomicOr(&r.control[4], 1u);
 }
 
@@ -186,7 +190,7 @@ __global__ void k_checkContactTimestep(const __grid_constant__ Params P) {
     float motion = __fmul_rn(dt, __fadd_rn(__fadd_rn(speed, __fmul_rn(r.body[id].z, spin)), 0.0f));
     bool finite = isfinite(rates.x) && isfinite(rates.y) && isfinite(motion) && isfinite(spin);
     if (!finite) { fail(r, F_NONFINITE); return; }
-    f3 rate = abs3(xyz(r.cell[1]));
+    f3 rate = abs3(xyz(r.cell[3 * specimenOf(r, id) + 1]));
     if (__fmul_rn(dt, __fsqrt_rn(rates.x)) > 0.1f || __fmul_rn(dt, rates.y) > 0.1f || __fmul_rn(dt, spin) > 0.01f ||
         motion > __fmul_rn(0.25f, c.skin) || __fmul_rn(rate.x, dt) > 0.01f || __fmul_rn(rate.y, dt) > 0.01f ||
         __fmul_rn(rate.z, dt) > 0.01f)
@@ -260,7 +264,7 @@ int launch_state(const std::string_view& name, const Params& P, uint32_t count, 
     uint32_t n = count ? count : 1;
     if (name == "beginStep") k_beginStep<<<blocks(n, T), T, 0, s>>>(P);
     else if (name == "captureContactKinematics") k_captureContactKinematics<<<blocks(n, T), T, 0, s>>>(P);
-    else if (name == "advanceCell") k_advanceCell<<<1, 1, 0, s>>>(P);
+    else if (name == "advanceCell") k_advanceCell<<<blocks(P.c.specimens, 64), 64, 0, s>>>(P);
     else if (name == "checkRebuild") k_checkRebuild<<<blocks(n, T), T, 0, s>>>(P);
     else if (name == "finishStep") k_finishStep<<<blocks(n, T), T, 0, s>>>(P);
     else if (name == "checkContactTimestep") k_checkContactTimestep<<<blocks(n, T), T, 0, s>>>(P);

@@ -33,7 +33,7 @@ EXTENSION_ORDER = (
     "byJPairs", "dpairBranch", "dpairLeafCount", "dpairCandOffset", "leafMask", "candidates",
     "candHitCount", "candHitOffset", "candHitMask", "contactPair", "sidePairOffsets", "sidePairB",
     "sideContactStart", "oldPairOffsets", "oldPairB", "oldContactStart", "work", "scanPartials",
-    "hitScratch", "candHitBase",
+    "hitScratch", "candHitBase", "dpairPlane", "grainSpecimen", "specimenBins",
 )
 BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
 # History side fields: (name bound as the side being written, name bound as committed).
@@ -134,8 +134,17 @@ class GB300Device:
 class Engine:
     """GPU-resident mesh-surface DEM engine (periodic, plane-free, mesh geometry)."""
 
+    @classmethod
+    def batch(cls, library, spec, specimens, **kwargs):
+        """Independent periodic specimens stepped together in one launch per
+        phase: ``specimens`` is a sequence of (positions, cell, shape_ids,
+        scales).  Per-specimen cell rates are set with ``advance(rate=...)``
+        given one row per specimen."""
+        layout = HostLayout.batch(library, spec, specimens)
+        return cls(library, spec, None, None, None, None, layout=layout, **kwargs)
+
     def __init__(self, library, spec, positions, cell, shape_ids, scales, *, metal=None, device=None,
-                 use_graph=True):
+                 use_graph=True, layout=None):
         torch = _torch()
         if metal is not None:
             raise ValueError("The GB300 engine owns its device; no adapter may be passed")
@@ -144,7 +153,8 @@ class Engine:
         self.lib = native.load()
         if self.lib.sdg_buffer_count() != len(BUFFER_ORDER):
             raise RuntimeError("GB300 library buffer ABI mismatch")
-        self.layout = h = HostLayout(library, spec, positions, cell, shape_ids, scales)
+        self.layout = h = layout or HostLayout(library, spec, positions, cell, shape_ids, scales)
+        self.specimens = h.specimens
         self.spec, self.library, self.n = spec, library, h.n
         self.viscous = spec.viscous
         self.wall_count = 0
@@ -183,7 +193,7 @@ class Engine:
             "candidates": 8 * self.candidate_capacity, "candHitCount": 4 * (self.candidate_capacity + 1),
             "candHitOffset": 4 * (self.candidate_capacity + 1), "candHitMask": 8 * self.candidate_capacity,
             "contactPair": 4 * cc, "work": 4 * 64, "scanPartials": 4 * 2 * SCAN_BLOCKS,
-            "hitScratch": 32 * cc, "candHitBase": 4 * self.candidate_capacity,
+            "hitScratch": 32 * cc, "candHitBase": 4 * self.candidate_capacity, "dpairPlane": 16 * 2 * pc,
         }
         for name, nbytes in sizes.items():
             self.buffers[name] = DeviceBuffer(self, nbytes)
@@ -241,7 +251,7 @@ class Engine:
 
     def _values(self, config):
         values = list(self.layout.config_values(config)) + [
-            float(self.leaf_words), float(self.candidate_capacity), 0.0
+            float(self.leaf_words), float(self.candidate_capacity), 0.0, float(self.specimens)
         ]
         return (ct.c_double * len(values))(*values), len(values)
 
@@ -295,7 +305,9 @@ class Engine:
 
         if type(steps) is not int or steps < 0:
             raise ValueError("Nonnegative integer step count required")
-        rate = finite_array(rate, (3,))
+        rate = finite_array(rate)
+        if rate.shape not in {(3,), (self.specimens, 3)}:
+            raise ValueError("Cell rate must be (3,) or one row per specimen")
         if not self.spec.periodic and np.any(rate != 0):
             raise ValueError("Affine cell rates require a periodic domain")
         if not np.isfinite(drag) or drag < 0:
@@ -323,9 +335,15 @@ class Engine:
                 log = self.capacity_retries + [
                     {"step": self.step, "flags": exc.flags, "new_capacities": settings}
                 ]
+                positions = state["position"][:, :3] * self.length_unit
+                starts = np.cumsum([0] + self.layout.counts)
+                specimens = [
+                    (positions[a:b], state["cell"][3 * k, :3] * self.length_unit, self.ids[a:b], self.scales[a:b])
+                    for k, (a, b) in enumerate(zip(starts[:-1], starts[1:]))
+                ]
                 replacement = Engine(
-                    self.library, replace(old, **settings), state["position"][:, :3] * self.length_unit,
-                    state["cell"][0, :3] * self.length_unit, self.ids, self.scales,
+                    self.library, replace(old, **settings), None, None, None, None,
+                    layout=HostLayout.batch(self.library, replace(old, **settings), specimens),
                     device=self.device, use_graph=self.use_graph,
                 )
                 replacement.initial_cell = self.initial_cell.copy()
@@ -371,9 +389,9 @@ class Engine:
             raise RuntimeError("Engine is invalid; restore a checkpoint")
         if steps < 1:
             return
-        cell = self.read("cell", np.float32, (3, 4))
+        cell = self.read("cell", np.float32, (3 * self.specimens, 4))
         original_cell = cell.copy()
-        cell[1, :3] = np.asarray(rate) * self.time_unit
+        cell[1::3, :3] = np.broadcast_to(np.asarray(rate, float), (self.specimens, 3)) * self.time_unit
         self.buffers["cell"].copy_from_numpy(cell)
         self._backup()
         original_active, original_history = self.active, self.history
@@ -409,7 +427,7 @@ class Engine:
         """Checkpoint arrays (``gpu.py:893-936``)."""
         out = {}
         for name in STATE_NAMES:
-            rows = 3 if name == "cell" else 2 if name == "cellLog" else self.n
+            rows = 3 * self.specimens if name == "cell" else 2 * self.specimens if name == "cellLog" else self.n
             out[name] = self.read(name, np.float32, (rows, 4))
         if self.viscous:
             for name in DAMPING_STATE:

@@ -106,14 +106,41 @@ def conservative_timestep(library, spec, ids, scales):
 
 
 class HostLayout:
-    """Units, per-grain rows, capacities and static geometry of one specimen."""
+    """Units, per-grain rows, capacities and static geometry of the grains.
 
-    def __init__(self, library, spec, positions, cell, shape_ids, scales):
+    One periodic specimen (the reference ``Engine``), or with
+    :meth:`batch` several independent specimens sharing one library and
+    material: grains concatenated, one cell per specimen, one bin grid per
+    specimen, one set of capacities for all.
+    """
+
+    @classmethod
+    def batch(cls, library, spec, specimens):
+        """``specimens``: sequence of (positions, cell, shape_ids, scales)."""
+        specimens = list(specimens)
+        if not specimens:
+            raise ValueError("At least one specimen required")
+        positions = np.concatenate([np.asarray(s[0], float) for s in specimens])
+        ids = np.concatenate([np.asarray(s[2], np.uint32) for s in specimens])
+        scales = np.concatenate([np.asarray(s[3], float) for s in specimens])
+        cells = np.array([finite_array(s[1], (3,), positive=True) for s in specimens])
+        counts = [len(s[0]) for s in specimens]
+        return cls(library, spec, positions, cells[0], ids, scales, cells=cells, counts=counts)
+
+    def __init__(self, library, spec, positions, cell, shape_ids, scales, *, cells=None, counts=None):
         positions = finite_array(positions)
         cell = finite_array(cell, (3,), positive=True)
+        if cells is None:
+            cells, counts = cell[None, :], [len(positions)]
+        self.cells = np.asarray(cells, float)
+        self.counts = list(counts)
+        self.specimens = len(self.counts)
+        if sum(self.counts) != len(positions) or len(self.cells) != self.specimens:
+            raise ValueError("Specimen grain counts and cells do not match the grains")
         if positions.ndim != 2 or positions.shape[1] != 3 or len(positions) < 1:
             raise ValueError("At least one three-dimensional position required")
-        if not spec.periodic and (np.any(positions < 0) or np.any(positions >= cell)):
+        self.grain_specimen = np.repeat(np.arange(self.specimens, dtype=np.uint32), self.counts)
+        if not spec.periodic and (np.any(positions < 0) or np.any(positions >= self.cells[self.grain_specimen])):
             raise ValueError("Nonperiodic particle centres must lie in [0, cell)")
         if spec.contact_geometry != "mesh":
             raise ValueError("The GB300 backend implements the mesh contact geometry only")
@@ -160,12 +187,17 @@ class HostLayout:
         self.invI = f4(inertia.reshape(-1, 3))
         self.skin = float(spec.skin * 2 * self.body[:, 2].max())
         self.cutoff = float(2 * self.body[:, 2].max() + self.skin)
-        box = np.asarray(cell, float) / l
-        if spec.periodic and self.cutoff >= 0.5 * box.min():
+        boxes = self.cells / l
+        if spec.periodic and self.cutoff >= 0.5 * boxes.min():
             raise ValueError("Cell too small for unique periodic images")
-        self.box = box
-        self.bins = np.maximum(1, np.minimum(64, np.floor(box / self.cutoff))).astype(np.uint32)
-        self.bin_count = int(self.bins.prod())
+        self.boxes = boxes
+        self.box = boxes[0]
+        bins = np.maximum(1, np.minimum(64, np.floor(boxes / self.cutoff))).astype(np.uint32)
+        self.specimen_bins = np.zeros((self.specimens, 4), np.uint32)
+        self.specimen_bins[:, :3] = bins
+        self.specimen_bins[1:, 3] = np.cumsum(bins.prod(axis=1))[:-1]
+        self.bins = bins[0]
+        self.bin_count = int(bins.prod(axis=1).sum())
         self.pair_capacity = max(1, self.n * spec.pairs_per_particle)
         self.contact_capacity = max(16, self.n * spec.contacts_per_particle)
         self.hash_size = 1 << math.ceil(math.log2(max(32, 2 * self.contact_capacity)))
@@ -268,9 +300,13 @@ class HostLayout:
             if name == "positionRemainder":
                 residual[:, :3] = p - p.astype(np.float32).astype(float)
             state[name] = residual
-        box = self.box
-        state["cell"] = np.array([list(box) + [0], [0, 0, 0, 0], list(box) + [0]], np.float32)
-        state["referenceCell"] = np.array([list(box) + [0], [0, 0, 0, self.cutoff]], np.float32)
+        state["cell"] = np.concatenate(
+            [np.array([list(b) + [0], [0, 0, 0, 0], list(b) + [0]], np.float32) for b in self.boxes])
+        state["referenceCell"] = np.concatenate(
+            [np.array([list(b) + [0], [0, 0, 0, self.cutoff]], np.float32) for b in self.boxes])
+        state["cellLog"] = np.zeros((2 * self.specimens, 4), np.float32)
+        state["grainSpecimen"] = self.grain_specimen.copy()
+        state["specimenBins"] = self.specimen_bins.copy()
         ctrl = np.zeros(16, np.uint32)
         ctrl[4] = 1
         state["control"] = ctrl

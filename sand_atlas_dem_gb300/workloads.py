@@ -188,6 +188,169 @@ def dense_packing(library, n, target, *, seed=42, scale_sigma=0.2, speedup=3.0, 
                 history=history, engine=e)
 
 
+def _write(engine, name, array):
+    buffer = engine.buffers[name]
+    if isinstance(buffer, np.ndarray):
+        buffer[...] = np.asarray(array, buffer.dtype).reshape(buffer.shape)
+    else:
+        buffer.copy_from_numpy(np.ascontiguousarray(array))
+
+
+def _read(engine, name, dtype, shape):
+    buffer = engine.buffers[name]
+    if isinstance(buffer, np.ndarray):
+        return buffer.reshape(-1).view(dtype)[: int(np.prod(shape))].reshape(shape).copy()
+    return engine.read(name, dtype, shape)
+
+
+def descent_packing(library, n, target, *, seed=42, scale_sigma=0.2, growth=1.003, overlap=0.03,
+                    max_evaluations=30_000, log=None, device=None, engine_cls=None):
+    """Seeded dense periodic packing by affine compression and force descent.
+
+    Starts from :func:`dilute_lattice` with random orientations.  Each round
+    shrinks the periodic cell (solid fraction x ``growth``, larger while the
+    packing is loose; centres scaled affinely) and then relaxes the grains
+    under their frictionless contact forces and torques of the exact
+    mesh-surface law (the engine's own force pass at zero timestep) by FIRE
+    on the centres with each grain's summed nodal contact stiffness as its
+    mass, plus a Jacobi rotation step, moves capped at 0.3% of a diameter,
+    until the deepest overlap is below ``overlap`` of a diameter.  The
+    perturbed grains are rough and jam below 0.58 when overlaps must stay
+    under 1%, so the dense benchmark packing uses a 3% tolerance.
+    """
+    from dataclasses import replace
+
+    positions, cell, ids, scales = dilute_lattice(library, n, seed=seed, scale_sigma=scale_sigma)
+    run = material_spec(library, ids, scales)
+    prep = replace(run, friction=0.0, normal_viscosity=0.0, timestep_policy="active-contact",
+                   max_overlap_fraction=0.5, contacts_per_particle=512)
+    if engine_cls is None:
+        from .engine import Engine
+
+        e = Engine(library, prep, positions, cell, ids, scales, device=device)
+    else:
+        e = engine_cls(library, prep, positions, cell, ids, scales)
+    l0 = e.length_unit
+    x = np.asarray(positions, float) / l0
+    box = np.asarray(cell, float) / l0
+    volume = sum(library.shapes[int(i)].volume * s**3 for i, s in zip(ids, scales)) / l0**3
+    config = e.config(dt=0, history=False)
+    evaluations = 0
+
+    def place():
+        x[:] = x - np.floor(x / box) * box
+        hi = x.astype(np.float32)
+        lo = (x - hi.astype(float)).astype(np.float32)
+        _write(e, "position", np.pad(hi, ((0, 0), (0, 1))))
+        _write(e, "positionRemainder", np.pad(lo, ((0, 0), (0, 1))))
+        rows = _read(e, "cell", np.float32, (3, 4))
+        rows[0, :3] = box
+        rows[2, :3] = box
+        rows[1] = 0
+        _write(e, "cell", rows)
+        _write(e, "cellLog", np.zeros((2, 4), np.float32))
+        ctrl = np.zeros(16, np.uint32)
+        ctrl[4] = 1
+        _write(e, "control", ctrl)
+
+    def contacts_of():
+        count = int(_read(e, "control", np.uint32, (16,))[2])
+        side = e.sides[e.active]
+        if isinstance(side["meta"], np.ndarray):
+            return side["meta"][:count].copy(), side["normalArea"][:count].copy()
+        return (e.m.read_prefix(side["meta"], 4 * count, np.uint32, shape=(count, 4)),
+                e.m.read_prefix(side["normalArea"], 4 * count, np.float32, shape=(count, 4)))
+
+    def forces():
+        nonlocal evaluations
+        place()
+        e.forces(config, capture_kinematics=False)
+        evaluations += 1
+        f = _read(e, "force", np.float32, (n, 4))
+        ctrl = _read(e, "control", np.uint32, (16,))
+        if int(ctrl[0]) & ~4:
+            from .model import RejectedStep
+
+            raise RejectedStep(ctrl[0])
+        meta, normal = contacts_of()
+        stiffness = np.zeros(n)
+        np.add.at(stiffness, meta[:, 0].astype(np.int64), 0.5 * normal[:, 3].astype(float))
+        np.add.at(stiffness, meta[:, 1].astype(np.int64), 0.5 * normal[:, 3].astype(float))
+        torque = _read(e, "torque", np.float32, (n, 4))[:, :3].astype(float)
+        return f[:, :3].astype(float), float(f[:, 3].max()), int(ctrl[2]), stiffness, torque
+
+    diameters = e.layout.body[:, 3].astype(float)
+    radii = e.layout.body[:, 2].astype(float)
+    cap = 0.003 * diameters
+    relax = 0.4
+    q = random_rotations(n, seed + 1).astype(float)
+    _write(e, "rotation", q.astype(np.float32))
+
+    def rotate(torque, stiffness):
+        # Jacobi rotation step about the torque: stiffness x radius^2.
+        angle = relax * torque / np.maximum(stiffness * radii**2, 1e-30)[:, None]
+        norm = np.linalg.norm(angle, axis=1)
+        angle *= np.minimum(1.0, 0.005 / np.maximum(norm, 1e-30))[:, None]
+        w = np.concatenate([0.5 * angle, np.zeros((n, 1))], axis=1)
+        # q' = q + 0.5 [angle, 0] (x) q, renormalized (world-frame spin).
+        a, b = w, q
+        prod = np.empty_like(q)
+        prod[:, :3] = a[:, 3:4] * b[:, :3] + b[:, 3:4] * a[:, :3] + np.cross(a[:, :3], b[:, :3])
+        prod[:, 3] = a[:, 3] * b[:, 3] - np.einsum("ij,ij->i", a[:, :3], b[:, :3])
+        q[:] = q + prod
+        q[:] = q / np.linalg.norm(q, axis=1)[:, None]
+        _write(e, "rotation", q.astype(np.float32))
+    history = []
+    phi = volume / np.prod(box)
+    # FIRE (Bitzek et al., PRL 97, 170201, 2006) on the centres, with each
+    # grain's summed contact stiffness as its mass (unit natural frequency),
+    # plus a Jacobi rotation step about the torque.
+    velocity = np.zeros((n, 3))
+    while True:
+        force, worst, contacts, stiffness, torque = forces()
+        inner = 0
+        dt, alpha, positive = 0.2, 0.1, 0
+        velocity[:] = 0
+        while worst > overlap:
+            if evaluations >= max_evaluations:
+                raise RuntimeError(f"descent did not converge within {max_evaluations} force evaluations")
+            mass = np.maximum(stiffness, 1e-3 * stiffness.max() if stiffness.max() > 0 else 1.0)
+            power = float(np.sum(force * velocity))
+            fnorm, vnorm = np.linalg.norm(force), np.linalg.norm(velocity)
+            if power > 0:
+                velocity = (1 - alpha) * velocity + alpha * vnorm * force / max(fnorm, 1e-30)
+                positive += 1
+                if positive > 5:
+                    dt, alpha = min(dt * 1.1, 1.0), alpha * 0.99
+            else:
+                velocity[:] = 0
+                dt, alpha, positive = dt * 0.5, 0.1, 0
+            velocity += dt * force / mass[:, None]
+            move = dt * velocity
+            norm = np.linalg.norm(move, axis=1)
+            move *= np.minimum(1.0, cap / np.maximum(norm, 1e-30))[:, None]
+            x += move
+            rotate(torque, stiffness)
+            force, worst, contacts, stiffness, torque = forces()
+            inner += 1
+        history.append(dict(phi=round(float(phi), 4), overlap=round(worst, 5), contacts=contacts, inner=inner,
+                            evaluations=evaluations))
+        if log and len(history) % 20 == 0:
+            log(history[-1])
+        if phi >= target * (1 - 1e-9):
+            break
+        # Larger increments while the packing is loose.
+        step = 1.05 if contacts == 0 else 1.01 if worst < 0.25 * overlap else growth
+        next_phi = min(target, phi * step)
+        factor = (phi / next_phi) ** (1 / 3)
+        x *= factor
+        box *= factor
+        phi = volume / np.prod(box)
+    _write(e, "velocity", np.zeros((n, 4), np.float32))
+    return dict(engine=e, ids=ids, scales=scales, history=history, evaluations=evaluations,
+                phi=float(phi), overlap=worst, spec=run)
+
+
 def save_packing(path, engine, ids, scales, meta):
     """Compact packing record: float64 centres, float32 orientations, cell."""
     state = engine.state()
@@ -245,15 +408,11 @@ def main(argv=None):
     start = time.perf_counter()
     meta = dict(library=args.library, grains=args.grains, solid_fraction=args.solid_fraction, seed=args.seed)
 
-    def checkpoint(engine):
-        save_packing(args.out + ".partial.npz", engine, engine.ids, engine.scales, dict(meta, partial=True))
-
-    out = dense_packing(library, args.grains, args.solid_fraction, seed=args.seed,
-                        log=lambda row: print(json.dumps(row), file=sys.stderr, flush=True),
-                        checkpoint=checkpoint)
-    meta.update(steps=out["steps"], seconds=round(time.perf_counter() - start, 1),
-                achieved_solid_fraction=solid_fraction(out["engine"]),
-                max_overlap_fraction=out["history"][-1]["overlap"] if out["history"] else 0.0)
+    out = descent_packing(library, args.grains, args.solid_fraction, seed=args.seed,
+                          log=lambda row: print(json.dumps(row), file=sys.stderr, flush=True))
+    meta.update(method="affine compression with frictionless force descent",
+                evaluations=out["evaluations"], seconds=round(time.perf_counter() - start, 1),
+                achieved_solid_fraction=out["phi"], max_overlap_fraction=out["overlap"])
     save_packing(args.out, out["engine"], out["ids"], out["scales"], meta)
     print(json.dumps(meta))
 

@@ -44,7 +44,7 @@ def test_buffer_and_value_counts(library):
     library.sdg_buffer_count.restype = ct.c_int
     library.sdg_value_count.restype = ct.c_int
     assert library.sdg_buffer_count() == buffers == len(BUFFER_ORDER) == len(RESOURCE_ORDER) + len(EXTENSION_ORDER)
-    assert library.sdg_value_count() == values == len(CONFIG_ORDER) + 3
+    assert library.sdg_value_count() == values == len(CONFIG_ORDER) + 4
     assert len(RESOURCE_ORDER) == 77
 
 
@@ -53,3 +53,10 @@ def test_argument_errors_are_reported_without_a_device(library):
     rc = lib.sdg_dispatch(b"beginStep", 1, None, None, None, 0, None)
     assert rc == 1
     assert b"buffers" in lib.sdg_last_error()
+
+
+def test_missing_library_fails_loudly(tmp_path, monkeypatch):
+    monkeypatch.setattr(native, "_LIB", None)
+    monkeypatch.setattr(native, "LIBRARY", tmp_path / "absent.so")
+    with pytest.raises(RuntimeError, match="not built"):
+        native.load()

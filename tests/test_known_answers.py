@@ -169,3 +169,30 @@ def test_strain_cell_and_drag(make):
     assert state["cell"][0, 0] * e.length_unit < 0.01
     accumulated = state["accumulated"]
     assert accumulated[:, 1].sum() > 0  # drag loss
+
+
+@pytest.mark.parametrize("make", ENGINES)
+def test_contact_capacity_growth_is_explicit_and_replays(make):
+    """``test_cpu_solver.py:518-549``: overflow grows capacity and retries."""
+    from sand_atlas_dem_gb300.shapes import ShapeLibrary, box_shape
+    from sand_atlas_dem_gb300.spec import Experiment
+    from sand_atlas_dem_gb300.shapes import surface_nodes
+
+    box = box_shape([1e-3] * 3)
+    v = box.vertices
+    samples, areas = surface_nodes(v, box.faces, 1024, 0)
+    box = box_shape([1e-3] * 3, nodes=(samples, areas))
+    spec = Experiment(particles=4, timestep=1e-9, contact_geometry="mesh", contacts_per_particle=16,
+                      pairs_per_particle=4, max_overlap_fraction=0.5)
+    positions = [[0.005] * 3, [0.00602, 0.005, 0.005], [0.005, 0.009, 0.005], [0.00602, 0.009, 0.005]]
+    e = make(ShapeLibrary([box]), spec, positions, [0.02] * 3, [0] * 4, [1] * 4)
+    e.initialize()
+    capacity = e.contact_capacity
+    velocity = np.zeros((4, 4), np.float32)
+    velocity[[1, 3], 0] = -0.00003 / spec.timestep * e.time_unit / e.length_unit
+    upload(e, "velocity", velocity)
+    if not hasattr(e, "capacity_retries"):
+        pytest.skip("the oracle engine does not grow capacities (reference host logic)")
+    e.advance(1)
+    assert e.state()["contacts"] > capacity
+    assert e.contact_capacity >= e.state()["contacts"] and e.capacity_retries
