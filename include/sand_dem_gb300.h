@@ -11,7 +11,7 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 106) this backend's extension buffers, in the order of
+ *   [77, 110) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
@@ -19,14 +19,17 @@
  *             counters, scan partials, the per-hit scratch, the first
  *             scratch slot of each item, per directed pair the target
  *             enclosure plane facing the source, the specimen of each
- *             grain and each specimen's bin grid).
+ *             grain and each specimen's bin grid, and the learned culler's
+ *             per-shape FP32 parameters, BF16 hidden weights, margins and
+ *             two counters).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
  * directed pair, (directed pair, leaf) item capacity, a flag that fuses
  * captureContactKinematics into beginStep, and the number of independent
  * periodic specimens batched in the buffers (cell rows 3 per specimen,
- * cellLog and referenceCell rows 2 per specimen; 1 = the reference case).
+ * cellLog and referenceCell rows 2 per specimen; 1 = the reference case),
+ * and whether the learned culler runs in front of the exact node query.
  *
  * Return codes: 0 success; 1 argument error; 2 CUDA error.  The message of
  * the last error on the calling thread is sdg_last_error().  Solver failures
@@ -43,8 +46,8 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 106
-#define SDG_VALUE_COUNT 29
+#define SDG_BUFFER_COUNT 110
+#define SDG_VALUE_COUNT 30
 #define SDG_PHASES 8
 
 /* ABI revision of this header. */
@@ -120,6 +123,38 @@ int sdg_engine_advance(void* engine, void* const* buffers, const uint64_t* bytes
  */
 int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes, const double* values,
                        uint32_t nvalues, float* phase_ms, void* stream);
+
+/*
+ * Learned culler (no reference counterpart): per-shape networks
+ * h0 = sin(W0 p + b0), h1 = relu(W1 h0 + b1), y = w2.h1 + b2 (64 wide)
+ * trained on exact signed distances.  sdg_culler_param_count() floats per
+ * shape.  sample: shell candidates labelled by the exact BVH distance;
+ * compact: keep accepted candidates in index order; train_step: one Adam
+ * step on every shape (forward/backward kernels); gradients: forward and
+ * backward only; round: BF16 hidden weights for inference; eval: FP32
+ * evaluation with BF16 hidden weights; tile_eval: the run-time tensor-core
+ * evaluation; inside_max: per-shape largest prediction at inside points
+ * (the calibrated margin, as an ordered integer).
+ */
+int sdg_culler_param_count(void);
+int sdg_culler_sample(void* const* buffers, const uint64_t* bytes, const double* values, uint32_t nvalues,
+                      uint32_t shapes, uint32_t count, uint32_t seed, float shell, uint32_t inside_only,
+                      void* out_points, void* accept, void* stream);
+int sdg_culler_compact(const void* points, const void* accept, const void* offsets, uint32_t shapes,
+                       uint32_t count, uint32_t capacity, void* out, void* stream);
+int sdg_culler_train_step(void* params, const void* points, uint32_t shapes, uint32_t points_per_shape,
+                          uint32_t batch, uint32_t step, uint32_t seed, float scale, float lr, void* grads,
+                          void* m, void* v, void* scratch, float* loss_out, void* stream);
+int sdg_culler_gradients(const void* params, const void* points, uint32_t shapes, uint32_t points_per_shape,
+                         uint32_t batch, uint32_t step, uint32_t seed, float scale, void* grads, void* scratch,
+                         void* stream);
+int sdg_culler_round(const void* params, void* w1_bf16, uint32_t shapes, void* stream);
+int sdg_culler_eval(const void* params, const void* w1_bf16, const void* points, uint32_t shapes, uint32_t count,
+                    void* out, void* stream);
+int sdg_culler_tile_eval(const void* params, const void* w1_bf16, const void* points, uint32_t shapes,
+                         uint32_t count, void* out, void* stream);
+int sdg_culler_inside_max(const void* points, const void* predictions, uint32_t shapes, uint32_t count,
+                          void* keys, void* stream);
 
 /* Kernel launches per captured step (0 before the first capture). */
 int sdg_engine_kernels_per_step(void* engine);

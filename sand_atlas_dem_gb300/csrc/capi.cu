@@ -46,6 +46,7 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
     c.wallCount = uint32_t(v[22]); c.wallBoxEnabled = uint32_t(v[23]); c.sourceSurfaceNormal = uint32_t(v[24]);
     c.leafWords = uint32_t(v[25]); c.candidateCapacity = uint32_t(v[26]); c.viscousCapture = uint32_t(v[27]);
     c.specimens = uint32_t(v[28]);
+    c.cullerEnabled = uint32_t(v[29]);
     if (c.specimens == 0) { g_error = "at least one specimen required"; return 1; }
     if (c.N == 0 || c.meshGeometry == 0 || c.wallCount != 0) {
         g_error = "the GB300 step needs N > 0, mesh geometry and no planes";
@@ -62,6 +63,11 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
         }
     }
     return 0;
+}
+
+int unpack_params(void* const* buffers, const uint64_t* bytes, const double* values, uint32_t nvalues,
+                  Params& P) {
+    return unpack(buffers, bytes, values, nvalues, P);
 }
 
 void launch_forces(const Params& P, cudaStream_t s, bool captureKinematics) {

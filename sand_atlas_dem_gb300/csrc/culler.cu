@@ -1,0 +1,363 @@
+// Learned conservative culler: one small signed-distance network per shape.
+//
+// Network (per shape s, coordinates in the shape frame, normalized units):
+//   h0 = sin(W0 p + b0)            64 Fourier features of the 3 coordinates
+//   h1 = relu(W1 h0 + b1)          64 -> 64
+//   y  = w2 . h1 + b2              predicted signed distance / shell width
+// Training data: points uniform in the shell |phi| <= shell around each
+// surface, labelled by the exact BVH distance (meshDistance, the same
+// function the contact query uses).  Training: full-batch-per-step mini
+// batches, mean squared error, Adam; FP32 master weights, every reduction in
+// a fixed order (bit-reproducible).  The culler never produces a force: a node
+// is skipped only when y exceeds a per-shape margin calibrated to be larger
+// than y at every sampled point inside the shape; every other node goes to
+// the exact query.
+//
+// All kernels are batched over shapes (blockIdx.y = shape).
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include "culler.cuh"
+#include "dem_device.cuh"
+#include "launch.h"
+
+namespace sdg {
+
+constexpr int H = 64;  // features and hidden width
+
+struct Net {  // per-shape parameter block, FP32, offsets in floats
+    static constexpr int W0 = 0, B0 = W0 + 3 * H, W1 = B0 + H, B1 = W1 + H * H, W2 = B1 + H, B2 = W2 + H,
+                         SIZE = B2 + 4;  // padded to 16 bytes
+};
+
+// Counter-based uniform in [0,1): a 32-bit mix of (seed, shape, index, axis).
+__device__ __forceinline__ float uniformHash(uint32_t seed, uint32_t shape, uint32_t index, uint32_t axis) {
+    uint32_t h = seed * 0x9E3779B9u ^ (shape * 0x85EBCA6Bu) ^ (index * 0xC2B2AE35u) ^ (axis * 0x27D4EB2Fu);
+    h ^= h >> 16; h *= 0x7FEB352Du; h ^= h >> 15; h *= 0x846CA68Bu; h ^= h >> 16;
+    return (h >> 8) * (1.0f / 16777216.0f);
+}
+
+// Candidate points uniform in the shape's root box grown by `shell`;
+// out[k] = (x, y, z, phi), accept[k] = |phi| <= shell (or phi <= 0 when
+// inside_only).  phi is the exact signed distance of the contact query.
+__global__ void k_shellCandidates(const __grid_constant__ Params P, uint32_t count, uint32_t seed, float shell,
+                                  uint32_t insideOnly, float4* out, uint32_t* accept) {
+    const Res& r = P.r;
+    uint32_t s = blockIdx.y;
+    uint32_t root = r.meshRoots[s].x;
+    f3 lo = xyz(r.meshMin[root]) - mk(shell, shell, shell), hi = xyz(r.meshMax[root]) + mk(shell, shell, shell);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        f3 u = mk(uniformHash(seed, s, k, 0), uniformHash(seed, s, k, 1), uniformHash(seed, s, k, 2));
+        f3 p = lo + u * (hi - lo);
+        float4 f = meshDistance(r, s, p, false);
+        size_t at = size_t(s) * count + k;
+        out[at] = w4(p, f.w);
+        accept[at] = insideOnly ? (f.w <= 0.0f) : (fabsf(f.w) <= shell);
+    }
+}
+// Stream compaction of accepted candidates in index order (exclusive scan
+// already in `offsets`), per shape, capped at `capacity` points.
+__global__ void k_compact(const float4* in, const uint32_t* accept, const uint32_t* offsets, uint32_t count,
+                          uint32_t capacity, float4* out) {
+    uint32_t s = blockIdx.y;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        size_t at = size_t(s) * count + k;
+        if (!accept[at]) continue;
+        uint32_t slot = offsets[at] - offsets[size_t(s) * count];
+        if (slot < capacity) out[size_t(s) * capacity + slot] = in[at];
+    }
+}
+
+// ---------------------------------------------------------------- network
+// Forward and backward of a batch: one thread per point, parameters of the
+// shape in shared memory, activations in registers.  Per-point gradient
+// contributions are written out; the parameter reductions are separate
+// fixed-order kernels.
+struct TrainArgs {
+    const float* params;       // shapes x Net::SIZE
+    const float4* points;      // shapes x pointsPerShape (x, y, z, phi)
+    uint32_t pointsPerShape, batch, step, seed;
+    float scale;               // target = phi / scale
+    float* dA1;                // shapes x batch x H   (dL/da1)
+    float* H0;                 // shapes x batch x H
+    float* dZ0;                // shapes x batch x H   (dL/dz0)
+    float* dY;                 // shapes x batch
+    float* H1;                 // shapes x batch x H
+    float* loss;               // shapes x batch       squared error per point
+    uint32_t* index;           // shapes x batch       sampled point of each row
+};
+
+__device__ __forceinline__ uint32_t batchIndex(const TrainArgs& a, uint32_t s, uint32_t i) {
+    uint32_t h = (a.step + 1) * 0x9E3779B9u ^ (i * 0x85EBCA6Bu) ^ (s * 0xC2B2AE35u) ^ a.seed;
+    h ^= h >> 16; h *= 0x7FEB352Du; h ^= h >> 15; h *= 0x846CA68Bu; h ^= h >> 16;
+    return h % a.pointsPerShape;
+}
+
+__global__ void __launch_bounds__(128) k_trainPoints(TrainArgs a) {
+    __shared__ float p[Net::SIZE];
+    uint32_t s = blockIdx.y;
+    const float* params = a.params + size_t(s) * Net::SIZE;
+    for (int k = threadIdx.x; k < Net::SIZE; k += blockDim.x) p[k] = params[k];
+    __syncthreads();
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.batch) return;
+    uint32_t pick = batchIndex(a, s, i);
+    float4 q = a.points[size_t(s) * a.pointsPerShape + pick];
+    size_t row = size_t(s) * a.batch + i;
+    a.index[row] = pick;
+    float h0[H], c0[H], h1[H];
+    for (int j = 0; j < H; ++j) {
+        float z = p[Net::W0 + 3 * j] * q.x + p[Net::W0 + 3 * j + 1] * q.y + p[Net::W0 + 3 * j + 2] * q.z + p[Net::B0 + j];
+        h0[j] = sinf(z);
+        c0[j] = cosf(z);
+    }
+    float y = p[Net::B2];
+    for (int j = 0; j < H; ++j) {
+        float acc = p[Net::B1 + j];
+        for (int k = 0; k < H; ++k) acc += p[Net::W1 + H * j + k] * h0[k];
+        h1[j] = acc > 0.f ? acc : 0.f;
+        y += p[Net::W2 + j] * h1[j];
+    }
+    float t = q.w / a.scale;
+    float err = y - t;
+    a.loss[row] = err * err;
+    float dy = 2.f * err / float(a.batch);
+    a.dY[row] = dy;
+    float dz[H];
+    for (int k = 0; k < H; ++k) dz[k] = 0.f;
+    for (int j = 0; j < H; ++j) {
+        float da = h1[j] > 0.f ? dy * p[Net::W2 + j] : 0.f;
+        a.dA1[row * H + j] = da;
+        a.H1[row * H + j] = h1[j];
+        for (int k = 0; k < H; ++k) dz[k] += da * p[Net::W1 + H * j + k];
+    }
+    for (int k = 0; k < H; ++k) {
+        a.H0[row * H + k] = h0[k];
+        a.dZ0[row * H + k] = dz[k] * c0[k];
+    }
+}
+
+// Parameter gradients, one thread per parameter, sums over the batch in row
+// order (deterministic).
+__global__ void k_trainGrads(TrainArgs a, float* grads) {
+    uint32_t s = blockIdx.y;
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= Net::SIZE) return;
+    size_t base = size_t(s) * a.batch;
+    float g = 0.f;
+    if (k < Net::B0) {  // W0[j][c]
+        uint32_t j = k / 3, c = k % 3;
+        for (uint32_t i = 0; i < a.batch; ++i) {
+            float4 q = a.points[size_t(s) * a.pointsPerShape + a.index[base + i]];
+            float coord = c == 0 ? q.x : (c == 1 ? q.y : q.z);
+            g += a.dZ0[(base + i) * H + j] * coord;
+        }
+    } else if (k < Net::W1) {
+        uint32_t j = k - Net::B0;
+        for (uint32_t i = 0; i < a.batch; ++i) g += a.dZ0[(base + i) * H + j];
+    } else if (k < Net::B1) {
+        uint32_t j = (k - Net::W1) / H, c = (k - Net::W1) % H;
+        for (uint32_t i = 0; i < a.batch; ++i) g += a.dA1[(base + i) * H + j] * a.H0[(base + i) * H + c];
+    } else if (k < Net::W2) {
+        uint32_t j = k - Net::B1;
+        for (uint32_t i = 0; i < a.batch; ++i) g += a.dA1[(base + i) * H + j];
+    } else if (k < Net::B2) {
+        uint32_t j = k - Net::W2;
+        for (uint32_t i = 0; i < a.batch; ++i) g += a.dY[base + i] * a.H1[(base + i) * H + j];
+    } else if (k == Net::B2) {
+        for (uint32_t i = 0; i < a.batch; ++i) g += a.dY[base + i];
+    }
+    grads[size_t(s) * Net::SIZE + k] = g;
+}
+
+// Adam (Kingma & Ba 2015) on every parameter of every shape.
+__global__ void k_adam(float* params, const float* grads, float* m, float* v, uint32_t total, float lr,
+                       float beta1, float beta2, float eps, uint32_t step) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= total) return;
+    float g = grads[k];
+    float mk1 = beta1 * m[k] + (1.f - beta1) * g;
+    float vk1 = beta2 * v[k] + (1.f - beta2) * g * g;
+    m[k] = mk1;
+    v[k] = vk1;
+    float mhat = mk1 / (1.f - powf(beta1, float(step)));
+    float vhat = vk1 / (1.f - powf(beta2, float(step)));
+    params[k] -= lr * mhat / (sqrtf(vhat) + eps);
+}
+
+// ------------------------------------------------------------- inference
+// Evaluation with the inference weights (W1 and the output row rounded to
+// BF16, FP32 accumulation): the exact function the culler applies in the
+// contact pass, here for calibration and tests.
+__device__ __forceinline__ float cullerEval(const float* p, const __nv_bfloat16* w1, float x, float y, float z) {
+    float h0[H];
+    for (int j = 0; j < H; ++j) {
+        float zz = p[Net::W0 + 3 * j] * x + p[Net::W0 + 3 * j + 1] * y + p[Net::W0 + 3 * j + 2] * z + p[Net::B0 + j];
+        h0[j] = __bfloat162float(__float2bfloat16(__sinf(zz)));
+    }
+    float out = p[Net::B2];
+    for (int j = 0; j < H; ++j) {
+        float acc = 0.f;
+        for (int k = 0; k < H; ++k) acc += __bfloat162float(w1[H * j + k]) * h0[k];
+        acc += p[Net::B1 + j];
+        out += p[Net::W2 + j] * (acc > 0.f ? acc : 0.f);
+    }
+    return out;
+}
+__global__ void k_cullerEval(const float* params, const __nv_bfloat16* w1, const float4* points, uint32_t count,
+                             float* out) {
+    uint32_t s = blockIdx.y;
+    const float* p = params + size_t(s) * Net::SIZE;
+    const __nv_bfloat16* w = w1 + size_t(s) * H * H;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        float4 q = points[size_t(s) * count + k];
+        out[size_t(s) * count + k] = cullerEval(p, w, q.x, q.y, q.z);
+    }
+}
+__global__ void k_roundWeights(const float* params, __nv_bfloat16* w1, uint32_t shapes) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= shapes * H * H) return;
+    uint32_t s = k / (H * H), e = k % (H * H);
+    w1[k] = __float2bfloat16(params[size_t(s) * Net::SIZE + Net::W1 + e]);
+}
+
+// The run-time culling function (tensor-core tile) on stored points: warp
+// per 64 points of shape blockIdx.y.
+__global__ void __launch_bounds__(256) k_cullerTileEval(const float* params, const uint32_t* w1, const float4* points,
+                                                         uint32_t count, float* out) {
+    __shared__ uint32_t tiles[8 * CULLER_TILE_WORDS];
+    uint32_t s = blockIdx.y, lane = threadIdx.x & 31u;
+    uint32_t* tile = tiles + (threadIdx.x >> 5) * CULLER_TILE_WORDS;
+    const float* p = params + size_t(s) * CULLER_PARAMS;
+    const uint32_t* w = w1 + size_t(s) * 2048;
+    uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t group = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); group * 64 < count; group += warps) {
+        uint32_t a = group * 64 + lane, b = a + 32;
+        float4 qa = a < count ? points[size_t(s) * count + a] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 qb = b < count ? points[size_t(s) * count + b] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float ya, yb;
+        cullerTile(p, w, xyz(qa), xyz(qb), tile, ya, yb);
+        if (a < count) out[size_t(s) * count + a] = ya;
+        if (b < count) out[size_t(s) * count + b] = yb;
+        __syncwarp();
+    }
+}
+__device__ __forceinline__ uint32_t orderedKey(float f) {
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+// Per shape: the largest prediction over points with phi <= 0 (inside).
+__global__ void k_insideMax(const float4* points, const float* y, uint32_t count, uint32_t* keys) {
+    uint32_t s = blockIdx.y;
+    uint32_t best = 0;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        size_t at = size_t(s) * count + k;
+        if (points[at].w <= 0.0f) best = max(best, orderedKey(y[at]));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if ((threadIdx.x & 31u) == 0 && best) atomicMax(&keys[s], best);
+}
+
+}  // namespace sdg
+
+using namespace sdg;
+
+extern "C" {
+
+int sdg_culler_param_count(void) { return Net::SIZE; }
+
+// Run-time culling predictions for stored points (shapes x count).
+int sdg_culler_tile_eval(const void* params, const void* w1_bf16, const void* points, uint32_t shapes,
+                         uint32_t count, void* out, void* stream) {
+    uint32_t groups = (count + 63) / 64;
+    dim3 grid((groups + 7) / 8 < 1024 ? (groups + 7) / 8 : 1024, shapes);
+    k_cullerTileEval<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float*>(params), static_cast<const uint32_t*>(w1_bf16), static_cast<const float4*>(points),
+        count, static_cast<float*>(out));
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+// Ordered-integer maximum of the predictions at inside points, per shape
+// (keys must be zeroed first; decode: k & 0x80000000 ? k ^ 0x80000000 : ~k).
+int sdg_culler_inside_max(const void* points, const void* predictions, uint32_t shapes, uint32_t count, void* keys,
+                          void* stream) {
+    dim3 grid((count + 255) / 256 < 256 ? (count + 255) / 256 : 256, shapes);
+    k_insideMax<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float4*>(points), static_cast<const float*>(predictions), count,
+        static_cast<uint32_t*>(keys));
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int sdg_culler_sample(void* const* buffers, const uint64_t* bytes, const double* values, uint32_t nvalues,
+                      uint32_t shapes, uint32_t count, uint32_t seed, float shell, uint32_t inside_only,
+                      void* out_points, void* accept, void* stream) {
+    Params P;
+    if (int rc = unpack_params(buffers, bytes, values, nvalues, P)) return rc;
+    dim3 grid((count + 255) / 256 < 512 ? (count + 255) / 256 : 512, shapes);
+    k_shellCandidates<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        P, count, seed, shell, inside_only, static_cast<float4*>(out_points), static_cast<uint32_t*>(accept));
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int sdg_culler_compact(const void* points, const void* accept, const void* offsets, uint32_t shapes,
+                       uint32_t count, uint32_t capacity, void* out, void* stream) {
+    dim3 grid((count + 255) / 256 < 512 ? (count + 255) / 256 : 512, shapes);
+    k_compact<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float4*>(points), static_cast<const uint32_t*>(accept),
+        static_cast<const uint32_t*>(offsets), count, capacity, static_cast<float4*>(out));
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+// One Adam step of every shape's network on a batch drawn from its points.
+// `scratch` holds 4*batch*64 + 3*batch floats per shape; `grads`, `m`, `v`
+// are shapes*param_count floats.
+int sdg_culler_train_step(void* params, const void* points, uint32_t shapes, uint32_t points_per_shape,
+                          uint32_t batch, uint32_t step, uint32_t seed, float scale, float lr, void* grads,
+                          void* m, void* v, void* scratch, float* loss_out, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    float* f = static_cast<float*>(scratch);
+    size_t rows = size_t(shapes) * batch;
+    TrainArgs a{static_cast<const float*>(params), static_cast<const float4*>(points), points_per_shape, batch,
+                step, seed, scale, f, f + rows * H, f + 2 * rows * H, f + 4 * rows * H, f + 3 * rows * H,
+                f + 4 * rows * H + rows, reinterpret_cast<uint32_t*>(f + 4 * rows * H + 2 * rows)};
+    k_trainPoints<<<dim3((batch + 127) / 128, shapes), 128, 0, s>>>(a);
+    k_trainGrads<<<dim3((Net::SIZE + 127) / 128, shapes), 128, 0, s>>>(a, static_cast<float*>(grads));
+    k_adam<<<(shapes * Net::SIZE + 255) / 256, 256, 0, s>>>(static_cast<float*>(params), static_cast<float*>(grads),
+                                                           static_cast<float*>(m), static_cast<float*>(v),
+                                                           shapes * Net::SIZE, lr, 0.9f, 0.999f, 1e-8f, step + 1);
+    if (loss_out) cudaMemcpyAsync(loss_out, a.loss, rows * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+// Forward and backward only (no update): per-parameter gradients of the mean
+// squared error for the batch of `step` (the gradient check entry).
+int sdg_culler_gradients(const void* params, const void* points, uint32_t shapes, uint32_t points_per_shape,
+                         uint32_t batch, uint32_t step, uint32_t seed, float scale, void* grads, void* scratch,
+                         void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    float* f = static_cast<float*>(scratch);
+    size_t rows = size_t(shapes) * batch;
+    TrainArgs a{static_cast<const float*>(params), static_cast<const float4*>(points), points_per_shape, batch,
+                step, seed, scale, f, f + rows * H, f + 2 * rows * H, f + 4 * rows * H, f + 3 * rows * H,
+                f + 4 * rows * H + rows, reinterpret_cast<uint32_t*>(f + 4 * rows * H + 2 * rows)};
+    k_trainPoints<<<dim3((batch + 127) / 128, shapes), 128, 0, s>>>(a);
+    k_trainGrads<<<dim3((Net::SIZE + 127) / 128, shapes), 128, 0, s>>>(a, static_cast<float*>(grads));
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int sdg_culler_round(const void* params, void* w1_bf16, uint32_t shapes, void* stream) {
+    k_roundWeights<<<(shapes * H * H + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float*>(params), static_cast<__nv_bfloat16*>(w1_bf16), shapes);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int sdg_culler_eval(const void* params, const void* w1_bf16, const void* points, uint32_t shapes, uint32_t count,
+                    void* out, void* stream) {
+    dim3 grid((count + 255) / 256 < 512 ? (count + 255) / 256 : 512, shapes);
+    k_cullerEval<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float*>(params), static_cast<const __nv_bfloat16*>(w1_bf16),
+        static_cast<const float4*>(points), count, static_cast<float*>(out));
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+}  // extern "C"

@@ -35,6 +35,7 @@ struct Config {
     uint32_t candidateCapacity;  // (directed pair, leaf cluster) work items
     uint32_t viscousCapture;     // fuse captureContactKinematics into beginStep
     uint32_t specimens;          // independent periodic specimens batched in one launch
+    uint32_t cullerEnabled;      // learned culler in front of the exact node query
 };
 
 // Buffers: the reference Resources block (solver.slang:20-100) in declaration
@@ -91,11 +92,16 @@ struct Res {
     float4* dpairPlane;               // 2*pairCapacity: enclosure plane of the target facing the source
     const uint32_t* grainSpecimen;    // N: specimen of each grain
     const uint4* specimenBins;        // specimens: bin grid x, y, z and first bin
+    const float* cullerParams;        // shapes x CULLER_PARAMS: FP32 network parameters
+    const uint32_t* cullerW1;         // shapes x 64 x 64 BF16 hidden weights (packed in pairs)
+    const float* cullerMargin;        // shapes: skip a node when the prediction exceeds this
+    uint32_t* cullerStats;            // 2 counters: nodes evaluated, nodes culled
 };
-constexpr int EXTENSION_COUNT = 29;
+constexpr int EXTENSION_COUNT = 33;
+constexpr int CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4;
 constexpr int BUFFER_COUNT = RESOURCE_COUNT + EXTENSION_COUNT;
 constexpr int CONFIG_VALUES = 25;
-constexpr int VALUE_COUNT = CONFIG_VALUES + 4;
+constexpr int VALUE_COUNT = CONFIG_VALUES + 5;
 constexpr int SCAN_BLOCKS = 608;  // 4 per SM on a 152-SM GB300
 // work[] slots
 constexpr int W_CANDIDATES = 0;

@@ -11,6 +11,7 @@
 // hits.  The history merge and the gather then walk sorted runs instead of a
 // hash table and linked lists, so every run is reproducible bit for bit.
 #include <cuda_runtime.h>
+#include "culler.cuh"
 #include "dem_device.cuh"
 #include "launch.h"
 
@@ -432,9 +433,11 @@ __global__ void k_leafEmit(const __grid_constant__ Params P) {
 // point/depth and normal/area are stored once in hitScratch at a slot taken
 // with one atomic per item; the emit pass copies them to canonical order.
 __global__ void __launch_bounds__(256) k_nodeQuery(const __grid_constant__ Params P) {
+    extern __shared__ uint32_t cullTiles[];
     const Res& r = P.r;
     const Config& c = P.c;
     uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
+    uint32_t* tile = cullTiles + (threadIdx.x >> 5) * CULLER_TILE_WORDS;
     for (uint32_t item = warpGlobal(); item < n; item += warpStride()) {
         // Leaves hold at most 64 nodes (packing splits larger sets), two per lane.
         bool hit0 = false, hit1 = false;
@@ -447,12 +450,34 @@ __global__ void __launch_bounds__(256) k_nodeQuery(const __grid_constant__ Param
             f3 branch = xyz(r.dpairBranch[d]);
             float4 plane = r.dpairPlane[d];
             uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
-            uint32_t k = laneId();
-            if (k < range.y)
-                hit0 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd0, na0, &plane);
-            k += WARP;
-            if (k < range.y)
-                hit1 = nodeContact(r, c, src, dst, __ldg(&r.meshSampleIndices[range.x + k]), branch, pd1, na1, &plane);
+            uint32_t k0 = laneId(), k1 = laneId() + WARP;
+            uint32_t node0 = k0 < range.y ? __ldg(&r.meshSampleIndices[range.x + k0]) : 0;
+            uint32_t node1 = k1 < range.y ? __ldg(&r.meshSampleIndices[range.x + k1]) : 0;
+            bool keep0 = k0 < range.y, keep1 = k1 < range.y;
+            if (c.cullerEnabled) {
+                // Learned culler: skip nodes the target's network places beyond
+                // its calibrated margin; every other node takes the exact query.
+                uint32_t sid = r.shapeId[src], target = r.shapeId[dst];
+                float4 qs = r.rotation[src], qd = r.rotation[dst];
+                float ss = r.body[src].x, sd = r.body[dst].x;
+                uint32_t base = __ldg(&r.sampleInfo[sid].x);
+                f3 l0 = qinv(qd, qrot(qs, xyz(__ldg(&r.sample[base + node0])) * ss) - branch) / sd;
+                f3 l1 = qinv(qd, qrot(qs, xyz(__ldg(&r.sample[base + node1])) * ss) - branch) / sd;
+                float y0, y1;
+                cullerTile(r.cullerParams + size_t(target) * CULLER_PARAMS, r.cullerW1 + size_t(target) * 2048, l0,
+                           l1, tile, y0, y1);
+                float margin = r.cullerMargin[target];
+                bool cut0 = keep0 && y0 > margin, cut1 = keep1 && y1 > margin;
+                uint32_t culled = __popc(__ballot_sync(0xffffffffu, cut0)) + __popc(__ballot_sync(0xffffffffu, cut1));
+                if (laneId() == 0) {
+                    atomicAdd(&r.cullerStats[0], range.y);
+                    atomicAdd(&r.cullerStats[1], culled);
+                }
+                keep0 = keep0 && !cut0;
+                keep1 = keep1 && !cut1;
+            }
+            if (keep0) hit0 = nodeContact(r, c, src, dst, node0, branch, pd0, na0, &plane);
+            if (keep1) hit1 = nodeContact(r, c, src, dst, node1, branch, pd1, na1, &plane);
         }
         uint32_t m0 = __ballot_sync(0xffffffffu, hit0), m1 = __ballot_sync(0xffffffffu, hit1);
         uint32_t hits = __popc(m0) + __popc(m1), base = 0;
@@ -776,7 +801,14 @@ static void collectCull(const Params& P, cudaStream_t s) {
     k_leafEmit<<<PERSISTENT, T, 0, s>>>(P);
 }
 static void collectQuery(const Params& P, cudaStream_t s) {
-    k_nodeQuery<<<PERSISTENT, 256, 0, s>>>(P);
+    size_t smem = P.c.cullerEnabled ? 8 * CULLER_TILE_WORDS * sizeof(uint32_t) : 0;
+    static bool attributed = false;
+    if (!attributed) {
+        cudaFuncSetAttribute(k_nodeQuery, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(8 * CULLER_TILE_WORDS * sizeof(uint32_t)));
+        attributed = true;
+    }
+    k_nodeQuery<<<PERSISTENT, 256, smem, s>>>(P);
 }
 // Canonical offsets of the hits, the contact records and per-pair starts.
 static void collectEmit(const Params& P, cudaStream_t s) {

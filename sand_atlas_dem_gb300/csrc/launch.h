@@ -7,6 +7,10 @@
 
 namespace sdg {
 
+// Buffer/value block to kernel parameters (capi.cu); 0 = ok.
+int unpack_params(void* const* buffers, const uint64_t* bytes, const double* values, uint32_t nvalues,
+                  Params& P);
+
 // Launch a reference-named kernel; 0 = launched, 1 = unknown name.
 int launch_state(const std::string_view& name, const Params& P, uint32_t count, cudaStream_t s);
 int launch_contacts(const std::string_view& name, const Params& P, uint32_t count, cudaStream_t s);

@@ -1,0 +1,189 @@
+"""Learned conservative culler for the exact node query (no reference counterpart).
+
+One small signed-distance network per shape,
+``h0 = sin(W0 p + b0)``, ``h1 = relu(W1 h0 + b1)``, ``y = w2 . h1 + b2``
+(3 -> 64 Fourier features -> 64 -> 1), trained on the GPU by this
+package's own forward/backward kernels (``csrc/culler.cu``) on points
+uniform in a shell of +-``shell`` around each surface, labelled by the exact
+BVH distance the contact query itself computes.  At run time the hidden
+layer runs on tensor cores (BF16 weights, FP32 accumulation, ``csrc/
+culler.cuh``) inside the node-query warps.
+
+Conservative by construction of its margin: a node is skipped only when its
+prediction exceeds the shape's margin, the largest prediction at any of
+(2 x points) sampled inside points (shell and deep interior, fresh seeds)
+plus ``slack``.  Every other node takes the exact query, which alone
+decides contacts and forces.  Missed contacts are counted against the exact
+path by the tests.
+"""
+
+import ctypes as ct
+
+import numpy as np
+
+from . import native
+
+H = 64
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _ptr(t):
+    return ct.c_void_p(t.data_ptr())
+
+
+class LearnedCuller:
+    """Per-shape networks for one engine's shape library."""
+
+    def __init__(self, engine, *, shell=0.3, points=1 << 20, steps=2000, batch=8192, lr=1e-3, seed=7,
+                 slack=0.02):
+        self.engine = engine
+        self.lib = native.load()
+        self.shapes = len(engine.library.shapes)
+        self.params_per_shape = self.lib.sdg_culler_param_count()
+        radii = np.array([s.radius for s in engine.library.shapes]) / engine.length_unit
+        self.shell = float(shell * np.median(radii))  # normalized units
+        self.points, self.steps, self.batch, self.lr, self.seed, self.slack = points, steps, batch, lr, seed, slack
+        torch = _torch()
+        self.device = engine.device
+        self.stream = engine.stream
+        self.params = torch.from_numpy(self.initial_params()).to(self.device)
+        self.w1 = torch.zeros(self.shapes * H * H, dtype=torch.int16, device=self.device)
+        self.margins = None
+        self.losses = []
+
+    def initial_params(self):
+        """Seeded initialization: Fourier frequencies N(0, (3/shell)^2 ... ) scaled to the shell."""
+        rng = np.random.default_rng(self.seed)
+        p = np.zeros((self.shapes, self.params_per_shape), np.float32)
+        w0 = 3 * H
+        for s in range(self.shapes):
+            p[s, :w0] = rng.normal(0.0, 1.0 / self.shell, w0)
+            p[s, w0:w0 + H] = rng.uniform(-np.pi, np.pi, H)
+            p[s, 256:256 + H * H] = rng.normal(0.0, np.sqrt(2.0 / H), H * H)
+            p[s, 256 + H * H + H:256 + H * H + 2 * H] = rng.normal(0.0, np.sqrt(1.0 / H), H)
+        return p
+
+    # ------------------------------------------------------------ data
+    def sample(self, count, seed, *, inside_only=False):
+        """``count`` accepted points per shape (x, y, z, phi), exact labels."""
+        torch = _torch()
+        e = self.engine
+        candidates = 4 * count
+        out = torch.zeros((self.shapes * candidates, 4), dtype=torch.float32, device=self.device)
+        accept = torch.zeros(self.shapes * candidates, dtype=torch.int32, device=self.device)
+        ptrs, sizes = e._arrays(e.active)
+        values, nv = e._values(e.config())
+        s = ct.c_void_p(self.stream.cuda_stream)
+        native.check(self.lib.sdg_culler_sample(ptrs, sizes, values, nv, self.shapes, candidates, seed,
+                                                self.shell, int(inside_only), _ptr(out), _ptr(accept), s))
+        offsets = torch.zeros(self.shapes * candidates, dtype=torch.int32, device=self.device)
+        partials = torch.zeros(self.lib.sdg_scan_partials(), dtype=torch.int32, device=self.device)
+        native.check(self.lib.sdg_exclusive_scan(_ptr(accept), _ptr(offsets), self.shapes * candidates, None,
+                                                 _ptr(partials), s))
+        points = torch.zeros((self.shapes * count, 4), dtype=torch.float32, device=self.device)
+        native.check(self.lib.sdg_culler_compact(_ptr(out), _ptr(accept), _ptr(offsets), self.shapes, candidates,
+                                                 count, _ptr(points), s))
+        self.stream.synchronize()
+        accepted = accept.view(self.shapes, candidates).sum(dim=1).cpu().numpy()
+        if accepted.min() < count:
+            raise RuntimeError(f"shell sampling accepted only {accepted.min()} of {count} points for a shape")
+        return points
+
+    # ---------------------------------------------------------- training
+    def train(self, log=None):
+        torch = _torch()
+        self.training_points = self.sample(self.points, self.seed)
+        n = self.shapes * self.params_per_shape
+        grads = torch.zeros(n, dtype=torch.float32, device=self.device)
+        m = torch.zeros_like(grads)
+        v = torch.zeros_like(grads)
+        rows = self.shapes * self.batch
+        scratch = torch.zeros(4 * rows * H + 3 * rows, dtype=torch.float32, device=self.device)
+        loss = torch.zeros(rows, dtype=torch.float32, device=self.device)
+        s = ct.c_void_p(self.stream.cuda_stream)
+        for step in range(self.steps):
+            lr = self.lr * (0.1 ** (step / max(1, self.steps)))
+            native.check(self.lib.sdg_culler_train_step(
+                _ptr(self.params), _ptr(self.training_points), self.shapes, self.points, self.batch, step,
+                self.seed, self.shell, lr, _ptr(grads), _ptr(m), _ptr(v), _ptr(scratch),
+                ct.cast(ct.c_void_p(loss.data_ptr()), ct.POINTER(ct.c_float)), s))
+            if step % 100 == 0 or step == self.steps - 1:
+                self.stream.synchronize()
+                mse = float(loss.view(self.shapes, self.batch).mean())
+                self.losses.append((step, mse))
+                if log:
+                    log(dict(step=step, mse=mse))
+        self.stream.synchronize()
+        return self.losses
+
+    def gradients(self, step=0):
+        """Parameter gradients of the mean squared error on batch ``step``."""
+        torch = _torch()
+        grads = torch.zeros(self.shapes * self.params_per_shape, dtype=torch.float32, device=self.device)
+        rows = self.shapes * self.batch
+        scratch = torch.zeros(4 * rows * H + 3 * rows, dtype=torch.float32, device=self.device)
+        native.check(self.lib.sdg_culler_gradients(
+            _ptr(self.params), _ptr(self.training_points), self.shapes, self.points, self.batch, step, self.seed,
+            self.shell, _ptr(grads), _ptr(scratch), ct.c_void_p(self.stream.cuda_stream)))
+        self.stream.synchronize()
+        index = scratch[4 * rows * H + 2 * rows:].view(torch.int32)[:rows].cpu().numpy().view(np.uint32)
+        return grads.view(self.shapes, -1).cpu().numpy(), index.reshape(self.shapes, self.batch)
+
+    # ------------------------------------------------------- calibration
+    def predict(self, points):
+        """Run-time (tensor-core) predictions for stored points (shapes x count)."""
+        torch = _torch()
+        count = points.shape[0] // self.shapes
+        out = torch.zeros(self.shapes * count, dtype=torch.float32, device=self.device)
+        native.check(self.lib.sdg_culler_tile_eval(_ptr(self.params), _ptr(self.w1), _ptr(points), self.shapes,
+                                                   count, _ptr(out), ct.c_void_p(self.stream.cuda_stream)))
+        self.stream.synchronize()
+        return out
+
+    def calibrate(self):
+        """Margin per shape: the largest run-time prediction at 2 x points fresh
+        inside samples (shell and whole interior), plus ``slack``."""
+        torch = _torch()
+        s = ct.c_void_p(self.stream.cuda_stream)
+        native.check(self.lib.sdg_culler_round(_ptr(self.params), _ptr(self.w1), self.shapes, s))
+        keys = torch.zeros(self.shapes, dtype=torch.int32, device=self.device)
+        for seed, inside in ((self.seed + 101, False), (self.seed + 202, True)):
+            pts = self.sample(self.points, seed, inside_only=inside)
+            pred = self.predict(pts)
+            native.check(self.lib.sdg_culler_inside_max(_ptr(pts), _ptr(pred), self.shapes, self.points,
+                                                        _ptr(keys), s))
+            if not inside:
+                self.validation = (pts, pred)
+        self.stream.synchronize()
+        k = keys.cpu().numpy().view(np.uint32)
+        bits = np.where(k & 0x80000000, k ^ 0x80000000, ~k).astype(np.uint32)
+        self.margins = bits.view(np.float32) + np.float32(self.slack)
+        return self.margins
+
+    def cull_rate(self):
+        """Fraction of validation shell points outside the shape that are culled."""
+        pts, pred = self.validation
+        phi = pts[:, 3].cpu().numpy().reshape(self.shapes, -1)
+        y = pred.cpu().numpy().reshape(self.shapes, -1)
+        outside = phi > 0
+        culled = (y > self.margins[:, None]) & outside
+        return float(culled.sum() / max(outside.sum(), 1))
+
+    def attach(self, engine=None):
+        """Install parameters, BF16 weights and margins in an engine's buffers."""
+        e = engine or self.engine
+        if self.margins is None:
+            self.calibrate()
+        e.buffers["cullerParams"].copy_from_numpy(self.params.cpu().numpy())
+        e.buffers["cullerW1"].copy_from_numpy(self.w1.cpu().numpy())
+        e.buffers["cullerMargin"].copy_from_numpy(self.margins.astype(np.float32))
+        e.culler = self
+        return e
+
+    def detach(self, engine=None):
+        (engine or self.engine).culler = None

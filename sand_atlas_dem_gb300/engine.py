@@ -33,8 +33,10 @@ EXTENSION_ORDER = (
     "byJPairs", "dpairBranch", "dpairLeafCount", "dpairCandOffset", "leafMask", "candidates",
     "candHitCount", "candHitOffset", "candHitMask", "contactPair", "sidePairOffsets", "sidePairB",
     "sideContactStart", "oldPairOffsets", "oldPairB", "oldContactStart", "work", "scanPartials",
-    "hitScratch", "candHitBase", "dpairPlane", "grainSpecimen", "specimenBins",
+    "hitScratch", "candHitBase", "dpairPlane", "grainSpecimen", "specimenBins", "cullerParams", "cullerW1",
+    "cullerMargin", "cullerStats",
 )
+CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4
 BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
 # History side fields: (name bound as the side being written, name bound as committed).
 SIDE_FIELDS = (
@@ -163,6 +165,7 @@ class Engine:
         self.active = 0
         self.capacity_retries = []
         self.use_graph = use_graph
+        self.culler = None
         for name in ("length_unit", "time_unit", "mass_unit", "force_unit", "stress_unit", "energy_unit",
                      "ids", "scales", "body", "skin", "cutoff", "bins", "bin_count", "pair_capacity",
                      "contact_capacity", "hash_size", "bin_capacity", "initial_cell"):
@@ -194,6 +197,8 @@ class Engine:
             "candHitOffset": 4 * (self.candidate_capacity + 1), "candHitMask": 8 * self.candidate_capacity,
             "contactPair": 4 * cc, "work": 4 * 64, "scanPartials": 4 * 2 * SCAN_BLOCKS,
             "hitScratch": 32 * cc, "candHitBase": 4 * self.candidate_capacity, "dpairPlane": 16 * 2 * pc,
+            "cullerParams": 4 * CULLER_PARAMS * len(library.shapes), "cullerW1": 2 * 4096 * len(library.shapes),
+            "cullerMargin": 4 * len(library.shapes), "cullerStats": 16,
         }
         for name, nbytes in sizes.items():
             self.buffers[name] = DeviceBuffer(self, nbytes)
@@ -251,7 +256,8 @@ class Engine:
 
     def _values(self, config):
         values = list(self.layout.config_values(config)) + [
-            float(self.leaf_words), float(self.candidate_capacity), 0.0, float(self.specimens)
+            float(self.leaf_words), float(self.candidate_capacity), 0.0, float(self.specimens),
+            float(self.culler is not None),
         ]
         return (ct.c_double * len(values))(*values), len(values)
 

@@ -16,7 +16,7 @@ PACKAGE = Path(__file__).resolve().parent
 CSRC = PACKAGE / "csrc"
 LIBDIR = PACKAGE / "_lib"
 LIBRARY = LIBDIR / "libsanddem_gb300.so"
-SOURCES = ("kernels_state.cu", "kernels_contacts.cu", "capi.cu")
+SOURCES = ("kernels_state.cu", "kernels_contacts.cu", "capi.cu", "culler.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false keeps the reference's FP32 operation order (no contraction);
 # division and square root stay IEEE (no fast math).
@@ -91,6 +91,24 @@ def load():
                                        ct.c_void_p]
     lib.sdg_exclusive_scan.restype = ct.c_int
     lib.sdg_scan_partials.restype = ct.c_int
+    V = ct.c_void_p
+    U = ct.c_uint32
+    F = ct.c_float
+    culler = {
+        "sdg_culler_param_count": [],
+        "sdg_culler_sample": [P(V), P(ct.c_uint64), P(ct.c_double), U, U, U, U, F, U, V, V, V],
+        "sdg_culler_compact": [V, V, V, U, U, U, V, V],
+        "sdg_culler_train_step": [V, V, U, U, U, U, U, F, F, V, V, V, V, V, V],
+        "sdg_culler_gradients": [V, V, U, U, U, U, U, F, V, V, V],
+        "sdg_culler_round": [V, V, U, V],
+        "sdg_culler_eval": [V, V, V, U, U, V, V],
+        "sdg_culler_tile_eval": [V, V, V, U, U, V, V],
+        "sdg_culler_inside_max": [V, V, U, U, V, V],
+    }
+    for name, args in culler.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ct.c_int
     lib.sdg_engine_kernels_per_step.argtypes = [ct.c_void_p]
     lib.sdg_engine_kernels_per_step.restype = ct.c_int
     _LIB = lib
@@ -116,6 +134,15 @@ EXPORTS = (
     "sdg_engine_kernels_per_step",
     "sdg_exclusive_scan",
     "sdg_scan_partials",
+    "sdg_culler_param_count",
+    "sdg_culler_sample",
+    "sdg_culler_compact",
+    "sdg_culler_train_step",
+    "sdg_culler_gradients",
+    "sdg_culler_round",
+    "sdg_culler_eval",
+    "sdg_culler_tile_eval",
+    "sdg_culler_inside_max",
 )
 PHASES = ("drift", "neighbours", "pair_cull", "node_query", "contact_emit", "friction_and_history",
           "force_reduction", "final_kick")
