@@ -44,7 +44,10 @@ __global__ void k_shellCandidates(const __grid_constant__ Params P, uint32_t cou
     const Res& r = P.r;
     uint32_t s = blockIdx.y;
     uint32_t root = r.meshRoots[s].x;
-    f3 lo = xyz(r.meshMin[root]) - mk(shell, shell, shell), hi = xyz(r.meshMax[root]) + mk(shell, shell, shell);
+    // Inside points come from the shape's own box; shell points from the box
+    // grown by the shell width.
+    float pad = insideOnly ? 0.0f : shell;
+    f3 lo = xyz(r.meshMin[root]) - mk(pad, pad, pad), hi = xyz(r.meshMax[root]) + mk(pad, pad, pad);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
         f3 u = mk(uniformHash(seed, s, k, 0), uniformHash(seed, s, k, 1), uniformHash(seed, s, k, 2));
         f3 p = lo + u * (hi - lo);

@@ -10,6 +10,7 @@
 """
 
 import json
+import time
 import math
 
 import numpy as np
@@ -136,7 +137,10 @@ def dense_packing(library, n, target, *, seed=42, scale_sigma=0.2, speedup=3.0, 
     from .engine import Engine
     from .model import RejectedStep
 
-    positions, cell, ids, scales = dilute_lattice(library, n, seed=seed, scale_sigma=scale_sigma)
+    if start is None:
+        positions, cell, ids, scales = dilute_lattice(library, n, seed=seed, scale_sigma=scale_sigma)
+    else:
+        positions, cell, ids, scales = start["positions"], start["cell"], start["ids"], start["scales"]
     run = material_spec(library, ids, scales)
     dt = run.timestep * speedup
     prep = replace(run, friction=0.0, timestep_policy="active-contact", timestep=dt,
@@ -203,8 +207,9 @@ def _read(engine, name, dtype, shape):
     return engine.read(name, dtype, shape)
 
 
-def descent_packing(library, n, target, *, seed=42, scale_sigma=0.2, growth=1.003, overlap=0.03,
-                    max_evaluations=30_000, log=None, device=None, engine_cls=None):
+def descent_packing(library, n, target, *, seed=42, scale_sigma=0.2, growth=1.003, overlap=0.05,
+                    max_evaluations=40_000, max_inner=400, log=None, device=None, engine_cls=None, start=None,
+                    max_seconds=None):
     """Seeded dense periodic packing by affine compression and force descent.
 
     Starts from :func:`dilute_lattice` with random orientations.  Each round
@@ -216,11 +221,19 @@ def descent_packing(library, n, target, *, seed=42, scale_sigma=0.2, growth=1.00
     mass, plus a Jacobi rotation step, moves capped at 0.3% of a diameter,
     until the deepest overlap is below ``overlap`` of a diameter.  The
     perturbed grains are rough and jam below 0.58 when overlaps must stay
-    under 1%, so the dense benchmark packing uses a 3% tolerance.
+    under 1%, so the dense benchmark packing uses a 5% tolerance (up to 8%
+    when a round's relaxation stalls after ``max_inner`` iterations).
+
+    ``start`` (a :func:`load_packing` record) resumes from a saved state.
+    When ``max_evaluations`` (or ``max_seconds``) is spent before ``target`` the result has
+    ``converged`` False and holds the state reached, for a later resume.
     """
     from dataclasses import replace
 
-    positions, cell, ids, scales = dilute_lattice(library, n, seed=seed, scale_sigma=scale_sigma)
+    if start is None:
+        positions, cell, ids, scales = dilute_lattice(library, n, seed=seed, scale_sigma=scale_sigma)
+    else:
+        positions, cell, ids, scales = start["positions"], start["cell"], start["ids"], start["scales"]
     run = material_spec(library, ids, scales)
     prep = replace(run, friction=0.0, normal_viscosity=0.0, timestep_policy="active-contact",
                    max_overlap_fraction=0.5, contacts_per_particle=512)
@@ -273,9 +286,9 @@ def descent_packing(library, n, target, *, seed=42, scale_sigma=0.2, growth=1.00
 
             raise RejectedStep(ctrl[0])
         meta, normal = contacts_of()
-        stiffness = np.zeros(n)
-        np.add.at(stiffness, meta[:, 0].astype(np.int64), 0.5 * normal[:, 3].astype(float))
-        np.add.at(stiffness, meta[:, 1].astype(np.int64), 0.5 * normal[:, 3].astype(float))
+        half = 0.5 * normal[:, 3].astype(float)
+        stiffness = (np.bincount(meta[:, 0].astype(np.int64), half, minlength=n)
+                     + np.bincount(meta[:, 1].astype(np.int64), half, minlength=n))
         torque = _read(e, "torque", np.float32, (n, 4))[:, :3].astype(float)
         return f[:, :3].astype(float), float(f[:, 3].max()), int(ctrl[2]), stiffness, torque
 
@@ -283,7 +296,7 @@ def descent_packing(library, n, target, *, seed=42, scale_sigma=0.2, growth=1.00
     radii = e.layout.body[:, 2].astype(float)
     cap = 0.003 * diameters
     relax = 0.4
-    q = random_rotations(n, seed + 1).astype(float)
+    q = (random_rotations(n, seed + 1) if start is None else start["rotations"]).astype(float)
     _write(e, "rotation", q.astype(np.float32))
 
     def rotate(torque, stiffness):
@@ -306,14 +319,19 @@ def descent_packing(library, n, target, *, seed=42, scale_sigma=0.2, growth=1.00
     # grain's summed contact stiffness as its mass (unit natural frequency),
     # plus a Jacobi rotation step about the torque.
     velocity = np.zeros((n, 3))
+    converged = True
+    deadline = time.perf_counter() + max_seconds if max_seconds else None
     while True:
         force, worst, contacts, stiffness, torque = forces()
         inner = 0
         dt, alpha, positive = 0.2, 0.1, 0
         velocity[:] = 0
         while worst > overlap:
-            if evaluations >= max_evaluations:
-                raise RuntimeError(f"descent did not converge within {max_evaluations} force evaluations")
+            if evaluations >= max_evaluations or (deadline and time.perf_counter() > deadline):
+                converged = False
+                break
+            if inner >= max_inner and worst < 1.6 * overlap:
+                break  # slow tail: accept and keep compressing
             mass = np.maximum(stiffness, 1e-3 * stiffness.max() if stiffness.max() > 0 else 1.0)
             power = float(np.sum(force * velocity))
             fnorm, vnorm = np.linalg.norm(force), np.linalg.norm(velocity)
@@ -337,7 +355,7 @@ def descent_packing(library, n, target, *, seed=42, scale_sigma=0.2, growth=1.00
                             evaluations=evaluations))
         if log and len(history) % 20 == 0:
             log(history[-1])
-        if phi >= target * (1 - 1e-9):
+        if phi >= target * (1 - 1e-9) or not converged:
             break
         # Larger increments while the packing is loose.
         step = 1.05 if contacts == 0 else 1.01 if worst < 0.25 * overlap else growth
@@ -348,7 +366,7 @@ def descent_packing(library, n, target, *, seed=42, scale_sigma=0.2, growth=1.00
         phi = volume / np.prod(box)
     _write(e, "velocity", np.zeros((n, 4), np.float32))
     return dict(engine=e, ids=ids, scales=scales, history=history, evaluations=evaluations,
-                phi=float(phi), overlap=worst, spec=run)
+                phi=float(phi), overlap=worst, spec=run, converged=converged and worst <= 1.6 * overlap)
 
 
 def save_packing(path, engine, ids, scales, meta):
@@ -392,7 +410,6 @@ def main(argv=None):
     """``python -m sand_atlas_dem_gb300.workloads prepare --grains N --out file.npz``."""
     import argparse
     import sys
-    import time
 
     from .shapes import synthetic_library
 
@@ -403,18 +420,28 @@ def main(argv=None):
     p.add_argument("--solid-fraction", type=float, default=0.58)
     p.add_argument("--seed", type=int, default=42)
     p.add_argument("--out", required=True)
+    p.add_argument("--resume", help="continue from a saved (partial) packing record")
+    p.add_argument("--max-evaluations", type=int, default=40_000)
+    p.add_argument("--max-seconds", type=float, default=None)
     args = p.parse_args(argv)
     library = synthetic_library(args.library)
     start = time.perf_counter()
     meta = dict(library=args.library, grains=args.grains, solid_fraction=args.solid_fraction, seed=args.seed)
 
-    out = descent_packing(library, args.grains, args.solid_fraction, seed=args.seed,
+    resume = load_packing(args.resume) if args.resume else None
+    before = resume["meta"] if resume else {}
+    out = descent_packing(library, args.grains, args.solid_fraction, seed=args.seed, start=resume,
+                          max_evaluations=args.max_evaluations, max_seconds=args.max_seconds,
                           log=lambda row: print(json.dumps(row), file=sys.stderr, flush=True))
     meta.update(method="affine compression with frictionless force descent",
-                evaluations=out["evaluations"], seconds=round(time.perf_counter() - start, 1),
+                evaluations=out["evaluations"] + before.get("evaluations", 0),
+                seconds=round(time.perf_counter() - start + before.get("seconds", 0), 1),
                 achieved_solid_fraction=out["phi"], max_overlap_fraction=out["overlap"])
-    save_packing(args.out, out["engine"], out["ids"], out["scales"], meta)
-    print(json.dumps(meta))
+    path = args.out if out["converged"] else args.out + ".partial.npz"
+    save_packing(path, out["engine"], out["ids"], out["scales"], meta)
+    print(json.dumps(dict(meta, converged=out["converged"], saved=path)))
+    if not out["converged"]:
+        sys.exit(3)
 
 
 if __name__ == "__main__":

@@ -64,7 +64,7 @@ def test_batch_matches_single_specimens(gpu_library):
         se = e.state()
         rows = slice(starts[k], starts[k + 1])
         mine = sb["meta"][(sb["meta"][:, 0] >= starts[k]) & (sb["meta"][:, 0] < starts[k + 1])].copy()
-        mine[:, :2] -= starts[k]
+        mine[:, :2] -= np.uint32(starts[k])
         key = lambda m: m[np.lexsort(m[:, :3].T[::-1])]  # noqa: E731
         np.testing.assert_array_equal(key(mine), key(se["meta"]))
         np.testing.assert_array_equal(sb["cell"][3 * k:3 * k + 3], se["cell"])
