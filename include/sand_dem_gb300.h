@@ -98,6 +98,21 @@ int sdg_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* 
 int sdg_scan_partials(void);
 
 /*
+ * The same scan with its block partials in a fixed array of this library
+ * (4,864 bytes per device) instead of caller scratch; it allocates nothing.
+ * No counterpart in the reference: it serves callers that hold only the
+ * buffers they were handed and no device allocator (a cgo, JNI or ctypes
+ * stub), or whose device-memory budget is fixed after set-up.  The first call
+ * on a device, with that device current, looks the array up; it must come
+ * before any stream capture on that device.  n above SDG_SCAN_STATIC_MAX_N is
+ * rejected (returns 1, text in sdg_last_error).  Nothing needs zeroing
+ * beforehand.  Calls in flight at the same time on one device share the
+ * array and race: issue them on one stream.
+ */
+#define SDG_SCAN_STATIC_MAX_N (1u << 30)
+int sdg_exclusive_scan_static(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total, void* stream);
+
+/*
  * Engine handle holding the captured CUDA graphs of one step for each
  * history-side orientation.  Replaces the per-chunk command encoder of
  * Engine._advance_once (gpu.py:672-744): one graph launch per step.

@@ -20,6 +20,8 @@ namespace sdg {
 
 static thread_local std::string g_error;
 
+void set_last_error(const std::string& what) { g_error = what; }
+
 static int record(cudaError_t e, const char* where) {
     if (e == cudaSuccess) return 0;
     g_error = std::string(where) + ": " + cudaGetErrorString(e);

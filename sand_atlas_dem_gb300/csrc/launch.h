@@ -1,6 +1,7 @@
 // Host launchers shared by the kernel translation units and the C ABI.
 #pragma once
 #include <cstdint>
+#include <string>
 #include <string_view>
 #include <cuda_runtime.h>
 #include "dem_device.cuh"
@@ -10,6 +11,9 @@ namespace sdg {
 // Buffer/value block to kernel parameters (capi.cu); 0 = ok.
 int unpack_params(void* const* buffers, const uint64_t* bytes, const double* values, uint32_t nvalues,
                   Params& P);
+
+// Sets the text sdg_last_error returns on this thread (capi.cu).
+void set_last_error(const std::string& what);
 
 // Launch a reference-named kernel; 0 = launched, 1 = unknown name.
 int launch_state(const std::string_view& name, const Params& P, uint32_t count, cudaStream_t s);

@@ -16,7 +16,7 @@ PACKAGE = Path(__file__).resolve().parent
 CSRC = PACKAGE / "csrc"
 LIBDIR = PACKAGE / "_lib"
 LIBRARY = LIBDIR / "libsanddem_gb300.so"
-SOURCES = ("kernels_state.cu", "kernels_contacts.cu", "capi.cu", "culler.cu")
+SOURCES = ("kernels_state.cu", "kernels_contacts.cu", "capi.cu", "culler.cu", "scan_static.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false keeps the reference's FP32 operation order (no contraction);
 # division and square root stay IEEE (no fast math).
@@ -91,6 +91,8 @@ def load():
                                        ct.c_void_p]
     lib.sdg_exclusive_scan.restype = ct.c_int
     lib.sdg_scan_partials.restype = ct.c_int
+    lib.sdg_exclusive_scan_static.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_uint32, ct.c_void_p, ct.c_void_p]
+    lib.sdg_exclusive_scan_static.restype = ct.c_int
     V = ct.c_void_p
     U = ct.c_uint32
     F = ct.c_float
@@ -134,6 +136,7 @@ EXPORTS = (
     "sdg_engine_kernels_per_step",
     "sdg_exclusive_scan",
     "sdg_scan_partials",
+    "sdg_exclusive_scan_static",
     "sdg_culler_param_count",
     "sdg_culler_sample",
     "sdg_culler_compact",
