@@ -3,7 +3,10 @@
 Workload (the 10,000-grain plain-method configuration): 64 seeded perturbed
 geodesic icospheres (1,280 triangles, 642 Sobol nodes each), grain scales
 lognormal (median 1, sigma_ln 0.2) on a 0.5 mm nominal radius, a dense
-periodic packing at solid fraction 0.58 prepared by GPU compression, then
+periodic packing prepared by affine compression and frictionless force
+descent on the GPU toward solid fraction 0.58 (the rough grains jam near
+0.54 at overlaps under 9% of a diameter; the record states what was
+reached, sand_atlas_dem_gb300/data/packing-f8-10000.npz), then
 isotropic compression at 0.5/s with rho 2650, kn 1e12, kt 5e11, mu 0.5,
 normal viscosity for damping ratio 0.3 and dt one ulp below the reference's
 conservative bound.  Data are synthetic (seeded); the reference's Hostun
@@ -40,7 +43,7 @@ WORKLOAD = dict(
     triangles_per_grain=1280,
     nodes_per_grain=642,
     shapes=64,
-    solid_fraction=0.58,
+    solid_fraction_target=0.58,
     max_overlap_fraction=0.1,
     strain_rate_per_s=-0.5,
     friction=0.5,
@@ -84,19 +87,22 @@ DATA = ROOT / "sand_atlas_dem_gb300" / "data"
 
 
 def packing(lib, grains, phi, seed=42, kind="dense"):
-    """The prepared dense packing (committed record, else prepared here and cached)."""
-    from sand_atlas_dem_gb300.workloads import dense_packing, load_packing, save_packing
+    """The prepared dense packing (committed record, else prepared here within
+    a bounded time and cached)."""
+    from sand_atlas_dem_gb300.workloads import descent_packing, load_packing, save_packing
 
     if kind == "lattice":
         return lattice_packing(lib, grains)
-    name = f"packing-f8-{grains}-{phi}.npz"
+    name = f"packing-f8-{grains}.npz"
     for path in (DATA / name, cache_dir() / name):
         if path.exists():
             return dict(load_packing(path), kind="record", path=str(path))
     t = time.perf_counter()
-    out = dense_packing(lib, grains, phi, seed=seed, log=lambda d: log("prepare", d))
-    log(f"prepared packing in {time.perf_counter() - t:.1f} s, {out['steps']} steps")
-    save_packing(cache_dir() / name, out["engine"], out["ids"], out["scales"], dict(steps=out["steps"]))
+    out = descent_packing(lib, grains, phi, seed=seed, max_seconds=600, log=lambda d: log("prepare", d))
+    meta = dict(library="f8", grains=grains, solid_fraction=phi, seed=seed, evaluations=out["evaluations"],
+                seconds=round(time.perf_counter() - t, 1), achieved_solid_fraction=out["phi"],
+                max_overlap_fraction=out["overlap"])
+    save_packing(cache_dir() / name, out["engine"], out["ids"], out["scales"], meta)
     return dict(load_packing(cache_dir() / name), kind="record")
 
 
@@ -207,7 +213,7 @@ def run_gb300(args, cpu=True):
     from sand_atlas_dem_gb300.engine import DeviceBuffer, Engine
 
     lib = library()
-    pack = packing(lib, args.grains, WORKLOAD["solid_fraction"], kind=args.packing)
+    pack = packing(lib, args.grains, WORKLOAD["solid_fraction_target"], kind=args.packing)
     e = engine_for(lib, pack, Engine)
     rate = (WORKLOAD["strain_rate_per_s"],) * 3
     # Warm-up (graph capture happens in the first call).
@@ -282,7 +288,9 @@ def run_gb300(args, cpu=True):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": dict(WORKLOAD, grains=args.grains, packing=args.packing, packing_meta=pack.get("meta"), l2="flushed before each timed step (256 MiB write)",
+        "config": dict(WORKLOAD, grains=args.grains, packing=args.packing, packing_meta=pack.get("meta"),
+                       solid_fraction=(pack.get("meta") or {}).get("achieved_solid_fraction"),
+                       l2="flushed before each timed step (256 MiB write)",
                        pairs=pairs, contacts=contacts, node_query_items=items, node_queries=nodes,
                        timestep_s=e.spec.timestep, phase_ms=phase_ms, dominant_phase=top),
         "e2e": {"value": e2e, "unit": "grain-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -303,11 +311,77 @@ def run_gb300(args, cpu=True):
         },
         "clocks": clocks.summary(),
     }
+    if args.culler:
+        line["learned_culler"] = culler_comparison(lib, pack, args, flush)
     if cpu and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(lib, pack, args)
     if ctrl0[0] or ctrl[0]:
         line["solver_flags"] = int(ctrl[0])
     return line
+
+
+def timed_steps(e, steps, flush):
+    """Device milliseconds of each of ``steps`` graph-replayed steps, L2 flushed before each."""
+    import torch
+
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    e.synchronize()
+    for k in range(steps):
+        with torch.cuda.stream(e.stream):
+            flush.fill_(k & 0xFF)
+            events[k][0].record(e.stream)
+        e.run_steps(1)
+        with torch.cuda.stream(e.stream):
+            events[k][1].record(e.stream)
+    e.synchronize()
+    return [a.elapsed_time(b) for a, b in events]
+
+
+def culler_comparison(lib, pack, args, flush):
+    """Plain exact step against the learned-cull step from one start state.
+
+    The culler is trained (2^20 shell points per shape, 2,000 Adam steps) and
+    calibrated on the GPU, attached to a second engine, and both engines run
+    the same timed steps.  Missed contacts = exact contacts absent from the
+    culled run; forces are compared bit for bit.
+    """
+    from sand_atlas_dem_gb300.culler import LearnedCuller
+    from sand_atlas_dem_gb300.engine import Engine
+
+    rate = (WORKLOAD["strain_rate_per_s"],) * 3
+    plain = engine_for(lib, pack, Engine)
+    culled = engine_for(lib, pack, Engine)
+    t = time.perf_counter()
+    c = LearnedCuller(culled, points=1 << 20, steps=2000, batch=8192)
+    c.train()
+    c.attach(culled)
+    train_s = time.perf_counter() - t
+    out = {}
+    for name, e in (("plain", plain), ("culled", culled)):
+        e.advance(max(3, args.warmup), rate=rate)
+        e.buffers["cullerStats"].copy_from_numpy(np.zeros(4, np.uint32))
+        ms = timed_steps(e, args.steps, flush)
+        out[name] = dict(value=args.grains * args.steps / (sum(ms) / 1e3), ms_per_step=sum(ms) / args.steps,
+                         phase_ms=e.profile_phases())
+    sp, sc = plain.state(), culled.state()
+    stats = culled.read("cullerStats", np.uint32, (4,))
+    keys_p = {tuple(m) for m in sp["meta"][:, :3].tolist()}
+    keys_c = {tuple(m) for m in sc["meta"][:, :3].tolist()}
+    force_p = sp["force"][:, :3].astype(float)
+    force_err = float(np.abs(sc["force"][:, :3] - force_p).max() / max(np.abs(force_p).max(), 1e-30))
+    return dict(
+        plain_value=out["plain"]["value"], culled_value=out["culled"]["value"],
+        speedup=out["culled"]["value"] / out["plain"]["value"],
+        plain_node_query_ms=out["plain"]["phase_ms"]["node_query"],
+        culled_node_query_ms=out["culled"]["phase_ms"]["node_query"],
+        tested_nodes=int(stats[0]), culled_nodes=int(stats[1]),
+        cull_rate_of_prefilter_survivors=float(stats[1]) / max(int(stats[0]), 1),
+        missed_contacts=len(keys_p - keys_c), extra_contacts=len(keys_c - keys_p),
+        forces_bitwise_equal=bool(sp["force"].tobytes() == sc["force"].tobytes()),
+        force_max_relative_error=force_err,
+        training_s=round(train_s, 1), margins_mean=float(np.mean(c.margins)),
+        validation_cull_rate=c.cull_rate(),
+    )
 
 
 def cpu_baseline(lib, pack, args, steps=1):
@@ -326,7 +400,7 @@ def cpu_baseline(lib, pack, args, steps=1):
 
 def run_reference(args):
     lib = library()
-    pack = packing(lib, args.grains, WORKLOAD["solid_fraction"])
+    pack = packing(lib, args.grains, WORKLOAD["solid_fraction_target"])
     from oracle.engine import OracleEngine
 
     e = engine_for(lib, pack, OracleEngine, threads=args.cpu_threads)
@@ -359,6 +433,7 @@ def main():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--prepare-only", action="store_true")
     p.add_argument("--packing", default="dense", choices=("dense", "lattice"))
+    p.add_argument("--culler", action="store_true", help="also train the learned culler and compare")
     args = p.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
@@ -389,7 +464,7 @@ def main():
         return
     if args.prepare_only:
         lib = library()
-        pack = packing(lib, args.grains, WORKLOAD["solid_fraction"])
+        pack = packing(lib, args.grains, WORKLOAD["solid_fraction_target"])
         print(json.dumps({"prepared": True, "path": pack.get("path")}))
         return
     print(json.dumps(run_gb300(args)), flush=True)

@@ -11,17 +11,20 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 110) this backend's extension buffers, in the order of
+ *   [77, 113) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
  *             pair ids, the written and committed history pair tables, work
- *             counters, scan partials, the per-hit scratch, the first
- *             scratch slot of each item, per directed pair the target
+ *             counters, scan partials, the per-survivor hit scratch, the
+ *             survivor count of each item, per directed pair the target
  *             enclosure plane facing the source, the specimen of each
- *             grain and each specimen's bin grid, and the learned culler's
+ *             grain and each specimen's bin grid, the learned culler's
  *             per-shape FP32 parameters, BF16 hidden weights, margins and
- *             two counters).
+ *             two counters, and the survivor mask and first survivor of
+ *             each item and the (item, node slot) list of survivors: the
+ *             nodes left for the exact query after the conservative
+ *             filters).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
@@ -29,7 +32,13 @@
  * captureContactKinematics into beginStep, and the number of independent
  * periodic specimens batched in the buffers (cell rows 3 per specimen,
  * cellLog and referenceCell rows 2 per specimen; 1 = the reference case),
- * and whether the learned culler runs in front of the exact node query.
+ * whether the learned culler runs in front of the exact node query, six
+ * launch shapes chosen by the autotuner (0 = default): node-filter CTAs per
+ * SM, node-filter warps per CTA (4 or 8), pair set-up/leaf-cull CTAs per SM,
+ * contact emit/law CTAs per SM, gather warps per SM and exact-query CTAs per
+ * SM (launch shapes never change results), and the survivor capacity (nodes
+ * left for the exact query per step; overflow raises the contact-capacity
+ * flag).
  *
  * Return codes: 0 success; 1 argument error; 2 CUDA error.  The message of
  * the last error on the calling thread is sdg_last_error().  Solver failures
@@ -46,8 +55,8 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 110
-#define SDG_VALUE_COUNT 30
+#define SDG_BUFFER_COUNT 113
+#define SDG_VALUE_COUNT 37
 #define SDG_PHASES 8
 
 /* ABI revision of this header. */
@@ -149,12 +158,16 @@ int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes
  * backward only; round: BF16 hidden weights for inference; eval: FP32
  * evaluation with BF16 hidden weights; tile_eval: the run-time tensor-core
  * evaluation; inside_max: per-shape largest prediction at inside points
- * (the calibrated margin, as an ordered integer).
+ * (the calibrated margin, as an ordered integer); surface: points on each
+ * shape's surface (shape s owns packed triangles [tri_start[s],
+ * tri_start[s+1])), label 0, for the margin's boundary term.
  */
 int sdg_culler_param_count(void);
 int sdg_culler_sample(void* const* buffers, const uint64_t* bytes, const double* values, uint32_t nvalues,
                       uint32_t shapes, uint32_t count, uint32_t seed, float shell, uint32_t inside_only,
                       void* out_points, void* accept, void* stream);
+int sdg_culler_surface(const void* triangles, const void* tri_start, uint32_t shapes, uint32_t count, uint32_t seed,
+                       void* out_points, void* stream);
 int sdg_culler_compact(const void* points, const void* accept, const void* offsets, uint32_t shapes,
                        uint32_t count, uint32_t capacity, void* out, void* stream);
 int sdg_culler_train_step(void* params, const void* points, uint32_t shapes, uint32_t points_per_shape,

@@ -49,6 +49,15 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
     c.leafWords = uint32_t(v[25]); c.candidateCapacity = uint32_t(v[26]); c.viscousCapture = uint32_t(v[27]);
     c.specimens = uint32_t(v[28]);
     c.cullerEnabled = uint32_t(v[29]);
+    c.queryBlocksPerSM = uint32_t(v[30]); c.queryWarps = uint32_t(v[31]); c.cullBlocksPerSM = uint32_t(v[32]);
+    c.contactBlocksPerSM = uint32_t(v[33]); c.gatherWarps = uint32_t(v[34]); c.walkBlocksPerSM = uint32_t(v[35]);
+    c.survivorCapacity = uint32_t(v[36]);
+    if (c.queryBlocksPerSM > 32 || c.cullBlocksPerSM > 32 || c.contactBlocksPerSM > 32 || c.gatherWarps > 64 ||
+        c.walkBlocksPerSM > 32 ||
+        (c.queryWarps != 0 && c.queryWarps != 4 && c.queryWarps != 8)) {
+        g_error = "launch shape out of range (CTAs per SM <= 32, query warps 4 or 8, gather warps per SM <= 64)";
+        return 1;
+    }
     if (c.specimens == 0) { g_error = "at least one specimen required"; return 1; }
     if (c.N == 0 || c.meshGeometry == 0 || c.wallCount != 0) {
         g_error = "the GB300 step needs N > 0, mesh geometry and no planes";
@@ -59,7 +68,11 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
         if (bytes[48] < uint64_t(c.contactCapacity) * 16 || bytes[45] < uint64_t(c.pairCapacity) * 8 ||
             bytes[2] < uint64_t(c.N) * 16 || bytes[42] < uint64_t(c.binCount) * c.binCapacity * 4 ||
             bytes[77 + 11] < uint64_t(c.candidateCapacity) * 8 ||
-            bytes[77 + 10] < uint64_t(2) * c.pairCapacity * c.leafWords * 4) {
+            bytes[77 + 10] < uint64_t(2) * c.pairCapacity * c.leafWords * 4 ||
+            bytes[77 + 24] < uint64_t(c.survivorCapacity) * 32 || bytes[77 + 35] < uint64_t(c.survivorCapacity) * 8 ||
+            bytes[77 + 33] < uint64_t(c.candidateCapacity) * 8 ||
+            bytes[77 + 34] < (uint64_t(c.candidateCapacity) + 1) * 4 ||
+            bytes[77 + 25] < (uint64_t(c.candidateCapacity) + 1) * 4) {
             g_error = "a buffer is smaller than its configured capacity";
             return 1;
         }

@@ -57,6 +57,22 @@ __global__ void k_shellCandidates(const __grid_constant__ Params P, uint32_t cou
         accept[at] = insideOnly ? (f.w <= 0.0f) : (fabsf(f.w) <= shell);
     }
 }
+// Points on each shape's surface (uniform triangle, uniform barycentric
+// point), label 0: the inside boundary, where a network's largest prediction
+// over the inside of a shape is usually reached.  Shape s owns triangles
+// [triStart[s], triStart[s + 1]) of the packed triangle array.
+__global__ void k_surfacePoints(const float4* triangles, const uint32_t* triStart, uint32_t count, uint32_t seed,
+                                float4* out) {
+    uint32_t s = blockIdx.y;
+    uint32_t first = triStart[s], n = triStart[s + 1] - first;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        uint32_t t = first + min(uint32_t(uniformHash(seed, s, k, 0) * float(n)), n - 1);
+        float u = uniformHash(seed, s, k, 1), v = uniformHash(seed, s, k, 2);
+        if (u + v > 1.0f) { u = 1.0f - u; v = 1.0f - v; }
+        f3 a = xyz(triangles[3 * t]), b = xyz(triangles[3 * t + 1]), c = xyz(triangles[3 * t + 2]);
+        out[size_t(s) * count + k] = w4(a + (b - a) * u + (c - a) * v, 0.0f);
+    }
+}
 // Stream compaction of accepted candidates in index order (exclusive scan
 // already in `offsets`), per shape, capped at `capacity` points.
 __global__ void k_compact(const float4* in, const uint32_t* accept, const uint32_t* offsets, uint32_t count,
@@ -299,6 +315,16 @@ int sdg_culler_sample(void* const* buffers, const uint64_t* bytes, const double*
     dim3 grid((count + 255) / 256 < 512 ? (count + 255) / 256 : 512, shapes);
     k_shellCandidates<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
         P, count, seed, shell, inside_only, static_cast<float4*>(out_points), static_cast<uint32_t*>(accept));
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int sdg_culler_surface(const void* triangles, const void* tri_start, uint32_t shapes, uint32_t count, uint32_t seed,
+                       void* out_points, void* stream) {
+    if (!triangles || !tri_start || !out_points) return 1;
+    dim3 grid((count + 255) / 256 < 512 ? (count + 255) / 256 : 512, shapes);
+    k_surfacePoints<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float4*>(triangles), static_cast<const uint32_t*>(tri_start), count, seed,
+        static_cast<float4*>(out_points));
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 

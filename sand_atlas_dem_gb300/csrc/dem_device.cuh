@@ -36,6 +36,16 @@ struct Config {
     uint32_t viscousCapture;     // fuse captureContactKinematics into beginStep
     uint32_t specimens;          // independent periodic specimens batched in one launch
     uint32_t cullerEnabled;      // learned culler in front of the exact node query
+    // Launch shapes chosen by the autotuner (0 = built-in default).  They
+    // change how work is spread over the SMs, never which work or its order
+    // of accumulation, so every choice gives bit-identical results.
+    uint32_t queryBlocksPerSM;   // node query CTAs per SM
+    uint32_t queryWarps;         // node query warps per CTA (4 or 8)
+    uint32_t cullBlocksPerSM;    // pair set-up, leaf cull and leaf emit CTAs per SM
+    uint32_t contactBlocksPerSM; // node emit, contact starts and contact law CTAs per SM
+    uint32_t gatherWarps;        // gather warps (grains in flight) per SM
+    uint32_t walkBlocksPerSM;    // exact-query CTAs (256 threads, one node each) per SM
+    uint32_t survivorCapacity;   // nodes that pass the conservative filters, per step
 };
 
 // Buffers: the reference Resources block (solver.slang:20-100) in declaration
@@ -87,8 +97,8 @@ struct Res {
     const uint32_t* oldContactStart;  // pairCapacity+1
     uint32_t* work;                   // 64 counters
     uint32_t* scanPartials;           // 2*SCAN_BLOCKS
-    float4* hitScratch;               // 2*contactCapacity: (point/depth, normal/area) per hit
-    uint32_t* candHitBase;            // candidateCapacity: first hitScratch slot of each item
+    float4* hitScratch;               // 2*survivorCapacity: (point/depth, normal/area) per survivor
+    uint32_t* candSurvCount;          // candidateCapacity+1: nodes of each item left for the exact query
     float4* dpairPlane;               // 2*pairCapacity: enclosure plane of the target facing the source
     const uint32_t* grainSpecimen;    // N: specimen of each grain
     const uint4* specimenBins;        // specimens: bin grid x, y, z and first bin
@@ -96,16 +106,19 @@ struct Res {
     const uint32_t* cullerW1;         // shapes x 64 x 64 BF16 hidden weights (packed in pairs)
     const float* cullerMargin;        // shapes: skip a node when the prediction exceeds this
     uint32_t* cullerStats;            // 2 counters: nodes evaluated, nodes culled
+    uint2* candSurvMask;              // candidateCapacity: 64-bit mask of the item's surviving nodes
+    uint32_t* candSurvOffset;         // candidateCapacity+1: first survivor of each item
+    uint2* survivors;                 // survivorCapacity: (item, node slot) of each surviving node
 };
-constexpr int EXTENSION_COUNT = 33;
+constexpr int EXTENSION_COUNT = 36;
 constexpr int CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4;
 constexpr int BUFFER_COUNT = RESOURCE_COUNT + EXTENSION_COUNT;
 constexpr int CONFIG_VALUES = 25;
-constexpr int VALUE_COUNT = CONFIG_VALUES + 5;
+constexpr int VALUE_COUNT = CONFIG_VALUES + 12;
 constexpr int SCAN_BLOCKS = 608;  // 4 per SM on a 152-SM GB300
 // work[] slots
 constexpr int W_CANDIDATES = 0;
-constexpr int W_HITS = 1;
+constexpr int W_SURVIVORS = 2;
 
 struct Params {
     Config c;
@@ -388,39 +401,52 @@ __device__ __forceinline__ void meshPairBounds(const Res& r, uint32_t direction,
     high = high + mk(pad, pad, pad);
 }
 // solver.slang:319-343; the directed-pair branch is precomputed (same bits).
-// With `plane`, the reference CPU backend's per-directed-pair enclosure-plane
-// prefilter (cpu.py:56-76) rejects first; like the hull cull it is
-// conservative and changes no contact.
-__device__ __forceinline__ bool nodeContact(const Res& r, const Config& c, uint32_t src, uint32_t dst, uint32_t node,
-                                            f3 branch, float4& pd, float4& na, const float4* plane = nullptr) {
+// Split in two so that work can be filtered between the cheap conservative
+// rejections and the exact query: nodePrefilter places the node in the
+// target's frame and applies, with `plane`, the reference CPU backend's
+// per-directed-pair enclosure-plane prefilter (cpu.py:56-76), then the hull
+// cull; nodeExact is the exact distance query and the contact record.  Both
+// rejections are conservative and change no contact.
+__device__ __forceinline__ bool nodePrefilter(const Res& r, uint32_t src, uint32_t dst, uint32_t node, f3 branch,
+                                              const float4* plane, f3& arm, f3& local) {
     uint32_t sid = r.shapeId[src];
     float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[sid].x) + node]);
     float4 qs = r.rotation[src], qd = r.rotation[dst];
-    float4 bs = r.body[src], bd = r.body[dst];
-    f3 arm = qrot(qs, xyz(sp) * bs.x);
-    f3 local = qinv(qd, arm - branch) / bd.x;
-    uint32_t targetShape = r.shapeId[dst];
+    arm = qrot(qs, xyz(sp) * r.body[src].x);
+    local = qinv(qd, arm - branch) / r.body[dst].x;
     if (plane) {
         float pad = __fmul_rn(0.00000762939453125f,
                               __fadd_rn(1.0f, mx(mx(fabsf(local.x), fabsf(local.y)), fabsf(local.z))));
         if (__fadd_rn(dot(xyz(*plane), local), plane->w) > pad) return false;
     }
-    if (!meshMayContain(r, targetShape, local)) return false;
+    return meshMayContain(r, r.shapeId[dst], local);
+}
+__device__ __forceinline__ bool nodeExact(const Res& r, const Config& c, uint32_t src, uint32_t dst, uint32_t node,
+                                          f3 arm, f3 local, float4& pd, float4& na) {
+    uint32_t sid = r.shapeId[src], targetShape = r.shapeId[dst];
+    float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[sid].x) + node]);
+    float4 bs = r.body[src], bd = r.body[dst];
     float4 f = meshDistance(r, targetShape, local, false);
     pd = w4(arm, __fmul_rn(-f.w, bd.x));
     if (pd.w <= 0.0f) return false;
-    f3 grad = qrot(qd, xyz(f));
+    f3 grad = qrot(r.rotation[dst], xyz(f));
     float len = length(grad);
     if (c.sourceSurfaceNormal != 0) {
         float4 own = meshDistance(r, sid, xyz(sp), true);
         if (fabsf(own.w) > 0.00000999999974738f) { fail(r, F_DEGENERATE); return false; }
-        grad = -qrot(qs, xyz(own));
+        grad = -qrot(r.rotation[src], xyz(own));
         len = length(grad);
     }
     if (len < 1.00000001168609742e-07f || !isfinite(pd.w)) { fail(r, F_DEGENERATE); return false; }
     na = w4(grad / len, __fmul_rn(__fmul_rn(sp.w, bs.x), bs.x));
     if (pd.w > __fmul_rn(c.maxOverlap, mn(bs.w, bd.w))) fail(r, F_PENETRATION);
     return true;
+}
+__device__ __forceinline__ bool nodeContact(const Res& r, const Config& c, uint32_t src, uint32_t dst, uint32_t node,
+                                            f3 branch, float4& pd, float4& na, const float4* plane = nullptr) {
+    f3 arm, local;
+    if (!nodePrefilter(r, src, dst, node, branch, plane, arm, local)) return false;
+    return nodeExact(r, c, src, dst, node, arm, local, pd, na);
 }
 
 // ---------------------------------------------------------------- helpers

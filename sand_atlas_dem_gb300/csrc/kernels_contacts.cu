@@ -347,12 +347,25 @@ __global__ void k_resetContacts(const __grid_constant__ Params P) {
     r.control[2] = 0;
     r.control[6] = 0;
     r.work[W_CANDIDATES] = 0;
-    r.work[W_HITS] = 0;
 }
 // Flat leaf cull: one warp per directed pair; meshPairBounds (solver.slang:
 // 404-417) + meshBoxMayContact (:274-288) on every leaf, gated by the root
 // mask.  Equivalent in contacts to the reference's hierarchical walks since
 // every test is conservative and each node's decision is exact.
+// True when every point of the box [low, high] (a leaf's nodes in the target
+// frame, meshPairBounds) lies beyond the enclosure plane by more than the
+// largest per-node pad nodePrefilter could allow there, with a relative
+// slack far above the FP32 rounding of either evaluation: then the plane
+// test rejects every node of the leaf and the leaf need not become an item.
+__device__ __forceinline__ bool leafBeyondPlane(float4 plane, f3 low, f3 high) {
+    f3 n = xyz(plane), centre = 0.5f * (low + high), half = 0.5f * (high - low);
+    float nearest = __fsub_rn(__fadd_rn(dot(n, centre), plane.w), dot(abs3(n), half));
+    float extent = mx(mx(mx(fabsf(low.x), fabsf(high.x)), mx(fabsf(low.y), fabsf(high.y))),
+                      mx(fabsf(low.z), fabsf(high.z)));
+    float pad = __fmul_rn(0.00000762939453125f, __fadd_rn(1.0f, extent));
+    float slack = __fmul_rn(1e-5f, __fadd_rn(__fadd_rn(1.0f, fabsf(plane.w)), dot(abs3(n), abs3(centre) + half)));
+    return nearest > __fadd_rn(pad, slack);
+}
 __global__ void k_leafCull(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
@@ -366,6 +379,7 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
         if (live && ((r.meshPairMask[p] >> pass) & 1u)) {
             uint4 li = __ldg(&r.meshLeafInfo[r.shapeId[i]]);
             uint32_t targetShape = r.shapeId[j];
+            float4 plane;
             // Enclosure plane of the target most violated by the source centre
             // (cpu_scheduling.slang:58-71): warp arg-max, lowest index on ties.
             {
@@ -377,8 +391,8 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
                 float best = -1e30f;
                 uint32_t bestIndex = EMPTY;
                 for (uint32_t k = begin + laneId(); k < end; k += WARP) {
-                    float4 plane = __ldg(&r.meshPlanes[k]);
-                    float violation = __fadd_rn(dot(xyz(plane), centre), plane.w);
+                    float4 candidate = __ldg(&r.meshPlanes[k]);
+                    float violation = __fadd_rn(dot(xyz(candidate), centre), candidate.w);
                     if (violation > best) { best = violation; bestIndex = k; }
                 }
 #pragma unroll
@@ -387,8 +401,8 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
                     uint32_t oi = __shfl_xor_sync(0xffffffffu, bestIndex, o);
                     if (ob > best || (ob == best && oi < bestIndex)) { best = ob; bestIndex = oi; }
                 }
-                if (laneId() == 0)
-                    r.dpairPlane[d] = bestIndex == EMPTY ? make_float4(0.f, 0.f, 0.f, 0.f) : __ldg(&r.meshPlanes[bestIndex]);
+                plane = bestIndex == EMPTY ? make_float4(0.f, 0.f, 0.f, 0.f) : __ldg(&r.meshPlanes[bestIndex]);
+                if (laneId() == 0) r.dpairPlane[d] = plane;
             }
             for (uint32_t k0 = 0; k0 < li.y; k0 += WARP) {
                 uint32_t k = k0 + laneId();
@@ -396,7 +410,7 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
                 if (k < li.y) {
                     f3 low, high;
                     meshPairBounds(r, d, __ldg(&r.meshLeaves[li.x + k]), low, high);
-                    hit = meshBoxMayContact(r, targetShape, low, high);
+                    hit = meshBoxMayContact(r, targetShape, low, high) && !leafBeyondPlane(plane, low, high);
                 }
                 uint32_t m = __ballot_sync(0xffffffffu, hit);
                 if (laneId() == 0) r.leafMask[size_t(d) * c.leafWords + k0 / WARP] = m;
@@ -429,20 +443,29 @@ __global__ void k_leafEmit(const __grid_constant__ Params P) {
         }
     }
 }
-// Exact node queries, one warp per (directed pair, leaf) item.  Each hit's
-// point/depth and normal/area are stored once in hitScratch at a slot taken
-// with one atomic per item; the emit pass copies them to canonical order.
-__global__ void __launch_bounds__(256) k_nodeQuery(const __grid_constant__ Params P) {
+// Node query in two stages.  The filter stage (one warp per (directed pair,
+// leaf) item, two nodes per lane) applies the conservative rejections -- the
+// enclosure plane, the hull and, when enabled, the learned culler -- and
+// records each item's surviving nodes as a 64-bit mask.  A scan turns the
+// survivor counts into offsets, the survivors are listed in canonical order,
+// and the exact stage runs one thread per survivor: full warps of BVH walks
+// instead of warps in which most lanes were rejected and idle.  Each hit sets
+// its bit in the item's hit mask (integer atomics: the result does not depend
+// on their order) and keeps its record in the survivor's scratch slot; the
+// emit pass copies hits to their canonical offsets.
+template <bool CULL>
+__global__ void __launch_bounds__(256) k_nodeFilter(const __grid_constant__ Params P) {
     extern __shared__ uint32_t cullTiles[];
     const Res& r = P.r;
     const Config& c = P.c;
     uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
     uint32_t* tile = cullTiles + (threadIdx.x >> 5) * CULLER_TILE_WORDS;
     for (uint32_t item = warpGlobal(); item < n; item += warpStride()) {
-        // Leaves hold at most 64 nodes (packing splits larger sets), two per lane.
-        bool hit0 = false, hit1 = false;
-        float4 pd0, na0, pd1, na1;
-        if (r.control[0] == 0) {
+        // One read of the failure word per item, shared by the warp, so the
+        // warp-wide culler steps below are reached by every lane or none.
+        uint32_t live = __shfl_sync(0xffffffffu, r.control[0] == 0 ? 1u : 0u, 0);
+        bool keep0 = false, keep1 = false;
+        if (live) {
             uint2 cd = r.candidates[item];
             uint32_t d = cd.x, p = d >> 1, pass = d & 1;
             uint2 ij = r.pairs[p];
@@ -453,52 +476,85 @@ __global__ void __launch_bounds__(256) k_nodeQuery(const __grid_constant__ Param
             uint32_t k0 = laneId(), k1 = laneId() + WARP;
             uint32_t node0 = k0 < range.y ? __ldg(&r.meshSampleIndices[range.x + k0]) : 0;
             uint32_t node1 = k1 < range.y ? __ldg(&r.meshSampleIndices[range.x + k1]) : 0;
-            bool keep0 = k0 < range.y, keep1 = k1 < range.y;
-            if (c.cullerEnabled) {
-                // Learned culler: skip nodes the target's network places beyond
-                // its calibrated margin; every other node takes the exact query.
-                uint32_t sid = r.shapeId[src], target = r.shapeId[dst];
-                float4 qs = r.rotation[src], qd = r.rotation[dst];
-                float ss = r.body[src].x, sd = r.body[dst].x;
-                uint32_t base = __ldg(&r.sampleInfo[sid].x);
-                f3 l0 = qinv(qd, qrot(qs, xyz(__ldg(&r.sample[base + node0])) * ss) - branch) / sd;
-                f3 l1 = qinv(qd, qrot(qs, xyz(__ldg(&r.sample[base + node1])) * ss) - branch) / sd;
+            f3 arm0 = mk(0.f, 0.f, 0.f), local0 = arm0, arm1 = arm0, local1 = arm0;
+            keep0 = k0 < range.y && nodePrefilter(r, src, dst, node0, branch, &plane, arm0, local0);
+            keep1 = k1 < range.y && nodePrefilter(r, src, dst, node1, branch, &plane, arm1, local1);
+            if (CULL && __any_sync(0xffffffffu, keep0 || keep1)) {
+                // Learned culler: skip survivors the target's network places
+                // beyond its calibrated margin; the rest take the exact query.
+                uint32_t target = r.shapeId[dst];
                 float y0, y1;
-                cullerTile(r.cullerParams + size_t(target) * CULLER_PARAMS, r.cullerW1 + size_t(target) * 2048, l0,
-                           l1, tile, y0, y1);
+                cullerTile(r.cullerParams + size_t(target) * CULLER_PARAMS, r.cullerW1 + size_t(target) * 2048,
+                           local0, local1, tile, y0, y1);
                 float margin = r.cullerMargin[target];
                 bool cut0 = keep0 && y0 > margin, cut1 = keep1 && y1 > margin;
+                uint32_t tested = __popc(__ballot_sync(0xffffffffu, keep0)) + __popc(__ballot_sync(0xffffffffu, keep1));
                 uint32_t culled = __popc(__ballot_sync(0xffffffffu, cut0)) + __popc(__ballot_sync(0xffffffffu, cut1));
                 if (laneId() == 0) {
-                    atomicAdd(&r.cullerStats[0], range.y);
+                    atomicAdd(&r.cullerStats[0], tested);
                     atomicAdd(&r.cullerStats[1], culled);
                 }
                 keep0 = keep0 && !cut0;
                 keep1 = keep1 && !cut1;
             }
-            if (keep0) hit0 = nodeContact(r, c, src, dst, node0, branch, pd0, na0, &plane);
-            if (keep1) hit1 = nodeContact(r, c, src, dst, node1, branch, pd1, na1, &plane);
         }
-        uint32_t m0 = __ballot_sync(0xffffffffu, hit0), m1 = __ballot_sync(0xffffffffu, hit1);
-        uint32_t hits = __popc(m0) + __popc(m1), base = 0;
+        uint32_t m0 = __ballot_sync(0xffffffffu, keep0), m1 = __ballot_sync(0xffffffffu, keep1);
         if (laneId() == 0) {
-            if (hits) base = atomicAdd(&r.work[W_HITS], hits);
-            r.candHitMask[item] = make_uint2(m0, m1);
-            r.candHitCount[item] = hits;
-            r.candHitBase[item] = base;
-        }
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (hit0) {
-            uint32_t slot = base + __popc(m0 & lanesBelow());
-            if (slot < c.contactCapacity) { r.hitScratch[2 * slot] = pd0; r.hitScratch[2 * slot + 1] = na0; }
-        }
-        if (hit1) {
-            uint32_t slot = base + __popc(m0) + __popc(m1 & lanesBelow());
-            if (slot < c.contactCapacity) { r.hitScratch[2 * slot] = pd1; r.hitScratch[2 * slot + 1] = na1; }
+            r.candSurvMask[item] = make_uint2(m0, m1);
+            r.candSurvCount[item] = __popc(m0) + __popc(m1);
+            r.candHitMask[item] = make_uint2(0u, 0u);
+            r.candHitCount[item] = 0;
         }
     }
 }
-// Copies the hits of each item from hitScratch to their canonical offsets.
+// Survivor list in canonical (item, node slot) order.
+__global__ void k_survivorList(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
+    for (uint32_t item = warpGlobal(); item < n; item += warpStride()) {
+        uint2 m = r.candSurvMask[item];
+        if ((m.x | m.y) == 0) continue;
+        uint32_t base = r.candSurvOffset[item];
+#pragma unroll
+        for (uint32_t half = 0; half < 2; ++half) {
+            uint32_t word = half ? m.y : m.x;
+            if (!((word >> laneId()) & 1u)) continue;
+            uint32_t s = base + (half ? __popc(m.x) : 0) + __popc(word & lanesBelow());
+            if (s < c.survivorCapacity) r.survivors[s] = make_uint2(item, laneId() + half * WARP);
+            else fail(r, F_CONTACT);
+        }
+    }
+}
+// Exact query, one thread per survivor.
+__global__ void __launch_bounds__(256) k_nodeWalk(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
+    for (uint32_t s = gtid(); s < n; s += gstride()) {
+        uint2 sv = r.survivors[s];
+        uint2 cd = r.candidates[sv.x];
+        uint32_t d = cd.x, p = d >> 1, pass = d & 1;
+        uint2 ij = r.pairs[p];
+        uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
+        uint32_t node = __ldg(&r.meshSampleIndices[__ldg(&r.meshClusterRanges[cd.y]).x + sv.y]);
+        // The same expressions as nodePrefilter: the same arm and local bits.
+        float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[r.shapeId[src]].x) + node]);
+        f3 arm = qrot(r.rotation[src], xyz(sp) * r.body[src].x);
+        f3 local = qinv(r.rotation[dst], arm - xyz(r.dpairBranch[d])) / r.body[dst].x;
+        float4 pd, na;
+        if (nodeExact(r, c, src, dst, node, arm, local, pd, na)) {
+            r.hitScratch[2 * s] = pd;
+            r.hitScratch[2 * s + 1] = na;
+            atomicOr(sv.y < WARP ? &r.candHitMask[sv.x].x : &r.candHitMask[sv.x].y, 1u << (sv.y & 31u));
+            atomicAdd(&r.candHitCount[sv.x], 1u);
+        }
+    }
+}
+// Copies the hits of each item from their survivor slots to their canonical
+// offsets.
 __global__ void __launch_bounds__(256) k_nodeEmit(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
@@ -512,14 +568,16 @@ __global__ void __launch_bounds__(256) k_nodeEmit(const __grid_constant__ Params
         uint2 ij = r.pairs[p];
         uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
         uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
-        uint32_t out = r.candHitOffset[item], in = r.candHitBase[item];
+        uint2 sm = r.candSurvMask[item];
+        uint32_t out = r.candHitOffset[item], in = r.candSurvOffset[item];
 #pragma unroll
         for (uint32_t half = 0; half < 2; ++half) {
             uint32_t word = half ? m.y : m.x;
             if (!((word >> laneId()) & 1u)) continue;
             uint32_t rank = (half ? __popc(m.x) : 0) + __popc(word & lanesBelow());
-            uint32_t slot = out + rank, from = in + rank;
-            if (slot >= c.contactCapacity || from >= c.contactCapacity) { fail(r, F_CONTACT); continue; }
+            uint32_t survivorRank = (half ? __popc(sm.x) : 0) + __popc((half ? sm.y : sm.x) & lanesBelow());
+            uint32_t slot = out + rank, from = in + survivorRank;
+            if (slot >= c.contactCapacity || from >= c.survivorCapacity) { fail(r, F_CONTACT); continue; }
             uint32_t node = __ldg(&r.meshSampleIndices[range.x + laneId() + half * WARP]);
             r.meta[slot] = make_uint4(src, dst, node, 0);
             r.pointDepth[slot] = r.hitScratch[2 * from];
@@ -769,6 +827,22 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Params P
 static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
 constexpr uint32_t PERSISTENT = 152 * 8;  // warps-per-item kernels: 8 CTAs of 256 per SM
 
+// SMs of the current device (152 on GB300), read once.
+static uint32_t smCount() {
+    static uint32_t sms = 0;
+    if (!sms) {
+        int device = 0, count = 0;
+        if (cudaGetDevice(&device) == cudaSuccess &&
+            cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && count > 0)
+            sms = uint32_t(count);
+        else
+            sms = 152;
+    }
+    return sms;
+}
+// Grid of `perSM` CTAs per SM (the tuned value, or `fallback` when 0).
+static inline uint32_t grid(uint32_t perSM, uint32_t fallback) { return smCount() * (perSM ? perSM : fallback); }
+
 static void neighbours(const Params& P, cudaStream_t s) {
     const Res& r = P.r;
     const Config& c = P.c;
@@ -794,21 +868,33 @@ static void collectCull(const Params& P, cudaStream_t s) {
     const Config& c = P.c;
     uint32_t T = 256;
     k_resetContacts<<<1, 1, 0, s>>>(P);
-    k_pairSetup<<<PERSISTENT, T, 0, s>>>(P);
-    k_leafCull<<<PERSISTENT, T, 0, s>>>(P);
+    uint32_t g = grid(c.cullBlocksPerSM, 8);
+    k_pairSetup<<<g, T, 0, s>>>(P);
+    k_leafCull<<<g, T, 0, s>>>(P);
     launch_scan(r.dpairLeafCount, r.dpairCandOffset, ScanCount{r.control + 1, c.pairCapacity, 2, 0}, true,
                 r.work + W_CANDIDATES, nullptr, r.scanPartials, s);
-    k_leafEmit<<<PERSISTENT, T, 0, s>>>(P);
+    k_leafEmit<<<g, T, 0, s>>>(P);
 }
 static void collectQuery(const Params& P, cudaStream_t s) {
-    size_t smem = P.c.cullerEnabled ? 8 * CULLER_TILE_WORDS * sizeof(uint32_t) : 0;
-    static bool attributed = false;
-    if (!attributed) {
-        cudaFuncSetAttribute(k_nodeQuery, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(8 * CULLER_TILE_WORDS * sizeof(uint32_t)));
-        attributed = true;
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t warps = c.queryWarps == 4 ? 4 : 8;
+    uint32_t g = grid(c.queryBlocksPerSM, 8);
+    if (c.cullerEnabled) {
+        static bool attributed = false;
+        if (!attributed) {
+            cudaFuncSetAttribute(k_nodeFilter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(8 * CULLER_TILE_WORDS * sizeof(uint32_t)));
+            attributed = true;
+        }
+        k_nodeFilter<true><<<g, 32 * warps, warps * CULLER_TILE_WORDS * sizeof(uint32_t), s>>>(P);
+    } else {
+        k_nodeFilter<false><<<g, 32 * warps, 0, s>>>(P);
     }
-    k_nodeQuery<<<PERSISTENT, 256, smem, s>>>(P);
+    launch_scan(r.candSurvCount, r.candSurvOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0},
+                true, r.work + W_SURVIVORS, nullptr, r.scanPartials, s);
+    k_survivorList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
+    k_nodeWalk<<<grid(c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
 }
 // Canonical offsets of the hits, the contact records and per-pair starts.
 static void collectEmit(const Params& P, cudaStream_t s) {
@@ -816,8 +902,9 @@ static void collectEmit(const Params& P, cudaStream_t s) {
     const Config& c = P.c;
     launch_scan(r.candHitCount, r.candHitOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0}, true,
                 r.control + 2, nullptr, r.scanPartials, s);
-    k_nodeEmit<<<PERSISTENT, 256, 0, s>>>(P);
-    k_contactStart<<<PERSISTENT, 256, 0, s>>>(P);
+    uint32_t g = grid(c.contactBlocksPerSM, 8);
+    k_nodeEmit<<<g, 256, 0, s>>>(P);
+    k_contactStart<<<g, 256, 0, s>>>(P);
 }
 static void contacts(const Params& P, cudaStream_t s) {
     collectCull(P, s);
@@ -833,8 +920,8 @@ int launch_contacts(const std::string_view& name, const Params& P, uint32_t coun
     else if (name == "collectCull") collectCull(P, s);
     else if (name == "collectQuery") collectQuery(P, s);
     else if (name == "collectEmit") collectEmit(P, s);
-    else if (name == "resolveContacts") k_resolve<<<PERSISTENT, T, 0, s>>>(P);
-    else if (name == "gather") k_gather<<<min(blocks(c.N, 8), PERSISTENT), T, 0, s>>>(P);
+    else if (name == "resolveContacts") k_resolve<<<grid(c.contactBlocksPerSM, 8), T, 0, s>>>(P);
+    else if (name == "gather") k_gather<<<min(blocks(c.N, 8), max(1u, grid(c.gatherWarps, 64) / 8)), T, 0, s>>>(P);
     else return 1;
     (void)count;
     return 0;

@@ -11,8 +11,9 @@ culler.cuh``) inside the node-query warps.
 
 Conservative by construction of its margin: a node is skipped only when its
 prediction exceeds the shape's margin, the largest prediction at any of
-(2 x points) sampled inside points (shell and deep interior, fresh seeds)
-plus ``slack``.  Every other node takes the exact query, which alone
+(3 x points) sampled inside points (the inside half of the shell, the whole
+interior and the surface itself, fresh seeds) plus ``slack`` (normalized
+length units).  Every other node takes the exact query, which alone
 decides contacts and forces.  Missed contacts are counted against the exact
 path by the tests.
 """
@@ -36,11 +37,24 @@ def _ptr(t):
     return ct.c_void_p(t.data_ptr())
 
 
+def _engine_stream(method):
+    """Run a method with the engine stream current, so that torch's
+    allocations, fills and reads are ordered with the kernels launched on it."""
+    import functools
+
+    @functools.wraps(method)
+    def wrapped(self, *args, **kwargs):
+        with _torch().cuda.stream(self.stream):
+            return method(self, *args, **kwargs)
+
+    return wrapped
+
+
 class LearnedCuller:
     """Per-shape networks for one engine's shape library."""
 
     def __init__(self, engine, *, shell=0.3, points=1 << 20, steps=2000, batch=8192, lr=1e-3, seed=7,
-                 slack=0.02):
+                 slack=0.05):
         self.engine = engine
         self.lib = native.load()
         self.shapes = len(engine.library.shapes)
@@ -51,8 +65,9 @@ class LearnedCuller:
         torch = _torch()
         self.device = engine.device
         self.stream = engine.stream
-        self.params = torch.from_numpy(self.initial_params()).to(self.device)
-        self.w1 = torch.zeros(self.shapes * H * H, dtype=torch.int16, device=self.device)
+        with torch.cuda.stream(self.stream):
+            self.params = torch.from_numpy(self.initial_params()).to(self.device)
+            self.w1 = torch.zeros(self.shapes * H * H, dtype=torch.int16, device=self.device)
         self.margins = None
         self.losses = []
 
@@ -69,6 +84,7 @@ class LearnedCuller:
         return p
 
     # ------------------------------------------------------------ data
+    @_engine_stream
     def sample(self, count, seed, *, inside_only=False):
         """``count`` accepted points per shape (x, y, z, phi), exact labels."""
         torch = _torch()
@@ -95,6 +111,7 @@ class LearnedCuller:
         return points
 
     # ---------------------------------------------------------- training
+    @_engine_stream
     def train(self, log=None):
         torch = _torch()
         self.training_points = self.sample(self.points, self.seed)
@@ -121,6 +138,7 @@ class LearnedCuller:
         self.stream.synchronize()
         return self.losses
 
+    @_engine_stream
     def gradients(self, step=0):
         """Parameter gradients of the mean squared error on batch ``step``."""
         torch = _torch()
@@ -135,6 +153,7 @@ class LearnedCuller:
         return grads.view(self.shapes, -1).cpu().numpy(), index.reshape(self.shapes, self.batch)
 
     # ------------------------------------------------------- calibration
+    @_engine_stream
     def predict(self, points):
         """Run-time (tensor-core) predictions for stored points (shapes x count)."""
         torch = _torch()
@@ -145,19 +164,37 @@ class LearnedCuller:
         self.stream.synchronize()
         return out
 
+    @_engine_stream
+    def surface(self, count, seed):
+        """``count`` points on each shape's surface (label 0)."""
+        torch = _torch()
+        faces = np.cumsum([0] + [len(sh.faces) for sh in self.engine.library.shapes]).astype(np.uint32)
+        starts = torch.from_numpy(faces.view(np.int32)).to(self.device)
+        triangles = self.engine.buffers["meshTriangles"]
+        out = torch.zeros((self.shapes * count, 4), dtype=torch.float32, device=self.device)
+        native.check(self.lib.sdg_culler_surface(ct.c_void_p(triangles.ptr()), _ptr(starts), self.shapes, count, seed,
+                                                 _ptr(out), ct.c_void_p(self.stream.cuda_stream)))
+        self.stream.synchronize()
+        return out
+
+    @_engine_stream
     def calibrate(self):
-        """Margin per shape: the largest run-time prediction at 2 x points fresh
-        inside samples (shell and whole interior), plus ``slack``."""
+        """Margin per shape: the largest run-time prediction at 3 x points fresh
+        inside samples (the inside half of a shell sample, the whole interior
+        and the surface itself), plus ``slack``."""
         torch = _torch()
         s = ct.c_void_p(self.stream.cuda_stream)
         native.check(self.lib.sdg_culler_round(_ptr(self.params), _ptr(self.w1), self.shapes, s))
         keys = torch.zeros(self.shapes, dtype=torch.int32, device=self.device)
-        for seed, inside in ((self.seed + 101, False), (self.seed + 202, True)):
-            pts = self.sample(self.points, seed, inside_only=inside)
+        for seed, kind in ((self.seed + 101, "shell"), (self.seed + 202, "inside"), (self.seed + 303, "surface")):
+            if kind == "surface":
+                pts = self.surface(self.points, seed)
+            else:
+                pts = self.sample(self.points, seed, inside_only=kind == "inside")
             pred = self.predict(pts)
             native.check(self.lib.sdg_culler_inside_max(_ptr(pts), _ptr(pred), self.shapes, self.points,
                                                         _ptr(keys), s))
-            if not inside:
+            if kind == "shell":
                 self.validation = (pts, pred)
         self.stream.synchronize()
         k = keys.cpu().numpy().view(np.uint32)
@@ -174,6 +211,7 @@ class LearnedCuller:
         culled = (y > self.margins[:, None]) & outside
         return float(culled.sum() / max(outside.sum(), 1))
 
+    @_engine_stream
     def attach(self, engine=None):
         """Install parameters, BF16 weights and margins in an engine's buffers."""
         e = engine or self.engine

@@ -28,13 +28,18 @@ from .model import (
     f4,
 )
 
+# Launch shapes the autotuner sets (values after the extension values; 0 =
+# built-in default).  They never change results.
+TUNING_KEYS = ("query_blocks_per_sm", "query_warps", "cull_blocks_per_sm", "contact_blocks_per_sm",
+               "gather_warps_per_sm", "walk_blocks_per_sm")
+
 EXTENSION_ORDER = (
     "meshLeafInfo", "meshLeaves", "meshSampleRank", "byJCounts", "byJOffsets", "byJCursor",
     "byJPairs", "dpairBranch", "dpairLeafCount", "dpairCandOffset", "leafMask", "candidates",
     "candHitCount", "candHitOffset", "candHitMask", "contactPair", "sidePairOffsets", "sidePairB",
     "sideContactStart", "oldPairOffsets", "oldPairB", "oldContactStart", "work", "scanPartials",
-    "hitScratch", "candHitBase", "dpairPlane", "grainSpecimen", "specimenBins", "cullerParams", "cullerW1",
-    "cullerMargin", "cullerStats",
+    "hitScratch", "candSurvCount", "dpairPlane", "grainSpecimen", "specimenBins", "cullerParams", "cullerW1",
+    "cullerMargin", "cullerStats", "candSurvMask", "candSurvOffset", "survivors",
 )
 CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4
 BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
@@ -166,6 +171,7 @@ class Engine:
         self.capacity_retries = []
         self.use_graph = use_graph
         self.culler = None
+        self.tuning = {}
         for name in ("length_unit", "time_unit", "mass_unit", "force_unit", "stress_unit", "energy_unit",
                      "ids", "scales", "body", "skin", "cutoff", "bins", "bin_count", "pair_capacity",
                      "contact_capacity", "hash_size", "bin_capacity", "initial_cell"):
@@ -173,6 +179,9 @@ class Engine:
         self.estimated_bytes = h.estimated_bytes()
         self.leaf_words = (h.max_leaves + 31) // 32
         self.candidate_capacity = max(1, 2 * h.pair_capacity * h.max_leaves)
+        # Nodes left for the exact query after the conservative filters, per
+        # step; overflow raises the contact-capacity flag and grows with it.
+        self.survivor_capacity = 2 * h.contact_capacity
         self.device = torch.device(device or "cuda")
         self.stream = torch.cuda.Stream(self.device)
         self.m = GB300Device(self)
@@ -196,7 +205,9 @@ class Engine:
             "candidates": 8 * self.candidate_capacity, "candHitCount": 4 * (self.candidate_capacity + 1),
             "candHitOffset": 4 * (self.candidate_capacity + 1), "candHitMask": 8 * self.candidate_capacity,
             "contactPair": 4 * cc, "work": 4 * 64, "scanPartials": 4 * 2 * SCAN_BLOCKS,
-            "hitScratch": 32 * cc, "candHitBase": 4 * self.candidate_capacity, "dpairPlane": 16 * 2 * pc,
+            "hitScratch": 32 * self.survivor_capacity, "candSurvCount": 4 * (self.candidate_capacity + 1),
+            "dpairPlane": 16 * 2 * pc, "candSurvMask": 8 * self.candidate_capacity,
+            "candSurvOffset": 4 * (self.candidate_capacity + 1), "survivors": 8 * self.survivor_capacity,
             "cullerParams": 4 * CULLER_PARAMS * len(library.shapes), "cullerW1": 2 * 4096 * len(library.shapes),
             "cullerMargin": 4 * len(library.shapes), "cullerStats": 16,
         }
@@ -258,7 +269,7 @@ class Engine:
         values = list(self.layout.config_values(config)) + [
             float(self.leaf_words), float(self.candidate_capacity), 0.0, float(self.specimens),
             float(self.culler is not None),
-        ]
+        ] + [float(self.tuning.get(k, 0)) for k in TUNING_KEYS] + [float(self.survivor_capacity)]
         return (ct.c_double * len(values))(*values), len(values)
 
     def dispatch(self, name, count, config, active=None):

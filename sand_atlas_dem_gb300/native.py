@@ -100,6 +100,7 @@ def load():
         "sdg_culler_param_count": [],
         "sdg_culler_sample": [P(V), P(ct.c_uint64), P(ct.c_double), U, U, U, U, F, U, V, V, V],
         "sdg_culler_compact": [V, V, V, U, U, U, V, V],
+        "sdg_culler_surface": [V, V, U, U, U, V, V],
         "sdg_culler_train_step": [V, V, U, U, U, U, U, F, F, V, V, V, V, V, V],
         "sdg_culler_gradients": [V, V, U, U, U, U, U, F, V, V, V],
         "sdg_culler_round": [V, V, U, V],
@@ -139,6 +140,7 @@ EXPORTS = (
     "sdg_exclusive_scan_static",
     "sdg_culler_param_count",
     "sdg_culler_sample",
+    "sdg_culler_surface",
     "sdg_culler_compact",
     "sdg_culler_train_step",
     "sdg_culler_gradients",

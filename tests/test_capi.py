@@ -12,7 +12,7 @@ from pathlib import Path
 import pytest
 
 from sand_atlas_dem_gb300 import native
-from sand_atlas_dem_gb300.engine import BUFFER_ORDER, EXTENSION_ORDER
+from sand_atlas_dem_gb300.engine import BUFFER_ORDER, EXTENSION_ORDER, TUNING_KEYS
 from sand_atlas_dem_gb300.model import CONFIG_ORDER, RESOURCE_ORDER
 
 HEADER = Path(__file__).resolve().parent.parent / "include" / "sand_dem_gb300.h"
@@ -44,7 +44,7 @@ def test_buffer_and_value_counts(library):
     library.sdg_buffer_count.restype = ct.c_int
     library.sdg_value_count.restype = ct.c_int
     assert library.sdg_buffer_count() == buffers == len(BUFFER_ORDER) == len(RESOURCE_ORDER) + len(EXTENSION_ORDER)
-    assert library.sdg_value_count() == values == len(CONFIG_ORDER) + 5
+    assert library.sdg_value_count() == values == len(CONFIG_ORDER) + 5 + len(TUNING_KEYS) + 1
     assert len(RESOURCE_ORDER) == 77
 
 
