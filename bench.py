@@ -1,29 +1,39 @@
 """Benchmark: grain-steps/s of the mesh-surface DEM step on one GB300.
 
-Workload (the 10,000-grain plain-method configuration): 64 seeded perturbed
-geodesic icospheres (1,280 triangles, 642 Sobol nodes each), grain scales
-lognormal (median 1, sigma_ln 0.2) on a 0.5 mm nominal radius, a dense
-periodic packing prepared by affine compression and frictionless force
-descent on the GPU toward solid fraction 0.58 (the rough grains jam near
-0.54 at overlaps under 9% of a diameter; the record states what was
-reached, sand_atlas_dem_gb300/data/packing-f8-10000.npz), then
-isotropic compression at 0.5/s with rho 2650, kn 1e12, kt 5e11, mu 0.5,
-normal viscosity for damping ratio 0.3 and dt one ulp below the reference's
-conservative bound.  Data are synthetic (seeded); the reference's Hostun
-assets are not used.
+Workloads (``--workload``):
+
+``dense-10k`` (default, the headline): the 10,000-grain plain-method
+    configuration.  64 seeded perturbed geodesic icospheres (1,280 triangles,
+    642 Sobol nodes each), grain scales lognormal (median 1, sigma_ln 0.2) on
+    a 0.5 mm nominal radius, a dense periodic packing prepared by affine
+    compression and frictionless force descent on the GPU toward solid
+    fraction 0.58 (the rough grains jam near 0.54 at overlaps under 9% of a
+    diameter; the record states what was reached,
+    sand_atlas_dem_gb300/data/packing-f8-10000.npz), then isotropic
+    compression at 0.5/s with rho 2650, kn 1e12, kt 5e11, mu 0.5, normal
+    viscosity for damping ratio 0.3 and dt one ulp below the reference's
+    conservative bound.
+``uneven-50k``: 50,653 grains from the uneven library (64 shapes, triangle
+    counts log-uniform 320..5,120, axis ratios U(0.6, 1)) on a jittered cubic
+    lattice at solid fraction 0.58, compressed at 0.5/s.
+``specimens-128``: 128 independent periodic specimens batched in one engine
+    (one launch per phase, one graph per step), 512..4,096 grains each from
+    the uneven library at solid fractions U(0.55, 0.60), each compressed at
+    its own rate U(0.1, 1.0)/s.
+
+Data are synthetic (seeded); the reference's Hostun assets are not used.
 
 ``value``  : device throughput, CUDA events on the engine stream around each
              graph-replayed step, L2 flushed (256 MiB write) before each step.
 ``e2e``    : the public API a caller uses (``Engine.advance`` chunks of 10
              steps plus ``diagnostics()``), host wall clock, including the
-             host<->device traffic of those calls.
+             host<->device traffic of those calls (counted by the engine).
 ``--impl reference`` times the CPU oracle port of the reference CPU backend
 on the host cores (``oracle/``), same workload and metric.
 """
 
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys
@@ -37,19 +47,21 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "grain-steps/s"
-WORKLOAD = dict(
-    workload="dense-periodic-10k-icosphere-f8",
-    grains=10_000,
-    triangles_per_grain=1280,
-    nodes_per_grain=642,
-    shapes=64,
-    solid_fraction_target=0.58,
-    max_overlap_fraction=0.1,
-    strain_rate_per_s=-0.5,
-    friction=0.5,
-    damping_ratio=0.3,
-    dtype_note="FP32 state with compensated residuals; FP64 minimum image",
-)
+COMMON = dict(shapes=64, friction=0.5, damping_ratio=0.3,
+              dtype_note="FP32 state with compensated residuals; FP64 minimum image")
+WORKLOADS = {
+    "dense-10k": dict(COMMON, workload="dense-periodic-10k-icosphere-f8", library="f8", grains=10_000,
+                      triangles_per_grain=1280, nodes_per_grain=642, solid_fraction_target=0.58,
+                      max_overlap_fraction=0.1, strain_rate_per_s=-0.5),
+    "uneven-50k": dict(COMMON, workload="lattice-periodic-50k-uneven", library="uneven", grains=37**3,
+                       triangles_per_grain="320..5120", solid_fraction=0.58, max_overlap_fraction=0.5,
+                       strain_rate_per_s=-0.5, packing="jittered cubic lattice"),
+    "specimens-128": dict(COMMON, workload="128-specimens-uneven", library="uneven", specimens=128,
+                          grains_per_specimen="512..4096", solid_fraction="U(0.55, 0.60)",
+                          strain_rate_per_s="-U(0.1, 1.0) per specimen", max_overlap_fraction=0.5,
+                          packing="jittered cubic lattice per specimen"),
+}
+DATA = ROOT / "sand_atlas_dem_gb300" / "data"
 
 
 def log(*args):
@@ -62,60 +74,79 @@ def cache_dir():
     return path
 
 
-def library():
+def library(kind):
     from sand_atlas_dem_gb300.shapes import synthetic_library
 
-    return synthetic_library("f8", WORKLOAD["shapes"])
+    return synthetic_library(kind, 64)
 
 
-def lattice_packing(lib, grains):
-    """Quick contact-rich lattice start (diagnostic workload, not the headline)."""
-    from sand_atlas_dem_gb300.engine import Engine
-    from sand_atlas_dem_gb300.workloads import contact_lattice, material_spec
-
-    side = round(grains ** (1 / 3))
-    case = contact_lattice(lib, side, spacing=0.985, scale_sigma=0.05)
-    spec = material_spec(lib, case["ids"], case["scales"], max_overlap_fraction=0.5)
-    e = Engine(lib, spec, case["positions"], case["cell"], case["ids"], case["scales"])
-    e.buffers["rotation"].copy_from_numpy(case["rotations"])
-    e.initialize()
-    return dict(state=e.state(), ids=case["ids"], scales=case["scales"], cell=case["cell"], steps=0,
-                overrides=dict(max_overlap_fraction=0.5))
-
-
-DATA = ROOT / "sand_atlas_dem_gb300" / "data"
-
-
-def packing(lib, grains, phi, seed=42, kind="dense"):
+def packing(lib, grains, phi, seed=42):
     """The prepared dense packing (committed record, else prepared here within
     a bounded time and cached)."""
     from sand_atlas_dem_gb300.workloads import descent_packing, load_packing, save_packing
 
-    if kind == "lattice":
-        return lattice_packing(lib, grains)
     name = f"packing-f8-{grains}.npz"
     for path in (DATA / name, cache_dir() / name):
         if path.exists():
-            return dict(load_packing(path), kind="record", path=str(path))
+            return dict(load_packing(path), path=str(path))
     t = time.perf_counter()
     out = descent_packing(lib, grains, phi, seed=seed, max_seconds=600, log=lambda d: log("prepare", d))
     meta = dict(library="f8", grains=grains, solid_fraction=phi, seed=seed, evaluations=out["evaluations"],
                 seconds=round(time.perf_counter() - t, 1), achieved_solid_fraction=out["phi"],
                 max_overlap_fraction=out["overlap"])
     save_packing(cache_dir() / name, out["engine"], out["ids"], out["scales"], meta)
-    return dict(load_packing(cache_dir() / name), kind="record")
+    return load_packing(cache_dir() / name)
 
 
-def engine_for(lib, pack, cls, **kwargs):
-    """Engine on a packing: a full checkpoint state, or a packing record
-    (centres, orientations, cell) started from rest and initialized."""
-    from sand_atlas_dem_gb300.workloads import material_spec
+class Workload:
+    """One benchmark workload: its library, how to build an initialized
+    engine of a given class on it, and each specimen's compression rate."""
 
-    overrides = pack.get("overrides", {"max_overlap_fraction": WORKLOAD["max_overlap_fraction"]})
-    spec = material_spec(lib, pack["ids"], pack["scales"], **overrides)
-    if pack.get("kind") == "record":
-        e = cls(lib, spec, pack["positions"], pack["cell"], pack["ids"], pack["scales"], **kwargs)
-        rotations = np.ascontiguousarray(pack["rotations"], np.float32)
+    def __init__(self, name, grains=None):
+        from sand_atlas_dem_gb300.workloads import lattice_at, material_spec, specimen_set
+
+        self.name = name
+        self.config = dict(WORKLOADS[name])
+        self.lib = library(self.config["library"])
+        if name == "dense-10k":
+            grains = grains or self.config["grains"]
+            pack = packing(self.lib, grains, self.config["solid_fraction_target"])
+            self.specimens = [(pack["positions"], pack["cell"], pack["ids"], pack["scales"])]
+            self.rotations = pack["rotations"]
+            self.rates = np.full((1, 3), self.config["strain_rate_per_s"])
+            self.config.update(grains=grains, packing_meta=pack["meta"],
+                               solid_fraction=pack["meta"].get("achieved_solid_fraction"))
+        elif name == "uneven-50k":
+            case = lattice_at(self.lib, round(self.config["grains"] ** (1 / 3)), self.config["solid_fraction"],
+                              seed=5)
+            self.specimens = [(case["positions"], case["cell"], case["ids"], case["scales"])]
+            self.rotations = case["rotations"]
+            self.rates = np.full((1, 3), self.config["strain_rate_per_s"])
+        else:
+            self.specimens, self.rotations, rates = specimen_set(self.lib, self.config["specimens"])
+            self.rates = -np.repeat(rates[:, None], 3, axis=1)
+            self.config.update(grains=int(sum(len(s[0]) for s in self.specimens)),
+                               specimen_grains=[len(s[0]) for s in self.specimens])
+        ids = np.concatenate([s[2] for s in self.specimens])
+        scales = np.concatenate([s[3] for s in self.specimens])
+        # Lattices have at most 26 neighbours in range: 16 pairs per grain
+        # leave room, and the engine grows on overflow.
+        pairs = {} if name == "dense-10k" else dict(pairs_per_particle=16)
+        self.spec = material_spec(self.lib, ids, scales,
+                                  max_overlap_fraction=self.config["max_overlap_fraction"], **pairs)
+        self.grains = len(ids)
+
+    def engine(self, cls, specimens=None, **kwargs):
+        """An initialized engine from rest on all (or the listed) specimens."""
+        chosen = list(range(len(self.specimens))) if specimens is None else list(specimens)
+        offsets = np.cumsum([0] + [len(s[0]) for s in self.specimens])
+        if len(chosen) == 1:
+            s = self.specimens[chosen[0]]
+            e = cls(self.lib, self.spec_for(chosen), s[0], s[1], s[2], s[3], **kwargs)
+        else:
+            e = cls.batch(self.lib, self.spec_for(chosen), [self.specimens[k] for k in chosen], **kwargs)
+        rotations = np.concatenate([self.rotations[offsets[k]:offsets[k + 1]] for k in chosen])
+        rotations = np.ascontiguousarray(rotations, np.float32)
         buffer = e.buffers["rotation"]
         if isinstance(buffer, np.ndarray):
             buffer[...] = rotations
@@ -123,13 +154,15 @@ def engine_for(lib, pack, cls, **kwargs):
             buffer.copy_from_numpy(rotations)
         e.initialize()
         return e
-    state = pack["state"]
-    length_unit = float(np.median([(6 * s.volume / np.pi) ** (1 / 3) for s in lib.shapes]))
-    positions = (state["position"][:, :3].astype(float) + state["positionRemainder"][:, :3]) * length_unit
-    cell = state["cell"][0, :3].astype(float) * length_unit
-    e = cls(lib, spec, positions, cell, pack["ids"], pack["scales"], **kwargs)
-    e.restore(state, 0)
-    return e
+
+    def spec_for(self, chosen):
+        from dataclasses import replace
+
+        return replace(self.spec, particles=int(sum(len(self.specimens[k][0]) for k in chosen)))
+
+    def rate(self, chosen=None):
+        rows = self.rates if chosen is None else self.rates[list(chosen)]
+        return tuple(rows[0]) if len(rows) == 1 else rows
 
 
 class ClockSampler:
@@ -193,131 +226,21 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def algorithmic_bytes(n, pairs, contacts, items, nodes, rebuild, library_bytes):
+def algorithmic_bytes(n, pairs, contacts, items, nodes, survivors, rebuild, library_bytes):
     """Per-step algorithmic HBM bytes of the whole step and of the node query.
 
     Step: 516 B/grain + 264 B/pair + 272 B/contact + 88 B/grain on rebuild
-    steps + the packed library once.  Node query (per launch): each
-    (directed pair, leaf) item reads its record, pair, branch and leaf range
-    (48 B) and writes its hit mask and count (12 B); each node reads its
-    sample index and sample (20 B); the packed library is read once.
+    steps + the packed library once.  Node query (filter, survivor list and
+    exact walks, one launch group): each (directed pair, leaf) item reads its
+    record, pair, branch, plane and leaf range and writes its survivor and
+    hit masks and counts (88 B); each node reads its sample index and sample
+    (20 B); each survivor is listed, read back with its item record, pair,
+    branch, sample, both rotations and bodies, and a hit writes its record
+    (132 B); the packed library is read once (it stays in L2).
     """
     step = 516 * n + 264 * pairs + 272 * contacts + 88 * n * rebuild + library_bytes
-    query = 60 * items + 20 * nodes + library_bytes
+    query = 88 * items + 20 * nodes + 132 * survivors + library_bytes
     return step, query
-
-
-def run_gb300(args, cpu=True):
-    import torch
-
-    from sand_atlas_dem_gb300.engine import DeviceBuffer, Engine
-
-    lib = library()
-    pack = packing(lib, args.grains, WORKLOAD["solid_fraction_target"], kind=args.packing)
-    e = engine_for(lib, pack, Engine)
-    rate = (WORKLOAD["strain_rate_per_s"],) * 3
-    # Warm-up (graph capture happens in the first call).
-    e.advance(max(3, args.warmup), rate=rate)
-    cell = e.read("cell", np.float32, (3, 4))
-    cell[1, :3] = np.asarray(rate) * e.time_unit
-    e.buffers["cell"].copy_from_numpy(cell)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=e.device)
-    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-              for _ in range(args.steps)]
-    ctrl0 = e.check_errors()
-    with ClockSampler() as clocks:
-        e.synchronize()
-        for k in range(args.steps):
-            with torch.cuda.stream(e.stream):
-                flush.fill_(k & 0xFF)
-                events[k][0].record(e.stream)
-            e.run_steps(1)
-            with torch.cuda.stream(e.stream):
-                events[k][1].record(e.stream)
-        e.synchronize()
-    ctrl = e.check_errors()
-    step_ms = [a.elapsed_time(b) for a, b in events]
-    device_s = sum(step_ms) / 1e3
-    value = args.grains * args.steps / device_s
-    kernels = e.lib.sdg_engine_kernels_per_step(e._native)
-    # Phase profile (cold L2 each), for the roofline of the dominant kernel.
-    phases = []
-    for _ in range(3):
-        with torch.cuda.stream(e.stream):
-            flush.fill_(1)
-        phases.append(e.profile_phases())
-    e.check_errors()
-    phase_ms = {k: float(np.median([p[k] for p in phases])) for k in phases[0]}
-    items = int(e.read("work", np.uint32, (64,))[0])
-    pairs, contacts = int(ctrl[1]), int(ctrl[2])
-    leaf_nodes = e.layout.geometry["meshClusterRanges"][:, 1]
-    cand = e.read("candidates", np.uint32, (e.candidate_capacity, 2))[:items]
-    nodes = int(leaf_nodes[cand[:, 1]].sum()) if items else 0
-    lib_bytes = sum(a.nbytes for k, a in e.layout.geometry.items() if k.startswith("mesh") or k == "sample")
-    step_bytes, query_bytes = algorithmic_bytes(args.grains, pairs, contacts, items, nodes, 0, lib_bytes)
-    hbm, peak_kind = peaks()
-    top = max(phase_ms, key=phase_ms.get)
-    query_gbs = query_bytes / (phase_ms["node_query"] / 1e3) / 1e9
-    # End to end through the public API: advance() chunks plus diagnostics().
-    chunk = 10
-    chunks = max(1, args.steps // chunk)
-    e2e_s = 0.0
-    for _ in range(chunks):
-        with torch.cuda.stream(e.stream):
-            flush.fill_(2)
-        e.synchronize()
-        t = time.perf_counter()
-        e.advance(chunk, rate=rate)
-        e.diagnostics()
-        e2e_s += time.perf_counter() - t
-    e2e = args.grains * chunk * chunks / e2e_s
-    # Host<->device bytes per step of advance()+diagnostics(): cell read and
-    # upload, control reads, diagnostic reductions read back.
-    h2d = (48 + 48) / chunk
-    d2h = (48 + 3 * 64 + 8 * 16 + 2 * 16 + 64) / chunk
-    line = {
-        "metric": METRIC,
-        "value": value,
-        "unit": "grain-steps/s",
-        "n_gpus": 1,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": 1e3 * device_s / args.steps,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32",
-        "data": "synthetic",
-        "config": dict(WORKLOAD, grains=args.grains, packing=args.packing, packing_meta=pack.get("meta"),
-                       solid_fraction=(pack.get("meta") or {}).get("achieved_solid_fraction"),
-                       l2="flushed before each timed step (256 MiB write)",
-                       pairs=pairs, contacts=contacts, node_query_items=items, node_queries=nodes,
-                       timestep_s=e.spec.timestep, phase_ms=phase_ms, dominant_phase=top),
-        "e2e": {"value": e2e, "unit": "grain-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "api": f"Engine.advance({chunk}) + Engine.diagnostics() per chunk"},
-        "gpu_launches": int(kernels) * args.steps,
-        "roofline": {
-            "bound": "hbm",
-            "kernel": "k_nodeQuery (exact node queries)",
-            "achieved": query_gbs,
-            "peak": hbm,
-            "peak_source": peak_kind,
-            "unit": "GB/s",
-            "frac": query_gbs / hbm,
-            "traffic": None,
-            "algorithmic_bytes": query_bytes,
-            "step_algorithmic_bytes": step_bytes,
-            "step_achieved_gbs": step_bytes / (device_s / args.steps) / 1e9,
-        },
-        "clocks": clocks.summary(),
-    }
-    if args.culler:
-        line["learned_culler"] = culler_comparison(lib, pack, args, flush)
-    if cpu and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(lib, pack, args)
-    if ctrl0[0] or ctrl[0]:
-        line["solver_flags"] = int(ctrl[0])
-    return line
 
 
 def timed_steps(e, steps, flush):
@@ -337,31 +260,142 @@ def timed_steps(e, steps, flush):
     return [a.elapsed_time(b) for a, b in events]
 
 
-def culler_comparison(lib, pack, args, flush):
+def set_rates(e, w):
+    """Write each specimen's strain-rate row into the cell (graph replay reads it)."""
+    rows = 3 * e.specimens
+    cell = e.read("cell", np.float32, (rows, 4))
+    cell[1::3, :3] = np.asarray(w.rates) * e.time_unit
+    e.buffers["cell"].copy_from_numpy(cell)
+
+
+def run_gb300(args, cpu=True):
+    import torch
+
+    from sand_atlas_dem_gb300.engine import Engine
+
+    w = Workload(args.workload, args.grains)
+    e = w.engine(Engine)
+    rate = w.rate()
+    # Warm-up (graph capture happens in the first call).
+    e.advance(max(3, args.warmup), rate=rate)
+    set_rates(e, w)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=e.device)
+    ctrl0 = e.check_errors()
+    with ClockSampler() as clocks:
+        step_ms = timed_steps(e, args.steps, flush)
+    ctrl = e.check_errors()
+    device_s = sum(step_ms) / 1e3
+    value = w.grains * args.steps / device_s
+    kernels = e.lib.sdg_engine_kernels_per_step(e._native)
+    # Phase profile (cold L2 each), for the roofline of the dominant launch group.
+    phases = []
+    for _ in range(3):
+        with torch.cuda.stream(e.stream):
+            flush.fill_(1)
+        phases.append(e.profile_phases())
+    e.check_errors()
+    phase_ms = {k: float(np.median([p[k] for p in phases])) for k in phases[0]}
+    work = e.read("work", np.uint32, (64,))
+    items, survivors = int(work[0]), int(work[2])
+    pairs, contacts = int(ctrl[1]), int(ctrl[2])
+    leaf_nodes = e.layout.geometry["meshClusterRanges"][:, 1]
+    cand = e.read("candidates", np.uint32, (e.candidate_capacity, 2))[:items]
+    nodes = int(leaf_nodes[cand[:, 1]].sum()) if items else 0
+    lib_bytes = sum(a.nbytes for k, a in e.layout.geometry.items() if k.startswith("mesh") or k == "sample")
+    step_bytes, query_bytes = algorithmic_bytes(w.grains, pairs, contacts, items, nodes, survivors, 0, lib_bytes)
+    hbm, peak_kind = peaks()
+    top = max(phase_ms, key=phase_ms.get)
+    query_ms = phase_ms["node_filter"] + phase_ms["node_query"]
+    query_gbs = query_bytes / (query_ms / 1e3) / 1e9
+    # End to end through the public API: advance() chunks plus diagnostics().
+    chunk = 10
+    chunks = max(1, args.steps // chunk)
+    e2e_s = 0.0
+    h2d0, d2h0 = e.h2d_bytes, e.d2h_bytes
+    for _ in range(chunks):
+        with torch.cuda.stream(e.stream):
+            flush.fill_(2)
+        e.synchronize()
+        t = time.perf_counter()
+        e.advance(chunk, rate=rate)
+        e.diagnostics()
+        e2e_s += time.perf_counter() - t
+    e2e = w.grains * chunk * chunks / e2e_s
+    h2d = (e.h2d_bytes - h2d0) / (chunk * chunks)
+    d2h = (e.d2h_bytes - d2h0) / (chunk * chunks)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "grain-steps/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * device_s / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": dict(w.config, l2="flushed before each timed step (256 MiB write)",
+                       pairs=pairs, contacts=contacts, node_query_items=items, node_queries=nodes,
+                       exact_queries=survivors, timestep_s=e.spec.timestep, phase_ms=phase_ms,
+                       dominant_phase=top, tuning=dict(e.tuning)),
+        "e2e": {"value": e2e, "unit": "grain-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "api": f"Engine.advance({chunk}) + Engine.diagnostics() per chunk"},
+        "gpu_launches": int(kernels) * args.steps,
+        "roofline": {
+            "bound": "hbm",
+            "kernel": "node query launch group (k_nodeFilter, survivor scan, k_survivorList, k_nodeWalk)",
+            "achieved": query_gbs,
+            "peak": hbm,
+            "peak_source": peak_kind,
+            "unit": "GB/s",
+            "frac": query_gbs / hbm,
+            "traffic": None,
+            "algorithmic_bytes": query_bytes,
+            "launch_group_ms": query_ms,
+            "step_algorithmic_bytes": step_bytes,
+            "step_achieved_gbs": step_bytes / (device_s / args.steps) / 1e9,
+        },
+        "clocks": clocks.summary(),
+    }
+    if args.culler:
+        line["learned_culler"] = culler_comparison(w, args, flush)
+    if cpu and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, args)
+    if ctrl0[0] or ctrl[0]:
+        line["solver_flags"] = int(ctrl[0])
+    return line
+
+
+def culler_comparison(w, args, flush):
     """Plain exact step against the learned-cull step from one start state.
 
-    The culler is trained (2^20 shell points per shape, 2,000 Adam steps) and
-    calibrated on the GPU, attached to a second engine, and both engines run
-    the same timed steps.  Missed contacts = exact contacts absent from the
-    culled run; forces are compared bit for bit.
+    The culler is trained (2^20 shell points and 2^18 interior points per
+    shape, 2,000 Adam steps) and calibrated on the GPU, attached to a second
+    engine, and both engines run the same timed steps.  Missed contacts =
+    exact contacts absent from the culled run; forces are compared bit for
+    bit.
     """
     from sand_atlas_dem_gb300.culler import LearnedCuller
     from sand_atlas_dem_gb300.engine import Engine
 
-    rate = (WORKLOAD["strain_rate_per_s"],) * 3
-    plain = engine_for(lib, pack, Engine)
-    culled = engine_for(lib, pack, Engine)
+    rate = w.rate()
+    plain = w.engine(Engine)
+    culled = w.engine(Engine)
     t = time.perf_counter()
     c = LearnedCuller(culled, points=1 << 20, steps=2000, batch=8192)
     c.train()
     c.attach(culled)
     train_s = time.perf_counter() - t
     out = {}
+    steps = min(args.steps, 50)
     for name, e in (("plain", plain), ("culled", culled)):
         e.advance(max(3, args.warmup), rate=rate)
+        set_rates(e, w)
         e.buffers["cullerStats"].copy_from_numpy(np.zeros(4, np.uint32))
-        ms = timed_steps(e, args.steps, flush)
-        out[name] = dict(value=args.grains * args.steps / (sum(ms) / 1e3), ms_per_step=sum(ms) / args.steps,
+        ms = timed_steps(e, steps, flush)
+        out[name] = dict(value=w.grains * steps / (sum(ms) / 1e3), ms_per_step=sum(ms) / steps,
                          phase_ms=e.profile_phases())
     sp, sc = plain.state(), culled.state()
     stats = culled.read("cullerStats", np.uint32, (4,))
@@ -370,12 +404,12 @@ def culler_comparison(lib, pack, args, flush):
     force_p = sp["force"][:, :3].astype(float)
     force_err = float(np.abs(sc["force"][:, :3] - force_p).max() / max(np.abs(force_p).max(), 1e-30))
     return dict(
-        plain_value=out["plain"]["value"], culled_value=out["culled"]["value"],
+        steps=steps, plain_value=out["plain"]["value"], culled_value=out["culled"]["value"],
         speedup=out["culled"]["value"] / out["plain"]["value"],
-        plain_node_query_ms=out["plain"]["phase_ms"]["node_query"],
-        culled_node_query_ms=out["culled"]["phase_ms"]["node_query"],
+        plain_node_query_ms=out["plain"]["phase_ms"]["node_filter"] + out["plain"]["phase_ms"]["node_query"],
+        culled_node_query_ms=out["culled"]["phase_ms"]["node_filter"] + out["culled"]["phase_ms"]["node_query"],
         tested_nodes=int(stats[0]), culled_nodes=int(stats[1]),
-        cull_rate_of_prefilter_survivors=float(stats[1]) / max(int(stats[0]), 1),
+        cull_rate_of_exact_queries=float(stats[1]) / max(int(stats[0]), 1),
         missed_contacts=len(keys_p - keys_c), extra_contacts=len(keys_c - keys_p),
         forces_bitwise_equal=bool(sp["force"].tobytes() == sc["force"].tobytes()),
         force_max_relative_error=force_err,
@@ -384,40 +418,54 @@ def culler_comparison(lib, pack, args, flush):
     )
 
 
-def cpu_baseline(lib, pack, args, steps=1):
-    """Oracle port of the reference CPU backend on this host's cores, one step."""
+def cpu_sample(w):
+    """Specimens the CPU oracle times: all of a single-specimen workload, the
+    first eight specimens (one at a time: the oracle has no batching) of a
+    batched one."""
+    return [[0]] if len(w.specimens) == 1 else [[k] for k in range(8)]
+
+
+def cpu_baseline(w, args, steps=1):
+    """Oracle port of the reference CPU backend on this host's cores."""
     from oracle.engine import OracleEngine
 
-    e = engine_for(lib, pack, OracleEngine, threads=args.cpu_threads)
-    rate = (WORKLOAD["strain_rate_per_s"],) * 3
-    t = time.perf_counter()
-    e.advance(steps, rate=rate)
-    seconds = time.perf_counter() - t
-    return {"value": args.grains * steps / seconds, "unit": "grain-steps/s", "cores": e.threads,
-            "kind": "port", "sample": f"{steps} full step(s) of the {args.grains}-grain workload, "
-            f"{seconds:.2f} s"}
+    grains, seconds, threads = 0, 0.0, 1
+    for chosen in cpu_sample(w):
+        e = w.engine(OracleEngine, chosen, threads=args.cpu_threads)
+        threads = e.threads
+        t = time.perf_counter()
+        e.advance(steps, rate=w.rate(chosen))
+        seconds += time.perf_counter() - t
+        grains += e.n * steps
+    what = "the whole workload" if len(w.specimens) == 1 else f"specimens 0-7 ({grains // steps} grains)"
+    return {"value": grains / seconds, "unit": "grain-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} full step(s) of {what}, {seconds:.2f} s"}
 
 
 def run_reference(args):
-    lib = library()
-    pack = packing(lib, args.grains, WORKLOAD["solid_fraction_target"])
     from oracle.engine import OracleEngine
 
-    e = engine_for(lib, pack, OracleEngine, threads=args.cpu_threads)
-    rate = (WORKLOAD["strain_rate_per_s"],) * 3
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        e.advance(1, rate=rate)
-    t = time.perf_counter()
-    e.advance(args.steps, rate=rate)
-    seconds = time.perf_counter() - t
-    value = args.grains * args.steps / seconds
+    w = Workload(args.workload, args.grains)
+    grains, seconds, threads = 0, 0.0, 1
+    for chosen in cpu_sample(w):
+        e = w.engine(OracleEngine, chosen, threads=args.cpu_threads)
+        threads = e.threads
+        rate = w.rate(chosen)
+        if args.warmup > 0:
+            e.advance(1, rate=rate)
+        t = time.perf_counter()
+        e.advance(args.steps, rate=rate)
+        seconds += time.perf_counter() - t
+        grains += e.n * args.steps
+    value = grains / seconds
     return {
         "metric": METRIC, "value": value, "unit": "grain-steps/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * seconds / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(WORKLOAD, grains=args.grains), "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": "grain-steps/s", "cores": e.threads, "kind": "port",
-                         "sample": f"{args.steps} full steps after 1 warm-up step"},
+        "config": dict(w.config), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "grain-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full steps after {min(args.warmup, 1)} warm-up step, "
+                                   f"{len(cpu_sample(w))} specimen(s)"},
         "e2e": {"value": value, "unit": "grain-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -425,18 +473,20 @@ def run_reference(args):
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=500)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
-    p.add_argument("--grains", type=int, default=WORKLOAD["grains"])
+    p.add_argument("--workload", default="dense-10k", choices=tuple(WORKLOADS))
+    p.add_argument("--grains", type=int, default=None, help="dense-10k only: grains of the packing record")
     p.add_argument("--cpu-threads", type=int, default=os.cpu_count() or 1)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--prepare-only", action="store_true")
-    p.add_argument("--packing", default="dense", choices=("dense", "lattice"))
     p.add_argument("--culler", action="store_true", help="also train the learned culler and compare")
     args = p.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
+        if args.steps > 20:
+            args.steps = 20  # a bounded CPU sample: each oracle step of 10k grains takes a fraction of a second
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)
         return
@@ -452,7 +502,8 @@ def main():
         dist.init_process_group("nccl")
         dist.barrier()
         line = run_gb300(args, cpu=rank == 0)
-        job = aggregate(args.grains * args.steps, line["ms_per_step"] * args.steps / 1e3, device="cuda")
+        grains = line["config"]["grains"]
+        job = aggregate(grains * args.steps, line["ms_per_step"] * args.steps / 1e3, device="cuda")
         if rank == 0:
             line["n_gpus"] = job["ranks"]
             line["ms_per_step"] = 1e3 * job["seconds"] / args.steps
@@ -463,9 +514,8 @@ def main():
         dist.destroy_process_group()
         return
     if args.prepare_only:
-        lib = library()
-        pack = packing(lib, args.grains, WORKLOAD["solid_fraction_target"])
-        print(json.dumps({"prepared": True, "path": pack.get("path")}))
+        w = Workload(args.workload, args.grains)
+        print(json.dumps({"prepared": True, "grains": w.grains}))
         return
     print(json.dumps(run_gb300(args)), flush=True)
 

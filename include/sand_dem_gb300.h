@@ -11,7 +11,7 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 113) this backend's extension buffers, in the order of
+ *   [77, 117) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
@@ -21,10 +21,13 @@
  *             enclosure plane facing the source, the specimen of each
  *             grain and each specimen's bin grid, the learned culler's
  *             per-shape FP32 parameters, BF16 hidden weights, margins and
- *             two counters, and the survivor mask and first survivor of
- *             each item and the (item, node slot) list of survivors: the
- *             nodes left for the exact query after the conservative
- *             filters).
+ *             two counters, the survivor mask and first survivor of each
+ *             item and the (item, node slot) list of survivors -- the nodes
+ *             left for the exact query after the conservative filters --
+ *             and, for the learned culler, a keep flag per survivor, its
+ *             exclusive scan and the list of kept survivors, and per
+ *             directed pair the enclosure plane carried into the source
+ *             grain's frame with its rejection-bound terms).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
@@ -55,9 +58,9 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 113
+#define SDG_BUFFER_COUNT 117
 #define SDG_VALUE_COUNT 37
-#define SDG_PHASES 8
+#define SDG_PHASES 9
 
 /* ABI revision of this header. */
 int sdg_abi_version(void);
@@ -141,8 +144,9 @@ int sdg_engine_advance(void* engine, void* const* buffers, const uint64_t* bytes
 
 /*
  * One committed step with CUDA events between phases; writes SDG_PHASES
- * device milliseconds: drift, neighbours, pair cull, node queries, contact
- * emit, friction history + contact law, force gather, final kick.
+ * device milliseconds: drift, neighbours, pair cull, node filter (with the
+ * survivor list and the learned culler), exact node queries, contact emit,
+ * friction history + contact law, force gather, final kick.
  * Replaces Engine.profile_step's timestamp queries (gpu.py:938-1014).
  */
 int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes, const double* values,

@@ -33,10 +33,10 @@ SPACE = {
     "walk_blocks_per_sm": (2, 4, 8, 16),
 }
 PHASES = {
-    "query_warps": ("node_query",),
-    "query_blocks_per_sm": ("node_query",),
+    "query_warps": ("node_filter",),
+    "query_blocks_per_sm": ("node_filter",),
     "cull_blocks_per_sm": ("pair_cull",),
-    "contact_blocks_per_sm": ("contact_emit", "friction_and_history"),
+    "contact_blocks_per_sm": ("node_filter", "contact_emit", "friction_and_history"),
     "gather_warps_per_sm": ("force_reduction",),
     "walk_blocks_per_sm": ("node_query",),
 }

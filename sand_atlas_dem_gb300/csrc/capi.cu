@@ -72,7 +72,10 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
             bytes[77 + 24] < uint64_t(c.survivorCapacity) * 32 || bytes[77 + 35] < uint64_t(c.survivorCapacity) * 8 ||
             bytes[77 + 33] < uint64_t(c.candidateCapacity) * 8 ||
             bytes[77 + 34] < (uint64_t(c.candidateCapacity) + 1) * 4 ||
-            bytes[77 + 25] < (uint64_t(c.candidateCapacity) + 1) * 4) {
+            bytes[77 + 25] < (uint64_t(c.candidateCapacity) + 1) * 4 ||
+            bytes[77 + 36] < (uint64_t(c.survivorCapacity) + 1) * 4 ||
+            bytes[77 + 37] < (uint64_t(c.survivorCapacity) + 1) * 4 || bytes[77 + 38] < uint64_t(c.survivorCapacity) * 4 ||
+            bytes[77 + 39] < uint64_t(4) * c.pairCapacity * 16) {
             g_error = "a buffer is smaller than its configured capacity";
             return 1;
         }
@@ -190,15 +193,15 @@ int sdg_dispatch(const char* kernel, uint32_t count, void* const* buffers, const
 // Phase timing of one step (events between the launch groups of
 // launch_step; not graph-captured).  phase_ms receives SDG_PHASES values:
 // drift (checkContactTimestep, beginStep, advanceCell, checkRebuild),
-// neighbours, pair setup + leaf cull + item emit, exact node queries,
-// contact emit, friction history + contact law, force gather, final kick.
+// neighbours, pair setup + leaf cull + item emit, node filter + survivor
+// list, exact node queries, contact emit, friction history + contact law, force gather, final kick.
 int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes, const double* values,
                        uint32_t nvalues, float* phase_ms, void* stream) {
     if (!engine || !phase_ms) { g_error = "null argument"; return 1; }
     Params P;
     if (int rc = unpack(buffers, bytes, values, nvalues, P)) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const int phases = 8;
+    const int phases = 9;
     cudaEvent_t ev[phases + 1];
     for (auto& e : ev)
         if (int rc = record(cudaEventCreate(&e), "event")) return rc;
@@ -215,17 +218,19 @@ int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes
     cudaEventRecord(ev[2], s);
     launch_contacts("collectCull", P, 0, s);
     cudaEventRecord(ev[3], s);
-    launch_contacts("collectQuery", P, 0, s);
+    launch_contacts("collectFilter", P, 0, s);
     cudaEventRecord(ev[4], s);
-    launch_contacts("collectEmit", P, 0, s);
+    launch_contacts("collectWalk", P, 0, s);
     cudaEventRecord(ev[5], s);
-    launch_contacts("resolveContacts", P, 0, s);
+    launch_contacts("collectEmit", P, 0, s);
     cudaEventRecord(ev[6], s);
+    launch_contacts("resolveContacts", P, 0, s);
+    cudaEventRecord(ev[7], s);
     launch_contacts("gather", P, c.N, s);
     if (c.activeTimestep) launch_state("checkContactTimestep", P, c.N, s);
-    cudaEventRecord(ev[7], s);
-    launch_state("finishStep", P, c.N, s);
     cudaEventRecord(ev[8], s);
+    launch_state("finishStep", P, c.N, s);
+    cudaEventRecord(ev[9], s);
     int rc = record(cudaEventSynchronize(ev[phases]), "profile sync");
     for (int k = 0; k < phases && !rc; ++k) rc = record(cudaEventElapsedTime(&phase_ms[k], ev[k], ev[k + 1]), "elapsed");
     for (auto& e : ev) cudaEventDestroy(e);

@@ -109,8 +109,12 @@ struct Res {
     uint2* candSurvMask;              // candidateCapacity: 64-bit mask of the item's surviving nodes
     uint32_t* candSurvOffset;         // candidateCapacity+1: first survivor of each item
     uint2* survivors;                 // survivorCapacity: (item, node slot) of each surviving node
+    uint32_t* survKeep;               // survivorCapacity+1: 1 = the learned culler keeps the survivor
+    uint32_t* keepOffset;             // survivorCapacity+1: exclusive scan of survKeep
+    uint32_t* walkList;               // survivorCapacity: survivors left for the exact query
+    float4* dpairSourcePlane;         // 4*pairCapacity: the enclosure plane in the source frame, and its bound terms
 };
-constexpr int EXTENSION_COUNT = 36;
+constexpr int EXTENSION_COUNT = 40;
 constexpr int CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4;
 constexpr int BUFFER_COUNT = RESOURCE_COUNT + EXTENSION_COUNT;
 constexpr int CONFIG_VALUES = 25;
@@ -119,6 +123,7 @@ constexpr int SCAN_BLOCKS = 608;  // 4 per SM on a 152-SM GB300
 // work[] slots
 constexpr int W_CANDIDATES = 0;
 constexpr int W_SURVIVORS = 2;
+constexpr int W_KEPT = 3;
 
 struct Params {
     Config c;
@@ -299,18 +304,25 @@ __device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 
     f3 nearest = mk(0.f, 0.f, 0.f);
     uint32_t nearestNormal = 0;
     bool found = false;
+    // "While-while" form: each lane pops and expands internal nodes until it
+    // pops a leaf (or empties its stack), then the lanes test their leaves'
+    // triangles together.  Every lane visits the same nodes in the same order
+    // as the single loop, so the result is the same; only the SIMT schedule
+    // differs.
     while (top > 0) {
-        uint32_t slot = --top, node = pending[slot];
-        if (pendingDistance[slot] > best) continue;
-        uint4 link = __ldg(&r.meshLinks[node]);
-        if (link.z == 0) {
+        uint4 link = make_uint4(0u, 0u, 0u, 0u);
+        while (top > 0) {
+            uint32_t slot = --top, node = pending[slot];
+            if (pendingDistance[slot] > best) continue;
+            link = __ldg(&r.meshLinks[node]);
+            if (link.z != 0) break;
             uint32_t a = node + 1, b = __ldg(&r.meshLinks[a].x);
             float da = meshBoxDistance(r, a, p), db = meshBoxDistance(r, b, p);
             if (da < db) { uint32_t s = a; a = b; b = s; float ds = da; da = db; db = ds; }
             if (top + 2 > 32) { fail(r, F_STACK); return make_float4(0.f, 0.f, 0.f, 1e20f); }
             if (da <= best) { pending[top] = a; pendingDistance[top++] = da; }
             if (db <= best) { pending[top] = b; pendingDistance[top++] = db; }
-            continue;
+            link.z = 0;
         }
         for (uint32_t k = 0; k < link.z; ++k) {
             uint32_t triangle = link.y + k, feature;

@@ -352,19 +352,49 @@ __global__ void k_resetContacts(const __grid_constant__ Params P) {
 // 404-417) + meshBoxMayContact (:274-288) on every leaf, gated by the root
 // mask.  Equivalent in contacts to the reference's hierarchical walks since
 // every test is conservative and each node's decision is exact.
-// True when every point of the box [low, high] (a leaf's nodes in the target
-// frame, meshPairBounds) lies beyond the enclosure plane by more than the
-// largest per-node pad nodePrefilter could allow there, with a relative
-// slack far above the FP32 rounding of either evaluation: then the plane
-// test rejects every node of the leaf and the leaf need not become an item.
-__device__ __forceinline__ bool leafBeyondPlane(float4 plane, f3 low, f3 high) {
-    f3 n = xyz(plane), centre = 0.5f * (low + high), half = 0.5f * (high - low);
-    float nearest = __fsub_rn(__fadd_rn(dot(n, centre), plane.w), dot(abs3(n), half));
-    float extent = mx(mx(mx(fabsf(low.x), fabsf(high.x)), mx(fabsf(low.y), fabsf(high.y))),
-                      mx(fabsf(low.z), fabsf(high.z)));
-    float pad = __fmul_rn(0.00000762939453125f, __fadd_rn(1.0f, extent));
-    float slack = __fmul_rn(1e-5f, __fadd_rn(__fadd_rn(1.0f, fabsf(plane.w)), dot(abs3(n), abs3(centre) + half)));
-    return nearest > __fadd_rn(pad, slack);
+// The enclosure plane test in the source grain's own frame.  With m the
+// target-frame normal n rotated to the world, the plane value of a node at
+// x (source shape frame, unscaled) is n.local + w = n'.x + w' with
+// n' = (s_src/s_dst) qinv(q_src, m) and w' = w - m.branch/s_dst, so one
+// 3-term dot per node replaces the two quaternion rotations.  A node (or a
+// whole leaf box) is rejected only when n'.x + w' exceeds an upper bound of
+// the reference pad 2^-17 (1 + max|local|) -- |local| <= (s_src |x| +
+// |branch|) / s_dst -- plus a slack 1e-5 x the magnitudes involved, far
+// above the FP32 rounding of either evaluation order.  Such a node would be
+// rejected by the reference's own plane test: no contact changes.
+struct SourcePlane {
+    float4 plane;  // n', w'
+    float4 scale;  // s_src/s_dst, |branch|_1/s_dst, |w|, |n'|_1
+};
+__device__ __forceinline__ SourcePlane sourcePlane(float4 plane, float4 qs, float4 qd, float ss, float sd, f3 branch) {
+    SourcePlane sp;
+    f3 m = qrot(qd, xyz(plane));
+    float k = __fdiv_rn(ss, sd);
+    f3 n = qinv(qs, m) * k;
+    float w = __fsub_rn(plane.w, __fdiv_rn(dot(m, branch), sd));
+    float bn = __fdiv_rn(__fadd_rn(__fadd_rn(fabsf(branch.x), fabsf(branch.y)), fabsf(branch.z)), sd);
+    sp.plane = w4(n, w);
+    sp.scale = make_float4(k, bn, fabsf(plane.w), __fadd_rn(__fadd_rn(fabsf(n.x), fabsf(n.y)), fabsf(n.z)));
+    return sp;
+}
+// Rejection bound for points with |x|_1 <= extent.
+__device__ __forceinline__ float sourcePlaneBound(const SourcePlane& sp, float extent) {
+    float reach = __fadd_rn(__fmul_rn(sp.scale.x, extent), sp.scale.y);
+    float pad = __fmul_rn(0.00000762939453125f, __fadd_rn(1.0f, reach));
+    float slack = __fmul_rn(1e-5f, __fadd_rn(__fadd_rn(__fadd_rn(1.0f, sp.scale.z), reach),
+                                            __fmul_rn(sp.scale.w, extent)));
+    return __fadd_rn(pad, slack);
+}
+__device__ __forceinline__ bool nodeBeyondSourcePlane(const SourcePlane& sp, f3 x) {
+    float extent = __fadd_rn(__fadd_rn(fabsf(x.x), fabsf(x.y)), fabsf(x.z));
+    return __fadd_rn(dot(xyz(sp.plane), x), sp.plane.w) > sourcePlaneBound(sp, extent);
+}
+__device__ __forceinline__ bool leafBeyondSourcePlane(const SourcePlane& sp, f3 low, f3 high) {
+    f3 c = 0.5f * (low + high), h = 0.5f * (high - low);
+    float nearest = __fsub_rn(__fadd_rn(dot(xyz(sp.plane), c), sp.plane.w), dot(abs3(xyz(sp.plane)), h));
+    float extent = __fadd_rn(__fadd_rn(__fadd_rn(fabsf(c.x), fabsf(c.y)), fabsf(c.z)),
+                             __fadd_rn(__fadd_rn(h.x, h.y), h.z));
+    return nearest > sourcePlaneBound(sp, extent);
 }
 __global__ void k_leafCull(const __grid_constant__ Params P) {
     const Res& r = P.r;
@@ -380,6 +410,7 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
             uint4 li = __ldg(&r.meshLeafInfo[r.shapeId[i]]);
             uint32_t targetShape = r.shapeId[j];
             float4 plane;
+            SourcePlane source;
             // Enclosure plane of the target most violated by the source centre
             // (cpu_scheduling.slang:58-71): warp arg-max, lowest index on ties.
             {
@@ -402,15 +433,23 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
                     if (ob > best || (ob == best && oi < bestIndex)) { best = ob; bestIndex = oi; }
                 }
                 plane = bestIndex == EMPTY ? make_float4(0.f, 0.f, 0.f, 0.f) : __ldg(&r.meshPlanes[bestIndex]);
-                if (laneId() == 0) r.dpairPlane[d] = plane;
+                source = sourcePlane(plane, r.rotation[i], r.rotation[j], r.body[i].x, r.body[j].x, branch);
+                if (laneId() == 0) {
+                    r.dpairPlane[d] = plane;
+                    r.dpairSourcePlane[2 * d] = source.plane;
+                    r.dpairSourcePlane[2 * d + 1] = source.scale;
+                }
             }
             for (uint32_t k0 = 0; k0 < li.y; k0 += WARP) {
                 uint32_t k = k0 + laneId();
                 bool hit = false;
                 if (k < li.y) {
+                    uint32_t leaf = __ldg(&r.meshLeaves[li.x + k]);
                     f3 low, high;
-                    meshPairBounds(r, d, __ldg(&r.meshLeaves[li.x + k]), low, high);
-                    hit = meshBoxMayContact(r, targetShape, low, high) && !leafBeyondPlane(plane, low, high);
+                    meshPairBounds(r, d, leaf, low, high);
+                    hit = meshBoxMayContact(r, targetShape, low, high) &&
+                          !leafBeyondSourcePlane(source, xyz(__ldg(&r.meshClusterMin[leaf])),
+                                                 xyz(__ldg(&r.meshClusterMax[leaf])));
                 }
                 uint32_t m = __ballot_sync(0xffffffffu, hit);
                 if (laneId() == 0) r.leafMask[size_t(d) * c.leafWords + k0 / WARP] = m;
@@ -443,60 +482,44 @@ __global__ void k_leafEmit(const __grid_constant__ Params P) {
         }
     }
 }
-// Node query in two stages.  The filter stage (one warp per (directed pair,
+// Node query in stages.  The filter stage (one warp per (directed pair,
 // leaf) item, two nodes per lane) applies the conservative rejections -- the
-// enclosure plane, the hull and, when enabled, the learned culler -- and
-// records each item's surviving nodes as a 64-bit mask.  A scan turns the
-// survivor counts into offsets, the survivors are listed in canonical order,
-// and the exact stage runs one thread per survivor: full warps of BVH walks
-// instead of warps in which most lanes were rejected and idle.  Each hit sets
-// its bit in the item's hit mask (integer atomics: the result does not depend
-// on their order) and keeps its record in the survivor's scratch slot; the
-// emit pass copies hits to their canonical offsets.
-template <bool CULL>
+// enclosure plane and the hull -- and records each item's surviving nodes as
+// a 64-bit mask.  A scan turns the survivor counts into offsets and the
+// survivors are listed in canonical order.  With the learned culler on, one
+// pass evaluates the target's network for 64 survivors per warp on tensor
+// cores and a scan keeps the ones it cannot rule out.  The exact stage runs
+// one thread per remaining survivor: full warps of BVH walks instead of
+// warps in which most lanes were rejected and idle.  Each hit sets its bit in
+// the item's hit mask (integer atomics: the result does not depend on their
+// order) and keeps its record in the survivor's scratch slot; the emit pass
+// copies hits to their canonical offsets.
 __global__ void __launch_bounds__(256) k_nodeFilter(const __grid_constant__ Params P) {
-    extern __shared__ uint32_t cullTiles[];
     const Res& r = P.r;
     const Config& c = P.c;
     uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
-    uint32_t* tile = cullTiles + (threadIdx.x >> 5) * CULLER_TILE_WORDS;
     for (uint32_t item = warpGlobal(); item < n; item += warpStride()) {
-        // One read of the failure word per item, shared by the warp, so the
-        // warp-wide culler steps below are reached by every lane or none.
-        uint32_t live = __shfl_sync(0xffffffffu, r.control[0] == 0 ? 1u : 0u, 0);
         bool keep0 = false, keep1 = false;
-        if (live) {
+        if (r.control[0] == 0) {
             uint2 cd = r.candidates[item];
             uint32_t d = cd.x, p = d >> 1, pass = d & 1;
             uint2 ij = r.pairs[p];
             uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
             f3 branch = xyz(r.dpairBranch[d]);
             float4 plane = r.dpairPlane[d];
+            SourcePlane source{r.dpairSourcePlane[2 * d], r.dpairSourcePlane[2 * d + 1]};
             uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
+            const float4* samples = r.sample + __ldg(&r.sampleInfo[r.shapeId[src]].x);
             uint32_t k0 = laneId(), k1 = laneId() + WARP;
             uint32_t node0 = k0 < range.y ? __ldg(&r.meshSampleIndices[range.x + k0]) : 0;
             uint32_t node1 = k1 < range.y ? __ldg(&r.meshSampleIndices[range.x + k1]) : 0;
-            f3 arm0 = mk(0.f, 0.f, 0.f), local0 = arm0, arm1 = arm0, local1 = arm0;
-            keep0 = k0 < range.y && nodePrefilter(r, src, dst, node0, branch, &plane, arm0, local0);
-            keep1 = k1 < range.y && nodePrefilter(r, src, dst, node1, branch, &plane, arm1, local1);
-            if (CULL && __any_sync(0xffffffffu, keep0 || keep1)) {
-                // Learned culler: skip survivors the target's network places
-                // beyond its calibrated margin; the rest take the exact query.
-                uint32_t target = r.shapeId[dst];
-                float y0, y1;
-                cullerTile(r.cullerParams + size_t(target) * CULLER_PARAMS, r.cullerW1 + size_t(target) * 2048,
-                           local0, local1, tile, y0, y1);
-                float margin = r.cullerMargin[target];
-                bool cut0 = keep0 && y0 > margin, cut1 = keep1 && y1 > margin;
-                uint32_t tested = __popc(__ballot_sync(0xffffffffu, keep0)) + __popc(__ballot_sync(0xffffffffu, keep1));
-                uint32_t culled = __popc(__ballot_sync(0xffffffffu, cut0)) + __popc(__ballot_sync(0xffffffffu, cut1));
-                if (laneId() == 0) {
-                    atomicAdd(&r.cullerStats[0], tested);
-                    atomicAdd(&r.cullerStats[1], culled);
-                }
-                keep0 = keep0 && !cut0;
-                keep1 = keep1 && !cut1;
-            }
+            // One dot per node against the source-frame plane; the few nodes
+            // left take the exact placement, the target-frame plane and the hull.
+            keep0 = k0 < range.y && !nodeBeyondSourcePlane(source, xyz(__ldg(&samples[node0])));
+            keep1 = k1 < range.y && !nodeBeyondSourcePlane(source, xyz(__ldg(&samples[node1])));
+            f3 arm, local;
+            if (keep0) keep0 = nodePrefilter(r, src, dst, node0, branch, &plane, arm, local);
+            if (keep1) keep1 = nodePrefilter(r, src, dst, node1, branch, &plane, arm, local);
         }
         uint32_t m0 = __ballot_sync(0xffffffffu, keep0), m1 = __ballot_sync(0xffffffffu, keep1);
         if (laneId() == 0) {
@@ -506,6 +529,80 @@ __global__ void __launch_bounds__(256) k_nodeFilter(const __grid_constant__ Para
             r.candHitCount[item] = 0;
         }
     }
+}
+// Source node, partner and target-frame position of survivor s (the same
+// expressions as nodePrefilter: the same arm and local bits).
+struct SurvivorNode {
+    uint32_t item, slot, src, dst, node;
+    f3 arm, local;
+};
+__device__ __forceinline__ SurvivorNode survivorNode(const Res& r, uint32_t s) {
+    SurvivorNode v;
+    uint2 sv = r.survivors[s];
+    v.item = sv.x;
+    v.slot = sv.y;
+    uint2 cd = r.candidates[sv.x];
+    uint32_t d = cd.x, p = d >> 1, pass = d & 1;
+    uint2 ij = r.pairs[p];
+    v.src = pass ? ij.y : ij.x;
+    v.dst = pass ? ij.x : ij.y;
+    v.node = __ldg(&r.meshSampleIndices[__ldg(&r.meshClusterRanges[cd.y]).x + sv.y]);
+    float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[r.shapeId[v.src]].x) + v.node]);
+    v.arm = qrot(r.rotation[v.src], xyz(sp) * r.body[v.src].x);
+    v.local = qinv(r.rotation[v.dst], v.arm - xyz(r.dpairBranch[d])) / r.body[v.dst].x;
+    return v;
+}
+// Learned culler over the survivor list: 64 survivors per warp iteration
+// (two per lane), one tensor-core tile per distinct target shape among them.
+// keep[s] = 0 when the target's network places survivor s beyond the
+// shape's calibrated margin; the exact query decides every other survivor.
+__global__ void __launch_bounds__(256) k_cullSurvivors(const __grid_constant__ Params P) {
+    extern __shared__ uint32_t cullTiles[];
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t* tile = cullTiles + (threadIdx.x >> 5) * CULLER_TILE_WORDS;
+    uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
+    if (r.control[0] != 0) n = 0;
+    uint32_t groups = (n + 63) / 64;
+    for (uint32_t g = warpGlobal(); g < groups; g += warpStride()) {
+        uint32_t s0 = 64 * g + laneId(), s1 = s0 + WARP;
+        bool valid0 = s0 < n, valid1 = s1 < n;
+        f3 l0 = mk(0.f, 0.f, 0.f), l1 = l0;
+        uint32_t t0 = EMPTY, t1 = EMPTY;
+        if (valid0) { SurvivorNode v = survivorNode(r, s0); l0 = v.local; t0 = r.shapeId[v.dst]; }
+        if (valid1) { SurvivorNode v = survivorNode(r, s1); l1 = v.local; t1 = r.shapeId[v.dst]; }
+        bool pending0 = valid0, pending1 = valid1, cut0 = false, cut1 = false;
+        for (;;) {
+            uint32_t b0 = __ballot_sync(0xffffffffu, pending0), b1 = __ballot_sync(0xffffffffu, pending1);
+            if ((b0 | b1) == 0) break;
+            uint32_t target = b0 ? __shfl_sync(0xffffffffu, t0, __ffs(b0) - 1)
+                                 : __shfl_sync(0xffffffffu, t1, __ffs(b1) - 1);
+            bool in0 = pending0 && t0 == target, in1 = pending1 && t1 == target;
+            float y0, y1;
+            cullerTile(r.cullerParams + size_t(target) * CULLER_PARAMS, r.cullerW1 + size_t(target) * 2048,
+                       in0 ? l0 : mk(0.f, 0.f, 0.f), in1 ? l1 : mk(0.f, 0.f, 0.f), tile, y0, y1);
+            float margin = r.cullerMargin[target];
+            if (in0) { cut0 = y0 > margin; pending0 = false; }
+            if (in1) { cut1 = y1 > margin; pending1 = false; }
+        }
+        if (valid0) r.survKeep[s0] = cut0 ? 0u : 1u;
+        if (valid1) r.survKeep[s1] = cut1 ? 0u : 1u;
+        uint32_t tested = __popc(__ballot_sync(0xffffffffu, valid0)) + __popc(__ballot_sync(0xffffffffu, valid1));
+        uint32_t culled = __popc(__ballot_sync(0xffffffffu, cut0)) + __popc(__ballot_sync(0xffffffffu, cut1));
+        if (laneId() == 0) {
+            atomicAdd(&r.cullerStats[0], tested);
+            atomicAdd(&r.cullerStats[1], culled);
+        }
+    }
+}
+// Survivors the culler kept, in order (their survivor indices).
+__global__ void k_walkList(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
+    for (uint32_t s = gtid(); s < n; s += gstride())
+        if (r.survKeep[s]) r.walkList[r.keepOffset[s]] = s;
 }
 // Survivor list in canonical (item, node slot) order.
 __global__ void k_survivorList(const __grid_constant__ Params P) {
@@ -527,29 +624,21 @@ __global__ void k_survivorList(const __grid_constant__ Params P) {
         }
     }
 }
-// Exact query, one thread per survivor.
+// Exact query, one thread per survivor (per kept survivor with the culler).
 __global__ void __launch_bounds__(256) k_nodeWalk(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
     if (r.control[0] != 0) return;
-    uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
-    for (uint32_t s = gtid(); s < n; s += gstride()) {
-        uint2 sv = r.survivors[s];
-        uint2 cd = r.candidates[sv.x];
-        uint32_t d = cd.x, p = d >> 1, pass = d & 1;
-        uint2 ij = r.pairs[p];
-        uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
-        uint32_t node = __ldg(&r.meshSampleIndices[__ldg(&r.meshClusterRanges[cd.y]).x + sv.y]);
-        // The same expressions as nodePrefilter: the same arm and local bits.
-        float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[r.shapeId[src]].x) + node]);
-        f3 arm = qrot(r.rotation[src], xyz(sp) * r.body[src].x);
-        f3 local = qinv(r.rotation[dst], arm - xyz(r.dpairBranch[d])) / r.body[dst].x;
+    uint32_t n = min(r.work[c.cullerEnabled ? W_KEPT : W_SURVIVORS], c.survivorCapacity);
+    for (uint32_t t = gtid(); t < n; t += gstride()) {
+        uint32_t s = c.cullerEnabled ? r.walkList[t] : t;
+        SurvivorNode v = survivorNode(r, s);
         float4 pd, na;
-        if (nodeExact(r, c, src, dst, node, arm, local, pd, na)) {
+        if (nodeExact(r, c, v.src, v.dst, v.node, v.arm, v.local, pd, na)) {
             r.hitScratch[2 * s] = pd;
             r.hitScratch[2 * s + 1] = na;
-            atomicOr(sv.y < WARP ? &r.candHitMask[sv.x].x : &r.candHitMask[sv.x].y, 1u << (sv.y & 31u));
-            atomicAdd(&r.candHitCount[sv.x], 1u);
+            atomicOr(v.slot < WARP ? &r.candHitMask[v.item].x : &r.candHitMask[v.item].y, 1u << (v.slot & 31u));
+            atomicAdd(&r.candHitCount[v.item], 1u);
         }
     }
 }
@@ -875,26 +964,35 @@ static void collectCull(const Params& P, cudaStream_t s) {
                 r.work + W_CANDIDATES, nullptr, r.scanPartials, s);
     k_leafEmit<<<g, T, 0, s>>>(P);
 }
-static void collectQuery(const Params& P, cudaStream_t s) {
+// Node filter, survivor list and (with the learned culler) the kept list.
+static void collectFilter(const Params& P, cudaStream_t s) {
     const Res& r = P.r;
     const Config& c = P.c;
     uint32_t warps = c.queryWarps == 4 ? 4 : 8;
-    uint32_t g = grid(c.queryBlocksPerSM, 8);
-    if (c.cullerEnabled) {
-        static bool attributed = false;
-        if (!attributed) {
-            cudaFuncSetAttribute(k_nodeFilter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 int(8 * CULLER_TILE_WORDS * sizeof(uint32_t)));
-            attributed = true;
-        }
-        k_nodeFilter<true><<<g, 32 * warps, warps * CULLER_TILE_WORDS * sizeof(uint32_t), s>>>(P);
-    } else {
-        k_nodeFilter<false><<<g, 32 * warps, 0, s>>>(P);
-    }
+    k_nodeFilter<<<grid(c.queryBlocksPerSM, 8), 32 * warps, 0, s>>>(P);
     launch_scan(r.candSurvCount, r.candSurvOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0},
                 true, r.work + W_SURVIVORS, nullptr, r.scanPartials, s);
     k_survivorList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
-    k_nodeWalk<<<grid(c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
+    if (c.cullerEnabled) {
+        static bool attributed = false;
+        if (!attributed) {
+            cudaFuncSetAttribute(k_cullSurvivors, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(8 * CULLER_TILE_WORDS * sizeof(uint32_t)));
+            attributed = true;
+        }
+        k_cullSurvivors<<<grid(c.queryBlocksPerSM, 2), 256, 8 * CULLER_TILE_WORDS * sizeof(uint32_t), s>>>(P);
+        launch_scan(r.survKeep, r.keepOffset, ScanCount{r.work + W_SURVIVORS, c.survivorCapacity, 1, 0}, true,
+                    r.work + W_KEPT, nullptr, r.scanPartials, s);
+        k_walkList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
+    }
+}
+// The exact queries.
+static void collectWalk(const Params& P, cudaStream_t s) {
+    k_nodeWalk<<<grid(P.c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
+}
+static void collectQuery(const Params& P, cudaStream_t s) {
+    collectFilter(P, s);
+    collectWalk(P, s);
 }
 // Canonical offsets of the hits, the contact records and per-pair starts.
 static void collectEmit(const Params& P, cudaStream_t s) {
@@ -919,6 +1017,8 @@ int launch_contacts(const std::string_view& name, const Params& P, uint32_t coun
     else if (name == "collect") contacts(P, s);
     else if (name == "collectCull") collectCull(P, s);
     else if (name == "collectQuery") collectQuery(P, s);
+    else if (name == "collectFilter") collectFilter(P, s);
+    else if (name == "collectWalk") collectWalk(P, s);
     else if (name == "collectEmit") collectEmit(P, s);
     else if (name == "resolveContacts") k_resolve<<<grid(c.contactBlocksPerSM, 8), T, 0, s>>>(P);
     else if (name == "gather") k_gather<<<min(blocks(c.N, 8), max(1u, grid(c.gatherWarps, 64) / 8)), T, 0, s>>>(P);

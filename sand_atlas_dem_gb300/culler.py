@@ -4,8 +4,9 @@ One small signed-distance network per shape,
 ``h0 = sin(W0 p + b0)``, ``h1 = relu(W1 h0 + b1)``, ``y = w2 . h1 + b2``
 (3 -> 64 Fourier features -> 64 -> 1), trained on the GPU by this
 package's own forward/backward kernels (``csrc/culler.cu``) on points
-uniform in a shell of +-``shell`` around each surface, labelled by the exact
-BVH distance the contact query itself computes.  At run time the hidden
+uniform in a shell of +-``shell`` around each surface and, a quarter as many,
+uniform in the interior, labelled by the exact BVH distance the contact query
+itself computes.  At run time the hidden
 layer runs on tensor cores (BF16 weights, FP32 accumulation, ``csrc/
 culler.cuh``) inside the node-query warps.
 
@@ -114,7 +115,12 @@ class LearnedCuller:
     @_engine_stream
     def train(self, log=None):
         torch = _torch()
-        self.training_points = self.sample(self.points, self.seed)
+        # The shell (where the decisions are made) and, a quarter as many,
+        # the deep interior, so that predictions there are negative too.
+        shell = self.sample(self.points, self.seed).view(self.shapes, self.points, 4)
+        inside = self.sample(self.points // 4, self.seed + 17, inside_only=True).view(self.shapes, -1, 4)
+        self.training_points = torch.cat([shell, inside], dim=1).reshape(-1, 4).contiguous()
+        per_shape = self.training_points.shape[0] // self.shapes
         n = self.shapes * self.params_per_shape
         grads = torch.zeros(n, dtype=torch.float32, device=self.device)
         m = torch.zeros_like(grads)
@@ -126,7 +132,7 @@ class LearnedCuller:
         for step in range(self.steps):
             lr = self.lr * (0.1 ** (step / max(1, self.steps)))
             native.check(self.lib.sdg_culler_train_step(
-                _ptr(self.params), _ptr(self.training_points), self.shapes, self.points, self.batch, step,
+                _ptr(self.params), _ptr(self.training_points), self.shapes, per_shape, self.batch, step,
                 self.seed, self.shell, lr, _ptr(grads), _ptr(m), _ptr(v), _ptr(scratch),
                 ct.cast(ct.c_void_p(loss.data_ptr()), ct.POINTER(ct.c_float)), s))
             if step % 100 == 0 or step == self.steps - 1:
@@ -145,8 +151,9 @@ class LearnedCuller:
         grads = torch.zeros(self.shapes * self.params_per_shape, dtype=torch.float32, device=self.device)
         rows = self.shapes * self.batch
         scratch = torch.zeros(4 * rows * H + 3 * rows, dtype=torch.float32, device=self.device)
+        per_shape = self.training_points.shape[0] // self.shapes
         native.check(self.lib.sdg_culler_gradients(
-            _ptr(self.params), _ptr(self.training_points), self.shapes, self.points, self.batch, step, self.seed,
+            _ptr(self.params), _ptr(self.training_points), self.shapes, per_shape, self.batch, step, self.seed,
             self.shell, _ptr(grads), _ptr(scratch), ct.c_void_p(self.stream.cuda_stream)))
         self.stream.synchronize()
         index = scratch[4 * rows * H + 2 * rows:].view(torch.int32)[:rows].cpu().numpy().view(np.uint32)

@@ -39,7 +39,8 @@ EXTENSION_ORDER = (
     "candHitCount", "candHitOffset", "candHitMask", "contactPair", "sidePairOffsets", "sidePairB",
     "sideContactStart", "oldPairOffsets", "oldPairB", "oldContactStart", "work", "scanPartials",
     "hitScratch", "candSurvCount", "dpairPlane", "grainSpecimen", "specimenBins", "cullerParams", "cullerW1",
-    "cullerMargin", "cullerStats", "candSurvMask", "candSurvOffset", "survivors",
+    "cullerMargin", "cullerStats", "candSurvMask", "candSurvOffset", "survivors", "survKeep", "keepOffset",
+    "walkList", "dpairSourcePlane",
 )
 CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4
 BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
@@ -79,6 +80,7 @@ class DeviceBuffer:
         with torch.cuda.stream(engine.stream):
             self.tensor.copy_(torch.from_numpy(data.copy()), non_blocking=False)
         engine.stream.synchronize()
+        engine.h2d_bytes += data.size
 
     def write_prefix(self, array):
         torch = _torch()
@@ -90,11 +92,13 @@ class DeviceBuffer:
             with torch.cuda.stream(engine.stream):
                 self.tensor[: data.size].copy_(torch.from_numpy(data.copy()))
             engine.stream.synchronize()
+            engine.h2d_bytes += data.size
 
     def to_numpy(self, dtype=np.uint8, count=None):
         engine = self._engine()
         engine.stream.synchronize()
         nbytes = self.size if count is None else int(count) * np.dtype(dtype).itemsize
+        engine.d2h_bytes += nbytes
         return self.tensor[:nbytes].cpu().numpy().view(dtype).copy()
 
 
@@ -172,6 +176,8 @@ class Engine:
         self.use_graph = use_graph
         self.culler = None
         self.tuning = {}
+        # Host<->device bytes moved by this engine's own reads and uploads.
+        self.h2d_bytes = self.d2h_bytes = 0
         for name in ("length_unit", "time_unit", "mass_unit", "force_unit", "stress_unit", "energy_unit",
                      "ids", "scales", "body", "skin", "cutoff", "bins", "bin_count", "pair_capacity",
                      "contact_capacity", "hash_size", "bin_capacity", "initial_cell"):
@@ -208,6 +214,8 @@ class Engine:
             "hitScratch": 32 * self.survivor_capacity, "candSurvCount": 4 * (self.candidate_capacity + 1),
             "dpairPlane": 16 * 2 * pc, "candSurvMask": 8 * self.candidate_capacity,
             "candSurvOffset": 4 * (self.candidate_capacity + 1), "survivors": 8 * self.survivor_capacity,
+            "survKeep": 4 * (self.survivor_capacity + 1), "keepOffset": 4 * (self.survivor_capacity + 1),
+            "walkList": 4 * self.survivor_capacity, "dpairSourcePlane": 16 * 4 * pc,
             "cullerParams": 4 * CULLER_PARAMS * len(library.shapes), "cullerW1": 2 * 4096 * len(library.shapes),
             "cullerMargin": 4 * len(library.shapes), "cullerStats": 16,
         }
@@ -623,7 +631,7 @@ class Engine:
         seconds = {
             "drift": ms["drift"] / 1e3,
             "neighbours": ms["neighbours"] / 1e3,
-            "contact_geometry": (ms["pair_cull"] + ms["node_query"] + ms["contact_emit"]) / 1e3,
+            "contact_geometry": (ms["pair_cull"] + ms["node_filter"] + ms["node_query"] + ms["contact_emit"]) / 1e3,
             "friction_and_history": ms["friction_and_history"] / 1e3,
             "force_reduction": ms["force_reduction"] / 1e3,
             "final_kick": ms["final_kick"] / 1e3,

@@ -149,5 +149,5 @@ EXPORTS = (
     "sdg_culler_tile_eval",
     "sdg_culler_inside_max",
 )
-PHASES = ("drift", "neighbours", "pair_cull", "node_query", "contact_emit", "friction_and_history",
+PHASES = ("drift", "neighbours", "pair_cull", "node_filter", "node_query", "contact_emit", "friction_and_history",
           "force_reduction", "final_kick")
