@@ -226,20 +226,22 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def algorithmic_bytes(n, pairs, contacts, items, nodes, survivors, rebuild, library_bytes):
+def algorithmic_bytes(n, pairs, contacts, items, nodes, survivors, kept, rebuild, library_bytes):
     """Per-step algorithmic HBM bytes of the whole step and of the node query.
 
     Step: 516 B/grain + 264 B/pair + 272 B/contact + 88 B/grain on rebuild
-    steps + the packed library once.  Node query (filter, survivor list and
-    exact walks, one launch group): each (directed pair, leaf) item reads its
-    record, pair, branch, plane and leaf range and writes its survivor and
-    hit masks and counts (88 B); each node reads its sample index and sample
-    (20 B); each survivor is listed, read back with its item record, pair,
-    branch, sample, both rotations and bodies, and a hit writes its record
-    (132 B); the packed library is read once (it stays in L2).
+    steps + the packed library once.  Node query (filter, survivor list,
+    prefilter and exact walks, one launch group): each (directed pair, leaf)
+    item reads its record, pair, source plane and leaf range and writes its
+    survivor and hit masks and counts (88 B); each node considered reads its
+    sample index and sample (20 B); each survivor of the one-dot test is
+    listed and read back, and its keep flag written and scanned (24 B); each
+    exact query reads its list entry, item record, pair, branch, sample and
+    both grains' rotation and body, and a hit writes its record (132 B); the
+    packed library is read once (it stays in L2).
     """
     step = 516 * n + 264 * pairs + 272 * contacts + 88 * n * rebuild + library_bytes
-    query = 88 * items + 20 * nodes + 132 * survivors + library_bytes
+    query = 88 * items + 20 * nodes + 24 * survivors + 132 * kept + library_bytes
     return step, query
 
 
@@ -296,13 +298,14 @@ def run_gb300(args, cpu=True):
     e.check_errors()
     phase_ms = {k: float(np.median([p[k] for p in phases])) for k in phases[0]}
     work = e.read("work", np.uint32, (64,))
-    items, survivors = int(work[0]), int(work[2])
+    items, survivors, kept = int(work[0]), int(work[2]), int(work[3])
     pairs, contacts = int(ctrl[1]), int(ctrl[2])
     leaf_nodes = e.layout.geometry["meshClusterRanges"][:, 1]
     cand = e.read("candidates", np.uint32, (e.candidate_capacity, 2))[:items]
     nodes = int(leaf_nodes[cand[:, 1]].sum()) if items else 0
     lib_bytes = sum(a.nbytes for k, a in e.layout.geometry.items() if k.startswith("mesh") or k == "sample")
-    step_bytes, query_bytes = algorithmic_bytes(w.grains, pairs, contacts, items, nodes, survivors, 0, lib_bytes)
+    step_bytes, query_bytes = algorithmic_bytes(w.grains, pairs, contacts, items, nodes, survivors, kept, 0,
+                                                lib_bytes)
     hbm, peak_kind = peaks()
     top = max(phase_ms, key=phase_ms.get)
     query_ms = phase_ms["node_filter"] + phase_ms["node_query"]
@@ -338,14 +341,16 @@ def run_gb300(args, cpu=True):
         "data": "synthetic",
         "config": dict(w.config, l2="flushed before each timed step (256 MiB write)",
                        pairs=pairs, contacts=contacts, node_query_items=items, node_queries=nodes,
-                       exact_queries=survivors, timestep_s=e.spec.timestep, phase_ms=phase_ms,
+                       plane_survivors=survivors, exact_queries=kept, timestep_s=e.spec.timestep,
+                       phase_ms=phase_ms,
                        dominant_phase=top, tuning=dict(e.tuning)),
         "e2e": {"value": e2e, "unit": "grain-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": f"Engine.advance({chunk}) + Engine.diagnostics() per chunk"},
         "gpu_launches": int(kernels) * args.steps,
         "roofline": {
             "bound": "hbm",
-            "kernel": "node query launch group (k_nodeFilter, survivor scan, k_survivorList, k_nodeWalk)",
+            "kernel": "node query launch group (k_nodeFilter, k_survivorList, k_survivorPrefilter, k_nodeWalk "
+                      "and their scans)",
             "achieved": query_gbs,
             "peak": hbm,
             "peak_source": peak_kind,

@@ -11,7 +11,7 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 117) this backend's extension buffers, in the order of
+ *   [77, 118) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
@@ -27,7 +27,9 @@
  *             and, for the learned culler, a keep flag per survivor, its
  *             exclusive scan and the list of kept survivors, and per
  *             directed pair the enclosure plane carried into the source
- *             grain's frame with its rejection-bound terms).
+ *             grain's frame with its rejection-bound terms, and the
+ *             triangle BVH as one record per node with both children's
+ *             bounds).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
@@ -58,7 +60,7 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 117
+#define SDG_BUFFER_COUNT 118
 #define SDG_VALUE_COUNT 37
 #define SDG_PHASES 9
 

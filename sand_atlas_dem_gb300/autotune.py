@@ -60,8 +60,8 @@ def signature(engine):
 
 
 def _load(cache):
-    if cache and Path(cache).exists():
-        return json.loads(Path(cache).read_text())
+    if cache and Path(cache).expanduser().exists():
+        return json.loads(Path(cache).expanduser().read_text())
     return {}
 
 
@@ -104,8 +104,9 @@ def tune(engine, *, repeats=3, cache=None, log=None):
     engine.tuning = dict(choice)
     if cache:
         known[key] = dict(choice=choice, table=table)
-        Path(cache).parent.mkdir(parents=True, exist_ok=True)
-        Path(cache).write_text(json.dumps(known, indent=1, sort_keys=True))
+        path = Path(cache).expanduser()
+        path.parent.mkdir(parents=True, exist_ok=True)
+        path.write_text(json.dumps(known, indent=1, sort_keys=True))
     return engine.tuning, table
 
 

@@ -113,8 +113,9 @@ struct Res {
     uint32_t* keepOffset;             // survivorCapacity+1: exclusive scan of survKeep
     uint32_t* walkList;               // survivorCapacity: survivors left for the exact query
     float4* dpairSourcePlane;         // 4*pairCapacity: the enclosure plane in the source frame, and its bound terms
+    const float4* meshChildren;       // 4 per BVH node: both children's bounds (internal) or the triangle range
 };
-constexpr int EXTENSION_COUNT = 40;
+constexpr int EXTENSION_COUNT = 41;
 constexpr int CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4;
 constexpr int BUFFER_COUNT = RESOURCE_COUNT + EXTENSION_COUNT;
 constexpr int CONFIG_VALUES = 25;
@@ -287,10 +288,14 @@ __device__ __forceinline__ f3 closestTriangle(f3 p, f3 a, f3 b, f3 c, uint32_t& 
     return (a + ab * __fmul_rn(vb, inv)) + ac * __fmul_rn(vc, inv);
 }
 // solver.slang:220-223
-__device__ __forceinline__ float meshBoxDistance(const Res& r, uint32_t node, f3 p) {
-    f3 d = mx3(mx3(xyz(__ldg(&r.meshMin[node])) - p, p - xyz(__ldg(&r.meshMax[node]))), mk(0.f, 0.f, 0.f));
+__device__ __forceinline__ float boxDistance(f3 low, f3 high, f3 p) {
+    f3 d = mx3(mx3(low - p, p - high), mk(0.f, 0.f, 0.f));
     return dot(d, d);
 }
+__device__ __forceinline__ float meshBoxDistance(const Res& r, uint32_t node, f3 p) {
+    return boxDistance(xyz(__ldg(&r.meshMin[node])), xyz(__ldg(&r.meshMax[node])), p);
+}
+constexpr uint32_t LEAF_MARK = 0xFFFFFFFFu;
 // Nearest-first BVH walk with cached pushed box distances (the reference CPU
 // variant, cpu_scheduling.slang:18-48, bit-identical to solver.slang:224-252).
 __device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 p, bool surfaceNormal) {
@@ -304,28 +309,28 @@ __device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 
     f3 nearest = mk(0.f, 0.f, 0.f);
     uint32_t nearestNormal = 0;
     bool found = false;
-    // "While-while" form: each lane pops and expands internal nodes until it
-    // pops a leaf (or empties its stack), then the lanes test their leaves'
-    // triangles together.  Every lane visits the same nodes in the same order
-    // as the single loop, so the result is the same; only the SIMT schedule
-    // differs.
+    // Each node's record holds both children's bounds (the same floats as
+    // meshMin/meshMax) and the escape link of the first child, so a step of
+    // the walk is one round of independent loads instead of three dependent
+    // ones; the visit order and every distance are unchanged.
     while (top > 0) {
-        uint4 link = make_uint4(0u, 0u, 0u, 0u);
-        while (top > 0) {
-            uint32_t slot = --top, node = pending[slot];
-            if (pendingDistance[slot] > best) continue;
-            link = __ldg(&r.meshLinks[node]);
-            if (link.z != 0) break;
-            uint32_t a = node + 1, b = __ldg(&r.meshLinks[a].x);
-            float da = meshBoxDistance(r, a, p), db = meshBoxDistance(r, b, p);
+        uint32_t slot = --top, node = pending[slot];
+        if (pendingDistance[slot] > best) continue;
+        const float4* record = r.meshChildren + 4 * size_t(node);
+        float4 r0 = __ldg(record), r1 = __ldg(record + 1);
+        if (__float_as_uint(r0.w) != LEAF_MARK) {
+            float4 r2 = __ldg(record + 2), r3 = __ldg(record + 3);
+            uint32_t a = node + 1, b = __float_as_uint(r0.w);
+            float da = boxDistance(xyz(r0), xyz(r1), p), db = boxDistance(xyz(r2), xyz(r3), p);
             if (da < db) { uint32_t s = a; a = b; b = s; float ds = da; da = db; db = ds; }
             if (top + 2 > 32) { fail(r, F_STACK); return make_float4(0.f, 0.f, 0.f, 1e20f); }
             if (da <= best) { pending[top] = a; pendingDistance[top++] = da; }
             if (db <= best) { pending[top] = b; pendingDistance[top++] = db; }
-            link.z = 0;
+            continue;
         }
-        for (uint32_t k = 0; k < link.z; ++k) {
-            uint32_t triangle = link.y + k, feature;
+        uint32_t first = __float_as_uint(r0.x), count = __float_as_uint(r0.y);
+        for (uint32_t k = 0; k < count; ++k) {
+            uint32_t triangle = first + k, feature;
             f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * triangle])), xyz(__ldg(&r.meshTriangles[3 * triangle + 1])),
                                    xyz(__ldg(&r.meshTriangles[3 * triangle + 2])), feature);
             f3 dq = p - q;

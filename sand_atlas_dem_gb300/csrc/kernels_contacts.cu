@@ -483,14 +483,16 @@ __global__ void k_leafEmit(const __grid_constant__ Params P) {
     }
 }
 // Node query in stages.  The filter stage (one warp per (directed pair,
-// leaf) item, two nodes per lane) applies the conservative rejections -- the
-// enclosure plane and the hull -- and records each item's surviving nodes as
-// a 64-bit mask.  A scan turns the survivor counts into offsets and the
-// survivors are listed in canonical order.  With the learned culler on, one
-// pass evaluates the target's network for 64 survivors per warp on tensor
-// cores and a scan keeps the ones it cannot rule out.  The exact stage runs
-// one thread per remaining survivor: full warps of BVH walks instead of
-// warps in which most lanes were rejected and idle.  Each hit sets its bit in
+// leaf) item, two nodes per lane) applies the one-dot enclosure-plane test
+// in the source frame and records each item's surviving nodes as a 64-bit
+// mask.  A scan turns the survivor counts into offsets and the survivors are
+// listed in canonical order.  A dense pass (one thread per survivor) places
+// each in the target frame and applies the target-frame plane and the hull;
+// with the learned culler on, a second pass evaluates the target's network
+// for 64 survivors per warp on tensor cores.  A scan keeps the survivors no
+// test ruled out and the exact stage runs one thread per kept survivor: full
+// warps of BVH walks instead of warps in which most lanes were rejected and
+// idle.  Each hit sets its bit in
 // the item's hit mask (integer atomics: the result does not depend on their
 // order) and keeps its record in the survivor's scratch slot; the emit pass
 // copies hits to their canonical offsets.
@@ -504,22 +506,17 @@ __global__ void __launch_bounds__(256) k_nodeFilter(const __grid_constant__ Para
             uint2 cd = r.candidates[item];
             uint32_t d = cd.x, p = d >> 1, pass = d & 1;
             uint2 ij = r.pairs[p];
-            uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
-            f3 branch = xyz(r.dpairBranch[d]);
-            float4 plane = r.dpairPlane[d];
+            uint32_t src = pass ? ij.y : ij.x;
             SourcePlane source{r.dpairSourcePlane[2 * d], r.dpairSourcePlane[2 * d + 1]};
             uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
             const float4* samples = r.sample + __ldg(&r.sampleInfo[r.shapeId[src]].x);
             uint32_t k0 = laneId(), k1 = laneId() + WARP;
-            uint32_t node0 = k0 < range.y ? __ldg(&r.meshSampleIndices[range.x + k0]) : 0;
-            uint32_t node1 = k1 < range.y ? __ldg(&r.meshSampleIndices[range.x + k1]) : 0;
-            // One dot per node against the source-frame plane; the few nodes
-            // left take the exact placement, the target-frame plane and the hull.
-            keep0 = k0 < range.y && !nodeBeyondSourcePlane(source, xyz(__ldg(&samples[node0])));
-            keep1 = k1 < range.y && !nodeBeyondSourcePlane(source, xyz(__ldg(&samples[node1])));
-            f3 arm, local;
-            if (keep0) keep0 = nodePrefilter(r, src, dst, node0, branch, &plane, arm, local);
-            if (keep1) keep1 = nodePrefilter(r, src, dst, node1, branch, &plane, arm, local);
+            // One dot per node against the source-frame plane; the exact
+            // placement, target-frame plane and hull follow in a dense pass.
+            if (k0 < range.y)
+                keep0 = !nodeBeyondSourcePlane(source, xyz(__ldg(&samples[__ldg(&r.meshSampleIndices[range.x + k0])])));
+            if (k1 < range.y)
+                keep1 = !nodeBeyondSourcePlane(source, xyz(__ldg(&samples[__ldg(&r.meshSampleIndices[range.x + k1])])));
         }
         uint32_t m0 = __ballot_sync(0xffffffffu, keep0), m1 = __ballot_sync(0xffffffffu, keep1);
         if (laneId() == 0) {
@@ -552,10 +549,30 @@ __device__ __forceinline__ SurvivorNode survivorNode(const Res& r, uint32_t s) {
     v.local = qinv(r.rotation[v.dst], v.arm - xyz(r.dpairBranch[d])) / r.body[v.dst].x;
     return v;
 }
+// Exact placement, target-frame enclosure plane and hull of every survivor
+// of the one-dot test (nodePrefilter, one thread each): survKeep[s] = 1 for
+// the nodes that go on to the exact query.
+__global__ void __launch_bounds__(256) k_survivorPrefilter(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
+    for (uint32_t s = gtid(); s < n; s += gstride()) {
+        uint2 sv = r.survivors[s];
+        uint2 cd = r.candidates[sv.x];
+        uint32_t d = cd.x, p = d >> 1, pass = d & 1;
+        uint2 ij = r.pairs[p];
+        uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
+        uint32_t node = __ldg(&r.meshSampleIndices[__ldg(&r.meshClusterRanges[cd.y]).x + sv.y]);
+        float4 plane = r.dpairPlane[d];
+        f3 arm, local;
+        r.survKeep[s] = nodePrefilter(r, src, dst, node, xyz(r.dpairBranch[d]), &plane, arm, local) ? 1u : 0u;
+    }
+}
 // Learned culler over the survivor list: 64 survivors per warp iteration
 // (two per lane), one tensor-core tile per distinct target shape among them.
-// keep[s] = 0 when the target's network places survivor s beyond the
-// shape's calibrated margin; the exact query decides every other survivor.
+// Clears keep[s] when the target's network places a kept survivor s beyond
+// the shape's calibrated margin; the exact query decides every other one.
 __global__ void __launch_bounds__(256) k_cullSurvivors(const __grid_constant__ Params P) {
     extern __shared__ uint32_t cullTiles[];
     const Res& r = P.r;
@@ -566,7 +583,7 @@ __global__ void __launch_bounds__(256) k_cullSurvivors(const __grid_constant__ P
     uint32_t groups = (n + 63) / 64;
     for (uint32_t g = warpGlobal(); g < groups; g += warpStride()) {
         uint32_t s0 = 64 * g + laneId(), s1 = s0 + WARP;
-        bool valid0 = s0 < n, valid1 = s1 < n;
+        bool valid0 = s0 < n && r.survKeep[s0], valid1 = s1 < n && r.survKeep[s1];
         f3 l0 = mk(0.f, 0.f, 0.f), l1 = l0;
         uint32_t t0 = EMPTY, t1 = EMPTY;
         if (valid0) { SurvivorNode v = survivorNode(r, s0); l0 = v.local; t0 = r.shapeId[v.dst]; }
@@ -585,8 +602,8 @@ __global__ void __launch_bounds__(256) k_cullSurvivors(const __grid_constant__ P
             if (in0) { cut0 = y0 > margin; pending0 = false; }
             if (in1) { cut1 = y1 > margin; pending1 = false; }
         }
-        if (valid0) r.survKeep[s0] = cut0 ? 0u : 1u;
-        if (valid1) r.survKeep[s1] = cut1 ? 0u : 1u;
+        if (cut0) r.survKeep[s0] = 0u;
+        if (cut1) r.survKeep[s1] = 0u;
         uint32_t tested = __popc(__ballot_sync(0xffffffffu, valid0)) + __popc(__ballot_sync(0xffffffffu, valid1));
         uint32_t culled = __popc(__ballot_sync(0xffffffffu, cut0)) + __popc(__ballot_sync(0xffffffffu, cut1));
         if (laneId() == 0) {
@@ -595,7 +612,7 @@ __global__ void __launch_bounds__(256) k_cullSurvivors(const __grid_constant__ P
         }
     }
 }
-// Survivors the culler kept, in order (their survivor indices).
+// Survivors kept for the exact query, in order (their survivor indices).
 __global__ void k_walkList(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
@@ -624,14 +641,14 @@ __global__ void k_survivorList(const __grid_constant__ Params P) {
         }
     }
 }
-// Exact query, one thread per survivor (per kept survivor with the culler).
+// Exact query, one thread per kept survivor.
 __global__ void __launch_bounds__(256) k_nodeWalk(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
     if (r.control[0] != 0) return;
-    uint32_t n = min(r.work[c.cullerEnabled ? W_KEPT : W_SURVIVORS], c.survivorCapacity);
+    uint32_t n = min(r.work[W_KEPT], c.survivorCapacity);
     for (uint32_t t = gtid(); t < n; t += gstride()) {
-        uint32_t s = c.cullerEnabled ? r.walkList[t] : t;
+        uint32_t s = r.walkList[t];
         SurvivorNode v = survivorNode(r, s);
         float4 pd, na;
         if (nodeExact(r, c, v.src, v.dst, v.node, v.arm, v.local, pd, na)) {
@@ -973,6 +990,7 @@ static void collectFilter(const Params& P, cudaStream_t s) {
     launch_scan(r.candSurvCount, r.candSurvOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0},
                 true, r.work + W_SURVIVORS, nullptr, r.scanPartials, s);
     k_survivorList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
+    k_survivorPrefilter<<<grid(c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
     if (c.cullerEnabled) {
         static bool attributed = false;
         if (!attributed) {
@@ -981,10 +999,10 @@ static void collectFilter(const Params& P, cudaStream_t s) {
             attributed = true;
         }
         k_cullSurvivors<<<grid(c.queryBlocksPerSM, 2), 256, 8 * CULLER_TILE_WORDS * sizeof(uint32_t), s>>>(P);
-        launch_scan(r.survKeep, r.keepOffset, ScanCount{r.work + W_SURVIVORS, c.survivorCapacity, 1, 0}, true,
-                    r.work + W_KEPT, nullptr, r.scanPartials, s);
-        k_walkList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
     }
+    launch_scan(r.survKeep, r.keepOffset, ScanCount{r.work + W_SURVIVORS, c.survivorCapacity, 1, 0}, true,
+                r.work + W_KEPT, nullptr, r.scanPartials, s);
+    k_walkList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
 }
 // The exact queries.
 static void collectWalk(const Params& P, cudaStream_t s) {

@@ -40,7 +40,7 @@ EXTENSION_ORDER = (
     "sideContactStart", "oldPairOffsets", "oldPairB", "oldContactStart", "work", "scanPartials",
     "hitScratch", "candSurvCount", "dpairPlane", "grainSpecimen", "specimenBins", "cullerParams", "cullerW1",
     "cullerMargin", "cullerStats", "candSurvMask", "candSurvOffset", "survivors", "survKeep", "keepOffset",
-    "walkList", "dpairSourcePlane",
+    "walkList", "dpairSourcePlane", "meshChildren",
 )
 CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4
 BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
@@ -66,7 +66,10 @@ class DeviceBuffer:
         torch = _torch()
         self._engine = weakref.ref(engine)
         self.size = int(max(16, nbytes))
-        self.tensor = torch.zeros(self.size, dtype=torch.uint8, device=engine.device)
+        # Allocated and zeroed on the engine stream, which every later use of
+        # the buffer is ordered on.
+        with torch.cuda.stream(engine.stream):
+            self.tensor = torch.zeros(self.size, dtype=torch.uint8, device=engine.device)
 
     def ptr(self):
         return self.tensor.data_ptr()
@@ -176,6 +179,7 @@ class Engine:
         self.use_graph = use_graph
         self.culler = None
         self.tuning = {}
+        self._reduce_scratch = {}
         # Host<->device bytes moved by this engine's own reads and uploads.
         self.h2d_bytes = self.d2h_bytes = 0
         for name in ("length_unit", "time_unit", "mass_unit", "force_unit", "stress_unit", "energy_unit",
@@ -183,11 +187,13 @@ class Engine:
                      "contact_capacity", "hash_size", "bin_capacity", "initial_cell"):
             setattr(self, name, getattr(h, name))
         self.estimated_bytes = h.estimated_bytes()
+        volumes = np.array([shape.volume for shape in library.shapes])
+        self.solid_volume = float(np.sum(volumes[self.ids] * np.asarray(self.scales, float) ** 3))
         self.leaf_words = (h.max_leaves + 31) // 32
         self.candidate_capacity = max(1, 2 * h.pair_capacity * h.max_leaves)
         # Nodes left for the exact query after the conservative filters, per
         # step; overflow raises the contact-capacity flag and grows with it.
-        self.survivor_capacity = 2 * h.contact_capacity
+        self.survivor_capacity = 4 * h.contact_capacity
         self.device = torch.device(device or "cuda")
         self.stream = torch.cuda.Stream(self.device)
         self.m = GB300Device(self)
@@ -527,15 +533,17 @@ class Engine:
         """Reference 256-wide tree reduction to one row set (``diagnostic.slang:3-28``)."""
         src = self.buffers[name]
         n = self.n if name == "diagnosticRows" else self.pair_capacity
-        scratch = []
+        level = 0
         while n > 1:
             groups = (n + 255) // 256
-            out = DeviceBuffer(self, 16 * rows * groups)
+            key = (name, level)
+            out = self._reduce_scratch.get(key)
+            if out is None or out.size < 16 * rows * groups:
+                out = self._reduce_scratch[key] = DeviceBuffer(self, 16 * rows * groups)
             native.check(self.lib.sdg_reduce_rows(ct.c_void_p(src.ptr()), ct.c_void_p(out.ptr()), n, rows,
                                                   max_row, ct.c_void_p(self.stream.cuda_stream)))
-            scratch.append(out)
-            src, n = out, groups
-        return self.m.read(src, np.float32, (rows, 4))
+            src, n, level = out, groups, level + 1
+        return self.m.read_prefix(src, 4 * rows, np.float32, shape=(rows, 4))
 
     def diagnostics(self):
         """Stress, energies, contact counts and fabric (``gpu.py:746-891``)."""
@@ -561,7 +569,7 @@ class Engine:
         total = contact + kinetic
         symmetric = 0.5 * (total + total.T)
         radial = 0.5 * (symmetric[0, 0] + symmetric[1, 1])
-        solid = sum(self.library.shapes[int(i)].volume * s**3 for i, s in zip(self.ids, self.scales))
+        solid = self.solid_volume
         return {
             "step": self.step,
             "elapsed_time": self.step * self.spec.timestep,

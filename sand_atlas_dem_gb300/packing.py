@@ -18,7 +18,9 @@ Two arrays are added for this backend and have no reference counterpart:
 ``meshLeafInfo`` (per shape: first leaf slot, leaf count) and ``meshLeaves``
 (leaf cluster ids in preorder), which let the collector cull all leaves of a
 shape in parallel; and ``meshSampleRank`` (per packed sample: its position in
-``meshSampleIndices``), the in-pair sort key of the friction-history merge.
+``meshSampleIndices``), the in-pair sort key of the friction-history merge;
+and ``meshChildren``, the triangle BVH re-laid as one record per node holding
+both children's bounds (see :func:`child_records`).
 """
 
 import numpy as np
@@ -250,7 +252,36 @@ def pack_library(library, length_unit):
     packed["meshLeafInfo"] = np.asarray(leaf_info, np.uint32)
     packed["meshLeaves"] = np.asarray(leaves, np.uint32)
     packed["meshSampleRank"] = np.concatenate(ranks).astype(np.uint32)
+    packed["meshChildren"] = child_records(packed["meshLinks"], packed["meshMin"], packed["meshMax"])
     return packed
+
+
+LEAF_MARK = np.uint32(0xFFFFFFFF)
+
+
+def child_records(links, low, high):
+    """One 64-byte record per triangle-BVH node, read by the exact walk in a
+    single round of loads.  Internal node n (children a = n + 1 and b = the
+    escape link of a): (low[a], b), (high[a], 0), (low[b], 0), (high[b], 0),
+    the bounds copied bit for bit.  Leaf: (first triangle, count, 0,
+    0xFFFFFFFF) as integers, the rest zero."""
+    n = len(links)
+    records = np.zeros((n, 4, 4), F32)
+    bits = records.view(np.uint32)
+    internal = links[:, 2] == 0
+    nodes = np.flatnonzero(internal)
+    a = nodes + 1
+    b = links[a, 0].astype(np.int64)
+    records[nodes, 0, :3] = low[a, :3]
+    records[nodes, 1, :3] = high[a, :3]
+    records[nodes, 2, :3] = low[b, :3]
+    records[nodes, 3, :3] = high[b, :3]
+    bits[nodes, 0, 3] = b
+    leaves = np.flatnonzero(~internal)
+    bits[leaves, 0, 0] = links[leaves, 1]
+    bits[leaves, 0, 1] = links[leaves, 2]
+    bits[leaves, 0, 3] = LEAF_MARK
+    return records.reshape(-1, 4)
 
 
 REFERENCE_ARRAYS = UINT_ARRAYS + FLOAT_ARRAYS
