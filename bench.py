@@ -62,6 +62,9 @@ WORKLOADS = {
                           packing="jittered cubic lattice per specimen"),
 }
 DATA = ROOT / "sand_atlas_dem_gb300" / "data"
+# DRAM bytes (read + write) of one k_nodeWalk launch from an ncu capture of
+# the same workload (profiles/walk-dense-10k.md); None where not captured.
+WALK_TRAFFIC = {"dense-10k": 43.94e6}
 
 
 def log(*args):
@@ -242,7 +245,8 @@ def algorithmic_bytes(n, pairs, contacts, items, nodes, survivors, kept, rebuild
     """
     step = 516 * n + 264 * pairs + 272 * contacts + 88 * n * rebuild + library_bytes
     query = 88 * items + 20 * nodes + 24 * survivors + 132 * kept + library_bytes
-    return step, query
+    walk = 132 * kept + library_bytes
+    return step, query, walk
 
 
 def timed_steps(e, steps, flush):
@@ -304,12 +308,14 @@ def run_gb300(args, cpu=True):
     cand = e.read("candidates", np.uint32, (e.candidate_capacity, 2))[:items]
     nodes = int(leaf_nodes[cand[:, 1]].sum()) if items else 0
     lib_bytes = sum(a.nbytes for k, a in e.layout.geometry.items() if k.startswith("mesh") or k == "sample")
-    step_bytes, query_bytes = algorithmic_bytes(w.grains, pairs, contacts, items, nodes, survivors, kept, 0,
-                                                lib_bytes)
+    step_bytes, query_bytes, walk_bytes = algorithmic_bytes(w.grains, pairs, contacts, items, nodes, survivors,
+                                                            kept, 0, lib_bytes)
     hbm, peak_kind = peaks()
     top = max(phase_ms, key=phase_ms.get)
     query_ms = phase_ms["node_filter"] + phase_ms["node_query"]
     query_gbs = query_bytes / (query_ms / 1e3) / 1e9
+    # The dominant kernel, k_nodeWalk, is the whole "node_query" phase (one launch).
+    walk_gbs = walk_bytes / (phase_ms["node_query"] / 1e3) / 1e9
     # End to end through the public API: advance() chunks plus diagnostics().
     chunk = 10
     chunks = max(1, args.steps // chunk)
@@ -349,16 +355,19 @@ def run_gb300(args, cpu=True):
         "gpu_launches": int(kernels) * args.steps,
         "roofline": {
             "bound": "hbm",
-            "kernel": "node query launch group (k_nodeFilter, k_survivorList, k_survivorPrefilter, k_nodeWalk "
-                      "and their scans)",
-            "achieved": query_gbs,
+            "kernel": "k_nodeWalk (exact BVH queries, one thread per kept node)",
+            "achieved": walk_gbs,
             "peak": hbm,
             "peak_source": peak_kind,
             "unit": "GB/s",
-            "frac": query_gbs / hbm,
-            "traffic": None,
-            "algorithmic_bytes": query_bytes,
+            "frac": walk_gbs / hbm,
+            "traffic": WALK_TRAFFIC.get(w.name),
+            "algorithmic_bytes": walk_bytes,
+            "kernel_ms": phase_ms["node_query"],
+            "launch_group": "k_nodeFilter, k_survivorList, k_survivorPrefilter, k_walkList, k_nodeWalk + scans",
+            "launch_group_algorithmic_bytes": query_bytes,
             "launch_group_ms": query_ms,
+            "launch_group_achieved_gbs": query_gbs,
             "step_algorithmic_bytes": step_bytes,
             "step_achieved_gbs": step_bytes / (device_s / args.steps) / 1e9,
         },
