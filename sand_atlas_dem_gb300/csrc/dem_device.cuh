@@ -378,6 +378,21 @@ __device__ __forceinline__ bool meshBoxMayContact(const Res& r, uint32_t shape, 
     }
     return true;
 }
+// The first half of meshBoxMayContact: the target's root box test, and the
+// centre, half extent and hull group its plane loop would use.
+__device__ __forceinline__ bool meshBoxGroup(const Res& r, uint32_t shape, f3 low, f3 high, f3& center, f3& half,
+                                             uint32_t& group) {
+    uint32_t root = __ldg(&r.meshRoots[shape].x);
+    f3 tl = xyz(__ldg(&r.meshMin[root])), th = xyz(__ldg(&r.meshMax[root]));
+    if (high.x < tl.x || high.y < tl.y || high.z < tl.z || low.x > th.x || low.y > th.y || low.z > th.z) return false;
+    center = 0.5f * (low + high);
+    half = 0.5f * (high - low);
+    f3 direction = (center - 0.5f * (tl + th)) / (th - tl);
+    f3 a = abs3(direction);
+    uint32_t axis = a.x >= a.y && a.x >= a.z ? 0 : (a.y >= a.z ? 1 : 2);
+    group = 2 * axis + (comp(direction, axis) >= 0 ? 1 : 0);
+    return true;
+}
 // solver.slang:290-305, with the directed-pair branch supplied.
 __device__ __forceinline__ bool meshClusterMayContact(const Res& r, uint32_t src, uint32_t dst, uint32_t cluster, f3 branch) {
     f3 sl = xyz(r.meshClusterMin[cluster]), sh = xyz(r.meshClusterMax[cluster]);
