@@ -383,53 +383,59 @@ def run_gb300(args, cpu=True):
 
 
 def culler_comparison(w, args, flush):
-    """Plain exact step against the learned-cull step from one start state.
+    """Exact step against the learned-cull step from one start state, with
+    and without the certified distance-bound grid.
 
     The culler is trained (2^20 shell points and 2^18 interior points per
-    shape, 2,000 Adam steps) and calibrated on the GPU, attached to a second
-    engine, and both engines run the same timed steps.  Missed contacts =
-    exact contacts absent from the culled run; forces are compared bit for
+    shape, 2,000 Adam steps) and calibrated on the GPU and attached to the
+    culled engines; every engine runs the same timed steps.  Missed contacts
+    = exact contacts absent from the culled run; forces are compared bit for
     bit.
     """
     from sand_atlas_dem_gb300.culler import LearnedCuller
     from sand_atlas_dem_gb300.engine import Engine
 
     rate = w.rate()
-    plain = w.engine(Engine)
-    culled = w.engine(Engine)
+    engines = {"plain": w.engine(Engine), "culled": w.engine(Engine),
+               "plain_no_grid": w.engine(Engine, distance_grid=False),
+               "culled_no_grid": w.engine(Engine, distance_grid=False)}
     t = time.perf_counter()
-    c = LearnedCuller(culled, points=1 << 20, steps=2000, batch=8192)
+    c = LearnedCuller(engines["culled"], points=1 << 20, steps=2000, batch=8192)
     c.train()
-    c.attach(culled)
+    c.attach(engines["culled"])
+    c.attach(engines["culled_no_grid"])
     train_s = time.perf_counter() - t
     out = {}
     steps = min(args.steps, 50)
-    for name, e in (("plain", plain), ("culled", culled)):
+    for name, e in engines.items():
         e.advance(max(3, args.warmup), rate=rate)
         set_rates(e, w)
         e.buffers["cullerStats"].copy_from_numpy(np.zeros(4, np.uint32))
         ms = timed_steps(e, steps, flush)
+        phases = e.profile_phases()
+        stats = e.read("cullerStats", np.uint32, (4,))
         out[name] = dict(value=w.grains * steps / (sum(ms) / 1e3), ms_per_step=sum(ms) / steps,
-                         phase_ms=e.profile_phases())
-    sp, sc = plain.state(), culled.state()
-    stats = culled.read("cullerStats", np.uint32, (4,))
-    keys_p = {tuple(m) for m in sp["meta"][:, :3].tolist()}
-    keys_c = {tuple(m) for m in sc["meta"][:, :3].tolist()}
-    force_p = sp["force"][:, :3].astype(float)
-    force_err = float(np.abs(sc["force"][:, :3] - force_p).max() / max(np.abs(force_p).max(), 1e-30))
-    return dict(
-        steps=steps, plain_value=out["plain"]["value"], culled_value=out["culled"]["value"],
-        speedup=out["culled"]["value"] / out["plain"]["value"],
-        plain_node_query_ms=out["plain"]["phase_ms"]["node_filter"] + out["plain"]["phase_ms"]["node_query"],
-        culled_node_query_ms=out["culled"]["phase_ms"]["node_filter"] + out["culled"]["phase_ms"]["node_query"],
-        tested_nodes=int(stats[0]), culled_nodes=int(stats[1]),
-        cull_rate_of_exact_queries=float(stats[1]) / max(int(stats[0]), 1),
-        missed_contacts=len(keys_p - keys_c), extra_contacts=len(keys_c - keys_p),
-        forces_bitwise_equal=bool(sp["force"].tobytes() == sc["force"].tobytes()),
-        force_max_relative_error=force_err,
-        training_s=round(train_s, 1), margins_mean=float(np.mean(c.margins)),
-        validation_cull_rate=c.cull_rate(),
-    )
+                         node_query_ms=phases["node_filter"] + phases["node_query"],
+                         tested=int(stats[0]), culled=int(stats[1]), state=e.state())
+    result = dict(steps=steps, training_s=round(train_s, 1), margins_mean=float(np.mean(c.margins)),
+                  validation_cull_rate=c.cull_rate())
+    for grid in ("", "_no_grid"):
+        p, q = out["plain" + grid], out["culled" + grid]
+        sp, sc = p.pop("state"), q.pop("state")
+        keys_p = {tuple(m) for m in sp["meta"][:, :3].tolist()}
+        keys_c = {tuple(m) for m in sc["meta"][:, :3].tolist()}
+        force_p = sp["force"][:, :3].astype(float)
+        err = float(np.abs(sc["force"][:, :3] - force_p).max() / max(np.abs(force_p).max(), 1e-30))
+        result["with_grid" if not grid else "without_grid"] = dict(
+            plain_value=p["value"], culled_value=q["value"], speedup=q["value"] / p["value"],
+            plain_node_query_ms=p["node_query_ms"], culled_node_query_ms=q["node_query_ms"],
+            tested_nodes=q["tested"], culled_nodes=q["culled"],
+            cull_rate_of_exact_queries=q["culled"] / max(q["tested"], 1),
+            missed_contacts=len(keys_p - keys_c), extra_contacts=len(keys_c - keys_p),
+            forces_bitwise_equal=bool(sp["force"].tobytes() == sc["force"].tobytes()),
+            force_max_relative_error=err)
+    result["grid_speedup_over_reference_filters"] = out["plain"]["value"] / out["plain_no_grid"]["value"]
+    return result
 
 
 def cpu_sample(w):

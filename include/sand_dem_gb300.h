@@ -11,7 +11,7 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 118) this backend's extension buffers, in the order of
+ *   [77, 120) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
@@ -29,7 +29,8 @@
  *             directed pair the enclosure plane carried into the source
  *             grain's frame with its rejection-bound terms, and the
  *             triangle BVH as one record per node with both children's
- *             bounds).
+ *             bounds, and per shape a 48^3 grid of certified lower bounds of
+ *             the signed distance with its origin and cell size).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
@@ -41,9 +42,10 @@
  * launch shapes chosen by the autotuner (0 = default): node-filter CTAs per
  * SM, node-filter warps per CTA (4 or 8), pair set-up/leaf-cull CTAs per SM,
  * contact emit/law CTAs per SM, gather warps per SM and exact-query CTAs per
- * SM (launch shapes never change results), and the survivor capacity (nodes
+ * SM (launch shapes never change results), the survivor capacity (nodes
  * left for the exact query per step; overflow raises the contact-capacity
- * flag).
+ * flag), and whether nodes the distance-bound grid certifies outside their
+ * target skip the exact query.
  *
  * Return codes: 0 success; 1 argument error; 2 CUDA error.  The message of
  * the last error on the calling thread is sdg_last_error().  Solver failures
@@ -60,8 +62,8 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 118
-#define SDG_VALUE_COUNT 37
+#define SDG_BUFFER_COUNT 120
+#define SDG_VALUE_COUNT 38
 #define SDG_PHASES 9
 
 /* ABI revision of this header. */

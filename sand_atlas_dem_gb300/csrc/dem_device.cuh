@@ -46,6 +46,7 @@ struct Config {
     uint32_t gatherWarps;        // gather warps (grains in flight) per SM
     uint32_t walkBlocksPerSM;    // exact-query CTAs (256 threads, one node each) per SM
     uint32_t survivorCapacity;   // nodes that pass the conservative filters, per step
+    uint32_t distanceGridEnabled;  // skip nodes the distance-bound grid certifies outside
 };
 
 // Buffers: the reference Resources block (solver.slang:20-100) in declaration
@@ -114,12 +115,15 @@ struct Res {
     uint32_t* walkList;               // survivorCapacity: survivors left for the exact query
     float4* dpairSourcePlane;         // 4*pairCapacity: the enclosure plane in the source frame, and its bound terms
     const float4* meshChildren;       // 4 per BVH node: both children's bounds (internal) or the triangle range
+    float* distanceGrid;              // shapes x GRID^3: certified lower bound of the signed distance per cell
+    float4* distanceGridInfo;         // shapes: grid origin xyz, cell size
 };
-constexpr int EXTENSION_COUNT = 41;
+constexpr int EXTENSION_COUNT = 43;
+constexpr uint32_t GRID = 48;  // cells per axis of each shape's distance-bound grid
 constexpr int CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4;
 constexpr int BUFFER_COUNT = RESOURCE_COUNT + EXTENSION_COUNT;
 constexpr int CONFIG_VALUES = 25;
-constexpr int VALUE_COUNT = CONFIG_VALUES + 12;
+constexpr int VALUE_COUNT = CONFIG_VALUES + 13;
 constexpr int SCAN_BLOCKS = 608;  // 4 per SM on a 152-SM GB300
 // work[] slots
 constexpr int W_CANDIDATES = 0;
@@ -479,6 +483,24 @@ __device__ __forceinline__ bool nodeContact(const Res& r, const Config& c, uint3
     f3 arm, local;
     if (!nodePrefilter(r, src, dst, node, branch, plane, arm, local)) return false;
     return nodeExact(r, c, src, dst, node, arm, local, pd, na);
+}
+
+// Certified lower bound of the target shape's signed distance at `local`
+// (shape frame, unscaled), from its cell of the distance-bound grid.  The
+// signed distance to a closed mesh is 1-Lipschitz, so every point of a cell
+// lies at least phi(centre) - (half diagonal) from the surface; the grid
+// stores that bound less a slack above the FP32 error of the centre query.
+// Points outside the grid (outside the shape's root box) get -inf.
+__device__ __forceinline__ float distanceBound(const Res& r, uint32_t shape, f3 local) {
+    float4 info = __ldg(&r.distanceGridInfo[shape]);
+    float inv = __fdiv_rn(1.0f, info.w);
+    float gx = floorf(__fmul_rn(__fsub_rn(local.x, info.x), inv));
+    float gy = floorf(__fmul_rn(__fsub_rn(local.y, info.y), inv));
+    float gz = floorf(__fmul_rn(__fsub_rn(local.z, info.z), inv));
+    if (!(gx >= 0.f && gy >= 0.f && gz >= 0.f && gx < float(GRID) && gy < float(GRID) && gz < float(GRID)))
+        return -1e30f;
+    uint32_t cell = (uint32_t(gz) * GRID + uint32_t(gy)) * GRID + uint32_t(gx);
+    return __ldg(&r.distanceGrid[size_t(shape) * GRID * GRID * GRID + cell]);
 }
 
 // ---------------------------------------------------------------- helpers

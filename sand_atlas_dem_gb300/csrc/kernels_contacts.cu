@@ -587,7 +587,37 @@ __global__ void __launch_bounds__(256) k_survivorPrefilter(const __grid_constant
         uint32_t node = __ldg(&r.meshSampleIndices[__ldg(&r.meshClusterRanges[cd.y]).x + sv.y]);
         float4 plane = r.dpairPlane[d];
         f3 arm, local;
-        r.survKeep[s] = nodePrefilter(r, src, dst, node, xyz(r.dpairBranch[d]), &plane, arm, local) ? 1u : 0u;
+        bool keep = nodePrefilter(r, src, dst, node, xyz(r.dpairBranch[d]), &plane, arm, local);
+        // A node certified outside the target by the distance-bound grid
+        // cannot be a contact (the exact query would find phi > 0).
+        if (keep && c.distanceGridEnabled && distanceBound(r, r.shapeId[dst], local) > 0.0f) keep = false;
+        r.survKeep[s] = keep ? 1u : 0u;
+    }
+}
+// Distance-bound grid of every shape (built once per library): one thread per
+// cell evaluates the exact signed distance at the cell centre (meshDistance,
+// the query the contacts use) and stores phi - (half diagonal) x 1.001 -
+// 1e-5 (1 + |centre|_1).  The grid spans the shape's root box with cubic
+// cells of edge (largest box extent) / GRID.
+__global__ void k_distanceGrid(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    const uint32_t cells = GRID * GRID * GRID;
+    for (uint32_t t = gtid(); t < c.shapes * cells; t += gstride()) {
+        uint32_t shape = t / cells, cell = t % cells;
+        uint32_t root = __ldg(&r.meshRoots[shape].x);
+        f3 low = xyz(__ldg(&r.meshMin[root])), high = xyz(__ldg(&r.meshMax[root]));
+        f3 extent = high - low;
+        float h = __fdiv_rn(mx(mx(extent.x, extent.y), extent.z), float(GRID));
+        if (cell == 0) r.distanceGridInfo[shape] = w4(low, h);
+        uint32_t gx = cell % GRID, gy = (cell / GRID) % GRID, gz = cell / (GRID * GRID);
+        f3 centre = low + mk(__fmul_rn(float(gx) + 0.5f, h), __fmul_rn(float(gy) + 0.5f, h),
+                             __fmul_rn(float(gz) + 0.5f, h));
+        float phi = meshDistance(r, shape, centre, false).w;
+        float reach = __fmul_rn(__fmul_rn(0.8660254f, h), 1.001f);
+        float slack = __fmul_rn(1e-5f, __fadd_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(centre.x), fabsf(centre.y)),
+                                                                 fabsf(centre.z))));
+        r.distanceGrid[t] = __fsub_rn(__fsub_rn(phi, reach), slack);
     }
 }
 // Learned culler over the survivor list: 64 survivors per warp iteration
@@ -1062,6 +1092,7 @@ int launch_contacts(const std::string_view& name, const Params& P, uint32_t coun
     else if (name == "collectWalk") collectWalk(P, s);
     else if (name == "collectEmit") collectEmit(P, s);
     else if (name == "resolveContacts") k_resolve<<<grid(c.contactBlocksPerSM, 8), T, 0, s>>>(P);
+    else if (name == "distanceGrid") k_distanceGrid<<<grid(0, 8), T, 0, s>>>(P);
     else if (name == "gather") k_gather<<<min(blocks(c.N, 8), max(1u, grid(c.gatherWarps, 64) / 8)), T, 0, s>>>(P);
     else return 1;
     (void)count;

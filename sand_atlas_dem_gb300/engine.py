@@ -40,8 +40,9 @@ EXTENSION_ORDER = (
     "sideContactStart", "oldPairOffsets", "oldPairB", "oldContactStart", "work", "scanPartials",
     "hitScratch", "candSurvCount", "dpairPlane", "grainSpecimen", "specimenBins", "cullerParams", "cullerW1",
     "cullerMargin", "cullerStats", "candSurvMask", "candSurvOffset", "survivors", "survKeep", "keepOffset",
-    "walkList", "dpairSourcePlane", "meshChildren",
+    "walkList", "dpairSourcePlane", "meshChildren", "distanceGrid", "distanceGridInfo",
 )
+DISTANCE_GRID = 48  # cells per axis of each shape's distance-bound grid (csrc GRID)
 CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4
 BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
 # History side fields: (name bound as the side being written, name bound as committed).
@@ -158,7 +159,7 @@ class Engine:
         return cls(library, spec, None, None, None, None, layout=layout, **kwargs)
 
     def __init__(self, library, spec, positions, cell, shape_ids, scales, *, metal=None, device=None,
-                 use_graph=True, layout=None):
+                 use_graph=True, layout=None, distance_grid=True):
         torch = _torch()
         if metal is not None:
             raise ValueError("The GB300 engine owns its device; no adapter may be passed")
@@ -179,6 +180,10 @@ class Engine:
         self.use_graph = use_graph
         self.culler = None
         self.tuning = {}
+        # Skip nodes the certified distance-bound grid places outside their
+        # target (exact: no contact changes); off reproduces the reference's
+        # own filters alone.
+        self.distance_grid = bool(distance_grid)
         self._reduce_scratch = {}
         # Host<->device bytes moved by this engine's own reads and uploads.
         self.h2d_bytes = self.d2h_bytes = 0
@@ -222,6 +227,7 @@ class Engine:
             "candSurvOffset": 4 * (self.candidate_capacity + 1), "survivors": 8 * self.survivor_capacity,
             "survKeep": 4 * (self.survivor_capacity + 1), "keepOffset": 4 * (self.survivor_capacity + 1),
             "walkList": 4 * self.survivor_capacity, "dpairSourcePlane": 16 * 4 * pc,
+            "distanceGrid": 4 * len(library.shapes) * DISTANCE_GRID**3, "distanceGridInfo": 16 * len(library.shapes),
             "cullerParams": 4 * CULLER_PARAMS * len(library.shapes), "cullerW1": 2 * 4096 * len(library.shapes),
             "cullerMargin": 4 * len(library.shapes), "cullerStats": 16,
         }
@@ -249,6 +255,8 @@ class Engine:
         if not self._native:
             raise MemoryError("GB300 engine allocation failed")
         self._finalizer = weakref.finalize(self, self.lib.sdg_engine_destroy, self._native)
+        # Certified distance bounds of every shape, built once from the packed library.
+        self.dispatch("distanceGrid", 0, self.config(dt=0))
         self.stream.synchronize()
 
     # ------------------------------------------------------------ plumbing
@@ -283,7 +291,8 @@ class Engine:
         values = list(self.layout.config_values(config)) + [
             float(self.leaf_words), float(self.candidate_capacity), 0.0, float(self.specimens),
             float(self.culler is not None),
-        ] + [float(self.tuning.get(k, 0)) for k in TUNING_KEYS] + [float(self.survivor_capacity)]
+        ] + [float(self.tuning.get(k, 0)) for k in TUNING_KEYS] + [float(self.survivor_capacity),
+                                                                     float(self.distance_grid)]
         return (ct.c_double * len(values))(*values), len(values)
 
     def dispatch(self, name, count, config, active=None):
@@ -375,9 +384,12 @@ class Engine:
                 replacement = Engine(
                     self.library, replace(old, **settings), None, None, None, None,
                     layout=HostLayout.batch(self.library, replace(old, **settings), specimens),
-                    device=self.device, use_graph=self.use_graph,
+                    device=self.device, use_graph=self.use_graph, distance_grid=self.distance_grid,
                 )
                 replacement.initial_cell = self.initial_cell.copy()
+                replacement.tuning = dict(self.tuning)
+                if self.culler is not None:
+                    self.culler.attach(replacement)
                 replacement.restore(state, self.step)
                 self._adopt(replacement)
                 self.capacity_retries = log

@@ -58,8 +58,10 @@ def test_training_reduces_loss_and_margin_covers_inside(gpu_library):
 @pytest.mark.parametrize("side", [4, 6])
 def test_culled_step_has_zero_missed_contacts(gpu_library, side):
     library, spec, case = lattice_case(side=side, viscosity=4e5)
-    exact = build(Engine, library, spec, case)
-    culled = build(Engine, library, spec, case)
+    # Against the reference's own filters (plane, hull): the certified
+    # distance-bound grid already skips what the network could, so it is off.
+    exact = build(Engine, library, spec, case, distance_grid=False)
+    culled = build(Engine, library, spec, case, distance_grid=False)
     c = small_culler(culled)
     c.train()
     c.attach(culled)
