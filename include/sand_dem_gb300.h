@@ -114,6 +114,14 @@ int sdg_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* 
 int sdg_scan_partials(void);
 
 /*
+ * Device-to-device copies of n buffers on `stream` (dst[k] <- src[k],
+ * bytes[k] each, one cudaMemcpyAsync per buffer).  The transactional backup
+ * of a chunk and its restore, which the reference does with encoder buffer
+ * copies (src/sand_atlas_dem/gpu.py:729-743, backend.py copy_buffer).
+ */
+int sdg_copy_buffers(void* const* dst, void* const* src, const uint64_t* bytes, uint32_t n, void* stream);
+
+/*
  * The same scan with its block partials in a fixed array of this library
  * (4,864 bytes per device) instead of caller scratch; it allocates nothing.
  * No counterpart in the reference: it serves callers that hold only the

@@ -261,6 +261,19 @@ int sdg_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* 
 
 int sdg_scan_partials(void) { return 2 * SCAN_BLOCKS; }
 
+// Device-to-device copies of n buffers on `stream`, one cudaMemcpyAsync each
+// (the engine's transactional backup before a chunk and its restore).
+int sdg_copy_buffers(void* const* dst, void* const* src, const uint64_t* bytes, uint32_t n, void* stream) {
+    if (n && (!dst || !src || !bytes)) { g_error = "null copy arguments"; return 1; }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    for (uint32_t k = 0; k < n; ++k) {
+        if (!bytes[k]) continue;
+        if (int rc = record(cudaMemcpyAsync(dst[k], src[k], bytes[k], cudaMemcpyDeviceToDevice, s), "copy"))
+            return rc;
+    }
+    return 0;
+}
+
 void* sdg_engine_create(void) { return new (std::nothrow) Engine(); }
 void sdg_engine_destroy(void* engine) { delete static_cast<Engine*>(engine); }
 

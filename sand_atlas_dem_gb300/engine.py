@@ -60,6 +60,9 @@ def _torch():
     return torch
 
 
+STAGING_BYTES = 1 << 16  # pinned host staging per engine for small uploads and reads
+
+
 class DeviceBuffer:
     """One device allocation; the reference Buffer surface (``cpu.py:431-447``)."""
 
@@ -76,33 +79,47 @@ class DeviceBuffer:
         return self.tensor.data_ptr()
 
     def copy_from_numpy(self, array):
-        torch = _torch()
         data = np.ascontiguousarray(array).view(np.uint8).reshape(-1)
         if data.size != self.size:
             raise ValueError("GB300 buffer upload size mismatch")
-        engine = self._engine()
-        with torch.cuda.stream(engine.stream):
-            self.tensor.copy_(torch.from_numpy(data.copy()), non_blocking=False)
-        engine.stream.synchronize()
-        engine.h2d_bytes += data.size
+        self._upload(data)
 
     def write_prefix(self, array):
-        torch = _torch()
         data = np.ascontiguousarray(array).view(np.uint8).reshape(-1)
         if data.size > self.size:
             raise ValueError("GB300 buffer prefix out of bounds")
         if data.size:
-            engine = self._engine()
-            with torch.cuda.stream(engine.stream):
-                self.tensor[: data.size].copy_(torch.from_numpy(data.copy()))
-            engine.stream.synchronize()
-            engine.h2d_bytes += data.size
+            self._upload(data)
+
+    def _upload(self, data):
+        """Host -> device on the engine stream; small uploads go through the
+        engine's pinned staging buffer (one DMA, no pageable bounce)."""
+        torch = _torch()
+        engine = self._engine()
+        n = data.size
+        with torch.cuda.stream(engine.stream):
+            if n <= STAGING_BYTES:
+                stage = engine._staging[:n]
+                stage.numpy()[:] = data
+                self.tensor[:n].copy_(stage, non_blocking=True)
+            else:
+                self.tensor[:n].copy_(torch.from_numpy(data.copy()))
+        engine.stream.synchronize()
+        engine.h2d_bytes += n
 
     def to_numpy(self, dtype=np.uint8, count=None):
+        torch = _torch()
         engine = self._engine()
-        engine.stream.synchronize()
         nbytes = self.size if count is None else int(count) * np.dtype(dtype).itemsize
         engine.d2h_bytes += nbytes
+        if nbytes <= STAGING_BYTES:
+            # Small reads land in the pinned staging buffer.
+            stage = engine._staging[:nbytes]
+            with torch.cuda.stream(engine.stream):
+                stage.copy_(self.tensor[:nbytes], non_blocking=True)
+            engine.stream.synchronize()
+            return stage.numpy().view(dtype).copy()
+        engine.stream.synchronize()
         return self.tensor[:nbytes].cpu().numpy().view(dtype).copy()
 
 
@@ -185,6 +202,7 @@ class Engine:
         # own filters alone.
         self.distance_grid = bool(distance_grid)
         self._reduce_scratch = {}
+        self._array_cache = {}
         # Host<->device bytes moved by this engine's own reads and uploads.
         self.h2d_bytes = self.d2h_bytes = 0
         for name in ("length_unit", "time_unit", "mass_unit", "force_unit", "stress_unit", "energy_unit",
@@ -201,6 +219,7 @@ class Engine:
         self.survivor_capacity = 4 * h.contact_capacity
         self.device = torch.device(device or "cuda")
         self.stream = torch.cuda.Stream(self.device)
+        self._staging = torch.empty(STAGING_BYTES, dtype=torch.uint8).pin_memory()
         self.m = GB300Device(self)
         self.buffers = {}
         n, pc, cc = h.n, h.pair_capacity, h.contact_capacity
@@ -276,10 +295,15 @@ class Engine:
         return view
 
     def _arrays(self, active):
-        view = self._bound(active)
-        ptrs = (ct.c_void_p * len(BUFFER_ORDER))(*(view[k].ptr() for k in BUFFER_ORDER))
-        sizes = (ct.c_uint64 * len(BUFFER_ORDER))(*(view[k].size for k in BUFFER_ORDER))
-        return ptrs, sizes
+        """Pointer and size blocks for one history-side orientation (built
+        once: the buffers never move while the engine lives)."""
+        cached = self._array_cache.get(active)
+        if cached is None:
+            view = self._bound(active)
+            ptrs = (ct.c_void_p * len(BUFFER_ORDER))(*(view[k].ptr() for k in BUFFER_ORDER))
+            sizes = (ct.c_uint64 * len(BUFFER_ORDER))(*(view[k].size for k in BUFFER_ORDER))
+            cached = self._array_cache[active] = (ptrs, sizes)
+        return cached
 
     def config(self, dt=None, drag=0.0, history=None):
         return self.layout.config(
@@ -406,25 +430,23 @@ class Engine:
             for buffer in group.values():
                 buffer._engine = me
 
-    def _copy(self, dst, src, nbytes=None):
-        torch = _torch()
-        n = min(dst.size, src.size) if nbytes is None else int(nbytes)
-        if n:
-            with torch.cuda.stream(self.stream):
-                dst.tensor[:n].copy_(src.tensor[:n], non_blocking=True)
-
     def _backup(self, restore=False):
         committed = self.sides[1 - self.active]
         count = int(self.read("control", np.uint32, (16,))[2]) if not restore else self._backup_count
         if count < 0 or count > self.contact_capacity:
             raise ValueError("Committed contact count is outside capacity")
+        copies = []
         for name, backup in self.backups.items():
             src, dst = (backup, self.buffers[name]) if restore else (self.buffers[name], backup)
-            self._copy(dst, src)
+            copies.append((dst, src, min(dst.size, src.size)))
         for name, backup in self.history_backup.items():
-            nbytes = 16 * count if name in ("meta", "slip", "normalArea") else None
             src, dst = (backup, committed[name]) if restore else (committed[name], backup)
-            self._copy(dst, src, nbytes)
+            nbytes = 16 * count if name in ("meta", "slip", "normalArea") else min(dst.size, src.size)
+            copies.append((dst, src, nbytes))
+        n = len(copies)
+        native.check(self.lib.sdg_copy_buffers(
+            (ct.c_void_p * n)(*(d.ptr() for d, _, _ in copies)), (ct.c_void_p * n)(*(s.ptr() for _, s, _ in copies)),
+            (ct.c_uint64 * n)(*(b for _, _, b in copies)), n, ct.c_void_p(self.stream.cuda_stream)))
         self._backup_count = count
 
     def _advance_once(self, steps, *, rate=(0, 0, 0), drag=0):

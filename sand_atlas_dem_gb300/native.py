@@ -91,6 +91,8 @@ def load():
                                        ct.c_void_p]
     lib.sdg_exclusive_scan.restype = ct.c_int
     lib.sdg_scan_partials.restype = ct.c_int
+    lib.sdg_copy_buffers.argtypes = [P(ct.c_void_p), P(ct.c_void_p), P(ct.c_uint64), ct.c_uint32, ct.c_void_p]
+    lib.sdg_copy_buffers.restype = ct.c_int
     lib.sdg_exclusive_scan_static.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_uint32, ct.c_void_p, ct.c_void_p]
     lib.sdg_exclusive_scan_static.restype = ct.c_int
     V = ct.c_void_p
@@ -137,6 +139,7 @@ EXPORTS = (
     "sdg_engine_kernels_per_step",
     "sdg_exclusive_scan",
     "sdg_scan_partials",
+    "sdg_copy_buffers",
     "sdg_exclusive_scan_static",
     "sdg_culler_param_count",
     "sdg_culler_sample",
