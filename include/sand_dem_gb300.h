@@ -11,7 +11,7 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 120) this backend's extension buffers, in the order of
+ *   [77, 121) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
@@ -30,7 +30,8 @@
  *             grain's frame with its rejection-bound terms, and the
  *             triangle BVH as one record per node with both children's
  *             bounds, and per shape a 48^3 grid of certified lower bounds of
- *             the signed distance with its origin and cell size).
+ *             the signed distance with its origin and cell size, and the
+ *             triangle nearest to each cell centre).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
@@ -62,7 +63,7 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 120
+#define SDG_BUFFER_COUNT 121
 #define SDG_VALUE_COUNT 38
 #define SDG_PHASES 9
 

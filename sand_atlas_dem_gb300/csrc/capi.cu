@@ -77,7 +77,8 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
             bytes[77 + 36] < (uint64_t(c.survivorCapacity) + 1) * 4 ||
             bytes[77 + 37] < (uint64_t(c.survivorCapacity) + 1) * 4 || bytes[77 + 38] < uint64_t(c.survivorCapacity) * 4 ||
             bytes[77 + 39] < uint64_t(4) * c.pairCapacity * 16 ||
-            bytes[77 + 41] < uint64_t(c.shapes) * GRID * GRID * GRID * 4 || bytes[77 + 42] < uint64_t(c.shapes) * 16) {
+            bytes[77 + 41] < uint64_t(c.shapes) * GRID * GRID * GRID * 4 || bytes[77 + 42] < uint64_t(c.shapes) * 16 ||
+            bytes[77 + 43] < uint64_t(c.shapes) * GRID * GRID * GRID * 4) {
             g_error = "a buffer is smaller than its configured capacity";
             return 1;
         }

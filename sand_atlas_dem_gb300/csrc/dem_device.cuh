@@ -117,8 +117,9 @@ struct Res {
     const float4* meshChildren;       // 4 per BVH node: both children's bounds (internal) or the triangle range
     float* distanceGrid;              // shapes x GRID^3: certified lower bound of the signed distance per cell
     float4* distanceGridInfo;         // shapes: grid origin xyz, cell size
+    uint32_t* distanceGridTriangle;   // shapes x GRID^3: triangle nearest to each cell centre
 };
-constexpr int EXTENSION_COUNT = 43;
+constexpr int EXTENSION_COUNT = 44;
 constexpr uint32_t GRID = 48;  // cells per axis of each shape's distance-bound grid
 constexpr int CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4;
 constexpr int BUFFER_COUNT = RESOURCE_COUNT + EXTENSION_COUNT;
@@ -302,7 +303,15 @@ __device__ __forceinline__ float meshBoxDistance(const Res& r, uint32_t node, f3
 constexpr uint32_t LEAF_MARK = 0xFFFFFFFFu;
 // Nearest-first BVH walk with cached pushed box distances (the reference CPU
 // variant, cpu_scheduling.slang:18-48, bit-identical to solver.slang:224-252).
-__device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 p, bool surfaceNormal) {
+// With `seed` (a triangle of the shape) the walk starts with its best
+// distance just above that triangle's squared distance, computed exactly as
+// the walk computes it.  That prunes every node that cannot hold a triangle
+// at least as near, and changes nothing else: the nearest triangles' nodes
+// are never pruned, the surviving nodes are visited in the same order, and
+// the first nearest triangle reached is recorded as before.
+// `nearestTriangle`, when given, receives the recorded triangle.
+__device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 p, bool surfaceNormal,
+                                               uint32_t seed = 0xFFFFFFFFu, uint32_t* nearestTriangle = nullptr) {
     uint32_t root = __ldg(&r.meshRoots[shape].x);
     uint32_t pending[32];
     float pendingDistance[32];
@@ -310,6 +319,13 @@ __device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 
     pending[0] = root;
     pendingDistance[0] = meshBoxDistance(r, root, p);
     float best = 1e30f;
+    if (seed != 0xFFFFFFFFu) {
+        uint32_t feature;
+        f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * seed])), xyz(__ldg(&r.meshTriangles[3 * seed + 1])),
+                               xyz(__ldg(&r.meshTriangles[3 * seed + 2])), feature);
+        f3 dq = p - q;
+        best = nextafterf(dot(dq, dq), 1e30f);
+    }
     f3 nearest = mk(0.f, 0.f, 0.f);
     uint32_t nearestNormal = 0;
     bool found = false;
@@ -342,6 +358,7 @@ __device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 
             if (distance < best) { best = distance; nearest = q; nearestNormal = 7 * triangle + feature; found = true; }
         }
     }
+    if (nearestTriangle) *nearestTriangle = found ? nearestNormal / 7 : 0xFFFFFFFFu;
     f3 pseudo = found ? xyz(__ldg(&r.meshNormals[nearestNormal])) : mk(0.f, 0.f, 0.f);
     float distance = __fsqrt_rn(best);
     f3 off = p - nearest;
@@ -458,11 +475,11 @@ __device__ __forceinline__ bool nodePrefilter(const Res& r, uint32_t src, uint32
     return meshMayContain(r, r.shapeId[dst], local);
 }
 __device__ __forceinline__ bool nodeExact(const Res& r, const Config& c, uint32_t src, uint32_t dst, uint32_t node,
-                                          f3 arm, f3 local, float4& pd, float4& na) {
+                                          f3 arm, f3 local, float4& pd, float4& na, uint32_t seed = 0xFFFFFFFFu) {
     uint32_t sid = r.shapeId[src], targetShape = r.shapeId[dst];
     float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[sid].x) + node]);
     float4 bs = r.body[src], bd = r.body[dst];
-    float4 f = meshDistance(r, targetShape, local, false);
+    float4 f = meshDistance(r, targetShape, local, false, seed);
     pd = w4(arm, __fmul_rn(-f.w, bd.x));
     if (pd.w <= 0.0f) return false;
     f3 grad = qrot(r.rotation[dst], xyz(f));
@@ -491,16 +508,29 @@ __device__ __forceinline__ bool nodeContact(const Res& r, const Config& c, uint3
 // lies at least phi(centre) - (half diagonal) from the surface; the grid
 // stores that bound less a slack above the FP32 error of the centre query.
 // Points outside the grid (outside the shape's root box) get -inf.
-__device__ __forceinline__ float distanceBound(const Res& r, uint32_t shape, f3 local) {
+// Index of the grid cell holding `local` in the shape's grid, or EMPTY
+// outside it.
+__device__ __forceinline__ uint32_t gridCell(const Res& r, uint32_t shape, f3 local) {
     float4 info = __ldg(&r.distanceGridInfo[shape]);
     float inv = __fdiv_rn(1.0f, info.w);
     float gx = floorf(__fmul_rn(__fsub_rn(local.x, info.x), inv));
     float gy = floorf(__fmul_rn(__fsub_rn(local.y, info.y), inv));
     float gz = floorf(__fmul_rn(__fsub_rn(local.z, info.z), inv));
     if (!(gx >= 0.f && gy >= 0.f && gz >= 0.f && gx < float(GRID) && gy < float(GRID) && gz < float(GRID)))
-        return -1e30f;
-    uint32_t cell = (uint32_t(gz) * GRID + uint32_t(gy)) * GRID + uint32_t(gx);
+        return 0xFFFFFFFFu;
+    return (uint32_t(gz) * GRID + uint32_t(gy)) * GRID + uint32_t(gx);
+}
+__device__ __forceinline__ float distanceBound(const Res& r, uint32_t shape, f3 local) {
+    uint32_t cell = gridCell(r, shape, local);
+    if (cell == 0xFFFFFFFFu) return -1e30f;
     return __ldg(&r.distanceGrid[size_t(shape) * GRID * GRID * GRID + cell]);
+}
+// The triangle nearest to the centre of the cell holding `local` (a seed
+// for meshDistance), or EMPTY outside the grid.
+__device__ __forceinline__ uint32_t gridSeed(const Res& r, uint32_t shape, f3 local) {
+    uint32_t cell = gridCell(r, shape, local);
+    if (cell == 0xFFFFFFFFu) return 0xFFFFFFFFu;
+    return __ldg(&r.distanceGridTriangle[size_t(shape) * GRID * GRID * GRID + cell]);
 }
 
 // ---------------------------------------------------------------- helpers

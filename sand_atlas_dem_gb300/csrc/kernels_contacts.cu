@@ -613,7 +613,9 @@ __global__ void k_distanceGrid(const __grid_constant__ Params P) {
         uint32_t gx = cell % GRID, gy = (cell / GRID) % GRID, gz = cell / (GRID * GRID);
         f3 centre = low + mk(__fmul_rn(float(gx) + 0.5f, h), __fmul_rn(float(gy) + 0.5f, h),
                              __fmul_rn(float(gz) + 0.5f, h));
-        float phi = meshDistance(r, shape, centre, false).w;
+        uint32_t nearest;
+        float phi = meshDistance(r, shape, centre, false, 0xFFFFFFFFu, &nearest).w;
+        r.distanceGridTriangle[t] = nearest;
         float reach = __fmul_rn(__fmul_rn(0.8660254f, h), 1.001f);
         float slack = __fmul_rn(1e-5f, __fadd_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(centre.x), fabsf(centre.y)),
                                                                  fabsf(centre.z))));
@@ -702,7 +704,9 @@ __global__ void __launch_bounds__(256) k_nodeWalk(const __grid_constant__ Params
         uint32_t s = r.walkList[t];
         SurvivorNode v = survivorNode(r, s);
         float4 pd, na;
-        if (nodeExact(r, c, v.src, v.dst, v.node, v.arm, v.local, pd, na)) {
+        // Seed the walk with the triangle nearest to the node's grid cell.
+        uint32_t seed = gridSeed(r, r.shapeId[v.dst], v.local);
+        if (nodeExact(r, c, v.src, v.dst, v.node, v.arm, v.local, pd, na, seed)) {
             r.hitScratch[2 * s] = pd;
             r.hitScratch[2 * s + 1] = na;
             atomicOr(v.slot < WARP ? &r.candHitMask[v.item].x : &r.candHitMask[v.item].y, 1u << (v.slot & 31u));

@@ -40,7 +40,7 @@ EXTENSION_ORDER = (
     "sideContactStart", "oldPairOffsets", "oldPairB", "oldContactStart", "work", "scanPartials",
     "hitScratch", "candSurvCount", "dpairPlane", "grainSpecimen", "specimenBins", "cullerParams", "cullerW1",
     "cullerMargin", "cullerStats", "candSurvMask", "candSurvOffset", "survivors", "survKeep", "keepOffset",
-    "walkList", "dpairSourcePlane", "meshChildren", "distanceGrid", "distanceGridInfo",
+    "walkList", "dpairSourcePlane", "meshChildren", "distanceGrid", "distanceGridInfo", "distanceGridTriangle",
 )
 DISTANCE_GRID = 48  # cells per axis of each shape's distance-bound grid (csrc GRID)
 CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4
@@ -247,6 +247,7 @@ class Engine:
             "survKeep": 4 * (self.survivor_capacity + 1), "keepOffset": 4 * (self.survivor_capacity + 1),
             "walkList": 4 * self.survivor_capacity, "dpairSourcePlane": 16 * 4 * pc,
             "distanceGrid": 4 * len(library.shapes) * DISTANCE_GRID**3, "distanceGridInfo": 16 * len(library.shapes),
+            "distanceGridTriangle": 4 * len(library.shapes) * DISTANCE_GRID**3,
             "cullerParams": 4 * CULLER_PARAMS * len(library.shapes), "cullerW1": 2 * 4096 * len(library.shapes),
             "cullerMargin": 4 * len(library.shapes), "cullerStats": 16,
         }
