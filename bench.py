@@ -64,7 +64,7 @@ WORKLOADS = {
 DATA = ROOT / "sand_atlas_dem_gb300" / "data"
 # DRAM bytes (read + write) of one k_nodeWalk launch from an ncu capture of
 # the same workload (profiles/walk-dense-10k.md); None where not captured.
-WALK_TRAFFIC = {"dense-10k": 41.07e6}
+WALK_TRAFFIC = {"dense-10k": 60.16e6}
 
 
 def log(*args):

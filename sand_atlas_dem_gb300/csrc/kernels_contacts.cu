@@ -1049,11 +1049,15 @@ static void collectFilter(const Params& P, cudaStream_t s) {
     k_survivorList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
     k_survivorPrefilter<<<grid(c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
     if (c.cullerEnabled) {
-        static bool attributed = false;
-        if (!attributed) {
+        // The 73.7 KB tile area needs the opt-in shared-memory limit, set
+        // once per device (the attribute is per device and function).
+        static uint64_t attributed = 0;
+        int device = 0;
+        cudaGetDevice(&device);
+        if (device < 64 && !((attributed >> device) & 1u)) {
             cudaFuncSetAttribute(k_cullSurvivors, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  int(8 * CULLER_TILE_WORDS * sizeof(uint32_t)));
-            attributed = true;
+            attributed |= uint64_t(1) << device;
         }
         k_cullSurvivors<<<grid(c.queryBlocksPerSM, 2), 256, 8 * CULLER_TILE_WORDS * sizeof(uint32_t), s>>>(P);
     }
