@@ -894,6 +894,11 @@ __global__ void __launch_bounds__(256, 3) k_gather(const __grid_constant__ Param
     const Config& c = P.c;
     if (r.control[0] != 0) return;
     uint32_t pairs = activePairs(r, c);
+    __shared__ uint32_t window[8][4][WARP];  // per warp: B candidates, merged pairs, offsets, range ends
+    uint32_t* wb = window[threadIdx.x >> 5][0];
+    uint32_t* wp = window[threadIdx.x >> 5][1];
+    uint32_t* wo = window[threadIdx.x >> 5][2];
+    uint32_t* we = window[threadIdx.x >> 5][3];
     for (uint32_t id = warpGlobal(); id < c.N; id += warpStride()) {
         f3 f = mk(0.f, 0.f, 0.f), t = f, fLow = f, tLow = f, stress0 = f, stress1 = f, stress2 = f;
         float energy = 0, denom = 0, maxDepth = 0, dissipation = 0, normalPower = 0, stiffnessRate = 0,
@@ -901,31 +906,74 @@ __global__ void __launch_bounds__(256, 3) k_gather(const __grid_constant__ Param
         f3 one = mk(1.f, 1.f, 1.f);
         float inverseInertia = mx(mx(dot(abs3(xyz(r.invI[3 * id])), one), dot(abs3(xyz(r.invI[3 * id + 1])), one)),
                                   dot(abs3(xyz(r.invI[3 * id + 2])), one));
-        float m = r.body[id].y, bw = r.body[id].w;
+        float m_ = r.body[id].y, bw = r.body[id].w;
         uint32_t aBegin = min(r.pairOffsets[id], pairs), aEnd = min(aBegin + r.pairCounts[id], pairs);
         uint32_t bBegin = r.byJOffsets[id], bEnd = r.byJOffsets[id + 1];
+        // The grain's pairs in descending pair id (the first-grain run
+        // aBegin..aEnd-1 and the second-grain run byJPairs[bBegin..bEnd),
+        // both ascending, merged from the top), taken 32 at a time: each
+        // window is merged by ranks, its pairs' contact ranges are scanned,
+        // and its contacts -- each pair's from the last -- are processed 32
+        // per round in that flattened order, the reference's LIFO order.
         uint32_t ia = aEnd, ib = bEnd;
         while (ia > aBegin || ib > bBegin) {
-            uint32_t p;
-            if (ib == bBegin || (ia > aBegin && ia - 1 > r.byJPairs[ib - 1])) p = --ia;
-            else p = r.byJPairs[--ib];
-            uint32_t begin = r.sideContactStart[p], end = r.sideContactStart[p + 1];
-            f3 branch0 = xyz(r.dpairBranch[2 * p]), branch1 = xyz(r.dpairBranch[2 * p + 1]);
-            for (uint32_t top = end; top > begin;) {
-                uint32_t count = min(top - begin, WARP);
+            uint32_t na = min(ia - aBegin, WARP), nb = min(ib - bBegin, WARP), lane = laneId();
+            uint32_t bv = lane < nb ? r.byJPairs[ib - 1 - lane] : 0u;  // descending
+            wb[lane] = bv;
+            __syncwarp();
+            // Rank of each candidate among the union of both windows.
+            uint32_t av = ia - 1 - lane;                                // descending, valid for lane < na
+            uint32_t rankA = WARP, rankB = WARP;
+            if (lane < na) {
+                uint32_t lo = 0, hi = nb;                               // B candidates greater than av
+                while (lo < hi) { uint32_t mid = (lo + hi) >> 1; if (wb[mid] > av) lo = mid + 1; else hi = mid; }
+                rankA = lane + lo;
+            }
+            if (lane < nb) {
+                uint32_t greater = bv >= ia - 1 ? 0u : min(na, ia - 1 - bv);  // A candidates greater than bv
+                rankB = lane + greater;
+            }
+            uint32_t takeA = __popc(__ballot_sync(0xffffffffu, rankA < WARP));
+            uint32_t takeB = __popc(__ballot_sync(0xffffffffu, rankB < WARP));
+            __syncwarp();
+            if (rankA < WARP) wp[rankA] = av;
+            if (rankB < WARP) wp[rankB] = bv;
+            __syncwarp();
+            uint32_t m = takeA + takeB, cnt = 0, pairId = 0, last = 0;
+            if (lane < m) {
+                pairId = wp[lane];
+                uint32_t begin = r.sideContactStart[pairId];
+                last = r.sideContactStart[pairId + 1];
+                cnt = last - begin;
+            }
+            uint32_t incl = cnt;
+#pragma unroll
+            for (uint32_t o = 1; o < WARP; o <<= 1) {
+                uint32_t t2 = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t2;
+            }
+            uint32_t total = __shfl_sync(0xffffffffu, incl, WARP - 1);
+            wo[lane] = incl - cnt;
+            we[lane] = last;
+            __syncwarp();
+            for (uint32_t q0 = 0; q0 < total; q0 += WARP) {
+                uint32_t count = min(total - q0, WARP);
                 GatherTerms g{};
-                if (laneId() < count) {
-                    uint32_t contact = top - 1 - laneId();
+                if (lane < count) {
+                    uint32_t q = q0 + lane, lo = 0, hi = m;             // last window slot with offset <= q
+                    while (hi - lo > 1) { uint32_t mid = (lo + hi) >> 1; if (wo[mid] <= q) lo = mid; else hi = mid; }
+                    uint32_t p = wp[lo];
+                    uint32_t contact = we[lo] - 1 - (q - wo[lo]);
                     uint4 key = r.meta[contact];
                     bool source = key.x == id;
                     float4 cf = r.contactForce[contact];
                     f3 force = xyz(cf);
                     float4 pdv = r.pointDepth[contact];
                     f3 arm = xyz(pdv);
-                    f3 branch = key.x > key.y ? branch1 : branch0;
+                    f3 branch = xyz(r.dpairBranch[2 * p + (key.x > key.y ? 1u : 0u)]);
                     if (c.activeTimestep != 0) {
                         f3 localArm = source ? arm : arm - branch;
-                        float mobility = __fadd_rn(__fdiv_rn(1.0f, m), __fmul_rn(dot(localArm, localArm), inverseInertia));
+                        float mobility = __fadd_rn(__fdiv_rn(1.0f, m_), __fmul_rn(dot(localArm, localArm), inverseInertia));
                         float half = __fmul_rn(r.normalArea[contact].w, 0.5f);
                         g.stiffness = __fmul_rn(__fmul_rn(__fmul_rn(2.0f, half), __fadd_rn(__fmul_rn(c.kn, __fadd_rn(1.0f, c.mu)), c.kt)), mobility);
                         g.viscous = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(2.0f, half), c.normalViscosity), __fadd_rn(1.0f, c.mu)), mobility);
@@ -944,24 +992,26 @@ __global__ void __launch_bounds__(256, 3) k_gather(const __grid_constant__ Param
                     g.normalPower = __fmul_rn(0.5f, r.normalLossPower[contact]);
                 }
                 for (uint32_t k = 0; k < count; ++k) {
-                    int lane = int(k);
+                    int src = int(k);
                     if (c.activeTimestep != 0) {
-                        stiffnessRate = __fadd_rn(stiffnessRate, __shfl_sync(0xffffffffu, g.stiffness, lane));
-                        viscousRate = __fadd_rn(viscousRate, __shfl_sync(0xffffffffu, g.viscous, lane));
+                        stiffnessRate = __fadd_rn(stiffnessRate, __shfl_sync(0xffffffffu, g.stiffness, src));
+                        viscousRate = __fadd_rn(viscousRate, __shfl_sync(0xffffffffu, g.viscous, src));
                     }
-                    compensated3(f, fLow, shfl3(g.force, lane));
-                    compensated3(t, tLow, shfl3(g.torque, lane));
-                    stress0 = stress0 - shfl3(g.s0, lane);
-                    stress1 = stress1 - shfl3(g.s1, lane);
-                    stress2 = stress2 - shfl3(g.s2, lane);
-                    energy = __fadd_rn(energy, __shfl_sync(0xffffffffu, g.energy, lane));
-                    denom = __fadd_rn(denom, __shfl_sync(0xffffffffu, g.denom, lane));
-                    maxDepth = mx(maxDepth, __shfl_sync(0xffffffffu, g.depth, lane));
-                    dissipation = __fadd_rn(dissipation, __shfl_sync(0xffffffffu, g.dissipation, lane));
-                    normalPower = __fadd_rn(normalPower, __shfl_sync(0xffffffffu, g.normalPower, lane));
+                    compensated3(f, fLow, shfl3(g.force, src));
+                    compensated3(t, tLow, shfl3(g.torque, src));
+                    stress0 = stress0 - shfl3(g.s0, src);
+                    stress1 = stress1 - shfl3(g.s1, src);
+                    stress2 = stress2 - shfl3(g.s2, src);
+                    energy = __fadd_rn(energy, __shfl_sync(0xffffffffu, g.energy, src));
+                    denom = __fadd_rn(denom, __shfl_sync(0xffffffffu, g.denom, src));
+                    maxDepth = mx(maxDepth, __shfl_sync(0xffffffffu, g.depth, src));
+                    dissipation = __fadd_rn(dissipation, __shfl_sync(0xffffffffu, g.dissipation, src));
+                    normalPower = __fadd_rn(normalPower, __shfl_sync(0xffffffffu, g.normalPower, src));
                 }
-                top -= count;
             }
+            __syncwarp();
+            ia -= takeA;
+            ib -= takeB;
         }
         if (laneId() == 0) {
             f = f + fLow;
@@ -976,7 +1026,7 @@ __global__ void __launch_bounds__(256, 3) k_gather(const __grid_constant__ Param
             r.particleStress[3 * id + 1] = w4(stress1, 0.f);
             r.particleStress[3 * id + 2] = w4(stress2, 0.f);
             f3 v = xyz(r.velocity[id]);
-            float kinetic = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(m, dot(v, v)), dot(xyz(r.momentum[id]), omegaOf(r, id))));
+            float kinetic = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(m_, dot(v, v)), dot(xyz(r.momentum[id]), omegaOf(r, id))));
             r.particleDiagnostic[id] = make_float4(kinetic, energy, length(f), denom);
             float4 high = r.accumulated[id], low = r.accumulatedRemainder[id];
             compensated4(high, low, make_float4(dissipation, 0.f, 0.f, 0.f));
