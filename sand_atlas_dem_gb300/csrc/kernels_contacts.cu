@@ -521,9 +521,13 @@ __global__ void __launch_bounds__(256) k_nodeFilter(const __grid_constant__ Para
     const Res& r = P.r;
     const Config& c = P.c;
     uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
-    for (uint32_t item = warpGlobal(); item < n; item += warpStride()) {
-        bool keep0 = false, keep1 = false;
-        if (r.control[0] == 0) {
+    // Two items per warp, one per half-warp, four node slots per lane
+    // (slot = lane in half + 16 j): twice the loads in flight per instruction.
+    uint32_t half = laneId() >> 4, hl = laneId() & 15u;
+    for (uint32_t pair0 = 2 * warpGlobal(); pair0 < n; pair0 += 2 * warpStride()) {
+        uint32_t item = pair0 + half;
+        bool keep[4] = {false, false, false, false};
+        if (item < n && r.control[0] == 0) {
             uint2 cd = r.candidates[item];
             uint32_t d = cd.x, p = d >> 1, pass = d & 1;
             uint2 ij = r.pairs[p];
@@ -531,16 +535,26 @@ __global__ void __launch_bounds__(256) k_nodeFilter(const __grid_constant__ Para
             SourcePlane source{r.dpairSourcePlane[2 * d], r.dpairSourcePlane[2 * d + 1]};
             uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
             const float4* samples = r.sample + __ldg(&r.sampleInfo[r.shapeId[src]].x);
-            uint32_t k0 = laneId(), k1 = laneId() + WARP;
             // One dot per node against the source-frame plane; the exact
             // placement, target-frame plane and hull follow in a dense pass.
-            if (k0 < range.y)
-                keep0 = !nodeBeyondSourcePlane(source, xyz(__ldg(&samples[__ldg(&r.meshSampleIndices[range.x + k0])])));
-            if (k1 < range.y)
-                keep1 = !nodeBeyondSourcePlane(source, xyz(__ldg(&samples[__ldg(&r.meshSampleIndices[range.x + k1])])));
+            float4 x[4];
+#pragma unroll
+            for (uint32_t j = 0; j < 4; ++j) {
+                uint32_t k = hl + 16 * j;
+                x[j] = k < range.y ? __ldg(&samples[__ldg(&r.meshSampleIndices[range.x + k])])
+                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (uint32_t j = 0; j < 4; ++j)
+                keep[j] = hl + 16 * j < range.y && !nodeBeyondSourcePlane(source, xyz(x[j]));
         }
-        uint32_t m0 = __ballot_sync(0xffffffffu, keep0), m1 = __ballot_sync(0xffffffffu, keep1);
-        if (laneId() == 0) {
+        uint32_t b[4];
+#pragma unroll
+        for (uint32_t j = 0; j < 4; ++j) b[j] = __ballot_sync(0xffffffffu, keep[j]);
+        if (hl == 0 && item < n) {
+            uint32_t sh = 16 * half;
+            uint32_t m0 = ((b[0] >> sh) & 0xFFFFu) | (((b[1] >> sh) & 0xFFFFu) << 16);
+            uint32_t m1 = ((b[2] >> sh) & 0xFFFFu) | (((b[3] >> sh) & 0xFFFFu) << 16);
             r.candSurvMask[item] = make_uint2(m0, m1);
             r.candSurvCount[item] = __popc(m0) + __popc(m1);
             r.candHitMask[item] = make_uint2(0u, 0u);
