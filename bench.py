@@ -65,6 +65,8 @@ DATA = ROOT / "sand_atlas_dem_gb300" / "data"
 # DRAM bytes (read + write) of one k_nodeWalk launch from an ncu capture of
 # the same workload (profiles/walk-dense-10k.md); None where not captured.
 WALK_TRAFFIC = {"dense-10k": 60.16e6}
+# work[] counters of the stored node-filter results (csrc/dem_device.cuh).
+W_FILTER_BUILDS, W_FILTER_STEPS = 9, 10
 
 
 def log(*args):
@@ -287,9 +289,14 @@ def run_gb300(args, cpu=True):
     set_rates(e, w)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=e.device)
     ctrl0 = e.check_errors()
+    work0 = e.read("work", np.uint32, (64,))
     with ClockSampler() as clocks:
         step_ms = timed_steps(e, args.steps, flush)
     ctrl = e.check_errors()
+    work1 = e.read("work", np.uint32, (64,))
+    filter_cache = {"margin": e.filter_margin,
+                    "builds_in_timed_steps": int(work1[W_FILTER_BUILDS] - work0[W_FILTER_BUILDS]),
+                    "timed_steps": int(work1[W_FILTER_STEPS] - work0[W_FILTER_STEPS])}
     device_s = sum(step_ms) / 1e3
     value = w.grains * args.steps / device_s
     kernels = e.lib.sdg_engine_kernels_per_step(e._native)
@@ -348,7 +355,7 @@ def run_gb300(args, cpu=True):
         "config": dict(w.config, l2="flushed before each timed step (256 MiB write)",
                        pairs=pairs, contacts=contacts, node_query_items=items, node_queries=nodes,
                        plane_survivors=survivors, exact_queries=kept, timestep_s=e.spec.timestep,
-                       phase_ms=phase_ms,
+                       phase_ms=phase_ms, filter_cache=filter_cache,
                        dominant_phase=top, tuning=dict(e.tuning)),
         "e2e": {"value": e2e, "unit": "grain-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": f"Engine.advance({chunk}) + Engine.diagnostics() per chunk"},
@@ -373,6 +380,8 @@ def run_gb300(args, cpu=True):
         },
         "clocks": clocks.summary(),
     }
+    if not args.no_plain:
+        line["plain_gpu_path"] = plain_comparison(w, args, flush)
     if args.culler:
         line["learned_culler"] = culler_comparison(w, args, flush)
     if cpu and not args.no_cpu_baseline:
@@ -380,6 +389,48 @@ def run_gb300(args, cpu=True):
     if ctrl0[0] or ctrl[0]:
         line["solver_flags"] = int(ctrl[0])
     return line
+
+
+def plain_comparison(w, args, flush):
+    """The plain GPU path against each acceleration, from one start state.
+
+    ``plain`` runs the reference's own conservative filters every step (no
+    distance-bound grid, no stored filter results); ``grid`` adds the
+    certified distance-bound grid; ``stored_filters`` adds only the stored
+    node-filter results; ``accelerated`` is the headline configuration (both).
+    Every engine runs the same warm-up and timed steps (L2 flushed before
+    each); contacts and forces must be bit-identical to ``plain``.
+    """
+    import torch
+
+    from sand_atlas_dem_gb300.engine import Engine
+
+    rate = w.rate()
+    configs = {"plain": dict(distance_grid=False, filter_margin=0.0),
+               "grid": dict(distance_grid=True, filter_margin=0.0),
+               "stored_filters": dict(distance_grid=False),
+               "accelerated": dict()}
+    steps = min(args.steps, 50)
+    out, states = {}, {}
+    for name, settings in configs.items():
+        e = w.engine(Engine, **settings)
+        e.advance(max(3, args.warmup), rate=rate)
+        set_rates(e, w)
+        ms = timed_steps(e, steps, flush)
+        phases = e.profile_phases()
+        states[name] = e.state()
+        out[name] = dict(value=w.grains * steps / (sum(ms) / 1e3), ms_per_step=sum(ms) / steps,
+                         collector_ms=phases["pair_cull"] + phases["node_filter"] + phases["node_query"],
+                         filter_margin=e.filter_margin, distance_grid=e.distance_grid)
+        del e
+        torch.cuda.empty_cache()
+    base = states["plain"]
+    for name in configs:
+        out[name]["bitwise_equal_to_plain"] = all(
+            v.tobytes() == states[name][k].tobytes() for k, v in base.items() if isinstance(v, np.ndarray))
+    result = dict(steps=steps, **out)
+    result["speedup_over_plain"] = {k: out[k]["value"] / out["plain"]["value"] for k in configs if k != "plain"}
+    return result
 
 
 def culler_comparison(w, args, flush):
@@ -502,6 +553,7 @@ def main():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--prepare-only", action="store_true")
     p.add_argument("--culler", action="store_true", help="also train the learned culler and compare")
+    p.add_argument("--no-plain", action="store_true", help="skip the plain-path comparison")
     args = p.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

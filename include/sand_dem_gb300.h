@@ -11,7 +11,7 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 121) this backend's extension buffers, in the order of
+ *   [77, 124) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
@@ -31,7 +31,9 @@
  *             triangle BVH as one record per node with both children's
  *             bounds, and per shape a 48^3 grid of certified lower bounds of
  *             the signed distance with its origin and cell size, and the
- *             triangle nearest to each cell centre).
+ *             triangle nearest to each cell centre, and the pose the stored
+ *             node-filter results were built at: each grain's orientation,
+ *             each pair's branch and the pair list itself).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
@@ -45,8 +47,12 @@
  * contact emit/law CTAs per SM, gather warps per SM and exact-query CTAs per
  * SM (launch shapes never change results), the survivor capacity (nodes
  * left for the exact query per step; overflow raises the contact-capacity
- * flag), and whether nodes the distance-bound grid certifies outside their
- * target skip the exact query.
+ * flag), whether nodes the distance-bound grid certifies outside their
+ * target skip the exact query, and the filter margin: the reach, in the
+ * target shape's unscaled frame, by which the leaf cull and node filter grow
+ * their tests when they store their results; the results are reused while
+ * no grain has moved that far relative to a partner (0 = run the filters
+ * every step; contacts are identical either way).
  *
  * Return codes: 0 success; 1 argument error; 2 CUDA error.  The message of
  * the last error on the calling thread is sdg_last_error().  Solver failures
@@ -63,8 +69,8 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 121
-#define SDG_VALUE_COUNT 38
+#define SDG_BUFFER_COUNT 124
+#define SDG_VALUE_COUNT 39
 #define SDG_PHASES 9
 
 /* ABI revision of this header. */

@@ -53,6 +53,11 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
     c.contactBlocksPerSM = uint32_t(v[33]); c.gatherWarps = uint32_t(v[34]); c.walkBlocksPerSM = uint32_t(v[35]);
     c.survivorCapacity = uint32_t(v[36]);
     c.distanceGridEnabled = uint32_t(v[37]);
+    c.filterMargin = float(v[38]);
+    if (!(c.filterMargin >= 0.0f) || c.filterMargin > 1.0f) {
+        g_error = "filter margin must lie in [0, 1] (target shape frame)";
+        return 1;
+    }
     if (c.queryBlocksPerSM > 32 || c.cullBlocksPerSM > 32 || c.contactBlocksPerSM > 32 || c.gatherWarps > 64 ||
         c.walkBlocksPerSM > 32 ||
         (c.queryWarps != 0 && c.queryWarps != 4 && c.queryWarps != 8)) {
@@ -78,7 +83,8 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
             bytes[77 + 37] < (uint64_t(c.survivorCapacity) + 1) * 4 || bytes[77 + 38] < uint64_t(c.survivorCapacity) * 4 ||
             bytes[77 + 39] < uint64_t(4) * c.pairCapacity * 16 ||
             bytes[77 + 41] < uint64_t(c.shapes) * GRID * GRID * GRID * 4 || bytes[77 + 42] < uint64_t(c.shapes) * 16 ||
-            bytes[77 + 43] < uint64_t(c.shapes) * GRID * GRID * GRID * 4) {
+            bytes[77 + 43] < uint64_t(c.shapes) * GRID * GRID * GRID * 4 || bytes[77 + 44] < uint64_t(c.N) * 16 ||
+            bytes[77 + 45] < uint64_t(c.pairCapacity) * 16 || bytes[77 + 46] < uint64_t(c.pairCapacity) * 8) {
             g_error = "a buffer is smaller than its configured capacity";
             return 1;
         }

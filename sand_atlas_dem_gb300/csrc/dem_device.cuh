@@ -47,6 +47,11 @@ struct Config {
     uint32_t walkBlocksPerSM;    // exact-query CTAs (256 threads, one node each) per SM
     uint32_t survivorCapacity;   // nodes that pass the conservative filters, per step
     uint32_t distanceGridEnabled;  // skip nodes the distance-bound grid certifies outside
+    // Reach of the cached filter results, in the target shape's unscaled
+    // frame: the leaf cull and node filter run with their tests grown by this
+    // distance and their survivors are reused while no node has moved that far
+    // relative to its partner (0 = run the filters every step).
+    float filterMargin;
 };
 
 // Buffers: the reference Resources block (solver.slang:20-100) in declaration
@@ -118,18 +123,27 @@ struct Res {
     float* distanceGrid;              // shapes x GRID^3: certified lower bound of the signed distance per cell
     float4* distanceGridInfo;         // shapes: grid origin xyz, cell size
     uint32_t* distanceGridTriangle;   // shapes x GRID^3: triangle nearest to each cell centre
+    float4* filterRefRotation;        // N: orientation when the filter results were built
+    float4* filterRefBranch;          // pairCapacity: first-to-second branch when they were built
+    uint2* filterRefPairs;            // pairCapacity: the pair list they were built on
 };
-constexpr int EXTENSION_COUNT = 44;
+constexpr int EXTENSION_COUNT = 47;
 constexpr uint32_t GRID = 48;  // cells per axis of each shape's distance-bound grid
 constexpr int CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4;
 constexpr int BUFFER_COUNT = RESOURCE_COUNT + EXTENSION_COUNT;
 constexpr int CONFIG_VALUES = 25;
-constexpr int VALUE_COUNT = CONFIG_VALUES + 13;
+constexpr int VALUE_COUNT = CONFIG_VALUES + 14;
 constexpr int SCAN_BLOCKS = 608;  // 4 per SM on a 152-SM GB300
 // work[] slots
 constexpr int W_CANDIDATES = 0;
 constexpr int W_SURVIVORS = 2;
 constexpr int W_KEPT = 3;
+constexpr int W_FILTER = 5;         // 1 = build the filter results this step, 0 = reuse them
+constexpr int W_FILTER_VALID = 6;   // 1 = the stored filter results are complete
+constexpr int W_FILTER_PAIRS = 7;   // pair count they were built on
+constexpr int W_FILTER_MARGIN = 8;  // margin they were built with (float bits)
+constexpr int W_FILTER_BUILDS = 9;  // steps that built them (counter)
+constexpr int W_FILTER_STEPS = 10;  // steps that ran the collector (counter)
 
 struct Params {
     Config c;
@@ -366,11 +380,19 @@ __device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 
     f3 normal = surfaceNormal ? pseudo : (distance > 1e-12f ? (side * off) / distance : pseudo);
     return w4(normal, __fmul_rn(side, distance));
 }
-// solver.slang:259-272
-__device__ __forceinline__ bool meshMayContain(const Res& r, uint32_t shape, f3 p) {
+// solver.slang:259-272.  With `grow` > 0 the root box and every hull plane
+// are moved out by that distance (unit normals): the test then admits every
+// point within `grow` of one it admits unmoved.
+__device__ __forceinline__ bool meshMayContain(const Res& r, uint32_t shape, f3 p, float grow = 0.0f) {
     uint32_t root = __ldg(&r.meshRoots[shape].x);
     f3 low = xyz(__ldg(&r.meshMin[root])), high = xyz(__ldg(&r.meshMax[root]));
-    if (p.x < low.x || p.y < low.y || p.z < low.z || p.x > high.x || p.y > high.y || p.z > high.z) return false;
+    if (grow > 0.0f) {
+        if (__fadd_rn(p.x, grow) < low.x || __fadd_rn(p.y, grow) < low.y || __fadd_rn(p.z, grow) < low.z ||
+            __fsub_rn(p.x, grow) > high.x || __fsub_rn(p.y, grow) > high.y || __fsub_rn(p.z, grow) > high.z)
+            return false;
+    } else if (p.x < low.x || p.y < low.y || p.z < low.z || p.x > high.x || p.y > high.y || p.z > high.z) {
+        return false;
+    }
     f3 direction = (p - 0.5f * (low + high)) / (high - low);
     f3 a = abs3(direction);
     uint32_t axis = a.x >= a.y && a.x >= a.z ? 0 : (a.y >= a.z ? 1 : 2);
@@ -378,7 +400,7 @@ __device__ __forceinline__ bool meshMayContain(const Res& r, uint32_t shape, f3 
     uint4 info = __ldg(&r.meshHullInfo[6 * shape + group]);
     for (uint32_t i = 0; i < info.y; ++i) {
         float4 plane = __ldg(&r.meshPlanes[info.x + i]);
-        if (__fadd_rn(dot(xyz(plane), p), plane.w) > 0) return false;
+        if (__fadd_rn(dot(xyz(plane), p), plane.w) > grow) return false;
     }
     return true;
 }
@@ -415,7 +437,10 @@ __device__ __forceinline__ bool meshBoxGroup(const Res& r, uint32_t shape, f3 lo
     return true;
 }
 // solver.slang:290-305, with the directed-pair branch supplied.
-__device__ __forceinline__ bool meshClusterMayContact(const Res& r, uint32_t src, uint32_t dst, uint32_t cluster, f3 branch) {
+// With `margin`, the box is grown by that distance (the test then holds for
+// every placement within `margin` of this one).
+__device__ __forceinline__ bool meshClusterMayContact(const Res& r, uint32_t src, uint32_t dst, uint32_t cluster, f3 branch,
+                                                      float margin = 0.0f) {
     f3 sl = xyz(r.meshClusterMin[cluster]), sh = xyz(r.meshClusterMax[cluster]);
     f3 low = mk(1e30f, 1e30f, 1e30f), high = mk(-1e30f, -1e30f, -1e30f);
     float4 qs = r.rotation[src], qd = r.rotation[dst];
@@ -429,12 +454,15 @@ __device__ __forceinline__ bool meshClusterMayContact(const Res& r, uint32_t src
     float pad = __fmul_rn(0.00000762939453125f,
         __fadd_rn(__fadd_rn(__fadd_rn(1.0f, mx(mx(fabsf(low.x), fabsf(low.y)), fabsf(low.z))),
                             mx(mx(fabsf(high.x), fabsf(high.y)), fabsf(high.z))), __fdiv_rn(length(branch), sd)));
+    if (margin > 0.0f) pad = __fadd_rn(pad, margin);
     low = low - mk(pad, pad, pad);
     high = high + mk(pad, pad, pad);
     return meshBoxMayContact(r, r.shapeId[dst], low, high);
 }
 // solver.slang:404-417
-__device__ __forceinline__ void meshPairBounds(const Res& r, uint32_t direction, uint32_t cluster, f3& low, f3& high) {
+// With `margin`, the bounds are grown by that distance.
+__device__ __forceinline__ void meshPairBounds(const Res& r, uint32_t direction, uint32_t cluster, f3& low, f3& high,
+                                               float margin = 0.0f) {
     f3 cmin = xyz(__ldg(&r.meshClusterMin[cluster])), cmax = xyz(__ldg(&r.meshClusterMax[cluster]));
     f3 center = 0.5f * (cmin + cmax);
     f3 half = 0.5f * (cmax - cmin);
@@ -450,6 +478,7 @@ __device__ __forceinline__ void meshPairBounds(const Res& r, uint32_t direction,
     float pad = __fmul_rn(0.000030517578125f,
         __fadd_rn(__fadd_rn(__fadd_rn(1.0f, mx(mx(fabsf(low.x), fabsf(low.y)), fabsf(low.z))),
                             mx(mx(fabsf(high.x), fabsf(high.y)), fabsf(high.z))), r.meshPairTransform[4 * direction + 3].x));
+    if (margin > 0.0f) pad = __fadd_rn(pad, margin);
     low = low - mk(pad, pad, pad);
     high = high + mk(pad, pad, pad);
 }
@@ -459,20 +488,26 @@ __device__ __forceinline__ void meshPairBounds(const Res& r, uint32_t direction,
 // target's frame and applies, with `plane`, the reference CPU backend's
 // per-directed-pair enclosure-plane prefilter (cpu.py:56-76), then the hull
 // cull; nodeExact is the exact distance query and the contact record.  Both
-// rejections are conservative and change no contact.
+// rejections are conservative and change no contact.  `grow` > 0 widens both
+// tests by that distance (for the stored filter results).
+__device__ __forceinline__ bool nodeTests(const Res& r, uint32_t targetShape, const float4* plane, f3 local,
+                                          float grow = 0.0f) {
+    if (plane) {
+        float pad = __fmul_rn(0.00000762939453125f,
+                              __fadd_rn(1.0f, mx(mx(fabsf(local.x), fabsf(local.y)), fabsf(local.z))));
+        if (grow > 0.0f) pad = __fadd_rn(pad, grow);
+        if (__fadd_rn(dot(xyz(*plane), local), plane->w) > pad) return false;
+    }
+    return meshMayContain(r, targetShape, local, grow);
+}
 __device__ __forceinline__ bool nodePrefilter(const Res& r, uint32_t src, uint32_t dst, uint32_t node, f3 branch,
-                                              const float4* plane, f3& arm, f3& local) {
+                                              const float4* plane, f3& arm, f3& local, float grow = 0.0f) {
     uint32_t sid = r.shapeId[src];
     float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[sid].x) + node]);
     float4 qs = r.rotation[src], qd = r.rotation[dst];
     arm = qrot(qs, xyz(sp) * r.body[src].x);
     local = qinv(qd, arm - branch) / r.body[dst].x;
-    if (plane) {
-        float pad = __fmul_rn(0.00000762939453125f,
-                              __fadd_rn(1.0f, mx(mx(fabsf(local.x), fabsf(local.y)), fabsf(local.z))));
-        if (__fadd_rn(dot(xyz(*plane), local), plane->w) > pad) return false;
-    }
-    return meshMayContain(r, r.shapeId[dst], local);
+    return nodeTests(r, r.shapeId[dst], plane, local, grow);
 }
 __device__ __forceinline__ bool nodeExact(const Res& r, const Config& c, uint32_t src, uint32_t dst, uint32_t node,
                                           f3 arm, f3 local, float4& pd, float4& na, uint32_t seed = 0xFFFFFFFFu) {
@@ -534,6 +569,10 @@ __device__ __forceinline__ uint32_t gridSeed(const Res& r, uint32_t shape, f3 lo
 }
 
 // ---------------------------------------------------------------- helpers
+// Whether the exact-query list itself is stored with the filter results
+// (built with grown tests, re-checked exactly before each walk).  Not with
+// the learned culler, whose calibrated decision is taken every step.
+__device__ __forceinline__ bool storedKeep(const Config& c) { return c.filterMargin > 0.0f && c.cullerEnabled == 0; }
 __device__ __forceinline__ uint32_t activePairs(const Res& r, const Config& c) {
     uint32_t n = r.control[1];
     return n < c.pairCapacity ? n : c.pairCapacity;

@@ -304,19 +304,71 @@ __global__ void k_byJSort(const __grid_constant__ Params P) {
 // Per pair: FP64 branches of both directions, root cull mask and 3x4
 // source-to-target transforms (prepareMeshPairs, solver.slang:468-489), and
 // the pair table of the history side being written.
+// Upper bound of |R(a) v - R(b) v| / |v| for the rotations of quaternions a
+// and b: with 2 alpha the angle between them (or between a and -b), the chord
+// 2 sin(2 alpha / 2) <= 4 sin(alpha / 2) = 2 |a -/+ b|.
+__device__ __forceinline__ float rotationChord(float4 a, float4 b) {
+    float4 d = make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+    float4 s = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+    float dd = d.x * d.x + d.y * d.y + d.z * d.z + d.w * d.w;
+    float ss = s.x * s.x + s.y * s.y + s.z * s.z + s.w * s.w;
+    return 2.0f * sqrtf(fminf(dd, ss));
+}
+// Whether the filter results stored for pair p no longer cover it.  They were
+// built with every test grown by `margin` (target frame, unscaled).  A node x
+// of grain i lies at local = R_j^T (R_i s_i x - b) / s_j in grain j's frame;
+// between the build (0) and now (1), for any node that can touch j now
+// (|R_i s_i x - b| <= r_j, the bounding radius),
+//   s_j |local1 - local0| <= chord_i r_i + |b1 - b0| + chord_j r_j,
+// and symmetrically for the other direction.  While that stays below
+// margin x min(s_i, s_j), every node that passes the tests now passed the
+// grown tests then, so the stored survivors contain every node the filters
+// would keep now.  The factor 1.001 and the 1e-5 term cover the FP32
+// rounding of the bound and of quaternions that are not exactly unit.
+__device__ __forceinline__ bool filterStale(const Res& r, float margin, uint32_t p, uint2 ij, f3 branch) {
+    uint2 ref = r.filterRefPairs[p];
+    if (ref.x != ij.x || ref.y != ij.y) return true;
+    float4 bi = r.body[ij.x], bj = r.body[ij.y];
+    float drift = rotationChord(r.rotation[ij.x], r.filterRefRotation[ij.x]) * bi.z +
+                  length(branch - xyz(r.filterRefBranch[p])) +
+                  rotationChord(r.rotation[ij.y], r.filterRefRotation[ij.y]) * bj.z;
+    float slack = 1e-5f * (1.0f + bi.z + bj.z + length(branch));
+    return 1.001f * drift + slack > margin * fminf(bi.x, bj.x);
+}
 __global__ void k_pairSetup(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
     if (r.control[0] != 0) return;
     uint32_t n = activePairs(r, c);
+    float margin = c.filterMargin > 0.0f ? c.filterMargin : 0.0f;
+    bool check = r.work[W_FILTER] == 0;
     for (uint32_t p = gtid(); p < n; p += gstride()) {
         uint2 ij = r.pairs[p];
         f3 branch[2] = {centerBranch64(r, c, ij.x, ij.y), centerBranch64(r, c, ij.y, ij.x)};
         r.dpairBranch[2 * p] = w4(branch[0], 0.f);
         r.dpairBranch[2 * p + 1] = w4(branch[1], 0.f);
+        if (check && filterStale(r, margin, p, ij, branch[0])) atomicOr(&r.work[W_FILTER], 1u);
+        r.sidePairB[p] = ij.y;
+    }
+    uint32_t grains = c.N;
+    for (uint32_t g = gtid(); g <= grains; g += gstride())
+        r.sidePairOffsets[g] = g < grains ? min(r.pairOffsets[g], n) : n;
+}
+// Root cull masks and source-to-target transforms of every directed pair
+// (prepareMeshPairs, solver.slang:468-489), on steps that build the filter
+// results, with the tests grown by the margin.
+__global__ void k_pairMasks(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0 || r.work[W_FILTER] == 0) return;
+    uint32_t n = activePairs(r, c);
+    float margin = c.filterMargin > 0.0f ? c.filterMargin : 0.0f;
+    for (uint32_t p = gtid(); p < n; p += gstride()) {
+        uint2 ij = r.pairs[p];
+        f3 branch[2] = {xyz(r.dpairBranch[2 * p]), xyz(r.dpairBranch[2 * p + 1])};
         uint32_t mask = 0;
-        if (meshClusterMayContact(r, ij.x, ij.y, r.meshClusterInfo[r.shapeId[ij.x]].x, branch[0])) mask |= 1;
-        if (meshClusterMayContact(r, ij.y, ij.x, r.meshClusterInfo[r.shapeId[ij.y]].x, branch[1])) mask |= 2;
+        if (meshClusterMayContact(r, ij.x, ij.y, r.meshClusterInfo[r.shapeId[ij.x]].x, branch[0], margin)) mask |= 1;
+        if (meshClusterMayContact(r, ij.y, ij.x, r.meshClusterInfo[r.shapeId[ij.y]].x, branch[1], margin)) mask |= 2;
         for (uint32_t pass = 0; pass < 2; ++pass) {
             if ((mask & (1u << pass)) == 0) continue;
             uint32_t i = pass == 0 ? ij.x : ij.y, j = pass == 0 ? ij.y : ij.x;
@@ -334,19 +386,24 @@ __global__ void k_pairSetup(const __grid_constant__ Params P) {
             r.meshPairTransform[base + 3] = make_float4(__fdiv_rn(length(branch[pass]), sj), 0.f, 0.f, 0.f);
         }
         r.meshPairMask[p] = mask;
-        r.sidePairB[p] = ij.y;
     }
-    uint32_t grains = c.N;
-    for (uint32_t g = gtid(); g <= grains; g += gstride())
-        r.sidePairOffsets[g] = g < grains ? min(r.pairOffsets[g], n) : n;
 }
 // resetMeshContacts (solver.slang:396-403)
+// The stored filter results (items, survivor masks and list) serve this step
+// if they are complete and were built with this margin on a pair list of
+// the same length; k_pairSetup then checks each pair and how far its grains
+// have moved, and asks for a build if any pair is no longer covered.
 __global__ void k_resetContacts(const __grid_constant__ Params P) {
     const Res& r = P.r;
+    const Config& c = P.c;
     if (r.control[0] != 0) return;
     r.control[2] = 0;
     r.control[6] = 0;
-    r.work[W_CANDIDATES] = 0;
+    bool build = !(c.filterMargin > 0.0f) || r.work[W_FILTER_VALID] == 0 || r.work[W_FILTER_PAIRS] != r.control[1] ||
+                 r.work[W_FILTER_MARGIN] != __float_as_uint(c.filterMargin);
+    r.work[W_FILTER] = build ? 1u : 0u;
+    r.work[W_FILTER_STEPS] += 1u;
+    if (build) r.work[W_CANDIDATES] = 0;
 }
 // Flat leaf cull: one warp per directed pair; meshPairBounds (solver.slang:
 // 404-417) + meshBoxMayContact (:274-288) on every leaf, gated by the root
@@ -385,54 +442,80 @@ __device__ __forceinline__ float sourcePlaneBound(const SourcePlane& sp, float e
                                             __fmul_rn(sp.scale.w, extent)));
     return __fadd_rn(pad, slack);
 }
-__device__ __forceinline__ bool nodeBeyondSourcePlane(const SourcePlane& sp, f3 x) {
+// `grow` widens a test for the stored filter results: the plane value moves
+// by at most |n| = 1 times a node's displacement in the target frame, so
+// `grow` = margin x 1.001 (FP32 unit normals) covers every placement within
+// the margin.
+__device__ __forceinline__ bool nodeBeyondSourcePlane(const SourcePlane& sp, f3 x, float grow = 0.0f) {
     float extent = __fadd_rn(__fadd_rn(fabsf(x.x), fabsf(x.y)), fabsf(x.z));
-    return __fadd_rn(dot(xyz(sp.plane), x), sp.plane.w) > sourcePlaneBound(sp, extent);
+    return __fadd_rn(dot(xyz(sp.plane), x), sp.plane.w) > __fadd_rn(sourcePlaneBound(sp, extent), grow);
 }
-__device__ __forceinline__ bool leafBeyondSourcePlane(const SourcePlane& sp, f3 low, f3 high) {
+__device__ __forceinline__ bool leafBeyondSourcePlane(const SourcePlane& sp, f3 low, f3 high, float grow = 0.0f) {
     f3 c = 0.5f * (low + high), h = 0.5f * (high - low);
     float nearest = __fsub_rn(__fadd_rn(dot(xyz(sp.plane), c), sp.plane.w), dot(abs3(xyz(sp.plane)), h));
     float extent = __fadd_rn(__fadd_rn(__fadd_rn(fabsf(c.x), fabsf(c.y)), fabsf(c.z)),
                              __fadd_rn(__fadd_rn(h.x, h.y), h.z));
-    return nearest > sourcePlaneBound(sp, extent);
+    return nearest > __fadd_rn(sourcePlaneBound(sp, extent), grow);
 }
+// Enclosure plane of the target most violated by the source centre
+// (cpu_scheduling.slang:58-71): warp arg-max, lowest index on ties.  Every
+// lane returns the plane.
+__device__ __forceinline__ float4 enclosurePlane(const Res& r, uint32_t j, uint32_t targetShape, f3 branch) {
+    f3 centre = (-qinv(r.rotation[j], branch)) / r.body[j].x;
+    uint4 first = __ldg(&r.meshHullInfo[6 * targetShape]);
+    uint4 last = __ldg(&r.meshHullInfo[6 * targetShape + 5]);
+    uint32_t begin = first.x, end = last.x + last.y;
+    float best = -1e30f;
+    uint32_t bestIndex = EMPTY;
+    for (uint32_t k = begin + laneId(); k < end; k += WARP) {
+        float4 candidate = __ldg(&r.meshPlanes[k]);
+        float violation = __fadd_rn(dot(xyz(candidate), centre), candidate.w);
+        if (violation > best) { best = violation; bestIndex = k; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        uint32_t oi = __shfl_xor_sync(0xffffffffu, bestIndex, o);
+        if (ob > best || (ob == best && oi < bestIndex)) { best = ob; bestIndex = oi; }
+    }
+    return bestIndex == EMPTY ? make_float4(0.f, 0.f, 0.f, 0.f) : __ldg(&r.meshPlanes[bestIndex]);
+}
+// Runs on steps that build the filter results: with a margin every test is
+// grown by it and the pose the results are built at is recorded.
 __global__ void k_leafCull(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
+    if (r.work[W_FILTER] == 0) return;
     uint32_t n = 2 * activePairs(r, c);
     bool live = r.control[0] == 0;
+    float margin = c.filterMargin > 0.0f ? c.filterMargin : 0.0f;
+    float grow = __fmul_rn(1.001f, margin);
+    if (margin > 0.0f) {
+        for (uint32_t g = gtid(); g < c.N; g += gstride()) r.filterRefRotation[g] = r.rotation[g];
+        if (gtid() == 0) {
+            r.work[W_FILTER_VALID] = 0;
+            r.work[W_FILTER_PAIRS] = r.control[1];
+            r.work[W_FILTER_MARGIN] = __float_as_uint(margin);
+            r.work[W_FILTER_BUILDS] += 1u;
+        }
+    }
     for (uint32_t d = warpGlobal(); d < n; d += warpStride()) {
         uint32_t p = d >> 1, pass = d & 1;
         uint2 ij = r.pairs[p];
         uint32_t i = pass ? ij.y : ij.x, j = pass ? ij.x : ij.y;
+        if (margin > 0.0f && pass == 0 && laneId() == 0) {
+            r.filterRefPairs[p] = ij;
+            r.filterRefBranch[p] = r.dpairBranch[d];
+        }
         uint32_t count = 0;
         if (live && ((r.meshPairMask[p] >> pass) & 1u)) {
             uint4 li = __ldg(&r.meshLeafInfo[r.shapeId[i]]);
             uint32_t targetShape = r.shapeId[j];
             float4 plane;
             SourcePlane source;
-            // Enclosure plane of the target most violated by the source centre
-            // (cpu_scheduling.slang:58-71): warp arg-max, lowest index on ties.
             {
                 f3 branch = xyz(r.dpairBranch[d]);
-                f3 centre = (-qinv(r.rotation[j], branch)) / r.body[j].x;
-                uint4 first = __ldg(&r.meshHullInfo[6 * targetShape]);
-                uint4 last = __ldg(&r.meshHullInfo[6 * targetShape + 5]);
-                uint32_t begin = first.x, end = last.x + last.y;
-                float best = -1e30f;
-                uint32_t bestIndex = EMPTY;
-                for (uint32_t k = begin + laneId(); k < end; k += WARP) {
-                    float4 candidate = __ldg(&r.meshPlanes[k]);
-                    float violation = __fadd_rn(dot(xyz(candidate), centre), candidate.w);
-                    if (violation > best) { best = violation; bestIndex = k; }
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    float ob = __shfl_xor_sync(0xffffffffu, best, o);
-                    uint32_t oi = __shfl_xor_sync(0xffffffffu, bestIndex, o);
-                    if (ob > best || (ob == best && oi < bestIndex)) { best = ob; bestIndex = oi; }
-                }
-                plane = bestIndex == EMPTY ? make_float4(0.f, 0.f, 0.f, 0.f) : __ldg(&r.meshPlanes[bestIndex]);
+                plane = enclosurePlane(r, j, targetShape, branch);
                 source = sourcePlane(plane, r.rotation[i], r.rotation[j], r.body[i].x, r.body[j].x, branch);
                 if (laneId() == 0) {
                     r.dpairPlane[d] = plane;
@@ -452,10 +535,10 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
                 if (k < li.y) {
                     uint32_t leaf = __ldg(&r.meshLeaves[li.x + k]);
                     f3 low, high;
-                    meshPairBounds(r, d, leaf, low, high);
+                    meshPairBounds(r, d, leaf, low, high, margin);
                     open = meshBoxGroup(r, targetShape, low, high, centre, half, group) &&
                            !leafBeyondSourcePlane(source, xyz(__ldg(&r.meshClusterMin[leaf])),
-                                                  xyz(__ldg(&r.meshClusterMax[leaf])));
+                                                  xyz(__ldg(&r.meshClusterMax[leaf])), grow);
                 }
                 uint32_t pending = __ballot_sync(0xffffffffu, open), m = 0;
                 while (pending) {
@@ -483,7 +566,7 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
 __global__ void k_leafEmit(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
-    if (r.control[0] != 0) return;
+    if (r.control[0] != 0 || r.work[W_FILTER] == 0) return;
     uint32_t n = 2 * activePairs(r, c);
     for (uint32_t d = warpGlobal(); d < n; d += warpStride()) {
         if (r.dpairLeafCount[d] == 0) continue;
@@ -521,6 +604,16 @@ __global__ void __launch_bounds__(256) k_nodeFilter(const __grid_constant__ Para
     const Res& r = P.r;
     const Config& c = P.c;
     uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
+    if (r.work[W_FILTER] == 0) {
+        // Stored survivors serve this step: only the hit masks start afresh.
+        if (r.control[0] != 0) return;
+        for (uint32_t item = gtid(); item < n; item += gstride()) {
+            r.candHitMask[item] = make_uint2(0u, 0u);
+            r.candHitCount[item] = 0;
+        }
+        return;
+    }
+    float grow = c.filterMargin > 0.0f ? __fmul_rn(1.001f, c.filterMargin) : 0.0f;
     // Two items per warp, one per half-warp, four node slots per lane
     // (slot = lane in half + 16 j): twice the loads in flight per instruction.
     uint32_t half = laneId() >> 4, hl = laneId() & 15u;
@@ -546,7 +639,7 @@ __global__ void __launch_bounds__(256) k_nodeFilter(const __grid_constant__ Para
             }
 #pragma unroll
             for (uint32_t j = 0; j < 4; ++j)
-                keep[j] = hl + 16 * j < range.y && !nodeBeyondSourcePlane(source, xyz(x[j]));
+                keep[j] = hl + 16 * j < range.y && !nodeBeyondSourcePlane(source, xyz(x[j]), grow);
         }
         uint32_t b[4];
 #pragma unroll
@@ -587,10 +680,16 @@ __device__ __forceinline__ SurvivorNode survivorNode(const Res& r, uint32_t s) {
 // Exact placement, target-frame enclosure plane and hull of every survivor
 // of the one-dot test (nodePrefilter, one thread each): survKeep[s] = 1 for
 // the nodes that go on to the exact query.
+// When the exact-query list is stored with the filter results, this pass
+// runs only on build steps, with the plane, hull and grid tests grown by the
+// margin (a node the grid bounds farther than the margin from the surface
+// cannot reach it while the results serve).
 __global__ void __launch_bounds__(256) k_survivorPrefilter(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
-    if (r.control[0] != 0) return;
+    bool stored = storedKeep(c);
+    if (r.control[0] != 0 || (stored && r.work[W_FILTER] == 0)) return;
+    float grow = stored ? __fmul_rn(1.001f, c.filterMargin) : 0.0f;
     uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
     for (uint32_t s = gtid(); s < n; s += gstride()) {
         uint2 sv = r.survivors[s];
@@ -601,10 +700,10 @@ __global__ void __launch_bounds__(256) k_survivorPrefilter(const __grid_constant
         uint32_t node = __ldg(&r.meshSampleIndices[__ldg(&r.meshClusterRanges[cd.y]).x + sv.y]);
         float4 plane = r.dpairPlane[d];
         f3 arm, local;
-        bool keep = nodePrefilter(r, src, dst, node, xyz(r.dpairBranch[d]), &plane, arm, local);
+        bool keep = nodePrefilter(r, src, dst, node, xyz(r.dpairBranch[d]), &plane, arm, local, grow);
         // A node certified outside the target by the distance-bound grid
         // cannot be a contact (the exact query would find phi > 0).
-        if (keep && c.distanceGridEnabled && distanceBound(r, r.shapeId[dst], local) > 0.0f) keep = false;
+        if (keep && c.distanceGridEnabled && distanceBound(r, r.shapeId[dst], local) > grow) keep = false;
         r.survKeep[s] = keep ? 1u : 0u;
     }
 }
@@ -683,17 +782,21 @@ __global__ void __launch_bounds__(256) k_cullSurvivors(const __grid_constant__ P
 __global__ void k_walkList(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
-    if (r.control[0] != 0) return;
+    if (r.control[0] != 0 || (storedKeep(c) && r.work[W_FILTER] == 0)) return;
     uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
     for (uint32_t s = gtid(); s < n; s += gstride())
         if (r.survKeep[s]) r.walkList[r.keepOffset[s]] = s;
 }
 // Survivor list in canonical (item, node slot) order.
+// On a build step with a margin, it also marks the stored results complete
+// when no list overflowed.
 __global__ void k_survivorList(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
-    if (r.control[0] != 0) return;
+    if (r.control[0] != 0 || r.work[W_FILTER] == 0) return;
     uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
+    if (gtid() == 0 && c.filterMargin > 0.0f)
+        r.work[W_FILTER_VALID] = r.work[W_CANDIDATES] <= c.candidateCapacity && r.work[W_SURVIVORS] <= c.survivorCapacity;
     for (uint32_t item = warpGlobal(); item < n; item += warpStride()) {
         uint2 m = r.candSurvMask[item];
         if ((m.x | m.y) == 0) continue;
@@ -1097,9 +1200,10 @@ static void collectCull(const Params& P, cudaStream_t s) {
     k_resetContacts<<<1, 1, 0, s>>>(P);
     uint32_t g = grid(c.cullBlocksPerSM, 8);
     k_pairSetup<<<g, T, 0, s>>>(P);
+    k_pairMasks<<<g, T, 0, s>>>(P);
     k_leafCull<<<g, T, 0, s>>>(P);
     launch_scan(r.dpairLeafCount, r.dpairCandOffset, ScanCount{r.control + 1, c.pairCapacity, 2, 0}, true,
-                r.work + W_CANDIDATES, nullptr, r.scanPartials, s);
+                r.work + W_CANDIDATES, r.work + W_FILTER, r.scanPartials, s);
     k_leafEmit<<<g, T, 0, s>>>(P);
 }
 // Node filter, survivor list and (with the learned culler) the kept list.
@@ -1109,7 +1213,7 @@ static void collectFilter(const Params& P, cudaStream_t s) {
     uint32_t warps = c.queryWarps == 4 ? 4 : 8;
     k_nodeFilter<<<grid(c.queryBlocksPerSM, 8), 32 * warps, 0, s>>>(P);
     launch_scan(r.candSurvCount, r.candSurvOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0},
-                true, r.work + W_SURVIVORS, nullptr, r.scanPartials, s);
+                true, r.work + W_SURVIVORS, r.work + W_FILTER, r.scanPartials, s);
     k_survivorList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
     k_survivorPrefilter<<<grid(c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
     if (c.cullerEnabled) {
@@ -1125,8 +1229,9 @@ static void collectFilter(const Params& P, cudaStream_t s) {
         }
         k_cullSurvivors<<<grid(c.queryBlocksPerSM, 2), 256, 8 * CULLER_TILE_WORDS * sizeof(uint32_t), s>>>(P);
     }
+    bool stored = c.filterMargin > 0.0f && c.cullerEnabled == 0;
     launch_scan(r.survKeep, r.keepOffset, ScanCount{r.work + W_SURVIVORS, c.survivorCapacity, 1, 0}, true,
-                r.work + W_KEPT, nullptr, r.scanPartials, s);
+                r.work + W_KEPT, stored ? r.work + W_FILTER : nullptr, r.scanPartials, s);
     k_walkList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
 }
 // The exact queries.

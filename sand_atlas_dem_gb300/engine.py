@@ -41,6 +41,7 @@ EXTENSION_ORDER = (
     "hitScratch", "candSurvCount", "dpairPlane", "grainSpecimen", "specimenBins", "cullerParams", "cullerW1",
     "cullerMargin", "cullerStats", "candSurvMask", "candSurvOffset", "survivors", "survKeep", "keepOffset",
     "walkList", "dpairSourcePlane", "meshChildren", "distanceGrid", "distanceGridInfo", "distanceGridTriangle",
+    "filterRefRotation", "filterRefBranch", "filterRefPairs",
 )
 DISTANCE_GRID = 48  # cells per axis of each shape's distance-bound grid (csrc GRID)
 CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4
@@ -52,6 +53,9 @@ SIDE_FIELDS = (
     ("sideContactStart", "oldContactStart"),
 )
 SCAN_BLOCKS = 608
+# Default reach of the stored node-filter results: 0.1% of a unit-median
+# shape's size in its own frame.
+FILTER_MARGIN = 1e-3
 
 
 def _torch():
@@ -176,7 +180,7 @@ class Engine:
         return cls(library, spec, None, None, None, None, layout=layout, **kwargs)
 
     def __init__(self, library, spec, positions, cell, shape_ids, scales, *, metal=None, device=None,
-                 use_graph=True, layout=None, distance_grid=True):
+                 use_graph=True, layout=None, distance_grid=True, filter_margin=FILTER_MARGIN):
         torch = _torch()
         if metal is not None:
             raise ValueError("The GB300 engine owns its device; no adapter may be passed")
@@ -201,6 +205,13 @@ class Engine:
         # target (exact: no contact changes); off reproduces the reference's
         # own filters alone.
         self.distance_grid = bool(distance_grid)
+        # Reach (target shape frame, unscaled) of the stored node-filter
+        # results: the leaf cull and node filter run with their tests grown by
+        # it and are reused while no grain has moved that far relative to a
+        # partner (exact: no contact changes); 0 runs them every step.
+        self.filter_margin = float(filter_margin)
+        if not np.isfinite(self.filter_margin) or self.filter_margin < 0:
+            raise ValueError("Finite nonnegative filter margin required")
         self._reduce_scratch = {}
         self._array_cache = {}
         # Host<->device bytes moved by this engine's own reads and uploads.
@@ -250,6 +261,7 @@ class Engine:
             "distanceGridTriangle": 4 * len(library.shapes) * DISTANCE_GRID**3,
             "cullerParams": 4 * CULLER_PARAMS * len(library.shapes), "cullerW1": 2 * 4096 * len(library.shapes),
             "cullerMargin": 4 * len(library.shapes), "cullerStats": 16,
+            "filterRefRotation": 16 * n, "filterRefBranch": 16 * pc, "filterRefPairs": 8 * pc,
         }
         for name, nbytes in sizes.items():
             self.buffers[name] = DeviceBuffer(self, nbytes)
@@ -317,7 +329,8 @@ class Engine:
             float(self.leaf_words), float(self.candidate_capacity), 0.0, float(self.specimens),
             float(self.culler is not None),
         ] + [float(self.tuning.get(k, 0)) for k in TUNING_KEYS] + [float(self.survivor_capacity),
-                                                                     float(self.distance_grid)]
+                                                                     float(self.distance_grid),
+                                                                     self.filter_margin]
         return (ct.c_double * len(values))(*values), len(values)
 
     def dispatch(self, name, count, config, active=None):
@@ -410,6 +423,7 @@ class Engine:
                     self.library, replace(old, **settings), None, None, None, None,
                     layout=HostLayout.batch(self.library, replace(old, **settings), specimens),
                     device=self.device, use_graph=self.use_graph, distance_grid=self.distance_grid,
+                    filter_margin=self.filter_margin,
                 )
                 replacement.initial_cell = self.initial_cell.copy()
                 replacement.tuning = dict(self.tuning)

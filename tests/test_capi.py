@@ -44,7 +44,7 @@ def test_buffer_and_value_counts(library):
     library.sdg_buffer_count.restype = ct.c_int
     library.sdg_value_count.restype = ct.c_int
     assert library.sdg_buffer_count() == buffers == len(BUFFER_ORDER) == len(RESOURCE_ORDER) + len(EXTENSION_ORDER)
-    assert library.sdg_value_count() == values == len(CONFIG_ORDER) + 5 + len(TUNING_KEYS) + 2
+    assert library.sdg_value_count() == values == len(CONFIG_ORDER) + 5 + len(TUNING_KEYS) + 3
     assert len(RESOURCE_ORDER) == 77
 
 
