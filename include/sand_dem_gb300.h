@@ -11,7 +11,7 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 124) this backend's extension buffers, in the order of
+ *   [77, 127) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
@@ -33,7 +33,10 @@
  *             the signed distance with its origin and cell size, and the
  *             triangle nearest to each cell centre, and the pose the stored
  *             node-filter results were built at: each grain's orientation,
- *             each pair's branch and the pair list itself).
+ *             each pair's branch and the pair list itself, and the walk
+ *             order of the stored exact-query list: each kept survivor's
+ *             bucket (target shape, coarse cell), and the count and first
+ *             slot of each bucket).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
@@ -69,7 +72,7 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 124
+#define SDG_BUFFER_COUNT 127
 #define SDG_VALUE_COUNT 39
 #define SDG_PHASES 9
 

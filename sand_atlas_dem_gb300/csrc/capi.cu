@@ -84,7 +84,10 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
             bytes[77 + 39] < uint64_t(4) * c.pairCapacity * 16 ||
             bytes[77 + 41] < uint64_t(c.shapes) * GRID * GRID * GRID * 4 || bytes[77 + 42] < uint64_t(c.shapes) * 16 ||
             bytes[77 + 43] < uint64_t(c.shapes) * GRID * GRID * GRID * 4 || bytes[77 + 44] < uint64_t(c.N) * 16 ||
-            bytes[77 + 45] < uint64_t(c.pairCapacity) * 16 || bytes[77 + 46] < uint64_t(c.pairCapacity) * 8) {
+            bytes[77 + 45] < uint64_t(c.pairCapacity) * 16 || bytes[77 + 46] < uint64_t(c.pairCapacity) * 8 ||
+            bytes[77 + 47] < uint64_t(c.survivorCapacity) * 4 ||
+            bytes[77 + 48] < (uint64_t(c.shapes) * WALK_BUCKETS + 1) * 4 ||
+            bytes[77 + 49] < (uint64_t(c.shapes) * WALK_BUCKETS + 1) * 4) {
             g_error = "a buffer is smaller than its configured capacity";
             return 1;
         }

@@ -126,8 +126,13 @@ struct Res {
     float4* filterRefRotation;        // N: orientation when the filter results were built
     float4* filterRefBranch;          // pairCapacity: first-to-second branch when they were built
     uint2* filterRefPairs;            // pairCapacity: the pair list they were built on
+    uint32_t* walkKey;                // survivorCapacity: bucket of each kept survivor (target shape, coarse cell)
+    uint32_t* walkBucketCount;        // shapes x WALK_BUCKETS + 1: kept survivors per bucket
+    uint32_t* walkBucketOffset;       // shapes x WALK_BUCKETS + 1: first walk-list slot of each bucket
 };
-constexpr int EXTENSION_COUNT = 47;
+constexpr int EXTENSION_COUNT = 50;
+constexpr uint32_t WALK_CELLS = 8;  // coarse cells per axis of a shape's grid box for the walk order
+constexpr uint32_t WALK_BUCKETS = WALK_CELLS * WALK_CELLS * WALK_CELLS;
 constexpr uint32_t GRID = 48;  // cells per axis of each shape's distance-bound grid
 constexpr int CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4;
 constexpr int BUFFER_COUNT = RESOURCE_COUNT + EXTENSION_COUNT;
@@ -555,6 +560,20 @@ __device__ __forceinline__ uint32_t gridCell(const Res& r, uint32_t shape, f3 lo
         return 0xFFFFFFFFu;
     return (uint32_t(gz) * GRID + uint32_t(gy)) * GRID + uint32_t(gx);
 }
+// Walk-order bucket of a node at `local` against `shape`: the shape, then
+// the coarse cell (WALK_CELLS per axis over the grid box, clamped).  Nodes
+// of one bucket take similar paths through the shape's BVH.
+__device__ __forceinline__ uint32_t walkBucket(const Res& r, uint32_t shape, f3 local) {
+    float4 info = __ldg(&r.distanceGridInfo[shape]);
+    float inv = __fdiv_rn(float(WALK_CELLS), __fmul_rn(info.w, float(GRID)));
+    float g[3] = {__fmul_rn(__fsub_rn(local.x, info.x), inv), __fmul_rn(__fsub_rn(local.y, info.y), inv),
+                  __fmul_rn(__fsub_rn(local.z, info.z), inv)};
+    uint32_t k[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        k[a] = g[a] >= float(WALK_CELLS - 1) ? WALK_CELLS - 1 : (g[a] >= 1.0f ? uint32_t(g[a]) : 0u);
+    return shape * WALK_BUCKETS + (k[2] * WALK_CELLS + k[1]) * WALK_CELLS + k[0];
+}
 __device__ __forceinline__ float distanceBound(const Res& r, uint32_t shape, f3 local) {
     uint32_t cell = gridCell(r, shape, local);
     if (cell == 0xFFFFFFFFu) return -1e30f;
@@ -570,8 +589,8 @@ __device__ __forceinline__ uint32_t gridSeed(const Res& r, uint32_t shape, f3 lo
 
 // ---------------------------------------------------------------- helpers
 // Whether the exact-query list itself is stored with the filter results
-// (built with grown tests, re-checked exactly before each walk).  Not with
-// the learned culler, whose calibrated decision is taken every step.
+// (built with grown tests and ordered by target shape and coarse cell).  Not
+// with the learned culler, whose calibrated decision is taken every step.
 __device__ __forceinline__ bool storedKeep(const Config& c) { return c.filterMargin > 0.0f && c.cullerEnabled == 0; }
 __device__ __forceinline__ uint32_t activePairs(const Res& r, const Config& c) {
     uint32_t n = r.control[1];

@@ -492,6 +492,8 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
     float grow = __fmul_rn(1.001f, margin);
     if (margin > 0.0f) {
         for (uint32_t g = gtid(); g < c.N; g += gstride()) r.filterRefRotation[g] = r.rotation[g];
+        if (storedKeep(c))
+            for (uint32_t b = gtid(); b <= c.shapes * WALK_BUCKETS; b += gstride()) r.walkBucketCount[b] = 0;
         if (gtid() == 0) {
             r.work[W_FILTER_VALID] = 0;
             r.work[W_FILTER_PAIRS] = r.control[1];
@@ -705,6 +707,11 @@ __global__ void __launch_bounds__(256) k_survivorPrefilter(const __grid_constant
         // cannot be a contact (the exact query would find phi > 0).
         if (keep && c.distanceGridEnabled && distanceBound(r, r.shapeId[dst], local) > grow) keep = false;
         r.survKeep[s] = keep ? 1u : 0u;
+        if (keep && stored) {
+            uint32_t bucket = walkBucket(r, r.shapeId[dst], local);
+            r.walkKey[s] = bucket;
+            atomicAdd(&r.walkBucketCount[bucket], 1u);
+        }
     }
 }
 // Distance-bound grid of every shape (built once per library): one thread per
@@ -778,14 +785,27 @@ __global__ void __launch_bounds__(256) k_cullSurvivors(const __grid_constant__ P
         }
     }
 }
-// Survivors kept for the exact query, in order (their survivor indices).
+// Survivors kept for the exact query (their survivor indices): in survivor
+// order, or, when the list is stored with the filter results, grouped by
+// walk bucket (each bucket filled from its end; the order within a bucket
+// is immaterial: every walk is independent and its hit lands in its
+// survivor's slot).
 __global__ void k_walkList(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
-    if (r.control[0] != 0 || (storedKeep(c) && r.work[W_FILTER] == 0)) return;
+    bool stored = storedKeep(c);
+    if (r.control[0] != 0 || (stored && r.work[W_FILTER] == 0)) return;
     uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
-    for (uint32_t s = gtid(); s < n; s += gstride())
-        if (r.survKeep[s]) r.walkList[r.keepOffset[s]] = s;
+    for (uint32_t s = gtid(); s < n; s += gstride()) {
+        if (!r.survKeep[s]) continue;
+        if (stored) {
+            uint32_t bucket = r.walkKey[s];
+            uint32_t slot = r.walkBucketOffset[bucket] + atomicSub(&r.walkBucketCount[bucket], 1u) - 1u;
+            r.walkList[slot] = s;
+        } else {
+            r.walkList[r.keepOffset[s]] = s;
+        }
+    }
 }
 // Survivor list in canonical (item, node slot) order.
 // On a build step with a margin, it also marks the stored results complete
@@ -1229,9 +1249,12 @@ static void collectFilter(const Params& P, cudaStream_t s) {
         }
         k_cullSurvivors<<<grid(c.queryBlocksPerSM, 2), 256, 8 * CULLER_TILE_WORDS * sizeof(uint32_t), s>>>(P);
     }
-    bool stored = c.filterMargin > 0.0f && c.cullerEnabled == 0;
-    launch_scan(r.survKeep, r.keepOffset, ScanCount{r.work + W_SURVIVORS, c.survivorCapacity, 1, 0}, true,
-                r.work + W_KEPT, stored ? r.work + W_FILTER : nullptr, r.scanPartials, s);
+    if (c.filterMargin > 0.0f && c.cullerEnabled == 0)
+        launch_scan(r.walkBucketCount, r.walkBucketOffset, ScanCount{nullptr, 0, 0, c.shapes * WALK_BUCKETS}, true,
+                    r.work + W_KEPT, r.work + W_FILTER, r.scanPartials, s);
+    else
+        launch_scan(r.survKeep, r.keepOffset, ScanCount{r.work + W_SURVIVORS, c.survivorCapacity, 1, 0}, true,
+                    r.work + W_KEPT, nullptr, r.scanPartials, s);
     k_walkList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
 }
 // The exact queries.

@@ -41,9 +41,10 @@ EXTENSION_ORDER = (
     "hitScratch", "candSurvCount", "dpairPlane", "grainSpecimen", "specimenBins", "cullerParams", "cullerW1",
     "cullerMargin", "cullerStats", "candSurvMask", "candSurvOffset", "survivors", "survKeep", "keepOffset",
     "walkList", "dpairSourcePlane", "meshChildren", "distanceGrid", "distanceGridInfo", "distanceGridTriangle",
-    "filterRefRotation", "filterRefBranch", "filterRefPairs",
+    "filterRefRotation", "filterRefBranch", "filterRefPairs", "walkKey", "walkBucketCount", "walkBucketOffset",
 )
 DISTANCE_GRID = 48  # cells per axis of each shape's distance-bound grid (csrc GRID)
+WALK_BUCKETS = 512  # walk-order buckets per shape (csrc WALK_BUCKETS)
 CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4
 BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
 # History side fields: (name bound as the side being written, name bound as committed).
@@ -262,6 +263,8 @@ class Engine:
             "cullerParams": 4 * CULLER_PARAMS * len(library.shapes), "cullerW1": 2 * 4096 * len(library.shapes),
             "cullerMargin": 4 * len(library.shapes), "cullerStats": 16,
             "filterRefRotation": 16 * n, "filterRefBranch": 16 * pc, "filterRefPairs": 8 * pc,
+            "walkKey": 4 * self.survivor_capacity, "walkBucketCount": 4 * (len(library.shapes) * WALK_BUCKETS + 1),
+            "walkBucketOffset": 4 * (len(library.shapes) * WALK_BUCKETS + 1),
         }
         for name, nbytes in sizes.items():
             self.buffers[name] = DeviceBuffer(self, nbytes)
