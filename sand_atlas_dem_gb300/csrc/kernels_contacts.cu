@@ -1013,13 +1013,20 @@ __global__ void k_resolve(const __grid_constant__ Params P) {
 // the order the reference's linked lists hold them (descending contact id):
 // pairs where g is first (a contiguous run) and second (the byJ run) merged
 // from the highest pair id down, each pair's contacts from the last.  Lanes
-// load and evaluate 32 contacts at a time; every lane then replays the
-// sequential (compensated) accumulation over the shuffled per-contact terms
-// in that order, so the sums are bit-identical to the serial loop.
+// load and evaluate 32 contacts at a time and store their terms in shared
+// memory; every accumulator component is an independent sequential chain
+// (the compensated force and torque sums are componentwise), so lane j then
+// replays chain j over the 32 terms in that order: the sums are
+// bit-identical to the serial loop, with 22 chains advancing in parallel.
 struct GatherTerms {
     f3 force, torque, s0, s1, s2;
     float energy, denom, depth, dissipation, normalPower, stiffness, viscous;
 };
+// Accumulator chains: 0-2 force and 3-5 torque (compensated), 6-14 the three
+// stress rows (subtracted), 15 energy, 16 denominator, 17 deepest overlap
+// (maximum), 18 dissipation, 19 normal loss power, 20-21 timestep rates.
+constexpr uint32_t GATHER_CHAINS = 22;
+constexpr uint32_t GATHER_STRIDE = WARP + 1;  // padded rows: conflict-free on both sides
 __device__ __forceinline__ f3 shfl3(f3 v, int lane) {
     return mk(__shfl_sync(0xffffffffu, v.x, lane), __shfl_sync(0xffffffffu, v.y, lane),
               __shfl_sync(0xffffffffu, v.z, lane));
@@ -1032,14 +1039,16 @@ __global__ void __launch_bounds__(256, 3) k_gather(const __grid_constant__ Param
     if (r.control[0] != 0) return;
     uint32_t pairs = activePairs(r, c);
     __shared__ uint32_t window[8][4][WARP];  // per warp: B candidates, merged pairs, offsets, range ends
+    __shared__ float termRows[8][GATHER_CHAINS][GATHER_STRIDE];
     uint32_t* wb = window[threadIdx.x >> 5][0];
     uint32_t* wp = window[threadIdx.x >> 5][1];
     uint32_t* wo = window[threadIdx.x >> 5][2];
     uint32_t* we = window[threadIdx.x >> 5][3];
+    float (*terms)[GATHER_STRIDE] = termRows[threadIdx.x >> 5];
+    const uint32_t chain = laneId();
     for (uint32_t id = warpGlobal(); id < c.N; id += warpStride()) {
-        f3 f = mk(0.f, 0.f, 0.f), t = f, fLow = f, tLow = f, stress0 = f, stress1 = f, stress2 = f;
-        float energy = 0, denom = 0, maxDepth = 0, dissipation = 0, normalPower = 0, stiffnessRate = 0,
-              viscousRate = 0;
+        // This lane's chain: running value and compensation residual.
+        float acc = 0.f, accLow = 0.f;
         f3 one = mk(1.f, 1.f, 1.f);
         float inverseInertia = mx(mx(dot(abs3(xyz(r.invI[3 * id])), one), dot(abs3(xyz(r.invI[3 * id + 1])), one)),
                                   dot(abs3(xyz(r.invI[3 * id + 2])), one));
@@ -1127,32 +1136,47 @@ __global__ void __launch_bounds__(256, 3) k_gather(const __grid_constant__ Param
                     g.depth = __fdiv_rn(pdv.w, wmin);
                     g.dissipation = __fmul_rn(0.5f, r.slip[contact].w);
                     g.normalPower = __fmul_rn(0.5f, r.normalLossPower[contact]);
+                    const float v[GATHER_CHAINS] = {g.force.x, g.force.y, g.force.z, g.torque.x, g.torque.y, g.torque.z,
+                                                    g.s0.x, g.s0.y, g.s0.z, g.s1.x, g.s1.y, g.s1.z,
+                                                    g.s2.x, g.s2.y, g.s2.z, g.energy, g.denom, g.depth,
+                                                    g.dissipation, g.normalPower, g.stiffness, g.viscous};
+#pragma unroll
+                    for (uint32_t j = 0; j < GATHER_CHAINS; ++j) terms[j][lane] = v[j];
                 }
-                for (uint32_t k = 0; k < count; ++k) {
-                    int src = int(k);
-                    if (c.activeTimestep != 0) {
-                        stiffnessRate = __fadd_rn(stiffnessRate, __shfl_sync(0xffffffffu, g.stiffness, src));
-                        viscousRate = __fadd_rn(viscousRate, __shfl_sync(0xffffffffu, g.viscous, src));
+                __syncwarp();
+                if (chain < 6) {
+                    for (uint32_t k = 0; k < count; ++k) {  // compensated3, one component
+                        float y = __fadd_rn(terms[chain][k], accLow);
+                        float nx = __fadd_rn(acc, y);
+                        accLow = __fsub_rn(y, __fsub_rn(nx, acc));
+                        acc = nx;
                     }
-                    compensated3(f, fLow, shfl3(g.force, src));
-                    compensated3(t, tLow, shfl3(g.torque, src));
-                    stress0 = stress0 - shfl3(g.s0, src);
-                    stress1 = stress1 - shfl3(g.s1, src);
-                    stress2 = stress2 - shfl3(g.s2, src);
-                    energy = __fadd_rn(energy, __shfl_sync(0xffffffffu, g.energy, src));
-                    denom = __fadd_rn(denom, __shfl_sync(0xffffffffu, g.denom, src));
-                    maxDepth = mx(maxDepth, __shfl_sync(0xffffffffu, g.depth, src));
-                    dissipation = __fadd_rn(dissipation, __shfl_sync(0xffffffffu, g.dissipation, src));
-                    normalPower = __fadd_rn(normalPower, __shfl_sync(0xffffffffu, g.normalPower, src));
+                } else if (chain < 15) {
+                    for (uint32_t k = 0; k < count; ++k) acc = __fsub_rn(acc, terms[chain][k]);
+                } else if (chain == 17) {
+                    for (uint32_t k = 0; k < count; ++k) acc = mx(acc, terms[chain][k]);
+                } else if (chain < GATHER_CHAINS && (chain < 20 || c.activeTimestep != 0)) {
+                    for (uint32_t k = 0; k < count; ++k) acc = __fadd_rn(acc, terms[chain][k]);
                 }
+                __syncwarp();
             }
             __syncwarp();
             ia -= takeA;
             ib -= takeB;
         }
+        // Collect the chains on lane 0.
+        float sums[GATHER_CHAINS], lows[6];
+#pragma unroll
+        for (uint32_t j = 0; j < GATHER_CHAINS; ++j) sums[j] = __shfl_sync(0xffffffffu, acc, int(j));
+#pragma unroll
+        for (uint32_t j = 0; j < 6; ++j) lows[j] = __shfl_sync(0xffffffffu, accLow, int(j));
         if (laneId() == 0) {
-            f = f + fLow;
-            t = t + tLow;
+            f3 f = mk(sums[0], sums[1], sums[2]) + mk(lows[0], lows[1], lows[2]);
+            f3 t = mk(sums[3], sums[4], sums[5]) + mk(lows[3], lows[4], lows[5]);
+            f3 stress0 = mk(sums[6], sums[7], sums[8]), stress1 = mk(sums[9], sums[10], sums[11]),
+               stress2 = mk(sums[12], sums[13], sums[14]);
+            float energy = sums[15], denom = sums[16], maxDepth = sums[17], dissipation = sums[18],
+                  normalPower = sums[19], stiffnessRate = sums[20], viscousRate = sums[21];
             r.timestepRows[id] = make_float4(stiffnessRate, viscousRate, 0.f, 0.f);
             float4 ns = r.normalDamping[id];
             ns.z = normalPower;

@@ -44,7 +44,7 @@ EXTENSION_ORDER = (
     "filterRefRotation", "filterRefBranch", "filterRefPairs", "walkKey", "walkBucketCount", "walkBucketOffset",
 )
 DISTANCE_GRID = 48  # cells per axis of each shape's distance-bound grid (csrc GRID)
-WALK_BUCKETS = 512  # walk-order buckets per shape (csrc WALK_BUCKETS)
+WALK_BUCKETS = 24**3  # walk-order buckets per shape (csrc WALK_BUCKETS)
 CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4
 BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
 # History side fields: (name bound as the side being written, name bound as committed).

@@ -60,3 +60,14 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.setattr(native, "LIBRARY", tmp_path / "absent.so")
     with pytest.raises(RuntimeError, match="not built"):
         native.load()
+
+
+def test_host_sizes_match_device_constants():
+    """Buffer sizes the host computes use the device layout's constants."""
+    from sand_atlas_dem_gb300 import engine
+
+    text = (native.CSRC / "dem_device.cuh").read_text()
+    cells = int(re.search(r"constexpr uint32_t WALK_CELLS = (\d+);", text)[1])
+    grid = int(re.search(r"constexpr uint32_t GRID = (\d+);", text)[1])
+    assert engine.WALK_BUCKETS == cells**3
+    assert engine.DISTANCE_GRID == grid
