@@ -66,7 +66,7 @@ DATA = ROOT / "sand_atlas_dem_gb300" / "data"
 # the same workload (profiles/walk-dense-10k.md); None where not captured.
 WALK_TRAFFIC = {"dense-10k": 60.16e6}
 # work[] counters of the stored node-filter results (csrc/dem_device.cuh).
-W_FILTER_BUILDS, W_FILTER_STEPS = 9, 10
+W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS = 8, 9, 10
 
 
 def log(*args):
@@ -295,6 +295,7 @@ def run_gb300(args, cpu=True):
     ctrl = e.check_errors()
     work1 = e.read("work", np.uint32, (64,))
     filter_cache = {"margin": e.filter_margin,
+                    "adapted_margin": float(work1[W_FILTER_MARGIN:W_FILTER_MARGIN + 1].view(np.float32)[0]),
                     "builds_in_timed_steps": int(work1[W_FILTER_BUILDS] - work0[W_FILTER_BUILDS]),
                     "timed_steps": int(work1[W_FILTER_STEPS] - work0[W_FILTER_STEPS])}
     device_s = sum(step_ms) / 1e3

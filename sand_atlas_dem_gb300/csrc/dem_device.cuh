@@ -149,6 +149,9 @@ constexpr int W_FILTER_PAIRS = 7;   // pair count they were built on
 constexpr int W_FILTER_MARGIN = 8;  // margin they were built with (float bits)
 constexpr int W_FILTER_BUILDS = 9;  // steps that built them (counter)
 constexpr int W_FILTER_STEPS = 10;  // steps that ran the collector (counter)
+constexpr int W_FILTER_AGE = 11;    // collector runs since they were built
+constexpr int W_FILTER_NEXT = 12;   // margin a build of this step uses (float bits)
+constexpr int W_FILTER_BASE = 13;   // configured margin they were built under (float bits)
 
 struct Params {
     Config c;
@@ -322,12 +325,15 @@ __device__ __forceinline__ float meshBoxDistance(const Res& r, uint32_t node, f3
 constexpr uint32_t LEAF_MARK = 0xFFFFFFFFu;
 // Nearest-first BVH walk with cached pushed box distances (the reference CPU
 // variant, cpu_scheduling.slang:18-48, bit-identical to solver.slang:224-252).
-// With `seed` (a triangle of the shape) the walk starts with its best
-// distance just above that triangle's squared distance, computed exactly as
-// the walk computes it.  That prunes every node that cannot hold a triangle
-// at least as near, and changes nothing else: the nearest triangles' nodes
-// are never pruned, the surviving nodes are visited in the same order, and
-// the first nearest triangle reached is recorded as before.
+// With `seed` (a triangle of the shape) the walk starts with its best just
+// above that triangle's squared distance d, computed exactly as the walk
+// computes it: d (1 + 2^-20), one float up.  That prunes only nodes whose
+// box lies farther than every triangle the walk could still record, and
+// changes nothing else: the surviving nodes are visited in the same order
+// and the first nearest triangle reached is recorded as before.  The 2^-20
+// keeps the nearest triangle's boxes in the walk even where FP32 rounding
+// puts a box distance a few units in the last place above the triangle's
+// own distance (an unseeded walk has no tighter bound than d there).
 // `nearestTriangle`, when given, receives the recorded triangle.
 __device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 p, bool surfaceNormal,
                                                uint32_t seed = 0xFFFFFFFFu, uint32_t* nearestTriangle = nullptr) {
@@ -343,7 +349,8 @@ __device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 
         f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * seed])), xyz(__ldg(&r.meshTriangles[3 * seed + 1])),
                                xyz(__ldg(&r.meshTriangles[3 * seed + 2])), feature);
         f3 dq = p - q;
-        best = nextafterf(dot(dq, dq), 1e30f);
+        float d = dot(dq, dq);
+        best = nextafterf(__fadd_rn(d, __fmul_rn(d, 9.5367431640625e-07f)), 1e30f);
     }
     f3 nearest = mk(0.f, 0.f, 0.f);
     uint32_t nearestNormal = 0;
@@ -592,6 +599,10 @@ __device__ __forceinline__ uint32_t gridSeed(const Res& r, uint32_t shape, f3 lo
 // (built with grown tests and ordered by target shape and coarse cell).  Not
 // with the learned culler, whose calibrated decision is taken every step.
 __device__ __forceinline__ bool storedKeep(const Config& c) { return c.filterMargin > 0.0f && c.cullerEnabled == 0; }
+// Margin the filter results are built with on this step (0 without them).
+__device__ __forceinline__ float buildMargin(const Res& r, const Config& c) {
+    return c.filterMargin > 0.0f ? __uint_as_float(r.work[W_FILTER_NEXT]) : 0.0f;
+}
 __device__ __forceinline__ uint32_t activePairs(const Res& r, const Config& c) {
     uint32_t n = r.control[1];
     return n < c.pairCapacity ? n : c.pairCapacity;

@@ -340,7 +340,7 @@ __global__ void k_pairSetup(const __grid_constant__ Params P) {
     const Config& c = P.c;
     if (r.control[0] != 0) return;
     uint32_t n = activePairs(r, c);
-    float margin = c.filterMargin > 0.0f ? c.filterMargin : 0.0f;
+    float margin = __uint_as_float(r.work[W_FILTER_MARGIN]);  // the margin the stored results were built with
     bool check = r.work[W_FILTER] == 0;
     for (uint32_t p = gtid(); p < n; p += gstride()) {
         uint2 ij = r.pairs[p];
@@ -362,7 +362,7 @@ __global__ void k_pairMasks(const __grid_constant__ Params P) {
     const Config& c = P.c;
     if (r.control[0] != 0 || r.work[W_FILTER] == 0) return;
     uint32_t n = activePairs(r, c);
-    float margin = c.filterMargin > 0.0f ? c.filterMargin : 0.0f;
+    float margin = buildMargin(r, c);
     for (uint32_t p = gtid(); p < n; p += gstride()) {
         uint2 ij = r.pairs[p];
         f3 branch[2] = {xyz(r.dpairBranch[2 * p]), xyz(r.dpairBranch[2 * p + 1])};
@@ -390,19 +390,35 @@ __global__ void k_pairMasks(const __grid_constant__ Params P) {
 }
 // resetMeshContacts (solver.slang:396-403)
 // The stored filter results (items, survivor masks and list) serve this step
-// if they are complete and were built with this margin on a pair list of
-// the same length; k_pairSetup then checks each pair and how far its grains
-// have moved, and asks for a build if any pair is no longer covered.
+// if they are complete and were built under this configured margin on a
+// pair list of the same length; k_pairSetup then checks each pair and how
+// far its grains have moved, and asks for a build if any pair is no longer
+// covered.  The margin adapts to the motion, between the configured margin m
+// and 16 m: a build within 8 collector runs of the last one doubles it, a
+// build after more than 64 halves it (a larger margin keeps a few more nodes
+// in the stored lists; it never changes a result).
 __global__ void k_resetContacts(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
     if (r.control[0] != 0) return;
     r.control[2] = 0;
     r.control[6] = 0;
-    bool build = !(c.filterMargin > 0.0f) || r.work[W_FILTER_VALID] == 0 || r.work[W_FILTER_PAIRS] != r.control[1] ||
-                 r.work[W_FILTER_MARGIN] != __float_as_uint(c.filterMargin);
+    bool on = c.filterMargin > 0.0f;
+    uint32_t base = __float_as_uint(c.filterMargin);
+    bool valid = r.work[W_FILTER_VALID] != 0 && r.work[W_FILTER_BASE] == base;
+    bool build = !on || !valid || r.work[W_FILTER_PAIRS] != r.control[1];
     r.work[W_FILTER] = build ? 1u : 0u;
     r.work[W_FILTER_STEPS] += 1u;
+    if (on) {
+        uint32_t age = r.work[W_FILTER_AGE] + 1u;
+        r.work[W_FILTER_AGE] = age;
+        float current = __uint_as_float(r.work[W_FILTER_MARGIN]);
+        float next = c.filterMargin;
+        if (valid)
+            next = age <= 8u ? fminf(2.0f * current, 16.0f * c.filterMargin)
+                             : (age > 64u ? fmaxf(0.5f * current, c.filterMargin) : current);
+        r.work[W_FILTER_NEXT] = __float_as_uint(next);
+    }
     if (build) r.work[W_CANDIDATES] = 0;
 }
 // Flat leaf cull: one warp per directed pair; meshPairBounds (solver.slang:
@@ -488,7 +504,7 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
     if (r.work[W_FILTER] == 0) return;
     uint32_t n = 2 * activePairs(r, c);
     bool live = r.control[0] == 0;
-    float margin = c.filterMargin > 0.0f ? c.filterMargin : 0.0f;
+    float margin = buildMargin(r, c);
     float grow = __fmul_rn(1.001f, margin);
     if (margin > 0.0f) {
         for (uint32_t g = gtid(); g < c.N; g += gstride()) r.filterRefRotation[g] = r.rotation[g];
@@ -498,6 +514,8 @@ __global__ void k_leafCull(const __grid_constant__ Params P) {
             r.work[W_FILTER_VALID] = 0;
             r.work[W_FILTER_PAIRS] = r.control[1];
             r.work[W_FILTER_MARGIN] = __float_as_uint(margin);
+            r.work[W_FILTER_BASE] = __float_as_uint(c.filterMargin);
+            r.work[W_FILTER_AGE] = 0;
             r.work[W_FILTER_BUILDS] += 1u;
         }
     }
@@ -615,7 +633,7 @@ __global__ void __launch_bounds__(256) k_nodeFilter(const __grid_constant__ Para
         }
         return;
     }
-    float grow = c.filterMargin > 0.0f ? __fmul_rn(1.001f, c.filterMargin) : 0.0f;
+    float grow = __fmul_rn(1.001f, buildMargin(r, c));
     // Two items per warp, one per half-warp, four node slots per lane
     // (slot = lane in half + 16 j): twice the loads in flight per instruction.
     uint32_t half = laneId() >> 4, hl = laneId() & 15u;
@@ -691,7 +709,7 @@ __global__ void __launch_bounds__(256) k_survivorPrefilter(const __grid_constant
     const Config& c = P.c;
     bool stored = storedKeep(c);
     if (r.control[0] != 0 || (stored && r.work[W_FILTER] == 0)) return;
-    float grow = stored ? __fmul_rn(1.001f, c.filterMargin) : 0.0f;
+    float grow = stored ? __fmul_rn(1.001f, buildMargin(r, c)) : 0.0f;
     uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
     for (uint32_t s = gtid(); s < n; s += gstride()) {
         uint2 sv = r.survivors[s];

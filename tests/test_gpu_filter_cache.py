@@ -16,7 +16,7 @@ from sand_atlas_dem_gb300.engine import Engine
 from tests.specimens import build, lattice_case
 
 pytestmark = pytest.mark.gpu
-W_FILTER_BUILDS, W_FILTER_STEPS = 9, 10
+W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS = 8, 9, 10
 RATE = (-0.5, -0.5, -0.5)
 
 
@@ -102,7 +102,8 @@ def test_margin_below_rounding_slack_builds_every_step(gpu_library):
 
 def test_many_steps_with_rebuilds_stay_identical(gpu_library):
     """Fast grains (2 m/s: a few 1e-6 of a diameter per step) against a
-    margin of 1e-4: builds and reuses alternate over a long run."""
+    margin of 1e-4: builds and reuses alternate over a long run, and the
+    margin grows toward 16 times the configured one as builds come early."""
     plain, stored = engines(1e-4, speed=2.0)
     for _ in range(4):
         for e in (plain, stored):
@@ -111,6 +112,8 @@ def test_many_steps_with_rebuilds_stay_identical(gpu_library):
     builds, steps = counters(stored)
     assert steps == 101
     assert 3 <= builds <= 90, builds
+    margin = stored.read("work", np.uint32, (64,))[W_FILTER_MARGIN:W_FILTER_MARGIN + 1].view(np.float32)[0]
+    assert 1e-4 < margin <= 16e-4 * (1 + 1e-6), margin
 
 
 def test_margin_is_validated(gpu_library):
