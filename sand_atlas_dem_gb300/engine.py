@@ -111,6 +111,7 @@ class DeviceBuffer:
                 self.tensor[:n].copy_(torch.from_numpy(data.copy()))
         engine.stream.synchronize()
         engine.h2d_bytes += n
+        engine._uploaded(self)
 
     def to_numpy(self, dtype=np.uint8, count=None):
         torch = _torch()
@@ -126,6 +127,28 @@ class DeviceBuffer:
             return stage.numpy().view(dtype).copy()
         engine.stream.synchronize()
         return self.tensor[:nbytes].cpu().numpy().view(dtype).copy()
+
+
+def read_batch(engine, requests):
+    """Several small reads ((buffer, bytes, dtype) each) staged side by side in
+    the engine's pinned buffer and waited for once."""
+    torch = _torch()
+    offsets, total = [], 0
+    for _, nbytes, _ in requests:
+        offsets.append(total)
+        total += (int(nbytes) + 15) // 16 * 16
+    if total > STAGING_BYTES:
+        return [buffer.to_numpy(dtype, nbytes // np.dtype(dtype).itemsize) for buffer, nbytes, dtype in requests]
+    with torch.cuda.stream(engine.stream):
+        for (buffer, nbytes, _), offset in zip(requests, offsets):
+            engine._staging[offset:offset + nbytes].copy_(buffer.tensor[:nbytes], non_blocking=True)
+    engine.stream.synchronize()
+    host = engine._staging.numpy()
+    out = []
+    for (_, nbytes, dtype), offset in zip(requests, offsets):
+        engine.d2h_bytes += nbytes
+        out.append(host[offset:offset + nbytes].view(dtype).copy())
+    return out
 
 
 class GB300Device:
@@ -215,6 +238,12 @@ class Engine:
             raise ValueError("Finite nonnegative filter margin required")
         self._reduce_scratch = {}
         self._array_cache = {}
+        # Host copies that spare a device read: the control words as last
+        # read (valid while no device work or upload followed) and the
+        # strain-rate rows last written into the cell.
+        self._device_version = 0
+        self._ctrl_cache = None
+        self._rates = None
         # Host<->device bytes moved by this engine's own reads and uploads.
         self.h2d_bytes = self.d2h_bytes = 0
         for name in ("length_unit", "time_unit", "mass_unit", "force_unit", "stress_unit", "energy_unit",
@@ -336,8 +365,18 @@ class Engine:
                                                                      self.filter_margin]
         return (ct.c_double * len(values))(*values), len(values)
 
+    def _touch(self):
+        """Device work or an upload follows: host copies of device words are stale."""
+        self._device_version += 1
+
+    def _uploaded(self, buffer):
+        self._touch()
+        if buffer is self.buffers.get("cell"):
+            self._rates = None
+
     def dispatch(self, name, count, config, active=None):
         """Launch one named kernel or phase on the engine stream (test and probe entry)."""
+        self._touch()
         ptrs, sizes = self._arrays(self.active if active is None else active)
         values, nv = self._values(config)
         native.check(self.lib.sdg_dispatch(name.encode(), int(count), ptrs, sizes, values, nv,
@@ -356,6 +395,10 @@ class Engine:
     # --------------------------------------------------------- public API
     def check_errors(self):
         ctrl = self.read("control", np.uint32, (16,))
+        return self._checked(ctrl)
+
+    def _checked(self, ctrl):
+        self._ctrl_cache = (self._device_version, ctrl.copy())
         if ctrl[15] != 0:
             raise RuntimeError("Arithmetic materialization mask must remain zero")
         if ctrl[0]:
@@ -450,7 +493,13 @@ class Engine:
 
     def _backup(self, restore=False):
         committed = self.sides[1 - self.active]
-        count = int(self.read("control", np.uint32, (16,))[2]) if not restore else self._backup_count
+        if restore:
+            count = self._backup_count
+            self._touch()
+        elif self._ctrl_cache is not None and self._ctrl_cache[0] == self._device_version:
+            count = int(self._ctrl_cache[1][2])
+        else:
+            count = int(self.read("control", np.uint32, (16,))[2])
         if count < 0 or count > self.contact_capacity:
             raise ValueError("Committed contact count is outside capacity")
         copies = []
@@ -472,10 +521,15 @@ class Engine:
             raise RuntimeError("Engine is invalid; restore a checkpoint")
         if steps < 1:
             return
-        cell = self.read("cell", np.float32, (3 * self.specimens, 4))
-        original_cell = cell.copy()
-        cell[1::3, :3] = np.broadcast_to(np.asarray(rate, float), (self.specimens, 3)) * self.time_unit
-        self.buffers["cell"].copy_from_numpy(cell)
+        rows = (np.broadcast_to(np.asarray(rate, float), (self.specimens, 3)) * self.time_unit).astype(np.float32)
+        original_cell = None
+        if self._rates is None or not np.array_equal(self._rates, rows):
+            # Only the rate rows change; the device advances the box rows.
+            cell = self.read("cell", np.float32, (3 * self.specimens, 4))
+            original_cell = cell.copy()
+            cell[1::3, :3] = rows
+            self.buffers["cell"].copy_from_numpy(cell)
+            self._rates = rows
         self._backup()
         original_active, original_history = self.active, self.history
         done = 0
@@ -492,13 +546,15 @@ class Engine:
             self.active, self.history = original_active, original_history
             self._backup(restore=True)
             self.synchronize()
-            self.buffers["cell"].copy_from_numpy(original_cell)
+            if original_cell is not None:
+                self.buffers["cell"].copy_from_numpy(original_cell)
             raise
         self.step += steps
 
     def _launch_steps(self, steps, drag):
         if steps <= 0:
             return
+        self._touch()
         ptrs, sizes = self._arrays(self.active)
         values, nv = self._values(self.config(drag=drag))
         native.check(self.lib.sdg_engine_advance(
@@ -581,8 +637,9 @@ class Engine:
         self.active = 1
         self.step = step
 
-    def _reduce(self, name, rows, max_row):
-        """Reference 256-wide tree reduction to one row set (``diagnostic.slang:3-28``)."""
+    def _reduce(self, name, rows, max_row, read=True):
+        """Reference 256-wide tree reduction to one row set (``diagnostic.slang:3-28``);
+        with ``read=False`` the device buffer holding the rows is returned."""
         src = self.buffers[name]
         n = self.n if name == "diagnosticRows" else self.pair_capacity
         level = 0
@@ -595,15 +652,21 @@ class Engine:
             native.check(self.lib.sdg_reduce_rows(ct.c_void_p(src.ptr()), ct.c_void_p(out.ptr()), n, rows,
                                                   max_row, ct.c_void_p(self.stream.cuda_stream)))
             src, n, level = out, groups, level + 1
-        return self.m.read_prefix(src, 4 * rows, np.float32, shape=(rows, 4))
+        return self.m.read_prefix(src, 4 * rows, np.float32, shape=(rows, 4)) if read else src
 
     def diagnostics(self):
         """Stress, energies, contact counts and fabric (``gpu.py:746-891``)."""
         c = self.config()
         self.dispatch("diagnosticRows", self.n, c)
-        data = self._reduce("diagnosticRows", 8, 4)
+        rows = self._reduce("diagnosticRows", 8, 4, read=False)
         self.dispatch("fabricRows", self.pair_capacity, c)
-        fabric_data = self._reduce("fabricRows", 2, -1)
+        fabric_rows = self._reduce("fabricRows", 2, -1, read=False)
+        # One wait for all four small reads.
+        data, fabric_data, cell, ctrl = read_batch(self, [
+            (rows, 16 * 8, np.float32), (fabric_rows, 16 * 2, np.float32),
+            (self.buffers["cell"], 16 * 3, np.float32), (self.buffers["control"], 4 * 16, np.uint32)])
+        data, fabric_data, cell = data.reshape(8, 4), fabric_data.reshape(2, 4), cell.reshape(3, 4)
+        ctrl = self._checked(ctrl)
         active_pairs = round(float(fabric_data[1, 2]))
         fabric = np.array(
             [
@@ -612,8 +675,6 @@ class Engine:
                 [fabric_data[1, 0], fabric_data[1, 1], fabric_data[0, 2]],
             ]
         ) / max(active_pairs, 1)
-        cell = self.read("cell", np.float32, (3, 4))
-        ctrl = self.check_errors()
         box = cell[0, :3].astype(float) * self.length_unit
         volume = float(box.prod())
         contact = data[:3, :3].astype(float) * self.energy_unit / volume
@@ -672,6 +733,7 @@ class Engine:
 
     def profile_phases(self, *, drag=0.0):
         """Device milliseconds per phase of one committed step (CUDA events)."""
+        self._touch()
         ptrs, sizes = self._arrays(self.active)
         values, nv = self._values(self.config(drag=drag))
         out = (ct.c_float * len(native.PHASES))()
