@@ -419,6 +419,54 @@ bool nodeContact(R& r, uint32_t src, uint32_t dst, uint32_t node, float4& pd, fl
     return true;
 }
 
+// solver.slang:188-200: trilinear signed distance and its gradient from the
+// shape's grid (FP32 order of the archived generated C++: lerp(x, y, s) =
+// x + (y - x) * s; products left to right).
+float4 sdf(R& r, uint32_t s, float3 p) {
+    uint4 meta = r.grids[s];
+    float4 o = r.gridOrigin[s];
+    float3 g = (p - xyz(o)) / o.w;
+    int32_t a[3] = {int32_t(std::floor(g.x)), int32_t(std::floor(g.y)), int32_t(std::floor(g.z))};
+    int32_t dims[3] = {int32_t(meta.y), int32_t(meta.z), int32_t(meta.w)};
+    for (int k = 0; k < 3; ++k)
+        if (a[k] < 0 || a[k] >= dims[k] - 1) return {0.0f, 0.0f, 0.0f, 1.00000002004087734e+20f};
+    float3 t = g - f3(float(a[0]), float(a[1]), float(a[2]));
+    float3 u = f3(1.0f, 1.0f, 1.0f) - t;
+    float value = 0.0f;
+    float3 grad = f3(0.0f, 0.0f, 0.0f);
+    for (uint32_t i = 0; i < 2; ++i)
+        for (uint32_t j = 0; j < 2; ++j)
+            for (uint32_t k = 0; k < 2; ++k) {
+                float3 b = f3(float(i), float(j), float(k));
+                float3 w = u + (t - u) * b;
+                uint32_t ix = uint32_t(a[0]) + i, iy = uint32_t(a[1]) + j, iz = uint32_t(a[2]) + k;
+                float f = r.distance[meta.x + (ix * meta.z + iy) * meta.w + iz];
+                value = value + f * w.x * w.y * w.z;
+                float3 v = f3((2.0f * float(i) - 1.0f) * w.y * w.z, (2.0f * float(j) - 1.0f) * w.x * w.z,
+                              (2.0f * float(k) - 1.0f) * w.x * w.y);
+                grad = grad + (f * v) / o.w;
+            }
+    return f4(grad, value);
+}
+// solver.slang:319-343 with the SDF geometry (meshGeometry == 0).
+bool nodeContactSdf(R& r, uint32_t src, uint32_t dst, uint32_t node, float4& pd, float4& na) {
+    uint32_t sid = r.shapeId[src];
+    float4 sp = r.sample[r.sampleInfo[sid].x + node];
+    float3 arm = qrot(r.rotation[src], xyz(sp) * r.body[src].x);
+    float3 branch = centerBranch(r, src, dst);
+    float3 local = qinv(r.rotation[dst], arm - branch) / r.body[dst].x;
+    float4 f = sdf(r, r.shapeId[dst], local);
+    pd = f4(arm, -f.w * r.body[dst].x);
+    na = {0, 0, 0, 0};
+    if (pd.w <= 0.0f) return false;
+    float3 grad = qrot(r.rotation[dst], xyz(f));
+    float len = length(grad);
+    if (len < 1.00000001168609742e-07f || !std::isfinite(pd.w)) { fail(r, 2); return false; }
+    na = f4(grad / len, sp.w * r.body[src].x * r.body[src].x);
+    if (pd.w > r.c.maxOverlap * mn(r.body[src].w, r.body[dst].w)) fail(r, 4);
+    return true;
+}
+
 // ---------------------------------------------------------------- kernels
 
 // solver.slang:858-888
@@ -586,6 +634,58 @@ void emitPairs(R& r, uint32_t id) {
         r.control[1] = r.pairOffsets[r.c.N - 1] + r.pairCounts[r.c.N - 1];
         r.referenceCell[0] = r.cell[0];
     }
+}
+// SDF geometry collector (solver.slang:536-572), serial: 64 lanes per pair,
+// lane l taking the pair's nodes l, l+64, ... (the first grain's nodes, then
+// the second's); a pair's contacts are written lane by lane.
+inline uint32_t sdfNodes(R& r, uint2 ij, uint32_t& a) {
+    a = r.sampleInfo[r.shapeId[ij.x]].y;
+    return a + r.sampleInfo[r.shapeId[ij.y]].y;
+}
+void countContacts(R& r, uint32_t pair) {
+    if (pair >= r.c.pairCapacity) return;
+    uint32_t count = 0;
+    if (pair < r.control[1] && r.control[0] == 0) {
+        uint2 ij = r.pairs[pair];
+        uint32_t a, total = sdfNodes(r, ij, a);
+        for (uint32_t s = 0; s < total; ++s) {
+            float4 pd, na;
+            if (nodeContactSdf(r, s < a ? ij.x : ij.y, s < a ? ij.y : ij.x, s < a ? s : s - a, pd, na)) count++;
+        }
+    }
+    r.contactCounts[pair] = count;
+}
+void scanContacts(R& r) {  // exclusive scan over the pair capacity (cpu.py:476-490)
+    uint32_t sum = 0;
+    for (uint32_t p = 0; p < r.c.pairCapacity; ++p) {
+        r.contactOffsets[p] = sum;
+        sum += r.contactCounts[p];
+    }
+}
+void contactTotal(R& r) {
+    uint32_t n = r.c.pairCapacity;
+    r.control[2] = r.contactOffsets[n - 1] + r.contactCounts[n - 1];
+    r.control[6] = 0;
+    if (r.control[2] > r.c.contactCapacity) fail(r, 32);
+}
+void emitContacts(R& r, uint32_t pair) {
+    uint32_t active = r.control[1] < r.c.pairCapacity ? r.control[1] : r.c.pairCapacity;
+    if (pair >= active || r.control[0] != 0) return;
+    uint2 ij = r.pairs[pair];
+    uint32_t a, total = sdfNodes(r, ij, a);
+    uint32_t offset = r.contactOffsets[pair];
+    for (uint32_t lane = 0; lane < 64; ++lane)
+        for (uint32_t s = lane; s < total; s += 64) {
+            uint32_t i = s < a ? ij.x : ij.y, j = s < a ? ij.y : ij.x, node = s < a ? s : s - a;
+            float4 pd, na;
+            if (nodeContactSdf(r, i, j, node, pd, na)) {
+                if (offset >= r.c.contactCapacity) { fail(r, 32); break; }
+                r.meta[offset] = uint4{i, j, node, 0};
+                r.pointDepth[offset] = pd;
+                r.normalArea[offset] = na;
+                offset++;
+            }
+        }
 }
 // solver.slang:396-403
 void resetMeshContacts(R& r, uint32_t id) {
@@ -981,6 +1081,10 @@ extern "C" int oracle_dispatch(const char* name, uint32_t count, void** buffers,
     else if (k == "prepareMeshPairs") each(prepareMeshPairs);
     else if (k == "collectMeshFrontiers") collectParallel(r, count, nvalues > 25 ? uint32_t(r.uni[0]) : 1u);
     else if (k == "exhaustiveContacts") exhaustiveContacts(r);
+    else if (k == "countContacts") each(countContacts);
+    else if (k == "scanContacts") scanContacts(r);
+    else if (k == "contactTotal") contactTotal(r);
+    else if (k == "emitContacts") each(emitContacts);
     else if (k == "clearContactStorage") each(clearContactStorage);
     else if (k == "resolveContacts") each(resolveContacts);
     else if (k == "buildHistoryHash") each(buildHistoryHash);
