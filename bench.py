@@ -60,6 +60,10 @@ WORKLOADS = {
                           grains_per_specimen="512..4096", solid_fraction="U(0.55, 0.60)",
                           strain_rate_per_s="-U(0.1, 1.0) per specimen", max_overlap_fraction=0.5,
                           packing="jittered cubic lattice per specimen"),
+    "sdf-spheres-1k": dict(workload="sdf-spheres-1k-simple-cubic", library="sphere", grains=1000, shapes=1,
+                           contact_geometry="sdf", sdf_resolution=32, nodes_per_grain=512,
+                           packing="simple cubic at 1.99 radii", timestep_s=1e-8, max_overlap_fraction=0.01,
+                           pairs_per_particle=8, contacts_per_particle=256, strain_rate_per_s=0.0),
 }
 DATA = ROOT / "sand_atlas_dem_gb300" / "data"
 # DRAM bytes (read + write) of one k_nodeWalk launch from an ncu capture of
@@ -80,8 +84,10 @@ def cache_dir():
 
 
 def library(kind):
-    from sand_atlas_dem_gb300.shapes import synthetic_library
+    from sand_atlas_dem_gb300.shapes import ShapeLibrary, analytic_sphere, synthetic_library
 
+    if kind == "sphere":
+        return ShapeLibrary([analytic_sphere(resolution=32, samples=512)])
     return synthetic_library(kind, 64)
 
 
@@ -121,6 +127,18 @@ class Workload:
             self.rates = np.full((1, 3), self.config["strain_rate_per_s"])
             self.config.update(grains=grains, packing_meta=pack["meta"],
                                solid_fraction=pack["meta"].get("achieved_solid_fraction"))
+        elif name == "sdf-spheres-1k":
+            # The reference's own benchmark case (benchmark.py:162-253 defaults):
+            # 1,000 analytical spheres on a simple cubic lattice at 1.99 radii.
+            radius = self.lib.shapes[0].radius
+            side = round(self.config["grains"] ** (1 / 3))
+            spacing = 1.99 * radius
+            idx = np.stack(np.meshgrid(*([np.arange(side)] * 3), indexing="ij"), -1).reshape(-1, 3)
+            n = len(idx)
+            self.specimens = [((idx + 0.5) * spacing, np.full(3, side * spacing), np.zeros(n, np.uint32),
+                               np.ones(n))]
+            self.rotations = np.tile(np.array([0, 0, 0, 1], np.float32), (n, 1))
+            self.rates = np.zeros((1, 3))
         elif name == "uneven-50k":
             case = lattice_at(self.lib, round(self.config["grains"] ** (1 / 3)), self.config["solid_fraction"],
                               seed=5)
@@ -137,8 +155,16 @@ class Workload:
         # Lattices have at most 26 neighbours in range: 16 pairs per grain
         # leave room, and the engine grows on overflow.
         pairs = {} if name == "dense-10k" else dict(pairs_per_particle=16)
-        self.spec = material_spec(self.lib, ids, scales,
-                                  max_overlap_fraction=self.config["max_overlap_fraction"], **pairs)
+        if name == "sdf-spheres-1k":
+            from sand_atlas_dem_gb300.spec import Experiment
+
+            self.spec = Experiment(particles=len(ids), contact_geometry="sdf", timestep=self.config["timestep_s"],
+                                   pairs_per_particle=self.config["pairs_per_particle"],
+                                   contacts_per_particle=self.config["contacts_per_particle"],
+                                   max_overlap_fraction=self.config["max_overlap_fraction"])
+        else:
+            self.spec = material_spec(self.lib, ids, scales,
+                                      max_overlap_fraction=self.config["max_overlap_fraction"], **pairs)
         self.grains = len(ids)
 
     def engine(self, cls, specimens=None, **kwargs):
@@ -318,9 +344,21 @@ def run_gb300(args, cpu=True):
     lib_bytes = sum(a.nbytes for k, a in e.layout.geometry.items() if k.startswith("mesh") or k == "sample")
     step_bytes, query_bytes, walk_bytes = algorithmic_bytes(w.grains, pairs, contacts, items, nodes, survivors,
                                                             kept, 0, lib_bytes)
+    kernel_name = "k_nodeWalk (exact BVH queries, one thread per kept node)"
+    group_name = "k_nodeFilter, k_survivorList, k_survivorPrefilter, k_walkList, k_nodeWalk + scans"
+    if e.sdf:
+        # SDF emit (k_sdfEmit, one warp per pair): every node of both grains
+        # evaluated twice (count and write passes: its sample, 16 B, and the
+        # 8 grid values of its cell, 32 B), 52 B written per contact.
+        node_count = pairs * 2 * w.config["nodes_per_grain"]
+        walk_bytes = 2 * 48 * node_count + 52 * contacts + sum(e.layout.geometry[k].nbytes for k in ("distance", "sample"))
+        query_bytes = walk_bytes + 48 * node_count
+        step_bytes = 516 * w.grains + 264 * pairs + 272 * contacts + query_bytes
+        kernel_name = "k_sdfEmit (SDF node queries and contact writes, one warp per pair)"
+        group_name = "k_sdfCount, contact scan, k_sdfEmit"
     hbm, peak_kind = peaks()
     top = max(phase_ms, key=phase_ms.get)
-    query_ms = phase_ms["node_filter"] + phase_ms["node_query"]
+    query_ms = phase_ms["node_filter"] + phase_ms["node_query"] + (phase_ms["pair_cull"] if e.sdf else 0.0)
     query_gbs = query_bytes / (query_ms / 1e3) / 1e9
     # The dominant kernel, k_nodeWalk, is the whole "node_query" phase (one launch).
     walk_gbs = walk_bytes / (phase_ms["node_query"] / 1e3) / 1e9
@@ -363,7 +401,7 @@ def run_gb300(args, cpu=True):
         "gpu_launches": int(kernels) * args.steps,
         "roofline": {
             "bound": "hbm",
-            "kernel": "k_nodeWalk (exact BVH queries, one thread per kept node)",
+            "kernel": kernel_name,
             "achieved": walk_gbs,
             "peak": hbm,
             "peak_source": peak_kind,
@@ -372,7 +410,7 @@ def run_gb300(args, cpu=True):
             "traffic": WALK_TRAFFIC.get(w.name),
             "algorithmic_bytes": walk_bytes,
             "kernel_ms": phase_ms["node_query"],
-            "launch_group": "k_nodeFilter, k_survivorList, k_survivorPrefilter, k_walkList, k_nodeWalk + scans",
+            "launch_group": group_name,
             "launch_group_algorithmic_bytes": query_bytes,
             "launch_group_ms": query_ms,
             "launch_group_achieved_gbs": query_gbs,
@@ -381,7 +419,7 @@ def run_gb300(args, cpu=True):
         },
         "clocks": clocks.summary(),
     }
-    if not args.no_plain:
+    if not args.no_plain and not e.sdf:  # the SDF geometry has no filters to compare
         line["plain_gpu_path"] = plain_comparison(w, args, flush)
     if args.culler:
         line["learned_culler"] = culler_comparison(w, args, flush)

@@ -173,6 +173,12 @@ class OracleEngine:
 
     def collect(self, c, exhaustive=False):
         pc = self.pair_capacity
+        if self.spec.contact_geometry == "sdf":  # gpu.py:537-543
+            self.dispatch("countContacts", pc, c)
+            self.dispatch("scanContacts", 1, c)
+            self.dispatch("contactTotal", 1, c)
+            self.dispatch("emitContacts", pc, c)
+            return
         if exhaustive:
             self.dispatch("exhaustiveContacts", 1, c)
             return

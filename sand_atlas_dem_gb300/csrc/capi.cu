@@ -65,8 +65,12 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
         return 1;
     }
     if (c.specimens == 0) { g_error = "at least one specimen required"; return 1; }
-    if (c.N == 0 || c.meshGeometry == 0 || c.wallCount != 0) {
-        g_error = "the GB300 step needs N > 0, mesh geometry and no planes";
+    if (c.N == 0 || c.wallCount != 0) {
+        g_error = "the GB300 step needs N > 0 and no planes";
+        return 1;
+    }
+    if (c.meshGeometry == 0 && c.sourceSurfaceNormal != 0) {
+        g_error = "the source-surface normal needs the mesh contact geometry";
         return 1;
     }
     if (bytes) {

@@ -923,6 +923,129 @@ __global__ void k_contactStart(const __grid_constant__ Params P) {
     }
 }
 
+// ------------------------------------------------------------ SDF geometry
+// solver.slang:188-200: trilinear signed distance and gradient from the
+// target shape's grid, in the FP32 order of the reference's generated CPU
+// code (lerp(x, y, s) = x + (y - x) * s, products left to right).
+__device__ __forceinline__ float4 sdfQuery(const Res& r, uint32_t shape, f3 p) {
+    uint4 meta = __ldg(&r.grids[shape]);
+    float4 o = __ldg(&r.gridOrigin[shape]);
+    f3 g = (p - xyz(o)) / o.w;
+    int ax = int(floorf(g.x)), ay = int(floorf(g.y)), az = int(floorf(g.z));
+    if (ax < 0 || ay < 0 || az < 0 || ax >= int(meta.y) - 1 || ay >= int(meta.z) - 1 || az >= int(meta.w) - 1)
+        return make_float4(0.f, 0.f, 0.f, 1.00000002004087734e+20f);
+    f3 t = g - mk(float(ax), float(ay), float(az));
+    f3 u = mk(1.f, 1.f, 1.f) - t;
+    float value = 0.f;
+    f3 grad = mk(0.f, 0.f, 0.f);
+#pragma unroll
+    for (uint32_t i = 0; i < 2; ++i)
+#pragma unroll
+        for (uint32_t j = 0; j < 2; ++j)
+#pragma unroll
+            for (uint32_t k = 0; k < 2; ++k) {
+                f3 w = u + (t - u) * mk(float(i), float(j), float(k));
+                float f = __ldg(&r.distance[meta.x + ((uint32_t(ax) + i) * meta.z + (uint32_t(ay) + j)) * meta.w +
+                                            (uint32_t(az) + k)]);
+                value = __fadd_rn(value, __fmul_rn(__fmul_rn(__fmul_rn(f, w.x), w.y), w.z));
+                f3 v = mk(__fmul_rn(__fmul_rn(__fsub_rn(__fmul_rn(2.0f, float(i)), 1.0f), w.y), w.z),
+                          __fmul_rn(__fmul_rn(__fsub_rn(__fmul_rn(2.0f, float(j)), 1.0f), w.x), w.z),
+                          __fmul_rn(__fmul_rn(__fsub_rn(__fmul_rn(2.0f, float(k)), 1.0f), w.x), w.y));
+                grad = grad + (f * v) / o.w;
+            }
+    return w4(grad, value);
+}
+// solver.slang:319-343 with the SDF geometry; the directed-pair branch is
+// the FP64 one k_pairSetup stored (the same bits as the per-call reference).
+__device__ __forceinline__ bool sdfNodeContact(const Res& r, const Config& c, uint32_t src, uint32_t dst,
+                                               uint32_t node, f3 branch, float4& pd, float4& na) {
+    uint32_t sid = r.shapeId[src];
+    float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[sid].x) + node]);
+    float4 bs = r.body[src], bd = r.body[dst];
+    f3 arm = qrot(r.rotation[src], xyz(sp) * bs.x);
+    f3 local = qinv(r.rotation[dst], arm - branch) / bd.x;
+    float4 f = sdfQuery(r, r.shapeId[dst], local);
+    pd = w4(arm, __fmul_rn(-f.w, bd.x));
+    if (pd.w <= 0.0f) return false;
+    f3 grad = qrot(r.rotation[dst], xyz(f));
+    float len = length(grad);
+    if (len < 1.00000001168609742e-07f || !isfinite(pd.w)) { fail(r, F_DEGENERATE); return false; }
+    na = w4(grad / len, __fmul_rn(__fmul_rn(sp.w, bs.x), bs.x));
+    if (pd.w > __fmul_rn(c.maxOverlap, mn(bs.w, bd.w))) fail(r, F_PENETRATION);
+    return true;
+}
+// The contacts of pair p on virtual lane v of the reference's 64-thread
+// group (solver.slang:536-565): its nodes s = v, v + 64, ... over the first
+// grain's nodes, then the second's.  With `emit`, they are written from
+// `slot` on; returns how many there are.
+__device__ __forceinline__ uint32_t sdfLane(const Res& r, const Config& c, uint32_t p, uint2 ij, uint32_t a,
+                                            uint32_t total, uint32_t v, bool emit, uint32_t slot) {
+    f3 b0 = xyz(r.dpairBranch[2 * p]), b1 = xyz(r.dpairBranch[2 * p + 1]);
+    uint32_t count = 0;
+    for (uint32_t s = v; s < total; s += 64) {
+        bool first = s < a;
+        uint32_t i = first ? ij.x : ij.y, j = first ? ij.y : ij.x, node = first ? s : s - a;
+        float4 pd, na;
+        if (!sdfNodeContact(r, c, i, j, node, first ? b0 : b1, pd, na)) continue;
+        if (emit) {
+            uint32_t out = slot + count;
+            if (out >= c.contactCapacity) { fail(r, F_CONTACT); return count; }
+            r.meta[out] = make_uint4(i, j, node, 0);
+            r.pointDepth[out] = pd;
+            r.normalArea[out] = na;
+            r.contactPair[out] = p;
+        }
+        count++;
+    }
+    return count;
+}
+// countContacts (solver.slang:538-549): one warp per pair, each lane two of
+// the 64 virtual lanes.
+__global__ void k_sdfCount(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = activePairs(r, c);
+    for (uint32_t p = warpGlobal(); p < n; p += warpStride()) {
+        uint2 ij = r.pairs[p];
+        uint32_t a = __ldg(&r.sampleInfo[r.shapeId[ij.x]].y), total = a + __ldg(&r.sampleInfo[r.shapeId[ij.y]].y);
+        uint32_t count = sdfLane(r, c, p, ij, a, total, laneId(), false, 0) +
+                         sdfLane(r, c, p, ij, a, total, laneId() + WARP, false, 0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
+        if (laneId() == 0) r.contactCounts[p] = count;
+    }
+}
+// emitContacts (solver.slang:551-565): each virtual lane writes its contacts
+// after those of the lanes below it, so a pair's contacts are in the
+// reference's order (lane, then node).  Also the per-pair contact starts of
+// the history side being written.
+__global__ void k_sdfEmit(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t n = activePairs(r, c);
+    uint32_t total = r.control[2];
+    if (total > c.contactCapacity) fail(r, F_CONTACT);
+    if (r.control[0] != 0) return;
+    for (uint32_t p = warpGlobal(); p < n; p += warpStride()) {
+        uint2 ij = r.pairs[p];
+        uint32_t a = __ldg(&r.sampleInfo[r.shapeId[ij.x]].y), nodes = a + __ldg(&r.sampleInfo[r.shapeId[ij.y]].y);
+        uint32_t low = sdfLane(r, c, p, ij, a, nodes, laneId(), false, 0);
+        uint32_t high = sdfLane(r, c, p, ij, a, nodes, laneId() + WARP, false, 0);
+        uint32_t incLow = low, incHigh = high;
+#pragma unroll
+        for (uint32_t o = 1; o < WARP; o <<= 1) {
+            uint32_t x = __shfl_up_sync(0xffffffffu, incLow, o), y = __shfl_up_sync(0xffffffffu, incHigh, o);
+            if (laneId() >= o) { incLow += x; incHigh += y; }
+        }
+        uint32_t lowTotal = __shfl_sync(0xffffffffu, incLow, WARP - 1);
+        uint32_t base = r.contactOffsets[p];
+        sdfLane(r, c, p, ij, a, nodes, laneId(), true, base + incLow - low);
+        sdfLane(r, c, p, ij, a, nodes, laneId() + WARP, true, base + lowTotal + incHigh - high);
+    }
+    for (uint32_t p = gtid(); p <= n; p += gstride()) r.sideContactStart[p] = p < n ? r.contactOffsets[p] : total;
+}
+
 // ---------------------------------------------------------------- friction
 // solver.slang:691-696
 __device__ __forceinline__ f3 transported(f3 x, f3 a, f3 b, float spin) {
@@ -947,14 +1070,23 @@ __device__ __forceinline__ void normalResponse(float depth, float area, float vn
 }
 // History key within a pair: direction (source > target) then the node's
 // position in its shape's cluster order; runs of one pair are sorted by it.
-__device__ __forceinline__ uint32_t pairKey(const Res& r, uint32_t src, uint32_t dst, uint32_t node) {
+// With the SDF geometry a pair's contacts are in the reference emit order:
+// s = node (first grain) or V_first + node (second grain), taken by virtual
+// lane s mod 64, then s / 64.
+__device__ __forceinline__ uint32_t pairKey(const Res& r, const Config& c, uint32_t src, uint32_t dst,
+                                            uint32_t node) {
+    if (c.meshGeometry == 0) {
+        uint32_t s = src > dst ? __ldg(&r.sampleInfo[r.shapeId[dst]].y) + node : node;
+        return ((s & 63u) << 24) | (s >> 6);
+    }
     return (src > dst ? 0x80000000u : 0u) | __ldg(&r.meshSampleRank[__ldg(&r.sampleInfo[r.shapeId[src]].x) + node]);
 }
 // Slot of key (src, dst, node) among the committed contacts, or EMPTY.
 // The committed side stores, per grain a, the run of its pairs (a, b) with
 // b > a and, per pair, its contacts sorted by pairKey: a sorted merge done as
 // a run lookup plus a binary search.
-__device__ __forceinline__ uint32_t historySlot(const Res& r, uint32_t src, uint32_t dst, uint32_t node) {
+__device__ __forceinline__ uint32_t historySlot(const Res& r, const Config& c, uint32_t src, uint32_t dst,
+                                                uint32_t node) {
     uint32_t a = min(src, dst), b = max(src, dst);
     uint32_t begin = r.oldPairOffsets[a], end = r.oldPairOffsets[a + 1];
     uint32_t q = EMPTY;
@@ -962,11 +1094,11 @@ __device__ __forceinline__ uint32_t historySlot(const Res& r, uint32_t src, uint
         if (r.oldPairB[k] == b) { q = k; break; }
     if (q == EMPTY) return EMPTY;
     uint32_t lo = r.oldContactStart[q], hi = r.oldContactStart[q + 1];
-    uint32_t key = pairKey(r, src, dst, node);
+    uint32_t key = pairKey(r, c, src, dst, node);
     while (lo < hi) {
         uint32_t mid = (lo + hi) >> 1;
         uint4 m = r.oldMeta[mid];
-        uint32_t mk2 = pairKey(r, m.x, m.y, m.z);
+        uint32_t mk2 = pairKey(r, c, m.x, m.y, m.z);
         if (mk2 < key) lo = mid + 1;
         else hi = mid;
     }
@@ -991,7 +1123,7 @@ __global__ void k_resolve(const __grid_constant__ Params P) {
         f3 wj = viscosity > 0 ? xyz(r.forceOmega[j]) : omegaOf(r, j);
         f3 elastic = mk(0.f, 0.f, 0.f);
         if (c.historyStep != 0) {
-            uint32_t old = historySlot(r, i, j, key.z);
+            uint32_t old = historySlot(r, c, i, j, key.z);
             if (old != EMPTY)
                 elastic = transported(xyz(r.oldSlip[old]), xyz(r.oldNormal[old]), nrm,
                                       __fmul_rn(__fmul_rn(0.5f, dot(wi + wj, nrm)), c.dt));
@@ -1254,7 +1386,8 @@ static void neighbours(const Params& P, cudaStream_t s) {
     k_byJSort<<<blocks(c.N, T), T, 0, s>>>(P);
 }
 
-// Pair set-up, leaf cull and the (directed pair, leaf) item list.
+// Pair set-up, leaf cull and the (directed pair, leaf) item list; with the
+// SDF geometry, pair set-up, contact counts and their scan.
 static void collectCull(const Params& P, cudaStream_t s) {
     const Res& r = P.r;
     const Config& c = P.c;
@@ -1262,6 +1395,12 @@ static void collectCull(const Params& P, cudaStream_t s) {
     k_resetContacts<<<1, 1, 0, s>>>(P);
     uint32_t g = grid(c.cullBlocksPerSM, 8);
     k_pairSetup<<<g, T, 0, s>>>(P);
+    if (c.meshGeometry == 0) {
+        k_sdfCount<<<grid(c.queryBlocksPerSM, 8), T, 0, s>>>(P);
+        launch_scan(r.contactCounts, r.contactOffsets, ScanCount{r.control + 1, c.pairCapacity, 1, 0}, false,
+                    r.control + 2, nullptr, r.scanPartials, s);
+        return;
+    }
     k_pairMasks<<<g, T, 0, s>>>(P);
     k_leafCull<<<g, T, 0, s>>>(P);
     launch_scan(r.dpairLeafCount, r.dpairCandOffset, ScanCount{r.control + 1, c.pairCapacity, 2, 0}, true,
@@ -1272,6 +1411,7 @@ static void collectCull(const Params& P, cudaStream_t s) {
 static void collectFilter(const Params& P, cudaStream_t s) {
     const Res& r = P.r;
     const Config& c = P.c;
+    if (c.meshGeometry == 0) return;
     uint32_t warps = c.queryWarps == 4 ? 4 : 8;
     k_nodeFilter<<<grid(c.queryBlocksPerSM, 8), 32 * warps, 0, s>>>(P);
     launch_scan(r.candSurvCount, r.candSurvOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0},
@@ -1301,7 +1441,8 @@ static void collectFilter(const Params& P, cudaStream_t s) {
 }
 // The exact queries.
 static void collectWalk(const Params& P, cudaStream_t s) {
-    k_nodeWalk<<<grid(P.c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
+    if (P.c.meshGeometry == 0) k_sdfEmit<<<grid(P.c.queryBlocksPerSM, 8), 256, 0, s>>>(P);
+    else k_nodeWalk<<<grid(P.c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
 }
 static void collectQuery(const Params& P, cudaStream_t s) {
     collectFilter(P, s);
@@ -1311,6 +1452,7 @@ static void collectQuery(const Params& P, cudaStream_t s) {
 static void collectEmit(const Params& P, cudaStream_t s) {
     const Res& r = P.r;
     const Config& c = P.c;
+    if (c.meshGeometry == 0) return;
     launch_scan(r.candHitCount, r.candHitOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0}, true,
                 r.control + 2, nullptr, r.scanPartials, s);
     uint32_t g = grid(c.contactBlocksPerSM, 8);
@@ -1334,7 +1476,9 @@ int launch_contacts(const std::string_view& name, const Params& P, uint32_t coun
     else if (name == "collectWalk") collectWalk(P, s);
     else if (name == "collectEmit") collectEmit(P, s);
     else if (name == "resolveContacts") k_resolve<<<grid(c.contactBlocksPerSM, 8), T, 0, s>>>(P);
-    else if (name == "distanceGrid") k_distanceGrid<<<grid(0, 8), T, 0, s>>>(P);
+    else if (name == "distanceGrid") {
+        if (c.meshGeometry != 0) k_distanceGrid<<<grid(0, 8), T, 0, s>>>(P);
+    }
     else if (name == "gather") k_gather<<<min(blocks(c.N, 8), max(1u, grid(c.gatherWarps, 64) / 8)), T, 0, s>>>(P);
     else return 1;
     (void)count;

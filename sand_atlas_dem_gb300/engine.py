@@ -236,6 +236,11 @@ class Engine:
         self.filter_margin = float(filter_margin)
         if not np.isfinite(self.filter_margin) or self.filter_margin < 0:
             raise ValueError("Finite nonnegative filter margin required")
+        # The SDF geometry queries every node of a pair on its grid: the mesh
+        # filters, their stored results and the distance-bound grid do not apply.
+        self.sdf = spec.contact_geometry == "sdf"
+        if self.sdf:
+            self.distance_grid, self.filter_margin = False, 0.0
         self._reduce_scratch = {}
         self._array_cache = {}
         # Host copies that spare a device read: the control words as last
@@ -320,7 +325,8 @@ class Engine:
             raise MemoryError("GB300 engine allocation failed")
         self._finalizer = weakref.finalize(self, self.lib.sdg_engine_destroy, self._native)
         # Certified distance bounds of every shape, built once from the packed library.
-        self.dispatch("distanceGrid", 0, self.config(dt=0))
+        if not self.sdf:
+            self.dispatch("distanceGrid", 0, self.config(dt=0))
         self.stream.synchronize()
 
     # ------------------------------------------------------------ plumbing
@@ -593,9 +599,14 @@ class Engine:
         if len(meta) and (src.max() >= n or dst.max() >= n):
             raise ValueError("Checkpoint contact refers to a missing grain")
         a, b = np.minimum(src, dst), np.maximum(src, dst)
-        base = g["sampleInfo"][self.ids[src], 0].astype(np.int64)
-        rank = g["meshSampleRank"][base + node].astype(np.int64)
-        key = ((src > dst).astype(np.int64) << 31) | rank
+        if self.sdf:
+            # The SDF emit order: s by virtual lane (s mod 64), then s / 64.
+            s = np.where(src > dst, g["sampleInfo"][self.ids[a], 1].astype(np.int64) + node, node)
+            key = ((s & 63) << 24) | (s >> 6)
+        else:
+            base = g["sampleInfo"][self.ids[src], 0].astype(np.int64)
+            rank = g["meshSampleRank"][base + node].astype(np.int64)
+            key = ((src > dst).astype(np.int64) << 31) | rank
         order = np.lexsort((key, b, a))
         a, b = a[order], b[order]
         pair_start = np.flatnonzero(np.r_[True, (a[1:] != a[:-1]) | (b[1:] != b[:-1])]) if len(a) else np.zeros(0, int)

@@ -142,8 +142,13 @@ class HostLayout:
         self.grain_specimen = np.repeat(np.arange(self.specimens, dtype=np.uint32), self.counts)
         if not spec.periodic and (np.any(positions < 0) or np.any(positions >= self.cells[self.grain_specimen])):
             raise ValueError("Nonperiodic particle centres must lie in [0, cell)")
-        if spec.contact_geometry != "mesh":
-            raise ValueError("The GB300 backend implements the mesh contact geometry only")
+        if spec.contact_geometry not in ("mesh", "sdf"):
+            raise ValueError("Contact geometry must be mesh or sdf")
+        if spec.contact_geometry == "sdf":
+            if any(getattr(s, "sdf", None) is None for s in library.shapes):
+                raise ValueError("The SDF contact geometry needs a signed-distance grid on every shape")
+            if spec.contact_normal == "source-surface-experimental":
+                raise ValueError("The source-surface normal needs the mesh contact geometry")
         if spec.planes:
             raise ValueError("The GB300 backend implements periodic and plane-free domains only")
         self.spec = spec
@@ -222,9 +227,13 @@ class HostLayout:
         return conservative_timestep(self.library, self.spec, self.ids, self.scales)
 
     def static_geometry(self):
-        """Packed mesh arrays plus the per-shape node table (``gpu.py:421-488``)."""
-        data = pack_library(self.library, self.length_unit)
+        """Packed mesh arrays (mesh geometry) or the signed-distance grids (SDF
+        geometry, with one-row mesh placeholders), plus the per-shape node
+        table (``gpu.py:421-488``)."""
         l = self.length_unit
+        if self.spec.contact_geometry == "sdf":
+            return self._sdf_geometry()
+        data = pack_library(self.library, self.length_unit)
         info, samples, offset = [], [], 0
         for s in self.library.shapes:
             info.append([offset, len(s.samples), 0, 0])
@@ -237,6 +246,40 @@ class HostLayout:
         data["grids"] = np.zeros((1, 4), np.uint32)
         data["gridOrigin"] = np.zeros((1, 4), np.float32)
         data["distance"] = np.zeros(4, np.float32)
+        return data
+
+    def _sdf_geometry(self):
+        """``gpu.py:421-488`` for the SDF geometry: each shape's grid packed as
+        (first value, nx, ny, nz), origin and spacing over the length unit, and
+        the values in x-major order; mesh arrays are one-row placeholders."""
+        l = self.length_unit
+        shapes = self.library.shapes
+        data = {name: np.zeros((1, 4), np.uint32) for name in
+                ("meshRoots", "meshLinks", "meshHullInfo", "meshFrontier", "meshClusterInfo", "meshClusterRanges")}
+        for name in ("meshPlanes", "meshMin", "meshMax", "meshTriangles", "meshNormals", "meshClusterMin",
+                     "meshClusterMax"):
+            data[name] = np.zeros((1, 4), np.float32)
+        data["meshSampleIndices"] = np.zeros(4, np.uint32)
+        # This backend's mesh extensions, empty: no shape has leaf clusters.
+        data["meshLeafInfo"] = np.zeros((len(shapes), 4), np.uint32)
+        data["meshLeaves"] = np.zeros(4, np.uint32)
+        data["meshChildren"] = np.zeros((4, 4), np.float32)
+        grids, origins, fields, info, samples = [], [], [], [], []
+        first = offset = 0
+        for s in shapes:
+            grids.append([first, *s.sdf.shape])
+            origins.append([*(np.asarray(s.origin) / l), s.spacing / l])
+            fields.append((s.sdf / l).astype(np.float32).ravel())
+            info.append([offset, len(s.samples), 0, 0])
+            samples.append(np.column_stack([s.samples / l, s.areas / l**2]).astype(np.float32))
+            first += s.sdf.size
+            offset += len(s.samples)
+        data["meshSampleRank"] = np.zeros(max(offset, 1), np.uint32)
+        data["grids"] = np.asarray(grids, np.uint32)
+        data["gridOrigin"] = np.asarray(origins, np.float32)
+        data["distance"] = np.concatenate(fields).astype(np.float32)
+        data["sampleInfo"] = np.asarray(info, np.uint32)
+        data["sample"] = np.concatenate(samples)
         return data
 
     def config(self, *, dt, drag=0.0, history=False):
@@ -263,7 +306,7 @@ class HostLayout:
             "drag": drag * self.time_unit,
             "maxOverlap": spec.max_overlap_fraction,
             "historyStep": int(history),
-            "meshGeometry": 1,
+            "meshGeometry": int(spec.contact_geometry == "mesh"),
             "sourceSurfaceNormal": int(spec.contact_normal == "source-surface-experimental"),
             "periodic": int(spec.periodic),
             "wallCount": 0,

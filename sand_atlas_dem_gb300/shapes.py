@@ -3,8 +3,11 @@
 A :class:`Shape` carries the fields the mesh path of the reference reads from a
 shape asset (``src/sand_atlas_dem/geometry.py:17-29``): triangle mesh, surface
 quadrature nodes with area weights, volume, unit-density inertia and bounding
-radius.  Lengths are metres.  Signed-distance grids are not carried: this
-backend implements the mesh contact geometry only.
+radius.  Lengths are metres.  For the SDF contact geometry a shape also
+carries its signed-distance grid (negative inside) with the grid origin and
+spacing (``geometry.py:24-26``); :func:`with_sdf` builds one from the mesh the
+way the reference lays it out, :func:`analytic_sphere` is the reference's
+exact-sphere fixture.
 
 The synthetic library follows the seeded recipe used for the benchmark
 workloads: geodesic icospheres of frequency ``nu`` (T = 20 nu^2 triangles,
@@ -30,12 +33,24 @@ class Shape:
     inertia: np.ndarray
     radius: float
     provenance: dict = field(default_factory=dict)
+    sdf: np.ndarray = None      # signed distance at the grid points, negative inside
+    origin: np.ndarray = None   # position of grid point (0, 0, 0)
+    spacing: float = 0.0        # grid spacing
 
     def validate(self):
-        """Checks of ``geometry.py:32-58`` that apply without an SDF grid."""
+        """Checks of ``geometry.py:32-58`` (the grid ones when a grid is carried)."""
         for a in (self.vertices, self.samples, self.areas, self.inertia):
             if not np.isfinite(a).all():
                 raise ValueError("Nonfinite shape data")
+        if self.sdf is not None:
+            g = self.sdf
+            if (g.ndim != 3 or min(g.shape) < 4 or not (g.min() < 0 < g.max()) or not np.isfinite(g).all()
+                    or not self.spacing > 0 or np.shape(self.origin) != (3,)):
+                raise ValueError("Invalid signed-distance grid")
+            faces = np.concatenate([g[0].ravel(), g[-1].ravel(), g[:, 0].ravel(), g[:, -1].ravel(),
+                                    g[:, :, 0].ravel(), g[:, :, -1].ravel()])
+            if faces.min() <= 0:
+                raise ValueError("Signed-distance grid boundary must lie outside the shape")
         if self.volume <= 0 or self.radius <= 0 or np.any(self.areas <= 0):
             raise ValueError("Invalid shape measure")
         if len(self.samples) != len(self.areas) or self.samples.shape[1:] != (3,):
@@ -194,6 +209,103 @@ def perturbed_grain(frequency, *, radius=5e-4, sigma=0.08, axes=(1.0, 1.0, 1.0),
             sample_count=count,
         ),
     )
+
+
+def _closest_on_triangles(p, a, b, c):
+    """Nearest points of triangles (a, b, c) to points p, all (..., 3), FP64
+    (the region test of the reference's closestTriangle, solver.slang:203-219)."""
+    ab, ac, ap = b - a, c - a, p - a
+    d1, d2 = np.einsum("...i,...i", ab, ap), np.einsum("...i,...i", ac, ap)
+    bp = p - b
+    d3, d4 = np.einsum("...i,...i", ab, bp), np.einsum("...i,...i", ac, bp)
+    cp = p - c
+    d5, d6 = np.einsum("...i,...i", ab, cp), np.einsum("...i,...i", ac, cp)
+    vc, vb, va = d1 * d4 - d3 * d2, d5 * d2 - d1 * d6, d3 * d6 - d5 * d4
+    with np.errstate(divide="ignore", invalid="ignore"):
+        denom = va + vb + vc
+        face = a + ab * (vb / denom)[..., None] + ac * (vc / denom)[..., None]
+        e_ab = a + ab * (d1 / (d1 - d3))[..., None]
+        e_ac = a + ac * (d2 / (d2 - d6))[..., None]
+        e_bc = b + (c - b) * ((d4 - d3) / ((d4 - d3) + (d5 - d6)))[..., None]
+    out = face
+    regions = [
+        ((va <= 0) & (d4 - d3 >= 0) & (d5 - d6 >= 0), e_bc),
+        ((vb <= 0) & (d2 >= 0) & (d6 <= 0), e_ac),
+        ((d6 >= 0) & (d5 <= d6), c),
+        ((vc <= 0) & (d1 >= 0) & (d3 <= 0), e_ab),
+        ((d3 >= 0) & (d4 <= d3), b),
+        ((d1 <= 0) & (d2 <= 0), a),
+    ]
+    for mask, value in regions:  # later entries take precedence, as the early returns do
+        out = np.where(mask[..., None], np.broadcast_to(value, out.shape), out)
+    return out
+
+
+def signed_distance(vertices, faces, points, chunk=1024):
+    """Exact signed distance of points to a closed, outward-wound triangle
+    mesh (negative inside), FP64: nearest point over all triangles, sign from
+    the generalized winding number (solid angles, Van Oosterom-Strackee)."""
+    tri = np.asarray(vertices, float)[np.asarray(faces)]
+    a, b, c = tri[None, :, 0], tri[None, :, 1], tri[None, :, 2]
+    points = np.asarray(points, float)
+    out = np.empty(len(points))
+    for start in range(0, len(points), chunk):
+        p = points[start:start + chunk, None, :]
+        q = _closest_on_triangles(p, a, b, c)
+        distance = np.sqrt(np.min(np.einsum("pti,pti->pt", p - q, p - q), axis=1))
+        x, y, z = a - p, b - p, c - p
+        lx, ly, lz = (np.linalg.norm(v, axis=-1) for v in (x, y, z))
+        det = np.einsum("pti,pti->pt", x, np.cross(y, z))
+        den = (lx * ly * lz + np.einsum("pti,pti->pt", x, y) * lz + np.einsum("pti,pti->pt", y, z) * lx
+               + np.einsum("pti,pti->pt", z, x) * ly)
+        winding = np.sum(np.arctan2(det, den), axis=1) / (2 * np.pi)
+        out[start:start + chunk] = np.where(winding > 0.5, -distance, distance)
+    return out
+
+
+def with_sdf(shape, resolution=32):
+    """The shape with a signed-distance grid laid out as the reference lays it
+    out (``geometry.py:195-215``): spacing = largest extent / (resolution - 1),
+    origin three spacings below the mesh bounds, ceil(extents / spacing) + 7
+    points per axis; values from :func:`signed_distance` in float32."""
+    from dataclasses import replace
+
+    vertices = np.asarray(shape.vertices, float)
+    low, high = vertices.min(0), vertices.max(0)
+    extents = high - low
+    dx = float(extents.max() / (resolution - 1))
+    origin = low - 3 * dx
+    dims = np.ceil(extents / dx).astype(int) + 7
+    ijk = np.stack(np.meshgrid(*(np.arange(d) for d in dims), indexing="ij"), -1).reshape(-1, 3)
+    sdf = signed_distance(vertices, shape.faces, origin + dx * ijk).reshape(tuple(dims)).astype(np.float32)
+    out = replace(shape, sdf=sdf, origin=origin, spacing=dx,
+                  provenance=dict(shape.provenance, sdf_sign="negative_inside", sdf_resolution=int(resolution)))
+    out.validate()
+    return out
+
+
+def analytic_sphere(radius=5e-4, resolution=32, samples=512):
+    """The reference's analytical sphere fixture (``geometry.py:285-315``):
+    exact grid values |x| - r over resolution + 6 points per axis, Fibonacci
+    nodes with equal areas, analytic volume and inertia.  Its mesh (a
+    frequency-4 geodesic sphere) serves only the host layout."""
+    dx = 2 * radius / (resolution - 1)
+    origin = np.full(3, -radius - 3 * dx)
+    dims = resolution + 6
+    grid = np.stack(np.meshgrid(*([np.arange(dims)] * 3), indexing="ij"), -1) * dx + origin
+    sdf = (np.linalg.norm(grid, axis=-1) - radius).astype(np.float32)
+    k = np.arange(samples)
+    z = 1 - 2 * (k + 0.5) / samples
+    angle = k * (np.pi * (3 - np.sqrt(5)))
+    nodes = radius * np.column_stack([np.sqrt(1 - z * z) * np.cos(angle), np.sqrt(1 - z * z) * np.sin(angle), z])
+    unit, faces = icosphere(4)
+    volume = 4 * np.pi * radius**3 / 3
+    shape = Shape("analytical-sphere", unit * radius, faces, nodes, np.full(samples, 4 * np.pi * radius**2 / samples),
+                  volume, np.eye(3) * 0.4 * volume * radius**2, radius,
+                  dict(fixture="analytical_sphere", radius_m=radius, display_mesh_only=True),
+                  sdf=sdf, origin=origin, spacing=dx)
+    shape.validate()
+    return shape
 
 
 def synthetic_library(kind, count=64, *, seed=1000, radius=5e-4):

@@ -61,13 +61,27 @@ def read(e, name, rows, dtype=np.float32, width=4):
     return e.read(name, dtype, (rows, width))
 
 
+_SDF_CUBE = []
+
+
+def sdf_cube():
+    """The exact cube with its signed-distance grid (built once per process)."""
+    from sand_atlas_dem_gb300.shapes import exact_cube, with_sdf
+
+    if not _SDF_CUBE:
+        _SDF_CUBE.append(with_sdf(exact_cube(), resolution=16))
+    return _SDF_CUBE[0]
+
+
 def cube_pair(engine_cls, *, separation=9.99e-5, friction=0.5, dt=1e-9, viscosity=0.0,
-              policy="active-contact"):
-    """Two exact six-node cubes, h = 0.1 mm (``tests/test_cpu_solver.py:121-173``)."""
+              policy="active-contact", geometry="mesh"):
+    """Two exact six-node cubes, h = 0.1 mm (``tests/test_cpu_solver.py:121-173``),
+    with the mesh or the SDF contact geometry."""
     from sand_atlas_dem_gb300.shapes import ShapeLibrary, exact_cube
 
-    spec = Experiment(particles=2, periodic=True, contact_geometry="mesh", timestep=dt, timestep_policy=policy,
+    spec = Experiment(particles=2, periodic=True, contact_geometry=geometry, timestep=dt, timestep_policy=policy,
                       normal_viscosity=viscosity, friction=friction, max_overlap_fraction=0.1,
                       contacts_per_particle=128)
     positions = [[0.005] * 3, [0.005 + separation, 0.005, 0.005]]
-    return engine_cls(ShapeLibrary([exact_cube()]), spec, positions, [0.01] * 3, [0, 0], [1, 1])
+    shape = sdf_cube() if geometry == "sdf" else exact_cube()
+    return engine_cls(ShapeLibrary([shape]), spec, positions, [0.01] * 3, [0, 0], [1, 1])

@@ -18,10 +18,13 @@ def physical(state, name):
     return state[name][:, :3].astype(float) + state[name + "Remainder"][:, :3].astype(float)
 
 
+@pytest.mark.parametrize("geometry", ["mesh", "sdf"])
 @pytest.mark.parametrize("make", ENGINES)
-def test_cube_pair_force_is_exact(make):
-    """``test_cpu_solver.py:176-209``: force on grain 0 is [-0.001, 0, 0] N."""
-    e = cube_pair(make)
+def test_cube_pair_force_is_exact(make, geometry):
+    """``test_cpu_solver.py:176-209``: force on grain 0 is [-0.001, 0, 0] N (the
+    cube's signed distance is linear near a face centre, so the trilinear
+    SDF query is exact there too)."""
+    e = cube_pair(make, geometry=geometry)
     e.initialize()
     force = read(e, "force", 2)[:, :3] * e.force_unit
     torque = read(e, "torque", 2)[:, :3] * e.energy_unit
@@ -70,10 +73,11 @@ def test_viscous_pair_force_and_galilean_invariance(make):
     np.testing.assert_allclose(forces[0], forces[1], rtol=2e-4, atol=1e-9)
 
 
+@pytest.mark.parametrize("geometry", ["mesh", "sdf"])
 @pytest.mark.parametrize("make", ENGINES)
-def test_friction_history_restart_replays(make):
+def test_friction_history_restart_replays(make, geometry):
     """``test_cpu_solver.py:212-238``: slip history survives a restart."""
-    e = cube_pair(make)
+    e = cube_pair(make, geometry=geometry)
     v = np.array([[0, 0.01, 0], [0, -0.01, 0]]) * e.time_unit / e.length_unit
     upload(e, "velocity", np.pad(v.astype(np.float32), ((0, 0), (0, 1))))
     e.initialize()
@@ -82,7 +86,7 @@ def test_friction_history_restart_replays(make):
     assert np.linalg.norm(state["slip"][:, :3]) > 0
     e.advance(5)
     expected = e.state()
-    restored = cube_pair(make)
+    restored = cube_pair(make, geometry=geometry)
     restored.restore(state, 7)
     restored.advance(5)
     actual = restored.state()

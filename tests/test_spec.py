@@ -33,7 +33,8 @@ def test_invalid_cases_raise(bad):
 
 def test_backend_scope_is_explicit():
     library = ShapeLibrary([exact_cube()])
-    with pytest.raises(ValueError, match="mesh contact geometry"):
+    # The default geometry is the SDF one, which needs a grid on every shape.
+    with pytest.raises(ValueError, match="signed-distance grid"):
         HostLayout(library, Experiment(particles=2, timestep=1e-9), [[0.005] * 3, [0.0051, 0.005, 0.005]],
                    [0.01] * 3, [0, 0], [1, 1])
     with pytest.raises(ValueError, match="conservative estimate"):
