@@ -347,12 +347,13 @@ def run_gb300(args, cpu=True):
     kernel_name = "k_nodeWalk (exact BVH queries, one thread per kept node)"
     group_name = "k_nodeFilter, k_survivorList, k_survivorPrefilter, k_walkList, k_nodeWalk + scans"
     if e.sdf:
-        # SDF emit (k_sdfEmit, one warp per pair): every node of both grains
-        # evaluated twice (count and write passes: its sample, 16 B, and the
-        # 8 grid values of its cell, 32 B), 52 B written per contact.
+        # SDF emit (k_sdfEmit, one warp per pair), counted at its minimum:
+        # every node of both grains read once (its sample, 16 B), the 8 grid
+        # values of each contact node's cell (32 B) and 52 B written per
+        # contact; the count pass reads the samples once more.
         node_count = pairs * 2 * w.config["nodes_per_grain"]
-        walk_bytes = 2 * 48 * node_count + 52 * contacts + sum(e.layout.geometry[k].nbytes for k in ("distance", "sample"))
-        query_bytes = walk_bytes + 48 * node_count
+        walk_bytes = 16 * node_count + (32 + 52) * contacts + sum(e.layout.geometry[k].nbytes for k in ("distance", "sample"))
+        query_bytes = walk_bytes + 16 * node_count + 32 * contacts
         step_bytes = 516 * w.grains + 264 * pairs + 272 * contacts + query_bytes
         kernel_name = "k_sdfEmit (SDF node queries and contact writes, one warp per pair)"
         group_name = "k_sdfCount, contact scan, k_sdfEmit"

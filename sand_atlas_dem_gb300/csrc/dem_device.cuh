@@ -129,8 +129,9 @@ struct Res {
     uint32_t* walkKey;                // survivorCapacity: bucket of each kept survivor (target shape, coarse cell)
     uint32_t* walkBucketCount;        // shapes x WALK_BUCKETS + 1: kept survivors per bucket
     uint32_t* walkBucketOffset;       // shapes x WALK_BUCKETS + 1: first walk-list slot of each bucket
+    uint32_t* sdfLaneCounts;          // SDF geometry, 32 x pairCapacity: contacts of virtual lanes l and l + 32
 };
-constexpr int EXTENSION_COUNT = 50;
+constexpr int EXTENSION_COUNT = 51;
 constexpr uint32_t WALK_CELLS = 24;  // coarse cells per axis of a shape's grid box for the walk order
 constexpr uint32_t WALK_BUCKETS = WALK_CELLS * WALK_CELLS * WALK_CELLS;
 constexpr uint32_t GRID = 48;  // cells per axis of each shape's distance-bound grid

@@ -964,6 +964,12 @@ __device__ __forceinline__ bool sdfNodeContact(const Res& r, const Config& c, ui
     float4 bs = r.body[src], bd = r.body[dst];
     f3 arm = qrot(r.rotation[src], xyz(sp) * bs.x);
     f3 local = qinv(r.rotation[dst], arm - branch) / bd.x;
+    // Beyond the target's bounding radius by more than a grid-cell diagonal,
+    // all eight grid values around the node are distances of points outside
+    // the shape (positive), so the interpolated distance is positive: no
+    // contact, as the full query would find; skip its grid loads.
+    float reach = __fadd_rn(__fdiv_rn(bd.z, bd.x), __fmul_rn(1.7339f, __ldg(&r.gridOrigin[r.shapeId[dst]].w)));
+    if (dot(local, local) > __fmul_rn(reach, reach)) return false;
     float4 f = sdfQuery(r, r.shapeId[dst], local);
     pd = w4(arm, __fmul_rn(-f.w, bd.x));
     if (pd.w <= 0.0f) return false;
@@ -1009,8 +1015,10 @@ __global__ void k_sdfCount(const __grid_constant__ Params P) {
     for (uint32_t p = warpGlobal(); p < n; p += warpStride()) {
         uint2 ij = r.pairs[p];
         uint32_t a = __ldg(&r.sampleInfo[r.shapeId[ij.x]].y), total = a + __ldg(&r.sampleInfo[r.shapeId[ij.y]].y);
-        uint32_t count = sdfLane(r, c, p, ij, a, total, laneId(), false, 0) +
-                         sdfLane(r, c, p, ij, a, total, laneId() + WARP, false, 0);
+        uint32_t low = sdfLane(r, c, p, ij, a, total, laneId(), false, 0);
+        uint32_t high = sdfLane(r, c, p, ij, a, total, laneId() + WARP, false, 0);
+        r.sdfLaneCounts[size_t(WARP) * p + laneId()] = low | (high << 16);  // at most 81 each
+        uint32_t count = low + high;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
         if (laneId() == 0) r.contactCounts[p] = count;
@@ -1030,8 +1038,8 @@ __global__ void k_sdfEmit(const __grid_constant__ Params P) {
     for (uint32_t p = warpGlobal(); p < n; p += warpStride()) {
         uint2 ij = r.pairs[p];
         uint32_t a = __ldg(&r.sampleInfo[r.shapeId[ij.x]].y), nodes = a + __ldg(&r.sampleInfo[r.shapeId[ij.y]].y);
-        uint32_t low = sdfLane(r, c, p, ij, a, nodes, laneId(), false, 0);
-        uint32_t high = sdfLane(r, c, p, ij, a, nodes, laneId() + WARP, false, 0);
+        uint32_t counts = r.sdfLaneCounts[size_t(WARP) * p + laneId()];  // from k_sdfCount
+        uint32_t low = counts & 0xFFFFu, high = counts >> 16;
         uint32_t incLow = low, incHigh = high;
 #pragma unroll
         for (uint32_t o = 1; o < WARP; o <<= 1) {
