@@ -11,7 +11,7 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 128) this backend's extension buffers, in the order of
+ *   [77, 130) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
@@ -38,7 +38,9 @@
  *             bucket (target shape, coarse cell), and the count and first
  *             slot of each bucket, and for the SDF geometry each pair's
  *             contact counts per virtual lane of the reference's 64-lane
- *             group, 32 words per pair).
+ *             group, 32 words per pair, and per stored walk-list slot its
+ *             nearest-triangle certificate: the point it was taken at with
+ *             the distance gap, and the triangle).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
@@ -74,7 +76,7 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 128
+#define SDG_BUFFER_COUNT 130
 #define SDG_VALUE_COUNT 39
 #define SDG_PHASES 9
 

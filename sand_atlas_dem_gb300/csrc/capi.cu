@@ -92,7 +92,8 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
             bytes[77 + 47] < uint64_t(c.survivorCapacity) * 4 ||
             bytes[77 + 48] < (uint64_t(c.shapes) * WALK_BUCKETS + 1) * 4 ||
             bytes[77 + 49] < (uint64_t(c.shapes) * WALK_BUCKETS + 1) * 4 ||
-            (c.meshGeometry == 0 && bytes[77 + 50] < uint64_t(c.pairCapacity) * 32 * 4)) {
+            (c.meshGeometry == 0 && bytes[77 + 50] < uint64_t(c.pairCapacity) * 32 * 4) ||
+            bytes[77 + 51] < uint64_t(c.survivorCapacity) * 16 || bytes[77 + 52] < uint64_t(c.survivorCapacity) * 4) {
             g_error = "a buffer is smaller than its configured capacity";
             return 1;
         }

@@ -130,8 +130,10 @@ struct Res {
     uint32_t* walkBucketCount;        // shapes x WALK_BUCKETS + 1: kept survivors per bucket
     uint32_t* walkBucketOffset;       // shapes x WALK_BUCKETS + 1: first walk-list slot of each bucket
     uint32_t* sdfLaneCounts;          // SDF geometry, 32 x pairCapacity: contacts of virtual lanes l and l + 32
+    float4* walkCertPoint;            // survivorCapacity: per stored walk slot, where its certificate was taken, and the gap
+    uint32_t* walkCertTriangle;       // survivorCapacity: its certified nearest triangle (EMPTY: none)
 };
-constexpr int EXTENSION_COUNT = 51;
+constexpr int EXTENSION_COUNT = 53;
 constexpr uint32_t WALK_CELLS = 24;  // coarse cells per axis of a shape's grid box for the walk order
 constexpr uint32_t WALK_BUCKETS = WALK_CELLS * WALK_CELLS * WALK_CELLS;
 constexpr uint32_t GRID = 48;  // cells per axis of each shape's distance-bound grid
@@ -324,6 +326,17 @@ __device__ __forceinline__ float meshBoxDistance(const Res& r, uint32_t node, f3
     return boxDistance(xyz(__ldg(&r.meshMin[node])), xyz(__ldg(&r.meshMax[node])), p);
 }
 constexpr uint32_t LEAF_MARK = 0xFFFFFFFFu;
+// Signed distance and direction from the recorded nearest point (the end of
+// solver.slang:224-252).
+__device__ __forceinline__ float4 distanceResult(const Res& r, f3 p, float best, f3 nearest, uint32_t nearestNormal,
+                                                 bool found, bool surfaceNormal) {
+    f3 pseudo = found ? xyz(__ldg(&r.meshNormals[nearestNormal])) : mk(0.f, 0.f, 0.f);
+    float distance = __fsqrt_rn(best);
+    f3 off = p - nearest;
+    float side = dot(off, pseudo) < 0 ? -1.0f : 1.0f;
+    f3 normal = surfaceNormal ? pseudo : (distance > 1e-12f ? (side * off) / distance : pseudo);
+    return w4(normal, __fmul_rn(side, distance));
+}
 // Nearest-first BVH walk with cached pushed box distances (the reference CPU
 // variant, cpu_scheduling.slang:18-48, bit-identical to solver.slang:224-252).
 // With `seed` (a triangle of the shape) the walk starts with its best just
@@ -386,12 +399,79 @@ __device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 
         }
     }
     if (nearestTriangle) *nearestTriangle = found ? nearestNormal / 7 : 0xFFFFFFFFu;
-    f3 pseudo = found ? xyz(__ldg(&r.meshNormals[nearestNormal])) : mk(0.f, 0.f, 0.f);
-    float distance = __fsqrt_rn(best);
-    f3 off = p - nearest;
-    float side = dot(off, pseudo) < 0 ? -1.0f : 1.0f;
-    f3 normal = surfaceNormal ? pseudo : (distance > 1e-12f ? (side * off) / distance : pseudo);
-    return w4(normal, __fmul_rn(side, distance));
+    return distanceResult(r, p, best, nearest, nearestNormal, found, surfaceNormal);
+}
+// The nearest triangle of the shape to p and the gap to every other one.
+// The same nearest-first walk, keeping the two smallest squared distances and
+// pruning by the second (times 1 + 2^-20, against FP32 box rounding), from
+// the cap B = (sqrt(d_seed) + reach)^2: it records the triangle the walk
+// records and returns, in `gap`, a lower bound of (distance to every other
+// triangle) - (distance to it), or 0 when a triangle ties it.  Only gaps up
+// to about `reach` are found.  `triangle` receives the recorded triangle.
+__device__ __forceinline__ float4 meshDistanceCertified(const Res& r, uint32_t shape, f3 p, uint32_t seed, float reach,
+                                                        uint32_t& triangle, float& gap) {
+    uint32_t root = __ldg(&r.meshRoots[shape].x);
+    uint32_t pending[32];
+    float pendingDistance[32];
+    uint32_t top = 1;
+    pending[0] = root;
+    pendingDistance[0] = meshBoxDistance(r, root, p);
+    float cap = 1e30f;
+    if (seed != 0xFFFFFFFFu) {
+        uint32_t feature;
+        f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * seed])), xyz(__ldg(&r.meshTriangles[3 * seed + 1])),
+                               xyz(__ldg(&r.meshTriangles[3 * seed + 2])), feature);
+        f3 dq = p - q;
+        float root2 = __fadd_rn(__fsqrt_rn(dot(dq, dq)), reach);
+        cap = nextafterf(__fmul_rn(__fmul_rn(root2, root2), 1.0000019073486328f), 1e30f);
+    }
+    float best = cap, second = cap;
+    f3 nearest = mk(0.f, 0.f, 0.f);
+    uint32_t nearestNormal = 0;
+    bool found = false;
+    while (top > 0) {
+        uint32_t slot = --top, node = pending[slot];
+        float limit = __fmul_rn(second, 1.00000095367431640625f);
+        if (pendingDistance[slot] > limit) continue;
+        const float4* record = r.meshChildren + 4 * size_t(node);
+        float4 r0 = __ldg(record), r1 = __ldg(record + 1);
+        if (__float_as_uint(r0.w) != LEAF_MARK) {
+            float4 r2 = __ldg(record + 2), r3 = __ldg(record + 3);
+            uint32_t a = node + 1, b = __float_as_uint(r0.w);
+            float da = boxDistance(xyz(r0), xyz(r1), p), db = boxDistance(xyz(r2), xyz(r3), p);
+            if (da < db) { uint32_t s = a; a = b; b = s; float ds = da; da = db; db = ds; }
+            if (top + 2 > 32) { fail(r, F_STACK); triangle = 0xFFFFFFFFu; gap = 0.f; return make_float4(0.f, 0.f, 0.f, 1e20f); }
+            if (da <= limit) { pending[top] = a; pendingDistance[top++] = da; }
+            if (db <= limit) { pending[top] = b; pendingDistance[top++] = db; }
+            continue;
+        }
+        uint32_t first = __float_as_uint(r0.x), count = __float_as_uint(r0.y);
+        for (uint32_t k = 0; k < count; ++k) {
+            uint32_t t = first + k, feature;
+            f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * t])), xyz(__ldg(&r.meshTriangles[3 * t + 1])),
+                                   xyz(__ldg(&r.meshTriangles[3 * t + 2])), feature);
+            f3 dq = p - q;
+            float distance = dot(dq, dq);
+            if (distance < best) {
+                second = best;
+                best = distance; nearest = q; nearestNormal = 7 * t + feature; found = true;
+            } else if (distance < second) {
+                second = distance;
+            }
+        }
+    }
+    triangle = found ? nearestNormal / 7 : 0xFFFFFFFFu;
+    gap = found ? __fsub_rn(__fsqrt_rn(second), __fsqrt_rn(best)) : 0.f;
+    return distanceResult(r, p, best, nearest, nearestNormal, found, false);
+}
+// The walk's result when `triangle` is known to be the unique nearest: the
+// same closest point, squared distance and feature the walk records for it.
+__device__ __forceinline__ float4 meshDistanceAt(const Res& r, f3 p, uint32_t triangle) {
+    uint32_t feature;
+    f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * triangle])), xyz(__ldg(&r.meshTriangles[3 * triangle + 1])),
+                           xyz(__ldg(&r.meshTriangles[3 * triangle + 2])), feature);
+    f3 dq = p - q;
+    return distanceResult(r, p, dot(dq, dq), q, 7 * triangle + feature, true, false);
 }
 // solver.slang:259-272.  With `grow` > 0 the root box and every hull plane
 // are moved out by that distance (unit normals): the test then admits every
@@ -522,12 +602,12 @@ __device__ __forceinline__ bool nodePrefilter(const Res& r, uint32_t src, uint32
     local = qinv(qd, arm - branch) / r.body[dst].x;
     return nodeTests(r, r.shapeId[dst], plane, local, grow);
 }
-__device__ __forceinline__ bool nodeExact(const Res& r, const Config& c, uint32_t src, uint32_t dst, uint32_t node,
-                                          f3 arm, f3 local, float4& pd, float4& na, uint32_t seed = 0xFFFFFFFFu) {
-    uint32_t sid = r.shapeId[src], targetShape = r.shapeId[dst];
+// The contact record from the target's signed distance f at the node.
+__device__ __forceinline__ bool nodeContactFrom(const Res& r, const Config& c, uint32_t src, uint32_t dst,
+                                                uint32_t node, f3 arm, float4 f, float4& pd, float4& na) {
+    uint32_t sid = r.shapeId[src];
     float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[sid].x) + node]);
     float4 bs = r.body[src], bd = r.body[dst];
-    float4 f = meshDistance(r, targetShape, local, false, seed);
     pd = w4(arm, __fmul_rn(-f.w, bd.x));
     if (pd.w <= 0.0f) return false;
     f3 grad = qrot(r.rotation[dst], xyz(f));
@@ -542,6 +622,11 @@ __device__ __forceinline__ bool nodeExact(const Res& r, const Config& c, uint32_
     na = w4(grad / len, __fmul_rn(__fmul_rn(sp.w, bs.x), bs.x));
     if (pd.w > __fmul_rn(c.maxOverlap, mn(bs.w, bd.w))) fail(r, F_PENETRATION);
     return true;
+}
+__device__ __forceinline__ bool nodeExact(const Res& r, const Config& c, uint32_t src, uint32_t dst, uint32_t node,
+                                          f3 arm, f3 local, float4& pd, float4& na, uint32_t seed = 0xFFFFFFFFu) {
+    float4 f = meshDistance(r, r.shapeId[dst], local, false, seed);
+    return nodeContactFrom(r, c, src, dst, node, arm, f, pd, na);
 }
 __device__ __forceinline__ bool nodeContact(const Res& r, const Config& c, uint32_t src, uint32_t dst, uint32_t node,
                                             f3 branch, float4& pd, float4& na, const float4* plane = nullptr) {

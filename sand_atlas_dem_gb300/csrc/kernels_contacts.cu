@@ -820,6 +820,7 @@ __global__ void k_walkList(const __grid_constant__ Params P) {
             uint32_t bucket = r.walkKey[s];
             uint32_t slot = r.walkBucketOffset[bucket] + atomicSub(&r.walkBucketCount[bucket], 1u) - 1u;
             r.walkList[slot] = s;
+            r.walkCertTriangle[slot] = EMPTY;
         } else {
             r.walkList[r.keepOffset[s]] = s;
         }
@@ -855,13 +856,43 @@ __global__ void __launch_bounds__(256) k_nodeWalk(const __grid_constant__ Params
     const Config& c = P.c;
     if (r.control[0] != 0) return;
     uint32_t n = min(r.work[W_KEPT], c.survivorCapacity);
+    // A stored list keeps its slots from step to step, and each slot keeps a
+    // certificate: the nearest triangle T found by a certifying walk at the
+    // point p0, and a gap g below which no other triangle's distance lies
+    // above T's.  Distances are 1-Lipschitz in the point, so while
+    // 2 |p - p0| + slack < g, T is still the unique nearest triangle at p and
+    // the walk would record it with the values closestTriangle gives for it:
+    // the step evaluates T alone.  Otherwise it walks, certifying again.  The
+    // slack, 1e-5 (1 + |p|_1), covers the FP32 rounding of the distances.
+    bool certify = storedKeep(c);
+    float reach = __fadd_rn(__fmul_rn(2.01f, __uint_as_float(r.work[W_FILTER_MARGIN])), 1e-4f);
     for (uint32_t t = gtid(); t < n; t += gstride()) {
         uint32_t s = r.walkList[t];
         SurvivorNode v = survivorNode(r, s);
-        float4 pd, na;
-        // Seed the walk with the triangle nearest to the node's grid cell.
-        uint32_t seed = gridSeed(r, r.shapeId[v.dst], v.local);
-        if (nodeExact(r, c, v.src, v.dst, v.node, v.arm, v.local, pd, na, seed)) {
+        float4 pd, na, f;
+        uint32_t shape = r.shapeId[v.dst];
+        if (certify) {
+            uint32_t triangle = r.walkCertTriangle[t];
+            bool known = false;
+            if (triangle != EMPTY) {
+                float4 cp = r.walkCertPoint[t];
+                float slack = __fmul_rn(1e-5f, __fadd_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(v.local.x), fabsf(v.local.y)),
+                                                                        fabsf(v.local.z))));
+                known = __fadd_rn(__fmul_rn(2.002f, length(v.local - xyz(cp))), slack) < cp.w;
+            }
+            if (known) {
+                f = meshDistanceAt(r, v.local, triangle);
+            } else {
+                float gap;
+                f = meshDistanceCertified(r, shape, v.local, gridSeed(r, shape, v.local), reach, triangle, gap);
+                r.walkCertTriangle[t] = triangle;
+                r.walkCertPoint[t] = w4(v.local, gap);
+            }
+        } else {
+            // Seed the walk with the triangle nearest to the node's grid cell.
+            f = meshDistance(r, shape, v.local, false, gridSeed(r, shape, v.local));
+        }
+        if (nodeContactFrom(r, c, v.src, v.dst, v.node, v.arm, f, pd, na)) {
             r.hitScratch[2 * s] = pd;
             r.hitScratch[2 * s + 1] = na;
             atomicOr(v.slot < WARP ? &r.candHitMask[v.item].x : &r.candHitMask[v.item].y, 1u << (v.slot & 31u));

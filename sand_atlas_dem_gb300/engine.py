@@ -42,7 +42,7 @@ EXTENSION_ORDER = (
     "cullerMargin", "cullerStats", "candSurvMask", "candSurvOffset", "survivors", "survKeep", "keepOffset",
     "walkList", "dpairSourcePlane", "meshChildren", "distanceGrid", "distanceGridInfo", "distanceGridTriangle",
     "filterRefRotation", "filterRefBranch", "filterRefPairs", "walkKey", "walkBucketCount", "walkBucketOffset",
-    "sdfLaneCounts",
+    "sdfLaneCounts", "walkCertPoint", "walkCertTriangle",
 )
 DISTANCE_GRID = 48  # cells per axis of each shape's distance-bound grid (csrc GRID)
 WALK_BUCKETS = 24**3  # walk-order buckets per shape (csrc WALK_BUCKETS)
@@ -301,6 +301,7 @@ class Engine:
             "walkKey": 4 * self.survivor_capacity, "walkBucketCount": 4 * (len(library.shapes) * WALK_BUCKETS + 1),
             "walkBucketOffset": 4 * (len(library.shapes) * WALK_BUCKETS + 1),
             "sdfLaneCounts": 4 * 32 * pc if spec.contact_geometry == "sdf" else 16,
+            "walkCertPoint": 16 * self.survivor_capacity, "walkCertTriangle": 4 * self.survivor_capacity,
         }
         for name, nbytes in sizes.items():
             self.buffers[name] = DeviceBuffer(self, nbytes)
