@@ -20,6 +20,10 @@ Workloads (``--workload``):
     (one launch per phase, one graph per step), 512..4,096 grains each from
     the uneven library at solid fractions U(0.55, 0.60), each compressed at
     its own rate U(0.1, 1.0)/s.
+``sdf-spheres-1k``: the SDF contact geometry on the reference's own benchmark
+    case (``benchmark.py:162-253`` defaults): 1,000 analytical spheres
+    (resolution 32, 512 nodes) on a simple cubic lattice at 1.99 radii,
+    dt 1e-8.
 
 Data are synthetic (seeded); the reference's Hostun assets are not used.
 
