@@ -72,7 +72,7 @@ WORKLOADS = {
 DATA = ROOT / "sand_atlas_dem_gb300" / "data"
 # DRAM bytes (read + write) of one k_nodeWalk launch from an ncu capture of
 # the same workload (profiles/walk-dense-10k.md); None where not captured.
-WALK_TRAFFIC = {"dense-10k": 59.63e6}
+WALK_TRAFFIC = {"dense-10k": 59.88e6}
 # work[] counters of the stored node-filter results (csrc/dem_device.cuh).
 W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS = 8, 9, 10
 
