@@ -851,53 +851,91 @@ __global__ void k_survivorList(const __grid_constant__ Params P) {
     }
 }
 // Exact query, one thread per kept survivor.
+__device__ __forceinline__ void recordHit(const Res& r, uint32_t s, const SurvivorNode& v, float4 pd, float4 na) {
+    r.hitScratch[2 * s] = pd;
+    r.hitScratch[2 * s + 1] = na;
+    atomicOr(v.slot < WARP ? &r.candHitMask[v.item].x : &r.candHitMask[v.item].y, 1u << (v.slot & 31u));
+    atomicAdd(&r.candHitCount[v.item], 1u);
+}
+// Exact queries of a list built every step (margin 0 or the learned culler):
+// one seeded walk per node.
 __global__ void __launch_bounds__(256) k_nodeWalk(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
     if (r.control[0] != 0) return;
     uint32_t n = min(r.work[W_KEPT], c.survivorCapacity);
-    // A stored list keeps its slots from step to step, and each slot keeps a
-    // certificate: the nearest triangle T found by a certifying walk at the
-    // point p0, and a gap g below which no other triangle's distance lies
-    // above T's.  Distances are 1-Lipschitz in the point, so while
-    // 2 |p - p0| + slack < g, T is still the unique nearest triangle at p and
-    // the walk would record it with the values closestTriangle gives for it:
-    // the step evaluates T alone.  Otherwise it walks, certifying again.  The
-    // slack, 1e-5 (1 + |p|_1), covers the FP32 rounding of the distances.
-    bool certify = storedKeep(c);
-    float reach = __fadd_rn(__fmul_rn(2.01f, __uint_as_float(r.work[W_FILTER_MARGIN])), 1e-4f);
     for (uint32_t t = gtid(); t < n; t += gstride()) {
         uint32_t s = r.walkList[t];
         SurvivorNode v = survivorNode(r, s);
-        float4 pd, na, f;
+        float4 pd, na;
         uint32_t shape = r.shapeId[v.dst];
-        if (certify) {
-            uint32_t triangle = r.walkCertTriangle[t];
-            bool known = false;
-            if (triangle != EMPTY) {
-                float4 cp = r.walkCertPoint[t];
-                float slack = __fmul_rn(1e-5f, __fadd_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(v.local.x), fabsf(v.local.y)),
-                                                                        fabsf(v.local.z))));
-                known = __fadd_rn(__fmul_rn(2.002f, length(v.local - xyz(cp))), slack) < cp.w;
-            }
+        // Seed the walk with the triangle nearest to the node's grid cell.
+        float4 f = meshDistance(r, shape, v.local, false, gridSeed(r, shape, v.local));
+        if (nodeContactFrom(r, c, v.src, v.dst, v.node, v.arm, f, pd, na)) recordHit(r, s, v, pd, na);
+    }
+}
+// Exact queries of a stored list.  A stored list keeps its slots from step
+// to step, and each slot keeps a certificate: the nearest triangle T found by
+// a certifying walk at the point p0, and a gap g below which no other
+// triangle's distance lies above T's.  Distances are 1-Lipschitz in the
+// point, so while 2 |p - p0| + slack < g, T is still the unique nearest
+// triangle at p and the walk would record it with the values closestTriangle
+// gives for it: the step evaluates T alone.  The slack, 1e-5 (1 + |p|_1),
+// covers the FP32 rounding of the distances.  The other slots are flagged
+// (survKeep, unused by a stored list while it is walked), listed in slot
+// order -- the walk-bucket order, so that a warp's walks stay coherent -- and
+// walked by k_nodeWalkSlow in full warps.
+__global__ void __launch_bounds__(256) k_nodeWalkKnown(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = min(r.work[W_KEPT], c.survivorCapacity);
+    for (uint32_t t = gtid(); t < n; t += gstride()) {
+        uint32_t triangle = r.walkCertTriangle[t];
+        bool known = false;
+        if (triangle != EMPTY) {
+            uint32_t s = r.walkList[t];
+            SurvivorNode v = survivorNode(r, s);
+            float4 cp = r.walkCertPoint[t];
+            float slack = __fmul_rn(1e-5f, __fadd_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(v.local.x), fabsf(v.local.y)),
+                                                                    fabsf(v.local.z))));
+            known = __fadd_rn(__fmul_rn(2.002f, length(v.local - xyz(cp))), slack) < cp.w;
             if (known) {
-                f = meshDistanceAt(r, v.local, triangle);
-            } else {
-                float gap;
-                f = meshDistanceCertified(r, shape, v.local, gridSeed(r, shape, v.local), reach, triangle, gap);
-                r.walkCertTriangle[t] = triangle;
-                r.walkCertPoint[t] = w4(v.local, gap);
+                float4 pd, na;
+                float4 f = meshDistanceAt(r, v.local, triangle);
+                if (nodeContactFrom(r, c, v.src, v.dst, v.node, v.arm, f, pd, na)) recordHit(r, s, v, pd, na);
             }
-        } else {
-            // Seed the walk with the triangle nearest to the node's grid cell.
-            f = meshDistance(r, shape, v.local, false, gridSeed(r, shape, v.local));
         }
-        if (nodeContactFrom(r, c, v.src, v.dst, v.node, v.arm, f, pd, na)) {
-            r.hitScratch[2 * s] = pd;
-            r.hitScratch[2 * s + 1] = na;
-            atomicOr(v.slot < WARP ? &r.candHitMask[v.item].x : &r.candHitMask[v.item].y, 1u << (v.slot & 31u));
-            atomicAdd(&r.candHitCount[v.item], 1u);
-        }
+        r.survKeep[t] = known ? 0u : 1u;
+    }
+}
+// The flagged slots in slot order (into walkKey, unused between builds).
+__global__ void k_slowList(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = min(r.work[W_KEPT], c.survivorCapacity);
+    for (uint32_t t = gtid(); t < n; t += gstride())
+        if (r.survKeep[t]) r.walkKey[r.keepOffset[t]] = t;
+}
+// A certifying walk for each listed slot, recording its new certificate.
+__global__ void __launch_bounds__(256) k_nodeWalkSlow(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = min(r.work[W_SLOW], c.survivorCapacity);
+    float reach = __fadd_rn(__fmul_rn(2.01f, __uint_as_float(r.work[W_FILTER_MARGIN])), 1e-4f);
+    for (uint32_t i = gtid(); i < n; i += gstride()) {
+        uint32_t t = r.walkKey[i];
+        uint32_t s = r.walkList[t];
+        SurvivorNode v = survivorNode(r, s);
+        uint32_t shape = r.shapeId[v.dst], triangle;
+        float gap;
+        float4 pd, na;
+        float4 f = meshDistanceCertified(r, shape, v.local, gridSeed(r, shape, v.local), reach, triangle, gap);
+        r.walkCertTriangle[t] = triangle;
+        r.walkCertPoint[t] = w4(v.local, gap);
+        if (nodeContactFrom(r, c, v.src, v.dst, v.node, v.arm, f, pd, na)) recordHit(r, s, v, pd, na);
     }
 }
 // Copies the hits of each item from their survivor slots to their canonical
@@ -1480,8 +1518,20 @@ static void collectFilter(const Params& P, cudaStream_t s) {
 }
 // The exact queries.
 static void collectWalk(const Params& P, cudaStream_t s) {
-    if (P.c.meshGeometry == 0) k_sdfEmit<<<grid(P.c.queryBlocksPerSM, 8), 256, 0, s>>>(P);
-    else k_nodeWalk<<<grid(P.c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (c.meshGeometry == 0) {
+        k_sdfEmit<<<grid(c.queryBlocksPerSM, 8), 256, 0, s>>>(P);
+    } else if (c.filterMargin > 0.0f && c.cullerEnabled == 0) {
+        uint32_t g = grid(c.walkBlocksPerSM, 8);
+        k_nodeWalkKnown<<<g, 256, 0, s>>>(P);
+        launch_scan(r.survKeep, r.keepOffset, ScanCount{r.work + W_KEPT, c.survivorCapacity, 1, 0}, true,
+                    r.work + W_SLOW, nullptr, r.scanPartials, s);
+        k_slowList<<<g, 256, 0, s>>>(P);
+        k_nodeWalkSlow<<<g, 256, 0, s>>>(P);
+    } else {
+        k_nodeWalk<<<grid(c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
+    }
 }
 static void collectQuery(const Params& P, cudaStream_t s) {
     collectFilter(P, s);
