@@ -408,7 +408,11 @@ __device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 
 // the cap B = (sqrt(d_seed) + reach)^2: it records the triangle the walk
 // records and returns, in `gap`, a lower bound of (distance to every other
 // triangle) - (distance to it), or 0 when a triangle ties it.  Only gaps up
-// to about `reach` are found.  `triangle` receives the recorded triangle.
+// to about `reach` are found.  `triangle` receives the recorded triangle; a
+// triangle that ties it exactly in the same BVH leaf (two faces meeting at
+// an edge) is not counted against the gap but returned as a partner, in the
+// top two bits (its offset after it in the leaf): between the two, the walk
+// records the partner only where it is strictly nearer.
 __device__ __forceinline__ float4 meshDistanceCertified(const Res& r, uint32_t shape, f3 p, uint32_t seed, float reach,
                                                         uint32_t& triangle, float& gap) {
     uint32_t root = __ldg(&r.meshRoots[shape].x);
@@ -428,7 +432,7 @@ __device__ __forceinline__ float4 meshDistanceCertified(const Res& r, uint32_t s
     }
     float best = cap, second = cap;
     f3 nearest = mk(0.f, 0.f, 0.f);
-    uint32_t nearestNormal = 0;
+    uint32_t nearestNormal = 0, bestNode = 0xFFFFFFFFu, partner = 0;
     bool found = false;
     while (top > 0) {
         uint32_t slot = --top, node = pending[slot];
@@ -456,23 +460,40 @@ __device__ __forceinline__ float4 meshDistanceCertified(const Res& r, uint32_t s
             if (distance < best) {
                 second = best;
                 best = distance; nearest = q; nearestNormal = 7 * t + feature; found = true;
+                bestNode = node;
+                partner = 0;
+            } else if (distance == best && found && node == bestNode && partner == 0) {
+                partner = t - nearestNormal / 7;  // 1..3: later in the same leaf
             } else if (distance < second) {
                 second = distance;
             }
         }
     }
-    triangle = found ? nearestNormal / 7 : 0xFFFFFFFFu;
+    triangle = found ? (nearestNormal / 7) | (partner << 30) : 0xFFFFFFFFu;
     gap = found ? __fsub_rn(__fsqrt_rn(second), __fsqrt_rn(best)) : 0.f;
     return distanceResult(r, p, best, nearest, nearestNormal, found, false);
 }
-// The walk's result when `triangle` is known to be the unique nearest: the
-// same closest point, squared distance and feature the walk records for it.
-__device__ __forceinline__ float4 meshDistanceAt(const Res& r, f3 p, uint32_t triangle) {
-    uint32_t feature;
+// The walk's result when the certified triangle (and its same-leaf partner,
+// encoded as by meshDistanceCertified) are known to be nearer than every
+// other: the same closest point, squared distance and feature the walk
+// records -- the partner's only where it is strictly nearer, as the leaf's
+// triangles are taken in order.
+__device__ __forceinline__ float4 meshDistanceAt(const Res& r, f3 p, uint32_t certified) {
+    uint32_t triangle = certified & 0x3FFFFFFFu, partner = certified >> 30, feature;
     f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * triangle])), xyz(__ldg(&r.meshTriangles[3 * triangle + 1])),
                            xyz(__ldg(&r.meshTriangles[3 * triangle + 2])), feature);
     f3 dq = p - q;
-    return distanceResult(r, p, dot(dq, dq), q, 7 * triangle + feature, true, false);
+    float best = dot(dq, dq);
+    uint32_t normal = 7 * triangle + feature;
+    if (partner != 0) {
+        uint32_t other = triangle + partner, otherFeature;
+        f3 q2 = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * other])), xyz(__ldg(&r.meshTriangles[3 * other + 1])),
+                                xyz(__ldg(&r.meshTriangles[3 * other + 2])), otherFeature);
+        f3 dq2 = p - q2;
+        float d2 = dot(dq2, dq2);
+        if (d2 < best) { best = d2; q = q2; normal = 7 * other + otherFeature; }
+    }
+    return distanceResult(r, p, best, q, normal, true, false);
 }
 // solver.slang:259-272.  With `grow` > 0 the root box and every hull plane
 // are moved out by that distance (unit normals): the test then admits every
