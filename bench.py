@@ -70,9 +70,10 @@ WORKLOADS = {
                            pairs_per_particle=8, contacts_per_particle=256, strain_rate_per_s=0.0),
 }
 DATA = ROOT / "sand_atlas_dem_gb300" / "data"
-# DRAM bytes (read + write) of one k_nodeWalk launch from an ncu capture of
-# the same workload (profiles/walk-dense-10k.md); None where not captured.
-WALK_TRAFFIC = {"dense-10k": 59.88e6}
+# DRAM bytes (read + write) of one step's exact queries (k_nodeWalkKnown and
+# k_nodeWalkSlow) from an ncu capture of the same workload
+# (profiles/walk-dense-10k.md); None where not captured.
+WALK_TRAFFIC = {"dense-10k": 74.51e6}
 # work[] counters of the stored node-filter results (csrc/dem_device.cuh).
 W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS = 8, 9, 10
 
@@ -348,7 +349,8 @@ def run_gb300(args, cpu=True):
     lib_bytes = sum(a.nbytes for k, a in e.layout.geometry.items() if k.startswith("mesh") or k == "sample")
     step_bytes, query_bytes, walk_bytes = algorithmic_bytes(w.grains, pairs, contacts, items, nodes, survivors,
                                                             kept, 0, lib_bytes)
-    kernel_name = "k_nodeWalk (exact BVH queries, one thread per kept node)"
+    kernel_name = ("k_nodeWalkKnown + k_nodeWalkSlow (exact queries: certified triangles, then full BVH walks)"
+                   if e.filter_margin > 0 and e.culler is None else "k_nodeWalk (exact BVH queries, one thread per kept node)")
     group_name = "k_nodeFilter, k_survivorList, k_survivorPrefilter, k_walkList, k_nodeWalk + scans"
     if e.sdf:
         # SDF emit (k_sdfEmit, one warp per pair), counted at its minimum:
