@@ -75,7 +75,7 @@ DATA = ROOT / "sand_atlas_dem_gb300" / "data"
 # (profiles/walk-dense-10k.md); None where not captured.
 WALK_TRAFFIC = {"dense-10k": 74.51e6}
 # work[] counters of the stored node-filter results (csrc/dem_device.cuh).
-W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS = 8, 9, 10
+W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS, W_CERTIFIED = 8, 9, 10, 15
 
 
 def log(*args):
@@ -328,7 +328,8 @@ def run_gb300(args, cpu=True):
     filter_cache = {"margin": e.filter_margin,
                     "adapted_margin": float(work1[W_FILTER_MARGIN:W_FILTER_MARGIN + 1].view(np.float32)[0]),
                     "builds_in_timed_steps": int(work1[W_FILTER_BUILDS] - work0[W_FILTER_BUILDS]),
-                    "timed_steps": int(work1[W_FILTER_STEPS] - work0[W_FILTER_STEPS])}
+                    "timed_steps": int(work1[W_FILTER_STEPS] - work0[W_FILTER_STEPS]),
+                    "certified_queries_per_step": float(work1[W_CERTIFIED] - work0[W_CERTIFIED]) / args.steps}
     device_s = sum(step_ms) / 1e3
     value = w.grains * args.steps / device_s
     kernels = e.lib.sdg_engine_kernels_per_step(e._native)

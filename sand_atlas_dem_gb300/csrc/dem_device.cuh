@@ -156,6 +156,7 @@ constexpr int W_FILTER_AGE = 11;    // collector runs since they were built
 constexpr int W_FILTER_NEXT = 12;   // margin a build of this step uses (float bits)
 constexpr int W_FILTER_BASE = 13;   // configured margin they were built under (float bits)
 constexpr int W_SLOW = 14;          // stored walk slots left for a full walk this step
+constexpr int W_CERTIFIED = 15;     // exact queries answered by a certificate (counter)
 
 struct Params {
     Config c;

@@ -924,6 +924,7 @@ __global__ void __launch_bounds__(256) k_nodeWalkSlow(const __grid_constant__ Pa
     const Config& c = P.c;
     if (r.control[0] != 0) return;
     uint32_t n = min(r.work[W_SLOW], c.survivorCapacity);
+    if (gtid() == 0) r.work[W_CERTIFIED] += min(r.work[W_KEPT], c.survivorCapacity) - n;
     float reach = __fadd_rn(__fmul_rn(2.01f, __uint_as_float(r.work[W_FILTER_MARGIN])), 1e-4f);
     for (uint32_t i = gtid(); i < n; i += gstride()) {
         uint32_t t = r.walkKey[i];
