@@ -11,7 +11,7 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 130) this backend's extension buffers, in the order of
+ *   [77, 134) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
@@ -40,7 +40,10 @@
  *             contact counts per virtual lane of the reference's 64-lane
  *             group, 32 words per pair, and per stored walk-list slot its
  *             nearest-triangle certificate: the point it was taken at with
- *             the distance gap, and the triangle).
+ *             the distance gap, and the triangle, and with planes the
+ *             plane-contact count of each (wall, grain), wall-major, its
+ *             exclusive scan, and the first contact of each (wall, grain)
+ *             on the side being written and on the committed side).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
@@ -76,7 +79,7 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 130
+#define SDG_BUFFER_COUNT 134
 #define SDG_VALUE_COUNT 39
 #define SDG_PHASES 9
 
@@ -96,9 +99,11 @@ const char* sdg_last_error(void);
  * src/sand_atlas_dem/backend.py:9-121.  Names: beginStep, advanceCell,
  * checkRebuild, finishStep, captureContactKinematics, checkContactTimestep,
  * diagnosticRows, fabricRows, neighbours (clearBins..emitPairs + Scan),
- * collect (resetMeshContacts, prepareMeshPairs, collectMeshFrontiers),
- * collectCull / collectQuery / collectEmit (its three parts),
- * resolveContacts (friction history + contact law), gather, and the
+ * collect (resetMeshContacts, prepareMeshPairs, collectMeshFrontiers,
+ * collectWallContacts), collectCull / collectQuery / collectEmit /
+ * collectWalls (its parts), resolveContacts (friction history + contact
+ * law, grain and plane contacts), gather, gatherWallRows, advanceWalls,
+ * refreshWallPower (solver.slang:669-687, :834-856, :950-955), and the
  * sequences forces / forcesNoCapture (Engine.forces, gpu.py:547-565) and
  * step (Engine._advance_once body, gpu.py:714-724).  `count` is the thread
  * count of per-element kernels (N grains, pairCapacity, ...).
@@ -115,6 +120,16 @@ int sdg_dispatch(const char* kernel, uint32_t count, void* const* buffers, const
  */
 int sdg_reduce_rows(const void* input, void* output, uint32_t n, uint32_t rows, int32_t max_row,
                     void* stream);
+
+/*
+ * One level of the per-wall reduction of the (wall, grain) rows (reaction |
+ * contact count, moment | power, work; 3 float4 per row, wall-major, n rows
+ * per wall): output holds ceil(n / 256) row sets per wall, the count summed
+ * as an integer.  Replaces the reference's reduceWallRows
+ * (src/sand_atlas_dem/shaders/diagnostic.slang:33-49) of Engine.diagnostics
+ * (gpu.py:774-786).
+ */
+int sdg_reduce_wall_rows(const void* input, void* output, uint32_t n, uint32_t walls, void* stream);
 
 /*
  * Device-wide exclusive scan of n uint32 values: out[i] = in[0] + ... +

@@ -469,6 +469,7 @@ bool nodeContactSdf(R& r, uint32_t src, uint32_t dst, uint32_t node, float4& pd,
 
 // ---------------------------------------------------------------- kernels
 
+float wallStepWork(R& r, uint32_t id, float dt);
 // solver.slang:858-888
 void beginStep(R& r, uint32_t id) {
     if (id >= r.c.N || r.control[0] != 0) return;
@@ -481,7 +482,8 @@ void beginStep(R& r, uint32_t id) {
     compensated3(l, ll, 0.5f * dt * xyz(r.torque[id]));
     float loss = -expm1Stable(-r.c.drag * dt) *
                  (0.5f * r.body[id].y * dot(v + vl, v + vl) + rotationalEnergy(r, id, l + ll));
-    accumulate(r, id, float4{0, loss, 0.5f * dt * cellPower(r, id), 0.0f});
+    float cp = 0.5f * dt * cellPower(r, id);
+    accumulate(r, id, float4{0, loss, cp, wallStepWork(r, id, 0.5f * dt)});
     float damping = expm1Stable(-0.5f * r.c.drag * dt);
     compensated3(v, vl, damping * (v + vl));
     compensated3(l, ll, damping * (l + ll));
@@ -539,7 +541,8 @@ void finishStep(R& r, uint32_t id) {
     compensated3(l, ll, 0.5f * r.c.dt * xyz(r.torque[id]));
     float loss = -expm1Stable(-r.c.drag * r.c.dt) *
                  (0.5f * r.body[id].y * dot(v + vl, v + vl) + rotationalEnergy(r, id, l + ll));
-    accumulate(r, id, float4{0, loss, 0.5f * r.c.dt * cellPower(r, id), 0.0f});
+    float cp = 0.5f * r.c.dt * cellPower(r, id);
+    accumulate(r, id, float4{0, loss, cp, wallStepWork(r, id, 0.5f * r.c.dt)});
     float damping = expm1Stable(-0.5f * r.c.drag * r.c.dt);
     compensated3(v, vl, damping * (v + vl));
     compensated3(l, ll, damping * (l + ll));
@@ -859,6 +862,172 @@ void exhaustiveContacts(R& r) {
         }
     }
 }
+// ------------------------------------------------------------------ planes
+// solver.slang:578-595: error-free two-sums (the materialisation mask
+// rounded1 is the identity while control[15] is zero).
+struct Sum2 { float hi, lo; };
+inline Sum2 wallTwoSum(float a, float b) {
+    float high = a + b, v = high - a;
+    float low = (a - (high - v)) + (b - v);
+    return {high, low};
+}
+inline Sum2 wallAdd(Sum2 a, float b) {
+    Sum2 sum = wallTwoSum(a.hi, b);
+    return wallTwoSum(sum.hi, sum.lo + a.lo);
+}
+inline Sum2 wallAddDot(Sum2 sum, float3 a, float3 b) {
+    float3 product = a * b;
+    float3 error{std::fma(a.x, b.x, -product.x), std::fma(a.y, b.y, -product.y), std::fma(a.z, b.z, -product.z)};
+    for (uint32_t axis = 0; axis < 3; ++axis) {
+        sum = wallAdd(sum, comp(product, axis));
+        sum = wallAdd(sum, comp(error, axis));
+    }
+    return sum;
+}
+// solver.slang:596-604: the plane's signed offset at the grain centre.
+Sum2 wallCentreDistance(R& r, uint32_t body, uint32_t wall) {
+    float4 plane = r.wallPlane[wall], low = r.wallRemainder[wall];
+    float3 p = xyz(r.position[body]), pl = xyz(r.positionRemainder[body]);
+    Sum2 sum{-plane.w, -low.w};
+    sum = wallAddDot(sum, xyz(plane), p);
+    sum = wallAddDot(sum, xyz(plane), pl);
+    sum = wallAddDot(sum, xyz(low), p);
+    return wallAddDot(sum, xyz(low), pl);
+}
+// solver.slang:605-610
+float localWallDistance(R& r, uint32_t body, uint32_t wall, float3 arm) {
+    Sum2 sum = wallCentreDistance(r, body, wall);
+    sum = wallAddDot(sum, xyz(r.wallPlane[wall]), arm);
+    sum = wallAddDot(sum, xyz(r.wallRemainder[wall]), arm);
+    return sum.hi + sum.lo;
+}
+// solver.slang:613-624
+bool wallClusterMayContact(R& r, uint32_t body, uint32_t wall, uint32_t cluster) {
+    float3 low = xyz(r.meshClusterMin[cluster]), high = xyz(r.meshClusterMax[cluster]);
+    float4 plane = r.wallPlane[wall];
+    float3 normal = qinv(r.rotation[body], xyz(plane)) * r.body[body].x;
+    float3 center = 0.5f * (low + high), half = 0.5f * (high - low);
+    Sum2 centreDistance = wallCentreDistance(r, body, wall);
+    float base = centreDistance.hi + centreDistance.lo;
+    float support = dot(normal, center) - dot(abs3(normal), half);
+    float pad = 64.0f * 1.1920928955078125e-7f *
+                (((1.0f + std::fabs(plane.w)) + length(xyz(r.position[body]))) +
+                 length(normal) * (length(center) + length(half)));
+    return base + support <= pad;
+}
+// solver.slang:625-638 (serial append)
+void appendWallContact(R& r, uint32_t body, uint32_t wall, uint32_t node) {
+    float4 point = r.sample[r.sampleInfo[r.shapeId[body]].x + node];
+    float3 arm = qrot(r.rotation[body], xyz(point) * r.body[body].x);
+    float4 plane = r.wallPlane[wall];
+    float phi = localWallDistance(r, body, wall, arm);
+    if (!std::isfinite(phi)) { fail(r, 512); return; }
+    if (phi >= 0) return;
+    if (-phi > r.c.maxOverlap * r.body[body].w) fail(r, 4);
+    uint32_t offset = r.control[2]++;
+    if (offset >= r.c.contactCapacity) { fail(r, 32); return; }
+    r.meta[offset] = uint4{body, r.c.N + wall, node, 1};
+    r.pointDepth[offset] = f4(arm, -phi);
+    r.normalArea[offset] = f4(xyz(plane), point.w * r.body[body].x * r.body[body].x);
+}
+// cpu_scheduling.slang:133-154: one (wall, grain) per id, wall-major; nodes
+// in order (SDF geometry) or the grain's sample clusters in preorder.
+void collectWallContacts(R& r, uint32_t id) {
+    uint32_t body = id % r.c.N, wall = id / r.c.N;
+    if (wall >= r.c.wallCount || r.control[0] != 0) return;
+    float4 plane = r.wallPlane[wall];
+    Sum2 centreDistance = wallCentreDistance(r, body, wall);
+    float phi = centreDistance.hi + centreDistance.lo;
+    float pad = 64.0f * 1.1920928955078125e-7f * ((1.0f + length(xyz(r.position[body]))) + std::fabs(plane.w));
+    if (phi > r.body[body].z + pad) return;
+    if (r.c.meshGeometry == 0) {
+        uint32_t count = r.sampleInfo[r.shapeId[body]].y;
+        for (uint32_t node = 0; node < count; ++node) appendWallContact(r, body, wall, node);
+        return;
+    }
+    uint4 info = r.meshClusterInfo[r.shapeId[body]];
+    uint32_t cluster = info.x;
+    while (cluster < info.x + info.y) {
+        bool candidate = wallClusterMayContact(r, body, wall, cluster);
+        uint4 range = r.meshClusterRanges[cluster];
+        if (candidate)
+            for (uint32_t lane = 0; lane < range.y; ++lane)
+                appendWallContact(r, body, wall, r.meshSampleIndices[range.x + lane]);
+        cluster = candidate ? cluster + 1 : range.z;
+    }
+}
+// solver.slang:669-687 (one thread)
+void advanceWalls(R& r) {
+    if (r.control[0] != 0) return;
+    for (uint32_t w = 0; w < r.c.wallCount; ++w) {
+        float4 plane = r.wallPlane[w], residual = r.wallRemainder[w];
+        float3 high{plane.w, 0, 0}, low{residual.w, 0, 0};
+        compensated3(high, low, f3(dot(xyz(plane), xyz(r.wallVelocity[w])) * r.c.dt, 0, 0));
+        plane.w = high.x;
+        residual.w = low.x;
+        if (!std::isfinite(high.x) || !std::isfinite(low.x)) { fail(r, 512); return; }
+        r.wallPlane[w] = plane;
+        r.wallRemainder[w] = residual;
+    }
+    if (r.c.wallBoxEnabled != 0) {
+        for (uint32_t axis = 0; axis < 3; ++axis) {
+            uint32_t lo = r.wallBoxIds[2 * axis], hi = r.wallBoxIds[2 * axis + 1];
+            float low = r.wallPlane[lo].w + r.wallRemainder[lo].w;
+            float high = -(r.wallPlane[hi].w + r.wallRemainder[hi].w);
+            if (low < 0 || high > comp(xyz(r.cell[0]), axis) || high <= low) fail(r, 4096);
+        }
+    }
+}
+// solver.slang:135-146: half-step wall work per (wall, grain) row.
+float wallStepWork(R& r, uint32_t id, float dt) {
+    float total = 0;
+    for (uint32_t w = 0; w < r.c.wallCount; ++w) {
+        uint32_t index = w * r.c.N + id;
+        float increment = dt * r.wallRows[3 * index + 1].w;
+        float4 state = r.wallAccumulated[index];
+        float3 high{state.x, 0, 0}, low{state.y, 0, 0};
+        compensated3(high, low, f3(increment, 0, 0));
+        r.wallAccumulated[index] = float4{high.x, low.x, 0, 0};
+        r.wallRows[3 * index + 2] = float4{high.x + low.x, 0, 0, 0};
+        total = total + increment;
+    }
+    return total;
+}
+// solver.slang:834-856
+void gatherWallRows(R& r, uint32_t index) {
+    if (index >= r.c.N * r.c.wallCount || r.control[0] != 0) return;
+    uint32_t body = index % r.c.N, wall = index / r.c.N, count = 0, visited = 0;
+    float3 reaction{0, 0, 0}, moment{0, 0, 0};
+    float power = 0;
+    uint32_t entry = r.heads[body];
+    while (entry != EMPTY) {
+        if (visited++ > 2 * r.c.contactCapacity) { fail(r, 128); return; }
+        uint32_t contact = entry / 2;
+        if (r.meta[contact].y == r.c.N + wall) {
+            float3 force = xyz(r.contactForce[contact]);
+            float3 point = (xyz(r.position[body]) + xyz(r.positionRemainder[body])) + xyz(r.pointDepth[contact]);
+            reaction = reaction - force;
+            moment = moment - cross(point, force);
+            power = power + dot(force, xyz(r.wallVelocity[wall]));
+            count++;
+        }
+        entry = r.next[entry];
+    }
+    float4 work = r.wallAccumulated[index];
+    float bits;
+    std::memcpy(&bits, &count, 4);
+    r.wallRows[3 * index] = f4(reaction, bits);
+    r.wallRows[3 * index + 1] = f4(moment, power);
+    r.wallRows[3 * index + 2] = float4{work.x + work.y, 0, 0, 0};
+}
+// solver.slang:950-955
+void refreshWallPower(R& r, uint32_t index) {
+    if (index >= r.c.N * r.c.wallCount) return;
+    float4 value = r.wallRows[3 * index + 1];
+    value.w = -dot(xyz(r.wallRows[3 * index]), xyz(r.wallVelocity[index / r.c.N]));
+    r.wallRows[3 * index + 1] = value;
+}
+
 // solver.slang:689-696
 inline uint32_t hashKey(R& r, uint4 key) {
     uint32_t h = key.x * 73856093u ^ key.y * 19349663u ^ key.z * 83492791u;
@@ -883,21 +1052,47 @@ NormalResponse normalResponse(float depth, float area, float normalVelocity, flo
     value.lossPower = mx(0.0f, (elastic - value.force) * normalVelocity);
     return value;
 }
+// plane.slang:6-36: one-sided penalty plane with Coulomb slip.
+struct PlaneResponse { float4 forceEnergy, slipLoss; bool sliding; float normalLossPower; };
+PlaneResponse planeViscousResponse(float3 normal, float signedDistance, float area, float3 relativeVelocity,
+                                   float3 oldSlip, float kn, float kt, float mu, float viscosity, float dt) {
+    PlaneResponse value{{0, 0, 0, 0}, {0, 0, 0, 0}, false, 0};
+    if (signedDistance >= 0) return value;
+    float depth = -signedDistance;
+    float3 tangent = relativeVelocity - normal * dot(relativeVelocity, normal);
+    float3 trial = oldSlip - normal * dot(oldSlip, normal) + dt * tangent;
+    float3 slip = trial;
+    NormalResponse response = normalResponse(depth, area, dot(relativeVelocity, normal), kn, viscosity, 1.0f);
+    float fn = response.force;
+    value.normalLossPower = response.lossPower;
+    float3 ft = -kt * area * slip;
+    float magnitude = length(ft);
+    if (magnitude > mu * fn && magnitude > 0) {
+        value.sliding = true;
+        ft = ft * (mu * fn / magnitude);
+        slip = -ft / (kt * area);
+    }
+    value.forceEnergy = f4(fn * normal + ft, 0.5f * area * (kn * depth * depth + kt * dot(slip, slip)));
+    value.slipLoss = f4(slip, mx(0.0f, -dot(ft, trial - slip)));
+    return value;
+}
 // solver.slang:697-701
 void clearContactStorage(R& r, uint32_t id) {
     if (id < r.c.hashSize) r.hash[id] = EMPTY;
     if (id < r.c.N) r.heads[id] = EMPTY;
 }
 inline uint32_t activeContacts(R& r) { return r.control[2] < r.c.contactCapacity ? r.control[2] : r.c.contactCapacity; }
-// solver.slang:702-749 (particle-particle branch; planes are outside this oracle)
+// solver.slang:702-749
 void resolveContacts(R& r, uint32_t id) {
     if (id >= activeContacts(r) || r.control[0] != 0) return;
     uint4 key = r.meta[id];
     uint32_t i = key.x, j = key.y;
     float3 n = xyz(r.normalArea[id]);
+    bool wall = j >= r.c.N;
     float viscosity = r.c.normalViscosity;
+    if (wall) viscosity = r.wallMaterial[j - r.c.N].w;
     float3 wi = viscosity > 0 ? xyz(r.forceOmega[i]) : omega(r, i), wj{0, 0, 0};
-    wj = viscosity > 0 ? xyz(r.forceOmega[j]) : omega(r, j);
+    if (!wall) wj = viscosity > 0 ? xyz(r.forceOmega[j]) : omega(r, j);
     float3 elastic{0, 0, 0};
     uint32_t slot = hashKey(r, key);
     if (r.c.historyStep != 0) {
@@ -913,6 +1108,26 @@ void resolveContacts(R& r, uint32_t id) {
         }
     }
     float3 arm = xyz(r.pointDepth[id]);
+    if (wall) {
+        uint32_t w = j - r.c.N;
+        float4 material = r.wallMaterial[w];
+        float3 v = viscosity > 0 ? xyz(r.forceVelocity[i]) : xyz(r.velocity[i]) + xyz(r.velocityRemainder[i]);
+        float3 rv = v + cross(wi, arm) - xyz(r.wallVelocity[w]);
+        PlaneResponse response = planeViscousResponse(n, -r.pointDepth[id].w, r.normalArea[id].w, rv, elastic,
+                                                      material.x, material.y, material.z, material.w, r.c.dt);
+        r.slip[id] = response.slipLoss;
+        r.contactForce[id] = response.forceEnergy;
+        r.normalLossPower[id] = response.normalLossPower;
+        float4 fe = response.forceEnergy;
+        if (!std::isfinite(fe.x) || !std::isfinite(fe.y) || !std::isfinite(fe.z) || !std::isfinite(fe.w) ||
+            !std::isfinite(response.normalLossPower)) { fail(r, 512); return; }
+        if (response.sliding) r.control[6]++;
+        uint32_t oldHead = r.heads[i];
+        r.heads[i] = 2 * id;
+        r.next[2 * id] = oldHead;
+        r.next[2 * id + 1] = EMPTY;
+        return;
+    }
     float3 branch = centerBranch(r, i, j);
     float3 translation = xyz(r.velocity[i]) - xyz(r.velocity[j]);
     if (viscosity > 0) translation = xyz(r.forceVelocity[i]) - xyz(r.forceVelocity[j]);
@@ -971,12 +1186,29 @@ void gather(R& r, uint32_t id) {
         float3 force = xyz(r.contactForce[contact]);
         float3 arm = xyz(r.pointDepth[contact]);
         if (r.c.activeTimestep != 0) {
+            bool wall = key.y >= r.c.N;
             float3 localArm = source ? arm : arm - centerBranch(r, key.x, key.y);
             float mobility = 1.0f / r.body[id].y + dot(localArm, localArm) * inverseInertia;
-            float area = r.normalArea[contact].w * 0.5f;
-            float coupling = 2.0f;
-            stiffnessRate = stiffnessRate + coupling * area * (r.c.kn * (1.0f + r.c.mu) + r.c.kt) * mobility;
-            viscousRate = viscousRate + coupling * area * r.c.normalViscosity * (1.0f + r.c.mu) * mobility;
+            float4 material{r.c.kn, r.c.kt, r.c.mu, r.c.normalViscosity};
+            if (wall) material = r.wallMaterial[key.y - r.c.N];
+            float area = r.normalArea[contact].w * (wall ? 1.0f : 0.5f);
+            float coupling = wall ? 1.0f : 2.0f;
+            stiffnessRate = stiffnessRate + coupling * area * (material.x * (1.0f + material.z) + material.y) * mobility;
+            viscousRate = viscousRate + coupling * area * material.w * (1.0f + material.z) * mobility;
+        }
+        if (key.y >= r.c.N) {
+            compensated3(f, fLow, force);
+            compensated3(t, tLow, cross(arm, force));
+            stress0 = stress0 - force.x * arm;
+            stress1 = stress1 - force.y * arm;
+            stress2 = stress2 - force.z * arm;
+            energy = energy + r.contactForce[contact].w;
+            denom = denom + length(force);
+            maxDepth = mx(maxDepth, r.pointDepth[contact].w / r.body[key.x].w);
+            dissipation = dissipation + r.slip[contact].w;
+            normalPower = normalPower + r.normalLossPower[contact];
+            entry = r.next[entry];
+            continue;
         }
         float3 branch = centerBranch(r, key.x, key.y);
         compensated3(f, fLow, source ? force : -force);
@@ -1007,7 +1239,7 @@ void gather(R& r, uint32_t id) {
     r.particleDiagnostic[id] = float4{kinetic, energy, length(f), denom};
     accumulate(r, id, float4{dissipation, 0, 0, 0});
 }
-// solver.slang:815-832 (plane-free)
+// solver.slang:815-832
 void checkContactTimestep(R& r, uint32_t id) {
     if (id >= r.c.N || r.control[0] != 0 || r.c.dt == 0) return;
     float dt = r.c.dt;
@@ -1019,6 +1251,7 @@ void checkContactTimestep(R& r, uint32_t id) {
                               dot(abs3(xyz(r.invI[3 * id + 2])), one));
     float spin = inverseInertia * (length(xyz(r.momentum[id]) + xyz(r.momentumRemainder[id])) + dt * length(xyz(r.torque[id])));
     float wallSpeed = 0;
+    for (uint32_t w = 0; w < r.c.wallCount; ++w) wallSpeed = mx(wallSpeed, length(xyz(r.wallVelocity[w])));
     float motion = dt * (speed + r.body[id].z * spin + wallSpeed);
     bool finite = std::isfinite(rx) && std::isfinite(ry) && std::isfinite(motion) && std::isfinite(spin);
     if (!finite) { fail(r, 512); return; }
@@ -1090,6 +1323,10 @@ extern "C" int oracle_dispatch(const char* name, uint32_t count, void** buffers,
     else if (k == "buildHistoryHash") each(buildHistoryHash);
     else if (k == "gather") each(gather);
     else if (k == "checkContactTimestep") each(checkContactTimestep);
+    else if (k == "collectWallContacts") each(collectWallContacts);
+    else if (k == "gatherWallRows") each(gatherWallRows);
+    else if (k == "advanceWalls") advanceWalls(r);
+    else if (k == "refreshWallPower") each(refreshWallPower);
     else if (k == "diagnosticRows") each(diagnosticRows);
     else if (k == "fabricRows") each(fabricRows);
     // Probes (entry-point uniforms after the Config scalars).
@@ -1116,6 +1353,26 @@ extern "C" int oracle_dispatch(const char* name, uint32_t count, void** buffers,
             meshPairBounds(r, direction, first + id, lo, hi);
             result[2 * id] = f4(lo, 0);
             result[2 * id + 1] = f4(hi, 0);
+        }
+    } else if (k == "planeProbe") {  // plane.slang:44-64: N; normal; offset, kn, kt, mu, dt
+        float3 normal{float(r.uni[1]), float(r.uni[2]), float(r.uni[3])};
+        float offset = float(r.uni[4]), kn = float(r.uni[5]), kt = float(r.uni[6]), mu = float(r.uni[7]);
+        float dt = float(r.uni[8]);
+        float4* pointArea = static_cast<float4*>(r.extra[0]);
+        float4* relativeVelocity = static_cast<float4*>(r.extra[1]);
+        float4* oldSlipActive = static_cast<float4*>(r.extra[2]);
+        float4* forceEnergy = static_cast<float4*>(r.extra[3]);
+        float4* slipLoss = static_cast<float4*>(r.extra[4]);
+        float4* torqueActive = static_cast<float4*>(r.extra[5]);
+        for (uint32_t id = 0; id < count; ++id) {
+            float4 point = pointArea[id];
+            float phi = dot(normal, xyz(point)) - offset;
+            float3 old = oldSlipActive[id].w != 0 ? xyz(oldSlipActive[id]) : float3{0, 0, 0};
+            PlaneResponse value = planeViscousResponse(normal, phi, point.w, xyz(relativeVelocity[id]), old, kn, kt,
+                                                       mu, 0.0f, dt);
+            forceEnergy[id] = value.forceEnergy;
+            slipLoss[id] = value.slipLoss;
+            torqueActive[id] = f4(cross(xyz(point), xyz(value.forceEnergy)), phi < 0 ? 1.0f : 0.0f);
         }
     } else if (k == "normalProbe") {  // normal.slang:166-174: stiffness, viscosity, weight
         float stiffness = float(r.uni[1]), viscosity = float(r.uni[2]), weight = float(r.uni[3]);

@@ -24,6 +24,7 @@ from sand_atlas_dem_gb300.model import (
     DAMPING_STATE,
     RESOURCE_ORDER,
     STATE_NAMES,
+    WALL_STATE,
     HostLayout,
     RejectedStep,
 )
@@ -116,10 +117,8 @@ class OracleEngine:
         b["pointDepth"] = _zeros4(cc)
         b["contactForce"] = _zeros4(cc)
         b["normalLossPower"] = np.zeros(cc, np.float32)
-        for name in ("wallPlane", "wallRemainder", "wallVelocity", "wallMaterial", "wallAccumulated",
-                     "wallRows"):
-            b[name] = _zeros4(1)
-        b["wallBoxIds"] = np.zeros(6, np.uint32)
+        self.wall_count = h.wall_count
+        b.update({k: v.copy() for k, v in h.walls.items()})
         self.buffers = b
         self.sides = [
             {
@@ -178,14 +177,15 @@ class OracleEngine:
             self.dispatch("scanContacts", 1, c)
             self.dispatch("contactTotal", 1, c)
             self.dispatch("emitContacts", pc, c)
-            return
-        if exhaustive:
+        elif exhaustive:
             self.dispatch("exhaustiveContacts", 1, c)
-            return
-        self.dispatch("resetMeshContacts", pc, c)
-        self.dispatch("prepareMeshPairs", pc, c)
-        ctrl = self.buffers["control"]
-        self.dispatch("collectMeshFrontiers", int(min(ctrl[1], pc)), c)
+        else:
+            self.dispatch("resetMeshContacts", pc, c)
+            self.dispatch("prepareMeshPairs", pc, c)
+            ctrl = self.buffers["control"]
+            self.dispatch("collectMeshFrontiers", int(min(ctrl[1], pc)), c)
+        if self.wall_count:  # gpu.py:544-545
+            self.dispatch("collectWallContacts", self.n * self.wall_count, c)
 
     def friction(self, c):
         self.dispatch("clearContactStorage", max(self.n, self.hash_size), c)
@@ -199,6 +199,8 @@ class OracleEngine:
         self.collect(c, exhaustive)
         self.friction(c)
         self.dispatch("gather", self.n, c)
+        if self.wall_count:
+            self.dispatch("gatherWallRows", self.n * self.wall_count, c)
         if self.spec.timestep_policy == "active-contact":
             self.dispatch("checkContactTimestep", self.n, c)
 
@@ -207,6 +209,8 @@ class OracleEngine:
             self.dispatch("checkContactTimestep", self.n, c)
         self.dispatch("beginStep", self.n, c)
         self.dispatch("advanceCell", 1, c)
+        if self.wall_count:
+            self.dispatch("advanceWalls", 1, c)
         self.dispatch("checkRebuild", self.n, c)
 
     def check_errors(self):
@@ -240,13 +244,24 @@ class OracleEngine:
                 s[k][...] = v
         self.active, self.history = active, history
 
-    def advance(self, steps, *, rate=(0, 0, 0), drag=0.0, exhaustive=False):
+    def advance(self, steps, *, rate=(0, 0, 0), drag=0.0, exhaustive=False, wall_velocities=None):
         if type(steps) is not int or steps < 0:
             raise ValueError("Nonnegative integer step count required")
         if steps < 1:
             return
         snap = self._snapshot()
         self.buffers["cell"][1, :3] = np.asarray(rate, float) * self.time_unit
+        if wall_velocities is not None:  # gpu.py:682-713
+            old = self.buffers["wallVelocity"].copy()
+            new = np.zeros((self.wall_count, 4), np.float32)
+            new[:, :3] = np.asarray(wall_velocities, float) * self.time_unit / self.length_unit
+            self.buffers["wallVelocity"][...] = new
+            if any(p.get("normal_viscosity", 0) > 0 for p in self.spec.planes) and not np.array_equal(old, new):
+                self.forces(self.config(dt=0, drag=drag))
+                self.active = 1 - self.active
+                self.history = True
+            else:
+                self.dispatch("refreshWallPower", self.n * self.wall_count, self.config(drag=drag))
         for _ in range(steps):
             c = self.config(drag=drag)
             self.begin(c)
@@ -277,6 +292,9 @@ class OracleEngine:
         out["contacts"] = count
         for name in ("meta", "slip", "normalArea"):
             out[name] = side[name][:count].copy()
+        if self.wall_count:
+            for name in WALL_STATE:
+                out[name] = self.buffers[name].copy()
         return out
 
     def restore(self, state, step):
@@ -284,6 +302,9 @@ class OracleEngine:
             self.buffers[name][...] = state[name] if self.viscous else 0
         for name in STATE_NAMES:
             self.buffers[name][...] = np.asarray(state[name], self.buffers[name].dtype)
+        if self.wall_count:
+            for name in WALL_STATE:
+                self.buffers[name][...] = np.asarray(state[name], np.float32)
         count = int(state["contacts"])
         if count < 0 or count > self.contact_capacity:
             raise ValueError("Checkpoint contact count is outside capacity")
@@ -316,6 +337,36 @@ class OracleEngine:
         rows = tree_reduce(self.buffers["diagnosticRows"].reshape(self.n, 8, 4), max_field=(4, 3))
         fabric = tree_reduce(self.buffers["fabricRows"].reshape(self.pair_capacity, 2, 4))
         return rows, fabric
+
+    def wall_rows(self):
+        """Per-wall (reaction | count, moment | power, work) rows reduced over
+        the grains in the reference tree order (``diagnostic.slang:33-49``)."""
+        rows = self.buffers["wallRows"].reshape(self.wall_count, self.n, 3, 4)
+        return np.stack([wall_tree_reduce(rows[w]) for w in range(self.wall_count)])
+
+
+def wall_tree_reduce(values):
+    """``reduceWallRows``: 256-wide tree sums with the contact count in row 0's
+    w carried as an integer."""
+    values = np.array(values, np.float32)
+    while len(values) > 1:
+        n = len(values)
+        groups = (n + 255) // 256
+        out = np.zeros((groups, 3, 4), np.float32)
+        for g in range(groups):
+            block = np.zeros((256, 3, 4), np.float32)
+            block[: min(256, n - 256 * g)] = values[256 * g : 256 * g + 256]
+            counts = block[:, 0, 3].copy().view(np.uint32)
+            block[:, 0, 3] = 0
+            step = 128
+            while step:
+                block[:step] += block[step : 2 * step]
+                counts[:step] += counts[step : 2 * step]
+                step //= 2
+            block[0, 0, 3] = counts[:1].view(np.float32)[0]
+            out[g] = block[0]
+        values = out
+    return values[0]
 
 
 def tree_reduce(values, max_field=None):

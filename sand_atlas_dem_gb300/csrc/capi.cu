@@ -65,8 +65,12 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
         return 1;
     }
     if (c.specimens == 0) { g_error = "at least one specimen required"; return 1; }
-    if (c.N == 0 || c.wallCount != 0) {
-        g_error = "the GB300 step needs N > 0 and no planes";
+    if (c.N == 0) {
+        g_error = "the GB300 step needs N > 0";
+        return 1;
+    }
+    if (c.wallCount != 0 && (c.specimens != 1 || c.periodic != 0)) {
+        g_error = "planes bound a single nonperiodic specimen";
         return 1;
     }
     if (c.meshGeometry == 0 && c.sourceSurfaceNormal != 0) {
@@ -93,7 +97,16 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
             bytes[77 + 48] < (uint64_t(c.shapes) * WALK_BUCKETS + 1) * 4 ||
             bytes[77 + 49] < (uint64_t(c.shapes) * WALK_BUCKETS + 1) * 4 ||
             (c.meshGeometry == 0 && bytes[77 + 50] < uint64_t(c.pairCapacity) * 32 * 4) ||
-            bytes[77 + 51] < uint64_t(c.survivorCapacity) * 16 || bytes[77 + 52] < uint64_t(c.survivorCapacity) * 4) {
+            bytes[77 + 51] < uint64_t(c.survivorCapacity) * 16 || bytes[77 + 52] < uint64_t(c.survivorCapacity) * 4 ||
+            (c.wallCount != 0 &&
+             (bytes[70] < uint64_t(c.wallCount) * 16 || bytes[71] < uint64_t(c.wallCount) * 16 ||
+              bytes[72] < uint64_t(c.wallCount) * 16 || bytes[73] < uint64_t(c.wallCount) * 16 ||
+              (c.wallBoxEnabled != 0 && bytes[74] < 6 * 4) ||
+              bytes[75] < uint64_t(c.wallCount) * c.N * 48 || bytes[76] < uint64_t(c.wallCount) * c.N * 16 ||
+              bytes[77 + 53] < uint64_t(c.wallCount) * c.N * 4 ||
+              bytes[77 + 54] < (uint64_t(c.wallCount) * c.N + 1) * 4 ||
+              bytes[77 + 55] < (uint64_t(c.wallCount) * c.N + 1) * 4 ||
+              bytes[77 + 56] < (uint64_t(c.wallCount) * c.N + 1) * 4))) {
             g_error = "a buffer is smaller than its configured capacity";
             return 1;
         }
@@ -113,6 +126,7 @@ void launch_forces(const Params& P, cudaStream_t s, bool captureKinematics) {
     launch_contacts("collect", P, 0, s);
     launch_contacts("resolveContacts", P, 0, s);
     launch_contacts("gather", P, c.N, s);
+    launch_contacts("gatherWallRows", P, c.N, s);
     if (c.activeTimestep) launch_state("checkContactTimestep", P, c.N, s);
 }
 
@@ -125,6 +139,7 @@ void launch_step(const Params& P, cudaStream_t s) {
     B.c.viscousCapture = c.normalViscosity > 0 ? 1u : 0u;
     launch_state("beginStep", B, c.N, s);
     launch_state("advanceCell", P, c.specimens, s);
+    if (c.wallCount) launch_state("advanceWalls", P, 1, s);
     launch_state("checkRebuild", P, c.N, s);
     launch_forces(P, s, false);
     launch_state("finishStep", P, c.N, s);
@@ -141,6 +156,7 @@ static Params swapSides(const Params& P) {
     std::swap(*reinterpret_cast<void**>(&r.sidePairOffsets), *reinterpret_cast<void**>(const_cast<uint32_t**>(&r.oldPairOffsets)));
     std::swap(*reinterpret_cast<void**>(&r.sidePairB), *reinterpret_cast<void**>(const_cast<uint32_t**>(&r.oldPairB)));
     std::swap(*reinterpret_cast<void**>(&r.sideContactStart), *reinterpret_cast<void**>(const_cast<uint32_t**>(&r.oldContactStart)));
+    std::swap(*reinterpret_cast<void**>(&r.sideWallStart), *reinterpret_cast<void**>(const_cast<uint32_t**>(&r.oldWallStart)));
     return Q;
 }
 
@@ -230,6 +246,7 @@ int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes
     B.c.viscousCapture = c.normalViscosity > 0 ? 1u : 0u;
     launch_state("beginStep", B, c.N, s);
     launch_state("advanceCell", P, c.specimens, s);
+    if (c.wallCount) launch_state("advanceWalls", P, 1, s);
     launch_state("checkRebuild", P, c.N, s);
     cudaEventRecord(ev[1], s);
     launch_contacts("neighbours", P, c.N, s);
@@ -241,10 +258,12 @@ int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes
     launch_contacts("collectWalk", P, 0, s);
     cudaEventRecord(ev[5], s);
     launch_contacts("collectEmit", P, 0, s);
+    launch_contacts("collectWalls", P, 0, s);
     cudaEventRecord(ev[6], s);
     launch_contacts("resolveContacts", P, 0, s);
     cudaEventRecord(ev[7], s);
     launch_contacts("gather", P, c.N, s);
+    launch_contacts("gatherWallRows", P, c.N, s);
     if (c.activeTimestep) launch_state("checkContactTimestep", P, c.N, s);
     cudaEventRecord(ev[8], s);
     launch_state("finishStep", P, c.N, s);
@@ -260,6 +279,14 @@ int sdg_reduce_rows(const void* input, void* output, uint32_t n, uint32_t rows, 
     launch_reduce_rows(static_cast<const float4*>(input), static_cast<float4*>(output), n, rows, max_row,
                        static_cast<cudaStream_t>(stream));
     return record(cudaGetLastError(), "reduce rows");
+}
+
+// Per-wall tree sums of the (wall, grain) rows, one level (diagnostic.slang:33-49).
+int sdg_reduce_wall_rows(const void* input, void* output, uint32_t n, uint32_t walls, void* stream) {
+    if (!input || !output || walls == 0 || n == 0) { g_error = "bad wall reduction arguments"; return 1; }
+    launch_reduce_wall_rows(static_cast<const float4*>(input), static_cast<float4*>(output), n, walls,
+                            static_cast<cudaStream_t>(stream));
+    return record(cudaGetLastError(), "reduce wall rows");
 }
 
 // Exclusive scan of n uint32 values (the reference's hierarchical Scan,

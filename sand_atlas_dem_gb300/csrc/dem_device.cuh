@@ -21,7 +21,7 @@ constexpr int RESOURCE_COUNT = 77;
 enum Flag : uint32_t {
     F_DEGENERATE = 2, F_PENETRATION = 4, F_BIN = 8, F_PAIR = 16, F_CONTACT = 32, F_HASH = 64,
     F_CYCLE = 128, F_IMAGE = 256, F_NONFINITE = 512, F_STACK = 1024, F_ESCAPE = 2048,
-    F_TIMESTEP = 8192, F_COINCIDENT = 16384, F_WAIT = 65536
+    F_BOX = 4096, F_TIMESTEP = 8192, F_COINCIDENT = 16384, F_WAIT = 65536
 };
 
 struct Config {
@@ -132,8 +132,12 @@ struct Res {
     uint32_t* sdfLaneCounts;          // SDF geometry, 32 x pairCapacity: contacts of virtual lanes l and l + 32
     float4* walkCertPoint;            // survivorCapacity: per stored walk slot, where its certificate was taken, and the gap
     uint32_t* walkCertTriangle;       // survivorCapacity: its certified nearest triangle (EMPTY: none)
+    uint32_t* wallCounts;             // wallCount x N: plane contacts of each (wall, grain), wall-major
+    uint32_t* wallOffsets;            // wallCount x N + 1: their exclusive scan
+    uint32_t* sideWallStart;          // wallCount x N + 1: first contact of each (wall, grain), side being written
+    const uint32_t* oldWallStart;     // wallCount x N + 1: the same on the committed side
 };
-constexpr int EXTENSION_COUNT = 53;
+constexpr int EXTENSION_COUNT = 57;
 constexpr uint32_t WALK_CELLS = 24;  // coarse cells per axis of a shape's grid box for the walk order
 constexpr uint32_t WALK_BUCKETS = WALK_CELLS * WALK_CELLS * WALK_CELLS;
 constexpr uint32_t GRID = 48;  // cells per axis of each shape's distance-bound grid
@@ -157,6 +161,7 @@ constexpr int W_FILTER_NEXT = 12;   // margin a build of this step uses (float b
 constexpr int W_FILTER_BASE = 13;   // configured margin they were built under (float bits)
 constexpr int W_SLOW = 14;          // stored walk slots left for a full walk this step
 constexpr int W_CERTIFIED = 15;     // exact queries answered by a certificate (counter)
+constexpr int W_WALL_BASE = 16;     // first plane contact: the grain-grain contact total
 
 struct Params {
     Config c;
@@ -722,5 +727,55 @@ __device__ __forceinline__ uint32_t activeContacts(const Res& r, const Config& c
 }
 __device__ __forceinline__ uint32_t gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
 __device__ __forceinline__ uint32_t gstride() { return gridDim.x * blockDim.x; }
+
+// ------------------------------------------------------------------ planes
+// Error-free two-sums of the plane offsets (solver.slang:578-595; the
+// materialisation mask is zero, so its rounding barriers are identities).
+struct Sum2 { float hi, lo; };
+__device__ __forceinline__ Sum2 wallTwoSum(float a, float b) {
+    float high = __fadd_rn(a, b), v = __fsub_rn(high, a);
+    return {high, __fadd_rn(__fsub_rn(a, __fsub_rn(high, v)), __fsub_rn(b, v))};
+}
+__device__ __forceinline__ Sum2 wallAdd(Sum2 a, float b) {
+    Sum2 sum = wallTwoSum(a.hi, b);
+    return wallTwoSum(sum.hi, __fadd_rn(sum.lo, a.lo));
+}
+__device__ __forceinline__ Sum2 wallAddDot(Sum2 sum, f3 a, f3 b) {
+    float px = __fmul_rn(a.x, b.x), py = __fmul_rn(a.y, b.y), pz = __fmul_rn(a.z, b.z);
+    sum = wallAdd(sum, px);
+    sum = wallAdd(sum, __fmaf_rn(a.x, b.x, -px));
+    sum = wallAdd(sum, py);
+    sum = wallAdd(sum, __fmaf_rn(a.y, b.y, -py));
+    sum = wallAdd(sum, pz);
+    return wallAdd(sum, __fmaf_rn(a.z, b.z, -pz));
+}
+// Signed offset of the grain centre from the plane, never forming a
+// world-space surface point (solver.slang:596-604).
+__device__ __forceinline__ Sum2 wallCentreDistance(const Res& r, uint32_t body, uint32_t wall) {
+    float4 plane = r.wallPlane[wall], low = r.wallRemainder[wall];
+    f3 p = xyz(r.position[body]), pl = xyz(r.positionRemainder[body]);
+    Sum2 sum{-plane.w, -low.w};
+    sum = wallAddDot(sum, xyz(plane), p);
+    sum = wallAddDot(sum, xyz(plane), pl);
+    sum = wallAddDot(sum, xyz(low), p);
+    return wallAddDot(sum, xyz(low), pl);
+}
+// Half-step work of every wall on grain id, added to its compensated
+// per-(wall, grain) total (solver.slang:135-146).
+__device__ __forceinline__ float wallStepWork(const Res& r, const Config& c, uint32_t id, float dt) {
+    float total = 0.f;
+    for (uint32_t w = 0; w < c.wallCount; ++w) {
+        uint32_t index = w * c.N + id;
+        float increment = __fmul_rn(dt, r.wallRows[3 * index + 1].w);
+        float4 state = r.wallAccumulated[index];
+        float y = __fadd_rn(increment, state.y);
+        float high = __fadd_rn(state.x, y);
+        float low = __fsub_rn(y, __fsub_rn(high, state.x));
+        r.wallAccumulated[index] = make_float4(high, low, 0.f, 0.f);
+        r.wallRows[3 * index + 2] = make_float4(__fadd_rn(high, low), 0.f, 0.f, 0.f);
+        total = __fadd_rn(total, increment);
+    }
+    return total;
+}
 
 }  // namespace sdg

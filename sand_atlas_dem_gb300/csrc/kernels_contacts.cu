@@ -1186,12 +1186,244 @@ __device__ __forceinline__ uint32_t historySlot(const Res& r, const Config& c, u
     }
     return EMPTY;
 }
+// ------------------------------------------------------------------ planes
+// Signed distance of a grain surface point (centre + arm) from the plane
+// (solver.slang:605-610), from the centre's two-sum.
+__device__ __forceinline__ float localWallDistance(const Res& r, uint32_t wall, Sum2 centre, f3 arm) {
+    Sum2 sum = wallAddDot(centre, xyz(r.wallPlane[wall]), arm);
+    sum = wallAddDot(sum, xyz(r.wallRemainder[wall]), arm);
+    return __fadd_rn(sum.hi, sum.lo);
+}
+// solver.slang:613-624: whether any node of a sample cluster can reach
+// behind the plane (fixed-normal support bound with an FP32 pad).
+__device__ __forceinline__ bool wallClusterMayContact(const Res& r, uint32_t body, uint32_t wall, float base,
+                                                      uint32_t cluster) {
+    f3 low = xyz(__ldg(&r.meshClusterMin[cluster])), high = xyz(__ldg(&r.meshClusterMax[cluster]));
+    float4 plane = r.wallPlane[wall];
+    f3 normal = qinv(r.rotation[body], xyz(plane)) * r.body[body].x;
+    f3 center = 0.5f * (low + high), half = 0.5f * (high - low);
+    float support = __fsub_rn(dot(normal, center), dot(abs3(normal), half));
+    float pad = __fmul_rn(__fmul_rn(64.0f, 1.1920928955078125e-7f),
+                          __fadd_rn(__fadd_rn(__fadd_rn(1.0f, fabsf(plane.w)), length(xyz(r.position[body]))),
+                                    __fmul_rn(length(normal), __fadd_rn(length(center), length(half)))));
+    return __fadd_rn(base, support) <= pad;
+}
+// solver.slang:625-638: node `node` of grain `body` behind the plane, with
+// its record (arm and depth; plane normal and node area).  `flag` raises the
+// non-finite and penetration flags (once per step: in the counting pass).
+__device__ __forceinline__ bool wallNode(const Res& r, const Config& c, uint32_t body, uint32_t wall, Sum2 centre,
+                                        uint32_t node, bool flag, float4& pd, float4& na) {
+    float4 point = __ldg(&r.sample[__ldg(&r.sampleInfo[r.shapeId[body]].x) + node]);
+    float4 b = r.body[body];
+    f3 arm = qrot(r.rotation[body], xyz(point) * b.x);
+    float phi = localWallDistance(r, wall, centre, arm);
+    if (!isfinite(phi)) {
+        if (flag) fail(r, F_NONFINITE);
+        return false;
+    }
+    if (phi >= 0) return false;
+    if (flag && -phi > __fmul_rn(c.maxOverlap, b.w)) fail(r, F_PENETRATION);
+    pd = w4(arm, -phi);
+    na = w4(xyz(r.wallPlane[wall]), __fmul_rn(__fmul_rn(point.w, b.x), b.x));
+    return true;
+}
+// The plane contacts of one (wall, grain) item in the reference CPU
+// collector's order (cpu_scheduling.slang:133-154): the grain's nodes in
+// order (SDF geometry), or its sample clusters in preorder -- a cluster the
+// plane cannot reach skips its subtree -- and each visited cluster's nodes in
+// order (mesh geometry).  One warp, 32 nodes per round, order kept by ballot
+// ranks; counted, or written from `slot` on.  Returns the count.
+__device__ uint32_t wallItem(const Res& r, const Config& c, uint32_t item, bool emit, uint32_t slot) {
+    uint32_t body = item % c.N, wall = item / c.N, lane = laneId();
+    float4 plane = r.wallPlane[wall];
+    Sum2 centre = wallCentreDistance(r, body, wall);
+    float phi = __fadd_rn(centre.hi, centre.lo);
+    float pad = __fmul_rn(__fmul_rn(64.0f, 1.1920928955078125e-7f),
+                          __fadd_rn(__fadd_rn(1.0f, length(xyz(r.position[body]))), fabsf(plane.w)));
+    if (phi > __fadd_rn(r.body[body].z, pad)) return 0;
+    uint32_t shape = r.shapeId[body], count = 0;
+    auto visit = [&](bool valid, uint32_t node) {
+        float4 pd, na;
+        bool hit = valid && wallNode(r, c, body, wall, centre, node, !emit, pd, na);
+        uint32_t mask = __ballot_sync(0xffffffffu, hit);
+        if (emit && hit) {
+            uint32_t out = slot + count + __popc(mask & ((1u << lane) - 1u));
+            if (out >= c.contactCapacity) {
+                fail(r, F_CONTACT);
+            } else {
+                r.meta[out] = make_uint4(body, c.N + wall, node, 1u);
+                r.pointDepth[out] = pd;
+                r.normalArea[out] = na;
+            }
+        }
+        count += __popc(mask);
+    };
+    if (c.meshGeometry == 0) {
+        uint32_t nodes = __ldg(&r.sampleInfo[shape].y);
+        for (uint32_t base = 0; base < nodes; base += WARP) visit(base + lane < nodes, base + lane);
+        return count;
+    }
+    uint4 info = __ldg(&r.meshClusterInfo[shape]);
+    uint32_t cluster = info.x;
+    // Escape links point forward, so each cluster is visited at most once.
+    for (uint32_t guard = 0; cluster < info.x + info.y && guard < info.y; ++guard) {
+        bool candidate = wallClusterMayContact(r, body, wall, phi, cluster);
+        uint4 range = __ldg(&r.meshClusterRanges[cluster]);
+        if (candidate)
+            for (uint32_t base = 0; base < range.y; base += WARP) {
+                uint32_t k = base + lane;
+                visit(k < range.y, k < range.y ? __ldg(&r.meshSampleIndices[range.x + k]) : 0u);
+            }
+        cluster = candidate ? cluster + 1 : range.z;
+    }
+    return count;
+}
+// Plane contacts per (wall, grain), wall-major; records where they start.
+__global__ void k_wallCount(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    if (gtid() == 0) r.work[W_WALL_BASE] = r.control[2];
+    uint32_t items = c.N * c.wallCount;
+    for (uint32_t item = warpGlobal(); item < items; item += warpStride()) {
+        uint32_t n = wallItem(r, c, item, false, 0);
+        if (laneId() == 0) r.wallCounts[item] = n;
+    }
+}
+// The plane contacts appended after the grain-grain ones (gpu.py:544-545),
+// per-(wall, grain) starts and the new contact total.
+__global__ void k_wallEmit(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t items = c.N * c.wallCount, base = r.work[W_WALL_BASE];
+    for (uint32_t i = gtid(); i <= items; i += gstride()) r.sideWallStart[i] = base + r.wallOffsets[i];
+    if (gtid() == 0) {
+        uint32_t total = base + r.wallOffsets[items];
+        r.control[2] = total;
+        if (total > c.contactCapacity) fail(r, F_CONTACT);
+    }
+    for (uint32_t item = warpGlobal(); item < items; item += warpStride())
+        if (r.wallCounts[item] != 0) wallItem(r, c, item, true, base + r.wallOffsets[item]);
+}
+// Within one (wall, grain) run, the order of a node's contact: its position in
+// the grain's cluster order (mesh) or its index (SDF).
+__device__ __forceinline__ uint32_t wallKey(const Res& r, const Config& c, uint32_t body, uint32_t node) {
+    return c.meshGeometry == 0 ? node : __ldg(&r.meshSampleRank[__ldg(&r.sampleInfo[r.shapeId[body]].x) + node]);
+}
+// Slot of the committed plane contact (body, wall, node), or EMPTY: binary
+// search of the committed (wall, grain) run.
+__device__ __forceinline__ uint32_t wallHistorySlot(const Res& r, const Config& c, uint32_t body, uint32_t wall,
+                                                    uint32_t node) {
+    uint32_t item = wall * c.N + body;
+    uint32_t lo = r.oldWallStart[item], end = r.oldWallStart[item + 1], hi = end;
+    uint32_t key = wallKey(r, c, body, node);
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (wallKey(r, c, body, r.oldMeta[mid].z) < key) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo < end) {
+        uint4 m = r.oldMeta[lo];
+        if (m.x == body && m.y == c.N + wall && m.z == node) return lo;
+    }
+    return EMPTY;
+}
+// solver.slang:702-733 with plane.slang:13-36: a plane contact.
+__device__ __forceinline__ void resolveWall(const Res& r, const Config& c, uint32_t id, uint4 key) {
+    uint32_t i = key.x, w = key.y - c.N;
+    float4 m = r.wallMaterial[w];
+    float viscosity = m.w;
+    f3 nrm = xyz(r.normalArea[id]);
+    f3 wi = viscosity > 0 ? xyz(r.forceOmega[i]) : omegaOf(r, i);
+    f3 elastic = mk(0.f, 0.f, 0.f);
+    if (c.historyStep != 0) {
+        uint32_t old = wallHistorySlot(r, c, i, w, key.z);
+        if (old != EMPTY)
+            elastic = transported(xyz(r.oldSlip[old]), xyz(r.oldNormal[old]), nrm,
+                                  __fmul_rn(__fmul_rn(0.5f, dot(wi + mk(0.f, 0.f, 0.f), nrm)), c.dt));
+    }
+    f3 arm = xyz(r.pointDepth[id]);
+    f3 v = viscosity > 0 ? xyz(r.forceVelocity[i]) : xyz(r.velocity[i]) + xyz(r.velocityRemainder[i]);
+    f3 rv = (v + cross(wi, arm)) - xyz(r.wallVelocity[w]);
+    float4 forceEnergy = make_float4(0.f, 0.f, 0.f, 0.f), slipLoss = forceEnergy;
+    float lossPower = 0.f;
+    bool sliding = false;
+    float signedDistance = -r.pointDepth[id].w, area = r.normalArea[id].w;
+    if (signedDistance < 0) {
+        float depth = -signedDistance;
+        f3 tangent = rv - nrm * dot(rv, nrm);
+        f3 trial = (elastic - nrm * dot(elastic, nrm)) + c.dt * tangent;
+        f3 slip = trial;
+        float fn;
+        normalResponse(depth, area, dot(rv, nrm), m.x, viscosity, 1.0f, fn, lossPower);
+        f3 ft = __fmul_rn(-m.y, area) * slip;
+        float magnitude = length(ft);
+        if (magnitude > __fmul_rn(m.z, fn) && magnitude > 0) {
+            sliding = true;
+            ft = ft * __fdiv_rn(__fmul_rn(m.z, fn), magnitude);
+            slip = (-ft) / __fmul_rn(m.y, area);
+        }
+        forceEnergy = w4(fn * nrm + ft, __fmul_rn(__fmul_rn(0.5f, area), __fadd_rn(__fmul_rn(__fmul_rn(m.x, depth), depth),
+                                                                               __fmul_rn(m.y, dot(slip, slip)))));
+        slipLoss = w4(slip, mx(0.0f, -dot(ft, trial - slip)));
+    }
+    r.slip[id] = slipLoss;
+    r.contactForce[id] = forceEnergy;
+    r.normalLossPower[id] = lossPower;
+    if (!isfinite(forceEnergy.x) || !isfinite(forceEnergy.y) || !isfinite(forceEnergy.z) || !isfinite(forceEnergy.w) ||
+        !isfinite(lossPower)) {
+        fail(r, F_NONFINITE);
+        return;
+    }
+    if (sliding) atomicAdd(&r.control[6], 1u);
+}
+// solver.slang:834-856: per (wall, grain), the reaction, its moment about
+// the origin and the wall power over the grain's contacts with that wall, in
+// its linked-list order (descending contact id), and the accumulated work.
+__global__ void k_gatherWallRows(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t items = c.N * c.wallCount;
+    for (uint32_t item = gtid(); item < items; item += gstride()) {
+        uint32_t body = item % c.N, wall = item / c.N;
+        uint32_t lo = r.sideWallStart[item], hi = r.sideWallStart[item + 1];
+        f3 centre = xyz(r.position[body]) + xyz(r.positionRemainder[body]);
+        f3 velocity = xyz(r.wallVelocity[wall]);
+        f3 reaction = mk(0.f, 0.f, 0.f), moment = reaction;
+        float power = 0.f;
+        for (uint32_t k = hi; k > lo; --k) {
+            f3 force = xyz(r.contactForce[k - 1]);
+            f3 point = centre + xyz(r.pointDepth[k - 1]);
+            reaction = reaction - force;
+            moment = moment - cross(point, force);
+            power = __fadd_rn(power, dot(force, velocity));
+        }
+        float4 work = r.wallAccumulated[item];
+        r.wallRows[3 * item] = w4(reaction, __uint_as_float(hi - lo));
+        r.wallRows[3 * item + 1] = w4(moment, power);
+        r.wallRows[3 * item + 2] = make_float4(__fadd_rn(work.x, work.y), 0.f, 0.f, 0.f);
+    }
+}
+
+// solver.slang:702-733: the plane contacts, after the grain-grain ones.
+__global__ void k_resolveWalls(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = activeContacts(r, c);
+    for (uint32_t id = min(r.work[W_WALL_BASE], n) + gtid(); id < n; id += gstride()) resolveWall(r, c, id, r.meta[id]);
+}
 // solver.slang:702-749 (particle-particle contacts)
 __global__ void k_resolve(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
     if (r.control[0] != 0) return;
     uint32_t n = activeContacts(r, c);
+    // With planes, the grain-grain contacts end where the plane contacts
+    // begin; those are resolved by k_resolveWalls.
+    if (c.wallCount != 0) n = min(n, r.work[W_WALL_BASE]);
     for (uint32_t id = gtid(); id < n; id += gstride()) {
         uint4 key = r.meta[id];
         uint32_t i = key.x, j = key.y;
@@ -1259,6 +1491,62 @@ __device__ __forceinline__ f3 shfl3(f3 v, int lane) {
     return mk(__shfl_sync(0xffffffffu, v.x, lane), __shfl_sync(0xffffffffu, v.y, lane),
               __shfl_sync(0xffffffffu, v.z, lane));
 }
+// Lane `chain` replays its accumulator chain over the `count` terms of one
+// round, in order (compensated sums, subtracted stress rows, maximum depth,
+// plain sums; the timestep rates only under the active-contact policy).
+__device__ __forceinline__ void replayChain(float (*terms)[GATHER_STRIDE], uint32_t count, uint32_t chain, bool rates,
+                                            float& acc, float& accLow) {
+    if (chain < 6) {
+        for (uint32_t k = 0; k < count; ++k) {  // compensated3, one component
+            float y = __fadd_rn(terms[chain][k], accLow);
+            float nx = __fadd_rn(acc, y);
+            accLow = __fsub_rn(y, __fsub_rn(nx, acc));
+            acc = nx;
+        }
+    } else if (chain < 15) {
+        for (uint32_t k = 0; k < count; ++k) acc = __fsub_rn(acc, terms[chain][k]);
+    } else if (chain == 17) {
+        for (uint32_t k = 0; k < count; ++k) acc = mx(acc, terms[chain][k]);
+    } else if (chain < GATHER_CHAINS && (chain < 20 || rates)) {
+        for (uint32_t k = 0; k < count; ++k) acc = __fadd_rn(acc, terms[chain][k]);
+    }
+}
+__device__ __forceinline__ void storeTerms(float (*terms)[GATHER_STRIDE], uint32_t lane, const GatherTerms& g) {
+    const float v[GATHER_CHAINS] = {g.force.x, g.force.y, g.force.z, g.torque.x, g.torque.y, g.torque.z,
+                                    g.s0.x, g.s0.y, g.s0.z, g.s1.x, g.s1.y, g.s1.z,
+                                    g.s2.x, g.s2.y, g.s2.z, g.energy, g.denom, g.depth,
+                                    g.dissipation, g.normalPower, g.stiffness, g.viscous};
+#pragma unroll
+    for (uint32_t j = 0; j < GATHER_CHAINS; ++j) terms[j][lane] = v[j];
+}
+// solver.slang:773-791, the plane branch: full force, moment about the
+// grain centre, virial with the arm, full energy and losses; the wall's own
+// material in the timestep rates with coupling 1.
+__device__ __forceinline__ GatherTerms wallTerms(const Res& r, const Config& c, uint32_t contact, uint32_t wall,
+                                                 float mass, float bw, float inverseInertia) {
+    GatherTerms g{};
+    float4 cf = r.contactForce[contact], pdv = r.pointDepth[contact];
+    f3 force = xyz(cf), arm = xyz(pdv);
+    if (c.activeTimestep != 0) {
+        float mobility = __fadd_rn(__fdiv_rn(1.0f, mass), __fmul_rn(dot(arm, arm), inverseInertia));
+        float4 m = r.wallMaterial[wall];
+        float area = __fmul_rn(1.0f, r.normalArea[contact].w);
+        float friction = __fadd_rn(1.0f, m.z);
+        g.stiffness = __fmul_rn(__fmul_rn(area, __fadd_rn(__fmul_rn(m.x, friction), m.y)), mobility);
+        g.viscous = __fmul_rn(__fmul_rn(__fmul_rn(area, m.w), friction), mobility);
+    }
+    g.force = force;
+    g.torque = cross(arm, force);
+    g.s0 = force.x * arm;
+    g.s1 = force.y * arm;
+    g.s2 = force.z * arm;
+    g.energy = cf.w;
+    g.denom = length(force);
+    g.depth = __fdiv_rn(pdv.w, bw);
+    g.dissipation = r.slip[contact].w;
+    g.normalPower = r.normalLossPower[contact];
+    return g;
+}
 // Three CTAs of 256 per SM (at most 80 registers): measured faster than the
 // unbounded 101-register build (two CTAs) and than four CTAs (spills).
 __global__ void __launch_bounds__(256, 3) k_gather(const __grid_constant__ Params P) {
@@ -1281,6 +1569,19 @@ __global__ void __launch_bounds__(256, 3) k_gather(const __grid_constant__ Param
         float inverseInertia = mx(mx(dot(abs3(xyz(r.invI[3 * id])), one), dot(abs3(xyz(r.invI[3 * id + 1])), one)),
                                   dot(abs3(xyz(r.invI[3 * id + 2])), one));
         float m_ = r.body[id].y, bw = r.body[id].w;
+        // Plane contacts come first in the grain's list: they were appended
+        // last (highest wall first, each run from its last contact).
+        for (uint32_t w = c.wallCount; w-- > 0;) {
+            uint32_t lo = r.sideWallStart[w * c.N + id], hi = r.sideWallStart[w * c.N + id + 1];
+            while (hi > lo) {
+                uint32_t count = min(hi - lo, WARP);
+                if (laneId() < count) storeTerms(terms, laneId(), wallTerms(r, c, hi - 1 - laneId(), w, m_, bw, inverseInertia));
+                __syncwarp();
+                replayChain(terms, count, chain, c.activeTimestep != 0, acc, accLow);
+                __syncwarp();
+                hi -= count;
+            }
+        }
         uint32_t aBegin = min(r.pairOffsets[id], pairs), aEnd = min(aBegin + r.pairCounts[id], pairs);
         uint32_t bBegin = r.byJOffsets[id], bEnd = r.byJOffsets[id + 1];
         // The grain's pairs in descending pair id (the first-grain run
@@ -1364,28 +1665,10 @@ __global__ void __launch_bounds__(256, 3) k_gather(const __grid_constant__ Param
                     g.depth = __fdiv_rn(pdv.w, wmin);
                     g.dissipation = __fmul_rn(0.5f, r.slip[contact].w);
                     g.normalPower = __fmul_rn(0.5f, r.normalLossPower[contact]);
-                    const float v[GATHER_CHAINS] = {g.force.x, g.force.y, g.force.z, g.torque.x, g.torque.y, g.torque.z,
-                                                    g.s0.x, g.s0.y, g.s0.z, g.s1.x, g.s1.y, g.s1.z,
-                                                    g.s2.x, g.s2.y, g.s2.z, g.energy, g.denom, g.depth,
-                                                    g.dissipation, g.normalPower, g.stiffness, g.viscous};
-#pragma unroll
-                    for (uint32_t j = 0; j < GATHER_CHAINS; ++j) terms[j][lane] = v[j];
+                    storeTerms(terms, lane, g);
                 }
                 __syncwarp();
-                if (chain < 6) {
-                    for (uint32_t k = 0; k < count; ++k) {  // compensated3, one component
-                        float y = __fadd_rn(terms[chain][k], accLow);
-                        float nx = __fadd_rn(acc, y);
-                        accLow = __fsub_rn(y, __fsub_rn(nx, acc));
-                        acc = nx;
-                    }
-                } else if (chain < 15) {
-                    for (uint32_t k = 0; k < count; ++k) acc = __fsub_rn(acc, terms[chain][k]);
-                } else if (chain == 17) {
-                    for (uint32_t k = 0; k < count; ++k) acc = mx(acc, terms[chain][k]);
-                } else if (chain < GATHER_CHAINS && (chain < 20 || c.activeTimestep != 0)) {
-                    for (uint32_t k = 0; k < count; ++k) acc = __fadd_rn(acc, terms[chain][k]);
-                }
+                replayChain(terms, count, chain, c.activeTimestep != 0, acc, accLow);
                 __syncwarp();
             }
             __syncwarp();
@@ -1549,10 +1832,22 @@ static void collectEmit(const Params& P, cudaStream_t s) {
     k_nodeEmit<<<g, 256, 0, s>>>(P);
     k_contactStart<<<g, 256, 0, s>>>(P);
 }
+// Plane contacts after the grain-grain ones: counts, their scan, records.
+static void collectWalls(const Params& P, cudaStream_t s) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (c.wallCount == 0) return;
+    uint32_t items = c.N * c.wallCount, g = min(blocks(items, 8), grid(0, 8));
+    k_wallCount<<<g, 256, 0, s>>>(P);
+    launch_scan(r.wallCounts, r.wallOffsets, ScanCount{nullptr, 0, 0, items}, true, nullptr, nullptr, r.scanPartials,
+                s);
+    k_wallEmit<<<g, 256, 0, s>>>(P);
+}
 static void contacts(const Params& P, cudaStream_t s) {
     collectCull(P, s);
     collectQuery(P, s);
     collectEmit(P, s);
+    collectWalls(P, s);
 }
 
 int launch_contacts(const std::string_view& name, const Params& P, uint32_t count, cudaStream_t s) {
@@ -1565,11 +1860,18 @@ int launch_contacts(const std::string_view& name, const Params& P, uint32_t coun
     else if (name == "collectFilter") collectFilter(P, s);
     else if (name == "collectWalk") collectWalk(P, s);
     else if (name == "collectEmit") collectEmit(P, s);
-    else if (name == "resolveContacts") k_resolve<<<grid(c.contactBlocksPerSM, 8), T, 0, s>>>(P);
+    else if (name == "resolveContacts") {
+        k_resolve<<<grid(c.contactBlocksPerSM, 8), T, 0, s>>>(P);
+        if (c.wallCount) k_resolveWalls<<<grid(0, 2), T, 0, s>>>(P);
+    }
     else if (name == "distanceGrid") {
         if (c.meshGeometry != 0) k_distanceGrid<<<grid(0, 8), T, 0, s>>>(P);
     }
     else if (name == "gather") k_gather<<<min(blocks(c.N, 8), max(1u, grid(c.gatherWarps, 64) / 8)), T, 0, s>>>(P);
+    else if (name == "collectWalls") collectWalls(P, s);
+    else if (name == "gatherWallRows") {
+        if (c.wallCount) k_gatherWallRows<<<blocks(c.N * c.wallCount, T), T, 0, s>>>(P);
+    }
     else return 1;
     (void)count;
     return 0;

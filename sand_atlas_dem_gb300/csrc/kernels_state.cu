@@ -53,7 +53,8 @@ __device__ __forceinline__ void halfKick(const Res& r, const Config& c, uint32_t
     float loss = __fmul_rn(-expm1Stable(__fmul_rn(-c.drag, dt)),
                            __fadd_rn(__fmul_rn(__fmul_rn(0.5f, m), dot(vs, vs)),
                                      rotationalEnergy(r, id, r.rotation[id], l + ll)));
-    accumulate(r, id, make_float4(0.f, loss, __fmul_rn(hdt, cellPower(r, id)), 0.0f));
+    float cp = __fmul_rn(hdt, cellPower(r, id));
+    accumulate(r, id, make_float4(0.f, loss, cp, wallStepWork(r, c, id, hdt)));
     float damping = expm1Stable(__fmul_rn(__fmul_rn(-0.5f, c.drag), dt));
     compensated3(v, vl, damping * (v + vl));
     compensated3(l, ll, damping * (l + ll));
@@ -174,7 +175,7 @@ __device__ __forceinline__ float inverseInertiaBound(const Res& r, uint32_t id) 
               dot(abs3(xyz(r.invI[3 * id + 2])), one));
 }
 
-// solver.slang:815-832 (plane-free)
+// solver.slang:815-832
 __global__ void k_checkContactTimestep(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
@@ -187,7 +188,9 @@ __global__ void k_checkContactTimestep(const __grid_constant__ Params P) {
     float inverseInertia = inverseInertiaBound(r, id);
     float spin = __fmul_rn(inverseInertia, __fadd_rn(length(xyz(r.momentum[id]) + xyz(r.momentumRemainder[id])),
                                                      __fmul_rn(dt, length(xyz(r.torque[id])))));
-    float motion = __fmul_rn(dt, __fadd_rn(__fadd_rn(speed, __fmul_rn(r.body[id].z, spin)), 0.0f));
+    float wallSpeed = 0.f;
+    for (uint32_t w = 0; w < c.wallCount; ++w) wallSpeed = mx(wallSpeed, length(xyz(r.wallVelocity[w])));
+    float motion = __fmul_rn(dt, __fadd_rn(__fadd_rn(speed, __fmul_rn(r.body[id].z, spin)), wallSpeed));
     bool finite = isfinite(rates.x) && isfinite(rates.y) && isfinite(motion) && isfinite(spin);
     if (!finite) { fail(r, F_NONFINITE); return; }
     f3 rate = abs3(xyz(r.cell[3 * specimenOf(r, id) + 1]));
@@ -257,6 +260,78 @@ __global__ void k_reduceRows(const float4* input, float4* output, uint32_t n, ui
     }
 }
 
+// solver.slang:669-687: the planes advance along their normals by
+// velocity . normal x dt (compensated offsets); with a boundary box, its six
+// planes must keep a positive gap inside the domain.  One thread.
+__global__ void k_advanceWalls(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (gtid() != 0 || r.control[0] != 0) return;
+    for (uint32_t w = 0; w < c.wallCount; ++w) {
+        float4 plane = r.wallPlane[w], residual = r.wallRemainder[w];
+        float inc = __fmul_rn(dot(xyz(plane), xyz(r.wallVelocity[w])), c.dt);
+        float y = __fadd_rn(inc, residual.w);
+        float high = __fadd_rn(plane.w, y);
+        float low = __fsub_rn(y, __fsub_rn(high, plane.w));
+        plane.w = high;
+        residual.w = low;
+        if (!isfinite(high) || !isfinite(low)) { fail(r, F_NONFINITE); return; }
+        r.wallPlane[w] = plane;
+        r.wallRemainder[w] = residual;
+    }
+    if (c.wallBoxEnabled != 0) {
+        float4 box = r.cell[0];
+        for (uint32_t axis = 0; axis < 3; ++axis) {
+            uint32_t lo = r.wallBoxIds[2 * axis], hi = r.wallBoxIds[2 * axis + 1];
+            float low = __fadd_rn(r.wallPlane[lo].w, r.wallRemainder[lo].w);
+            float high = -__fadd_rn(r.wallPlane[hi].w, r.wallRemainder[hi].w);
+            float extent = axis == 0 ? box.x : axis == 1 ? box.y : box.z;
+            if (low < 0 || high > extent || high <= low) fail(r, F_BOX);
+        }
+    }
+}
+// solver.slang:950-955: wall power of the committed rows at new wall
+// velocities (no contact is re-resolved).
+__global__ void k_refreshWallPower(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t total = c.N * c.wallCount;
+    for (uint32_t index = gtid(); index < total; index += gstride()) {
+        float4 value = r.wallRows[3 * index + 1];
+        value.w = -dot(xyz(r.wallRows[3 * index]), xyz(r.wallVelocity[index / c.N]));
+        r.wallRows[3 * index + 1] = value;
+    }
+}
+// diagnostic.slang:33-49: per wall, 256-row tree sums of the three
+// (wall, grain) rows, the contact count (row 0, w) summed as an integer.
+__global__ void k_reduceWallRows(const float4* input, float4* output, uint32_t n, uint32_t outputCount) {
+    __shared__ float4 values[256];
+    __shared__ uint32_t counts[256];
+    uint32_t lane = threadIdx.x, id = blockIdx.x * 256 + lane, wall = blockIdx.y;
+    for (uint32_t row = 0; row < 3; ++row) {
+        float4 value = id < n ? input[3 * (size_t(wall) * n + id) + row] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (row == 0) {
+            counts[lane] = __float_as_uint(value.w);
+            value.w = 0.f;
+        }
+        values[lane] = value;
+        __syncthreads();
+        for (uint32_t step = 128; step > 0; step /= 2) {
+            if (lane < step) {
+                values[lane] = add4(values[lane], values[lane + step]);
+                if (row == 0) counts[lane] += counts[lane + step];
+            }
+            __syncthreads();
+        }
+        if (lane == 0) {
+            float4 total = values[0];
+            if (row == 0) total.w = __uint_as_float(counts[0]);
+            output[3 * (size_t(wall) * outputCount + blockIdx.x) + row] = total;
+        }
+        __syncthreads();
+    }
+}
+
 static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
 
 int launch_state(const std::string_view& name, const Params& P, uint32_t count, cudaStream_t s) {
@@ -270,12 +345,19 @@ int launch_state(const std::string_view& name, const Params& P, uint32_t count, 
     else if (name == "checkContactTimestep") k_checkContactTimestep<<<blocks(n, T), T, 0, s>>>(P);
     else if (name == "diagnosticRows") k_diagnosticRows<<<blocks(n, T), T, 0, s>>>(P);
     else if (name == "fabricRows") k_fabricRows<<<blocks(n, T), T, 0, s>>>(P);
+    else if (name == "advanceWalls") k_advanceWalls<<<1, 32, 0, s>>>(P);
+    else if (name == "refreshWallPower") k_refreshWallPower<<<blocks(max(1u, P.c.N * P.c.wallCount), T), T, 0, s>>>(P);
     else return 1;
     return 0;
 }
 
 void launch_reduce_rows(const float4* input, float4* output, uint32_t n, uint32_t rows, int maxRow, cudaStream_t s) {
     k_reduceRows<<<blocks(n, 256), 256, 0, s>>>(input, output, n, rows, maxRow);
+}
+
+void launch_reduce_wall_rows(const float4* input, float4* output, uint32_t n, uint32_t walls, cudaStream_t s) {
+    uint32_t groups = blocks(n, 256);
+    k_reduceWallRows<<<dim3(groups, walls), 256, 0, s>>>(input, output, n, groups);
 }
 
 }  // namespace sdg

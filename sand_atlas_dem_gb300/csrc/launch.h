@@ -19,6 +19,7 @@ void set_last_error(const std::string& what);
 int launch_state(const std::string_view& name, const Params& P, uint32_t count, cudaStream_t s);
 int launch_contacts(const std::string_view& name, const Params& P, uint32_t count, cudaStream_t s);
 void launch_reduce_rows(const float4* input, float4* output, uint32_t n, uint32_t rows, int maxRow, cudaStream_t s);
+void launch_reduce_wall_rows(const float4* input, float4* output, uint32_t n, uint32_t walls, cudaStream_t s);
 
 // Device-wide exclusive scan of n uint32 values, n = constant or
 // min(*countPtr, cap) * mul read on the device.  Writes out[0..n), optionally

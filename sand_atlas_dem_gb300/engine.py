@@ -17,16 +17,19 @@ import weakref
 import numpy as np
 
 from . import native
+from .boundaries import box_extents
 from .model import (
     CAPACITY_FLAGS,
     DAMPING_STATE,
     RESIDUAL_STATE,
     RESOURCE_ORDER,
     STATE_NAMES,
+    WALL_STATE,
     HostLayout,
     RejectedStep,
     f4,
 )
+from .spec import finite_array
 
 # Launch shapes the autotuner sets (values after the extension values; 0 =
 # built-in default).  They never change results.
@@ -42,7 +45,8 @@ EXTENSION_ORDER = (
     "cullerMargin", "cullerStats", "candSurvMask", "candSurvOffset", "survivors", "survKeep", "keepOffset",
     "walkList", "dpairSourcePlane", "meshChildren", "distanceGrid", "distanceGridInfo", "distanceGridTriangle",
     "filterRefRotation", "filterRefBranch", "filterRefPairs", "walkKey", "walkBucketCount", "walkBucketOffset",
-    "sdfLaneCounts", "walkCertPoint", "walkCertTriangle",
+    "sdfLaneCounts", "walkCertPoint", "walkCertTriangle", "wallCounts", "wallOffsets", "sideWallStart",
+    "oldWallStart",
 )
 DISTANCE_GRID = 48  # cells per axis of each shape's distance-bound grid (csrc GRID)
 WALK_BUCKETS = 24**3  # walk-order buckets per shape (csrc WALK_BUCKETS)
@@ -52,7 +56,7 @@ BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
 SIDE_FIELDS = (
     ("meta", "oldMeta"), ("slip", "oldSlip"), ("normalArea", "oldNormal"), ("hash", "oldHash"),
     ("sidePairOffsets", "oldPairOffsets"), ("sidePairB", "oldPairB"),
-    ("sideContactStart", "oldContactStart"),
+    ("sideContactStart", "oldContactStart"), ("sideWallStart", "oldWallStart"),
 )
 SCAN_BLOCKS = 608
 # Default reach of the stored node-filter results: 0.1% of a unit-median
@@ -218,7 +222,7 @@ class Engine:
         self.specimens = h.specimens
         self.spec, self.library, self.n = spec, library, h.n
         self.viscous = spec.viscous
-        self.wall_count = 0
+        self.wall_count = h.wall_count
         self.step = 0
         self.history = False
         self.active = 0
@@ -274,14 +278,15 @@ class Engine:
             self._add(name, array)
         for name, array in h.initial_state().items():
             self._add(name, array)
+        for name, array in h.walls.items():
+            self._add(name, array)
+        walls = h.wall_count * n
         sizes = {
             "meshPairMask": 4 * pc, "meshPairTransform": 16 * 8 * pc, "fabricRows": 16 * 2 * pc,
             "binCounts": 4 * h.bin_count, "binParticles": 4 * h.bin_count * h.bin_capacity,
             "pairCounts": 4 * n, "pairOffsets": 4 * n, "pairs": 8 * pc, "contactCounts": 4 * pc,
             "contactOffsets": 4 * pc, "pointDepth": 16 * cc, "contactForce": 16 * cc,
             "normalLossPower": 4 * cc, "heads": 4 * n, "next": 16,
-            "wallPlane": 16, "wallRemainder": 16, "wallVelocity": 16, "wallMaterial": 16,
-            "wallBoxIds": 24, "wallRows": 16, "wallAccumulated": 16,
             "byJCounts": 4 * (n + 1), "byJOffsets": 4 * (n + 1), "byJCursor": 4 * n, "byJPairs": 4 * pc,
             "dpairBranch": 16 * 2 * pc, "dpairLeafCount": 4 * (2 * pc + 1),
             "dpairCandOffset": 4 * (2 * pc + 1), "leafMask": 4 * 2 * pc * self.leaf_words,
@@ -302,12 +307,14 @@ class Engine:
             "walkBucketOffset": 4 * (len(library.shapes) * WALK_BUCKETS + 1),
             "sdfLaneCounts": 4 * 32 * pc if spec.contact_geometry == "sdf" else 16,
             "walkCertPoint": 16 * self.survivor_capacity, "walkCertTriangle": 4 * self.survivor_capacity,
+            "wallCounts": 4 * walls, "wallOffsets": 4 * (walls + 1),
         }
         for name, nbytes in sizes.items():
             self.buffers[name] = DeviceBuffer(self, nbytes)
         side_sizes = {
             "meta": 16 * cc, "slip": 16 * cc, "normalArea": 16 * cc, "hash": 16,
             "sidePairOffsets": 4 * (n + 1), "sidePairB": 4 * pc, "sideContactStart": 4 * (pc + 1),
+            "sideWallStart": 4 * (walls + 1),
         }
         self.sides = [{k: DeviceBuffer(self, v) for k, v in side_sizes.items()} for _ in (0, 1)]
         for name in BUFFER_ORDER:
@@ -320,6 +327,7 @@ class Engine:
             "referenceCell", "control", "pairs", "pairCounts", "pairOffsets", "particleStress",
             "particleDiagnostic", "timestepRows", "accumulated", "referencePositionRemainder",
             *RESIDUAL_STATE, *DAMPING_STATE, "contactCounts", "byJOffsets", "byJPairs",
+            *(WALL_STATE if self.wall_count else ()),
         )
         self.backups = {name: DeviceBuffer(self, self.buffers[name].size) for name in backup_names}
         self.history_backup = {k: DeviceBuffer(self, self.sides[0][k].size) for k in side_sizes}
@@ -434,8 +442,6 @@ class Engine:
         """Transactional chunk with capacity growth (``gpu.py:597-647``)."""
         from dataclasses import replace
 
-        from .spec import finite_array
-
         if type(steps) is not int or steps < 0:
             raise ValueError("Nonnegative integer step count required")
         rate = finite_array(rate)
@@ -446,10 +452,12 @@ class Engine:
         if not np.isfinite(drag) or drag < 0:
             raise ValueError("Finite nonnegative drag required")
         if wall_velocities is not None:
-            raise ValueError("Wall velocities require planes")
+            if not self.wall_count:
+                raise ValueError("Wall velocities require planes")
+            wall_velocities = finite_array(wall_velocities, (self.wall_count, 3))
         for attempt in range(5):
             try:
-                return self._advance_once(steps, rate=rate, drag=drag)
+                return self._advance_once(steps, rate=rate, drag=drag, wall_velocities=wall_velocities)
             except RejectedStep as exc:
                 capacity = exc.flags & CAPACITY_FLAGS
                 if not capacity or exc.flags & ~CAPACITY_FLAGS or attempt == 4:
@@ -525,7 +533,7 @@ class Engine:
             (ct.c_uint64 * n)(*(b for _, _, b in copies)), n, ct.c_void_p(self.stream.cuda_stream)))
         self._backup_count = count
 
-    def _advance_once(self, steps, *, rate=(0, 0, 0), drag=0):
+    def _advance_once(self, steps, *, rate=(0, 0, 0), drag=0, wall_velocities=None):
         if getattr(self, "invalid", False):
             raise RuntimeError("Engine is invalid; restore a checkpoint")
         if steps < 1:
@@ -541,6 +549,25 @@ class Engine:
             self._rates = rows
         self._backup()
         original_active, original_history = self.active, self.history
+        original_velocity = None
+        if wall_velocities is not None:
+            # gpu.py:682-713: new wall velocities; the committed rows' wall
+            # power is refreshed, or with viscous planes (whose contact law
+            # reads the wall velocity) the committed contacts are re-resolved.
+            original_velocity = self.read("wallVelocity", np.float32, (self.wall_count, 4))
+            velocity = np.zeros((self.wall_count, 4), np.float32)
+            velocity[:, :3] = f4(wall_velocities * self.time_unit / self.length_unit)[:, :3]
+            if not np.isfinite(velocity).all():
+                raise ValueError("Wall velocities cannot be represented in normalized FP32 units")
+            self.buffers["wallVelocity"].copy_from_numpy(velocity)
+            if any(p.get("normal_viscosity", 0) > 0 for p in self.spec.planes) and not np.array_equal(
+                original_velocity, velocity
+            ):
+                self.forces(self.config(dt=0, drag=drag))
+                self.active = 1 - self.active
+                self.history = True
+            else:
+                self.dispatch("refreshWallPower", self.n * self.wall_count, self.config(drag=drag))
         done = 0
         if not self.history:
             # The first step after construction has no committed history.
@@ -557,6 +584,8 @@ class Engine:
             self.synchronize()
             if original_cell is not None:
                 self.buffers["cell"].copy_from_numpy(original_cell)
+            if original_velocity is not None:
+                self.buffers["wallVelocity"].copy_from_numpy(original_velocity)
             raise
         self.step += steps
 
@@ -587,20 +616,36 @@ class Engine:
         for name in ("meta", "slip", "normalArea"):
             out[name] = self.m.read_prefix(side[name], 4 * count, np.uint32 if name == "meta" else np.float32,
                                            shape=(count, 4))
+        if self.wall_count:
+            for name in WALL_STATE:
+                out[name] = self.read(name, np.float32, (self.buffers[name].size // 16, 4))
         return out
 
     def _history_tables(self, meta):
-        """Committed-side pair runs for a contact list in arbitrary order.
+        """Committed-side runs for a contact list in arbitrary order.
 
-        Sorts the contacts by (first grain, second grain, direction, node rank)
-        and returns the permutation with the per-grain pair runs and per-pair
-        contact starts the device merge reads.
+        Sorts the grain-grain contacts by (first grain, second grain,
+        direction, node rank) and the plane contacts after them by (wall,
+        grain, node rank); returns the permutation with the per-grain pair
+        runs, per-pair contact starts and per-(wall, grain) starts the device
+        merge reads.
         """
         g = self.layout.geometry
         n = self.n
         src, dst, node = (meta[:, k].astype(np.int64) for k in range(3))
-        if len(meta) and (src.max() >= n or dst.max() >= n):
+        if len(meta) and (src.max() >= n or dst.max() >= n + self.wall_count):
             raise ValueError("Checkpoint contact refers to a missing grain")
+        wall = dst >= n
+        grains, planes = np.flatnonzero(~wall), np.flatnonzero(wall)
+        if self.sdf:
+            wall_key = node[planes]
+        else:
+            wall_key = g["meshSampleRank"][g["sampleInfo"][self.ids[src[planes]], 0].astype(np.int64)
+                                           + node[planes]].astype(np.int64)
+        wall_order = planes[np.lexsort((wall_key, src[planes], dst[planes]))]
+        item = (dst[wall_order] - n) * n + src[wall_order]
+        wall_starts = (len(grains) + np.searchsorted(item, np.arange(self.wall_count * n + 1))).astype(np.uint32)
+        src, dst, node = src[grains], dst[grains], node[grains]
         a, b = np.minimum(src, dst), np.maximum(src, dst)
         if self.sdf:
             # The SDF emit order: s by virtual lane (s mod 64), then s / 64.
@@ -616,15 +661,31 @@ class Engine:
         pair_a = a[pair_start]
         offsets = np.searchsorted(pair_a, np.arange(n + 1)).astype(np.uint32)
         starts = np.r_[pair_start, len(a)].astype(np.uint32)
-        return order, offsets, b[pair_start].astype(np.uint32), starts
+        order = np.r_[grains[order], wall_order].astype(np.int64)
+        return order, offsets, b[pair_start].astype(np.uint32), starts, wall_starts
 
     def restore(self, state, step):
         """Restart from checkpoint arrays (``gpu.py:1016-1092``)."""
+        if self.wall_count:
+            for name in WALL_STATE:
+                value = finite_array(state[name])
+                if value.shape != (self.buffers[name].size // 16, 4):
+                    raise ValueError("Checkpoint wall state shape mismatch")
+            normals = np.array([p["normal"] for p in self.spec.planes], np.float32)
+            if not np.array_equal(np.asarray(state["wallPlane"])[:, :3], normals):
+                raise ValueError("Checkpoint plane normal identity mismatch")
+            if self.spec.boundary_box is not None:
+                offsets = (np.asarray(state["wallPlane"][:, 3], float) + state["wallRemainder"][:, 3]) * self.length_unit
+                box_extents(offsets, self.spec.boundary_box,
+                            np.asarray(state["cell"][0, :3], float) * self.length_unit)
         for name in DAMPING_STATE:
             value = state[name] if self.viscous else np.zeros((self.n, 4), np.float32)
             self.buffers[name].copy_from_numpy(np.asarray(value, np.float32))
         for name in STATE_NAMES:
             self.buffers[name].copy_from_numpy(np.asarray(state[name], np.float32))
+        if self.wall_count:
+            for name in WALL_STATE:
+                self.buffers[name].copy_from_numpy(np.asarray(state[name], np.float32))
         count = int(state["contacts"])
         if count < 0 or count > self.contact_capacity:
             raise ValueError("Checkpoint contact count is outside capacity")
@@ -634,13 +695,15 @@ class Engine:
             if v.shape != (count, 4):
                 raise ValueError("Checkpoint contact history shape mismatch")
             values[name] = v
-        order, offsets, pair_b, starts = self._history_tables(values["meta"])
+        order, offsets, pair_b, starts, wall_starts = self._history_tables(values["meta"])
         committed = self.sides[1]
         for name in ("meta", "slip", "normalArea"):
             committed[name].write_prefix(values[name][order])
         committed["sidePairOffsets"].write_prefix(offsets)
         committed["sidePairB"].write_prefix(pair_b)
         committed["sideContactStart"].write_prefix(starts)
+        if self.wall_count:
+            committed["sideWallStart"].write_prefix(wall_starts)
         ctrl = np.zeros(16, np.uint32)
         ctrl[2], ctrl[4] = count, 1
         self.buffers["control"].copy_from_numpy(ctrl)
@@ -668,17 +731,58 @@ class Engine:
             src, n, level = out, groups, level + 1
         return self.m.read_prefix(src, 4 * rows, np.float32, shape=(rows, 4)) if read else src
 
+    def _reduce_walls(self):
+        """Per-wall sums of the (wall, grain) rows (``gpu.py:774-786``); the
+        device buffer holding one row set per wall."""
+        src, n, level, w = self.buffers["wallRows"], self.n, 0, self.wall_count
+        while n > 1:
+            groups = (n + 255) // 256
+            key = ("wallRows", level)
+            out = self._reduce_scratch.get(key)
+            if out is None or out.size < 48 * w * groups:
+                out = self._reduce_scratch[key] = DeviceBuffer(self, 48 * w * groups)
+            native.check(self.lib.sdg_reduce_wall_rows(ct.c_void_p(src.ptr()), ct.c_void_p(out.ptr()), n, w,
+                                                       ct.c_void_p(self.stream.cuda_stream)))
+            src, n, level = out, groups, level + 1
+        return src
+
+    def _wall_results(self, wall_data, plane, remainder, velocity):
+        """The ``walls`` rows of :meth:`diagnostics` (``gpu.py:803-833``) and
+        the plane offsets in metres."""
+        plane, remainder = plane.astype(float), remainder.astype(float)
+        offsets = (plane[:, 3] + remainder[:, 3]) * self.length_unit
+        results = [
+            dict(
+                index=w,
+                normal=plane[w, :3].tolist(),
+                offset=float(offsets[w]),
+                velocity=(velocity[w, :3] * self.length_unit / self.time_unit).tolist(),
+                reaction=(wall_data[w, 0, :3] * self.force_unit).tolist(),
+                reaction_moment_origin=(wall_data[w, 1, :3] * self.energy_unit).tolist(),
+                active_surface_contacts=int(wall_data[w, 0, 3].view(np.uint32)),
+                power=float(wall_data[w, 1, 3] * self.energy_unit / self.time_unit),
+                work=float(wall_data[w, 2, 0] * self.energy_unit),
+            )
+            for w in range(self.wall_count)
+        ]
+        return results, offsets
+
     def diagnostics(self):
-        """Stress, energies, contact counts and fabric (``gpu.py:746-891``)."""
+        """Stress, energies, contact counts, fabric and wall rows (``gpu.py:746-891``)."""
         c = self.config()
         self.dispatch("diagnosticRows", self.n, c)
         rows = self._reduce("diagnosticRows", 8, 4, read=False)
         self.dispatch("fabricRows", self.pair_capacity, c)
         fabric_rows = self._reduce("fabricRows", 2, -1, read=False)
-        # One wait for all four small reads.
-        data, fabric_data, cell, ctrl = read_batch(self, [
-            (rows, 16 * 8, np.float32), (fabric_rows, 16 * 2, np.float32),
-            (self.buffers["cell"], 16 * 3, np.float32), (self.buffers["control"], 4 * 16, np.uint32)])
+        reads = [(rows, 16 * 8, np.float32), (fabric_rows, 16 * 2, np.float32),
+                 (self.buffers["cell"], 16 * 3, np.float32), (self.buffers["control"], 4 * 16, np.uint32)]
+        w = self.wall_count
+        if w:
+            reads += [(self._reduce_walls(), 48 * w, np.float32), (self.buffers["wallPlane"], 16 * w, np.float32),
+                      (self.buffers["wallRemainder"], 16 * w, np.float32),
+                      (self.buffers["wallVelocity"], 16 * w, np.float32)]
+        # One wait for all the small reads.
+        data, fabric_data, cell, ctrl, *wall_reads = read_batch(self, reads)
         data, fabric_data, cell = data.reshape(8, 4), fabric_data.reshape(2, 4), cell.reshape(3, 4)
         ctrl = self._checked(ctrl)
         active_pairs = round(float(fabric_data[1, 2]))
@@ -690,6 +794,14 @@ class Engine:
             ]
         ) / max(active_pairs, 1)
         box = cell[0, :3].astype(float) * self.length_unit
+        domain = box.copy()
+        walls = []
+        if w:
+            wall_data, plane, remainder, velocity = wall_reads
+            walls, offsets = self._wall_results(wall_data.reshape(w, 3, 4), plane.reshape(w, 4),
+                                                remainder.reshape(w, 4), velocity.reshape(w, 4))
+            if self.spec.boundary_box is not None:
+                box = box_extents(offsets, self.spec.boundary_box, domain)
         volume = float(box.prod())
         contact = data[:3, :3].astype(float) * self.energy_unit / volume
         kinetic = data[3:6, :3].astype(float) * self.energy_unit / volume
@@ -701,8 +813,8 @@ class Engine:
             "step": self.step,
             "elapsed_time": self.step * self.spec.timestep,
             "cell": box.tolist(),
-            "domain_cell": box.tolist(),
-            "walls": [],
+            "domain_cell": domain.tolist(),
+            "walls": walls,
             "stress": total.tolist(),
             "contact_stress": contact.tolist(),
             "kinetic_stress": kinetic.tolist(),

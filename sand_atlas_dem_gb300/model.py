@@ -1,4 +1,4 @@
-"""Host-side set-up of one periodic mesh-surface DEM specimen.
+"""Host-side set-up of one mesh-surface DEM specimen (periodic, or bounded by planes).
 
 Everything here runs once per engine on the host, in float64 numpy, and ends
 as the float32/uint32 arrays the device step reads.  It restates the set-up
@@ -14,6 +14,7 @@ import math
 
 import numpy as np
 
+from .boundaries import box_extents
 from .packing import pack_library
 from .spec import finite_array
 
@@ -63,6 +64,7 @@ CONFIG_ORDER = (
 )
 
 DAMPING_STATE = ("normalDamping", "forceVelocity", "forceOmega")
+WALL_STATE = ("wallPlane", "wallRemainder", "wallVelocity", "wallAccumulated", "wallRows")
 RESIDUAL_STATE = (
     "positionRemainder", "velocityRemainder", "momentumRemainder", "rotationRemainder",
     "accumulatedRemainder", "cellLog",
@@ -94,11 +96,16 @@ def conservative_timestep(library, spec, ids, scales):
     for i, s in zip(np.asarray(ids), np.asarray(scales, float)):
         sh = library.shapes[int(i)]
         mass = spec.density * sh.volume * s**3
-        stiffness = (spec.normal_stiffness + spec.tangential_stiffness) * sh.areas.sum() * s * s
+        stiffness = (
+            spec.normal_stiffness + spec.tangential_stiffness
+            + sum(p["normal_stiffness"] + p["tangential_stiffness"] for p in spec.planes)
+        ) * sh.areas.sum() * s * s
         smallest = np.linalg.eigvalsh(sh.inertia * spec.density * s**5).min()
         elastic = math.sqrt(min(mass / stiffness, smallest / (stiffness * (sh.radius * s) ** 2)))
         viscous = math.inf
-        viscosity = spec.normal_viscosity * sh.areas.sum() * s**2
+        viscosity = (
+            spec.normal_viscosity + sum(p.get("normal_viscosity", 0) for p in spec.planes)
+        ) * sh.areas.sum() * s**2
         if viscosity > 0:
             viscous = min(mass / viscosity, smallest / (viscosity * (sh.radius * s) ** 2))
         limits.append(0.1 * min(elastic, viscous))
@@ -149,8 +156,10 @@ class HostLayout:
                 raise ValueError("The SDF contact geometry needs a signed-distance grid on every shape")
             if spec.contact_normal == "source-surface-experimental":
                 raise ValueError("The source-surface normal needs the mesh contact geometry")
-        if spec.planes:
-            raise ValueError("The GB300 backend implements periodic and plane-free domains only")
+        if spec.planes and self.specimens != 1:
+            raise ValueError("Planes bound a single specimen")
+        if spec.boundary_box is not None:
+            box_extents(np.array([p["offset"] for p in spec.planes]), spec.boundary_box, self.cells[0])
         self.spec = spec
         self.library = library
         self.n = len(positions)
@@ -209,13 +218,53 @@ class HostLayout:
         self.bin_capacity = spec.bin_capacity
         self.preflight_dt()
         self.initial_cell = np.asarray(cell, float)
+        if spec.boundary_box is not None:
+            self.initial_cell = box_extents(np.array([p["offset"] for p in spec.planes]), spec.boundary_box, cell)
+        self.wall_count = len(spec.planes)
+        self.walls = self.wall_arrays()
         self.normalized_position = np.asarray(positions, float) / l
         self.geometry = self.static_geometry()
         self.max_leaves = int(self.geometry["meshLeafInfo"][:, 1].max())
         self.max_nodes = int(self.geometry["sampleInfo"][:, 1].max())
 
+    def wall_arrays(self):
+        """Normalized plane rows and per-(wall, grain) rows (``gpu.py:232-285``):
+        FP32 normal and offset with the offset's FP32 residual, velocity,
+        material (kn, kt relative to the grain kn; friction; viscosity over
+        the grain kn and time unit), box plane ids and zeroed work rows."""
+        spec, l, n = self.spec, self.length_unit, self.n
+        count = self.wall_count
+        plane = np.zeros((max(1, count), 4), np.float64)
+        velocity = np.zeros_like(plane)
+        material = np.zeros_like(plane)
+        for index, p in enumerate(spec.planes):
+            plane[index] = [*p["normal"], p["offset"] / l]
+            velocity[index, :3] = np.array(p["velocity"]) * self.time_unit / l
+            material[index, :3] = [p["normal_stiffness"] / spec.normal_stiffness,
+                                   p["tangential_stiffness"] / spec.normal_stiffness, p["friction"]]
+            material[index, 3] = p.get("normal_viscosity", 0) / (spec.normal_stiffness * self.time_unit)
+        rounded = plane.astype(np.float32)
+        residual = (plane - rounded).astype(np.float32)
+        if (not np.isfinite(rounded).all() or not np.isfinite(residual).all()
+                or not np.isfinite(velocity.astype(np.float32)).all()
+                or not np.isfinite(material.astype(np.float32)).all()
+                or (count and np.any(material[:count, :2].astype(np.float32) <= 0))):
+            raise ValueError("Plane data cannot be represented in normalized FP32 units")
+        for index, p in enumerate(spec.planes):
+            if p.get("normal_viscosity", 0) > 0 and np.float32(material[index, 3]) <= 0:
+                raise ValueError("Plane viscosity cannot be represented in normalized FP32 units")
+        return {
+            "wallPlane": rounded,
+            "wallRemainder": residual,
+            "wallVelocity": velocity.astype(np.float32),
+            "wallMaterial": material.astype(np.float32),
+            "wallBoxIds": np.array(spec.boundary_box or [0] * 6, np.uint32),
+            "wallAccumulated": np.zeros((max(1, count * n), 4), np.float32),
+            "wallRows": np.zeros((max(1, 3 * count * n), 4), np.float32),
+        }
+
     def preflight_dt(self):
-        """Conservative timestep bound (``gpu.py:370-413``), planes excluded."""
+        """Conservative timestep bound (``gpu.py:370-413``)."""
         spec = self.spec
         if spec.timestep_policy == "active-contact":
             return
@@ -309,8 +358,8 @@ class HostLayout:
             "meshGeometry": int(spec.contact_geometry == "mesh"),
             "sourceSurfaceNormal": int(spec.contact_normal == "source-surface-experimental"),
             "periodic": int(spec.periodic),
-            "wallCount": 0,
-            "wallBoxEnabled": 0,
+            "wallCount": self.wall_count,
+            "wallBoxEnabled": int(spec.boundary_box is not None),
         }
 
     def config_values(self, config):

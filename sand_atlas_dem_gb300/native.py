@@ -79,6 +79,8 @@ def load():
     lib.sdg_dispatch.restype = ct.c_int
     lib.sdg_reduce_rows.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_uint32, ct.c_uint32, ct.c_int32, ct.c_void_p]
     lib.sdg_reduce_rows.restype = ct.c_int
+    lib.sdg_reduce_wall_rows.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_uint32, ct.c_uint32, ct.c_void_p]
+    lib.sdg_reduce_wall_rows.restype = ct.c_int
     lib.sdg_engine_create.restype = ct.c_void_p
     lib.sdg_engine_destroy.argtypes = [ct.c_void_p]
     lib.sdg_engine_advance.argtypes = [ct.c_void_p, P(ct.c_void_p), P(ct.c_uint64), P(ct.c_double), ct.c_uint32,
@@ -132,6 +134,7 @@ EXPORTS = (
     "sdg_last_error",
     "sdg_dispatch",
     "sdg_reduce_rows",
+    "sdg_reduce_wall_rows",
     "sdg_engine_create",
     "sdg_engine_destroy",
     "sdg_engine_advance",

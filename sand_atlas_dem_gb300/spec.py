@@ -2,9 +2,7 @@
 
 Field names, defaults, units (SI) and validation follow the reference
 dataclass (``src/sand_atlas_dem/spec.py:12-193``) so a case JSON written for
-the ``metal``/``cpu`` backends loads unchanged.  Planes (walls) and the SDF
-contact geometry are accepted by the contract but rejected by this backend's
-engine, which implements the periodic mesh-surface step.
+the ``metal``/``cpu`` backends loads unchanged.
 """
 
 from dataclasses import asdict, dataclass, field
@@ -84,10 +82,9 @@ class Experiment:
             raise ValueError("shape_sampling must be random or balanced")
         if type(self.periodic) is not bool:
             raise ValueError("periodic must be an explicit boolean")
-        # Plane schema (``boundaries.py:20-56``): only the structural rule is
-        # restated; plane contacts are outside this backend.
-        if not isinstance(self.planes, list) or (self.planes and self.periodic):
-            raise ValueError("Planes require a nonperiodic domain and a list")
+        from .boundaries import validate_planes
+
+        validate_planes(self.planes, self.periodic, self.boundary_box)
         for name in ("particles", "seed", "contacts_per_particle", "pairs_per_particle",
                      "bin_capacity", "diagnostic_interval", "snapshot_interval"):
             value = getattr(self, name)

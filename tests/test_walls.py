@@ -1,0 +1,172 @@
+"""Penalty planes (walls): the input contract and the CPU oracle against the
+reference's own closed-form wall checks (``tests/test_wall_boundaries.py``,
+``tests/test_wall_coulomb.py``), whose tolerances these tests keep."""
+
+import numpy as np
+import pytest
+
+from oracle.engine import OracleEngine
+from sand_atlas_dem_gb300.boundaries import box_extents
+from sand_atlas_dem_gb300.shapes import ShapeLibrary, analytic_sphere, box_shape, surface_nodes, with_sdf
+from sand_atlas_dem_gb300.spec import Experiment
+from tests.specimens import box_planes, plane
+
+_CAP = []
+
+
+def cap_shape():
+    if not _CAP:
+        _CAP.append(analytic_sphere(samples=32768))
+    return _CAP[0]
+
+
+def cap_engine(**settings):
+    """One 0.5 mm sphere centred 2 mm above the origin, 0.05 mm into the plane
+    z = 1.55 mm (``tests/test_wall_boundaries.py:85-99``)."""
+    spec = Experiment(periodic=False, particles=1, timestep=1e-8, max_overlap_fraction=0.1,
+                      contacts_per_particle=4096, planes=[plane(**settings.pop("plane", {}))], **settings)
+    return OracleEngine(ShapeLibrary([cap_shape()]), spec, [[0.002] * 3], [0.006] * 3, [0], [1])
+
+
+def rows_of(e):
+    data, _ = e.diagnostic_rows()
+    return data, e.wall_rows()
+
+
+def test_wall_input_contract():
+    """``tests/test_wall_boundaries.py:44-80``."""
+    with pytest.raises(ValueError, match="nonperiodic"):
+        Experiment(planes=[plane()])
+    for change in (dict(normal=[0, 0, 2]), dict(offset=float("nan")), dict(velocity=[0, 0]),
+                   dict(normal_stiffness=0), dict(tangential_stiffness=-1), dict(friction=-1), dict(extra=0)):
+        value = plane()
+        value.update(change)
+        with pytest.raises(ValueError):
+            Experiment(periodic=False, planes=[value])
+    box = box_planes(0.0005, 0.0055)
+    for ids in ([0] * 6, [0, 1, 2, 3, 4, 6], list(range(5)), [0, 1, 2, 3, 5, 4]):
+        with pytest.raises(ValueError):
+            Experiment(periodic=False, planes=box, boundary_box=ids)
+    assert np.allclose(box_extents(np.array([p["offset"] for p in box]), list(range(6))), 0.005)
+    with pytest.raises(ValueError, match="nonpositive"):
+        Experiment(periodic=False, planes=box_planes(0.006, 0.0055), boundary_box=list(range(6)))
+    with pytest.raises(ValueError, match="planes"):
+        Experiment(periodic=False, stages=[dict(kind="wall", steps=2, wall_velocities=[])])
+    value = Experiment(periodic=False, planes=[plane()],
+                       stages=[dict(kind="wall", steps=2, wall_velocities=[[0, 0, 0.1]])])
+    assert Experiment(**value.to_dict()).planes == value.planes
+    assert value.checkpoint_format == "sand-dem-checkpoint/4"
+
+
+def test_oracle_full_area_cap_force_reaction_moment_and_energy():
+    """``tests/test_wall_boundaries.py:102-142``: penalty cap force pi kn R d^2,
+    energy pi kn R d^3 / 3, the wall reaction and its moment balance the grain."""
+    e = cap_engine()
+    e.initialize()
+    data, walls = rows_of(e)
+    radius, depth = 0.0005, 0.00005
+    force = np.pi * 1e12 * radius * depth**2
+    energy = np.pi * 1e12 * radius * depth**3 / 3
+    state = e.state()
+    actual = state["force"][0, :3] * e.force_unit
+    assert abs(actual[2] / force - 1) < 0.001
+    assert abs(data[1, 3] * e.energy_unit / energy - 1) < 0.001
+    reaction = walls[0, 0, :3] * e.force_unit
+    assert np.linalg.norm(actual + reaction) < force * 1e-5
+    torque = state["torque"][0, :3] * e.energy_unit
+    origin_moment = np.cross([0.002] * 3, actual) + torque
+    assert np.linalg.norm(origin_moment + walls[0, 1, :3] * e.energy_unit) < force * 0.006 * 1e-5
+    count = int(walls[0, 0, 3].view(np.uint32))
+    assert count == state["contacts"] > 0
+    assert np.all(state["meta"][:, 1] == 1) and np.all(state["meta"][:, 3] == 1)
+    assert data[6, 3] == 0 and walls[0, 2, 0] == 0
+    # Common-node virial without a half-weight wall factor.
+    nodes = cap_shape().samples + [0.002] * 3
+    depths = np.maximum(0, 0.00155 - nodes[:, 2])
+    nodal_force = 1e12 * cap_shape().areas * depths
+    expected_stress = -np.outer([0, 0, 1], np.sum(nodal_force[:, None] * cap_shape().samples, axis=0)) / 0.006**3
+    contact_stress = data[:3, :3].astype(float) * e.energy_unit / 0.006**3
+    assert np.linalg.norm(contact_stress - expected_stress) < force * radius / 0.006**3 * 1e-4
+
+
+def test_oracle_wall_partial_slip_matches_cap_force_torque_and_return_loss():
+    """``tests/test_wall_coulomb.py:19-71``: one step of a plane sliding by
+    25 um under the cap: Coulomb-limited traction integrals."""
+    radius, kn, kt, mu, slip, dt = 0.0005, 1e12, 5e11, 0.3, 0.000025, 1e-8
+    e = cap_engine()
+    e.initialize()
+    e.advance(1, wall_velocities=[[slip / dt, 0, 0]])
+    state = e.state()
+    data, _ = rows_of(e)
+    centre = (state["position"][0, :3].astype(float) + state["positionRemainder"][0, :3]) * e.length_unit
+    depth = radius + 0.00155 - centre[2]
+    c, a = mu * kn, kt * slip
+    h = min(depth, a / c)
+    j0 = c * h**2 / 2 + a * (depth - h)
+    j1 = c * h**3 / 3 + a * (depth**2 - h**2) / 2
+    expected_force = np.array([2 * np.pi * radius * j0, 0, np.pi * kn * radius * depth**2])
+    expected_torque = np.array([0, -2 * np.pi * radius * ((radius - depth) * j0 + j1), 0])
+    expected_loss = 2 * np.pi * radius * c * (slip * h**2 / 2 - c * h**3 / (3 * kt))
+    force = state["force"][0, :3] * e.force_unit
+    torque = state["torque"][0, :3] * e.energy_unit
+    assert np.linalg.norm(force - expected_force) < np.linalg.norm(expected_force) * 0.001
+    assert np.linalg.norm(torque - expected_torque) < np.linalg.norm(expected_torque) * 0.001
+    assert abs(data[6, 0] * e.energy_unit / expected_loss - 1) < 0.001
+    ctrl = e.check_errors()
+    assert 0 < ctrl[6] / ctrl[2] < 1
+    assert data[6, 3] > 0
+
+
+@pytest.mark.parametrize("geometry", ["sdf", "mesh"])
+def test_oracle_rotated_wall_collection_matches_exhaustive_nodes(geometry):
+    """``tests/test_wall_boundaries.py:145-195``: a rotated box against a
+    tilted plane; the collected nodes are exactly those behind it."""
+    from scipy.spatial.transform import Rotation
+
+    base = box_shape([1e-3, 8e-4, 6e-4])
+    shape = box_shape([1e-3, 8e-4, 6e-4], nodes=surface_nodes(base.vertices, base.faces, 4096, 0))
+    if geometry == "sdf":
+        shape = with_sdf(shape, resolution=16)
+    normal = np.array([1, 2, 3], float) / np.sqrt(14)
+    rotation = Rotation.from_euler("xyz", [0.2, -0.3, 0.4])
+    centre = np.array([0.002] * 3)
+    arms = rotation.apply(shape.samples)
+    offset = (arms @ normal).min() + centre @ normal + 0.00001
+    spec = Experiment(periodic=False, contact_geometry=geometry, particles=1, timestep=1e-9,
+                      max_overlap_fraction=0.03, contacts_per_particle=4096, planes=[plane(normal, offset)])
+    e = OracleEngine(ShapeLibrary([shape]), spec, [centre], [0.006] * 3, [0], [1])
+    e.buffers["rotation"][0] = rotation.as_quat().astype(np.float32)
+    e.initialize()
+    depth = np.maximum(0, offset - (arms + centre) @ normal)
+    force = shape.areas[:, None] * depth[:, None] * 1e12 * normal
+    expected_force, expected_torque = force.sum(0), np.cross(arms, force).sum(0)
+    state = e.state()
+    assert state["contacts"] == np.count_nonzero(depth)
+    assert set(state["meta"][:, 2]) == set(np.flatnonzero(depth))
+    scale = np.linalg.norm(expected_force)
+    assert np.linalg.norm(state["force"][0, :3] * e.force_unit - expected_force) < scale * 1e-4
+    assert np.linalg.norm(state["torque"][0, :3] * e.energy_unit - expected_torque) < scale * shape.radius * 1e-4
+
+
+def test_oracle_box_walls_advance_and_invalid_gap_flag():
+    """``tests/test_wall_boundaries.py:329-355``: the zmax plane moving at
+    -1 m/s for ten steps; a gap that closes raises the boundary-box flag."""
+    from sand_atlas_dem_gb300.model import RejectedStep
+
+    shape = analytic_sphere(samples=64)
+    spec = Experiment(periodic=False, particles=1, planes=box_planes(0.0005, 0.0055), boundary_box=list(range(6)),
+                      timestep=1e-8)
+    e = OracleEngine(ShapeLibrary([shape]), spec, [[0.003] * 3], [0.006] * 3, [0], [1])
+    e.initialize()
+    velocities = np.zeros((6, 3))
+    velocities[5, 2] = -1
+    e.advance(10, wall_velocities=velocities)
+    offsets = (e.buffers["wallPlane"][:, 3].astype(float) + e.buffers["wallRemainder"][:, 3]) * e.length_unit
+    assert np.allclose(box_extents(offsets, list(range(6)), [0.006] * 3), [0.005, 0.005, 0.005 - 1e-7], rtol=1e-7)
+    before = e.state()
+    velocities[5, 2] = -1e6
+    with pytest.raises(RejectedStep, match="invalid boundary box"):
+        e.advance(1, wall_velocities=velocities)
+    after = e.state()
+    for name, value in before.items():
+        assert np.array_equal(np.asarray(value), np.asarray(after[name])), name
