@@ -20,6 +20,9 @@ Workloads (``--workload``):
     (one launch per phase, one graph per step), 512..4,096 grains each from
     the uneven library at solid fractions U(0.55, 0.60), each compressed at
     its own rate U(0.1, 1.0)/s.
+``walled-10k``: 10,648 grains of the f8 library on a jittered cubic lattice
+    (solid fraction 0.58) in a nonperiodic domain, boxed by six penalty planes
+    that press the outer grains and move inward (the reference's wall stage).
 ``sdf-spheres-1k``: the SDF contact geometry on the reference's own benchmark
     case (``benchmark.py:162-253`` defaults): 1,000 analytical spheres
     (resolution 32, 512 nodes) on a simple cubic lattice at 1.99 radii,
@@ -64,6 +67,11 @@ WORKLOADS = {
                           grains_per_specimen="512..4096", solid_fraction="U(0.55, 0.60)",
                           strain_rate_per_s="-U(0.1, 1.0) per specimen", max_overlap_fraction=0.5,
                           packing="jittered cubic lattice per specimen"),
+    "walled-10k": dict(COMMON, workload="walled-lattice-10k-f8", library="f8", grains=22**3,
+                       triangles_per_grain=1280, nodes_per_grain=642, solid_fraction=0.58, max_overlap_fraction=0.5,
+                       strain_rate_per_s=0.0, walls="6 box planes 0.02 diameters into the outer grains, "
+                       "moving inward at 0.5/s of the box half-width, friction 0.3",
+                       packing="jittered cubic lattice, nonperiodic"),
     "sdf-spheres-1k": dict(workload="sdf-spheres-1k-simple-cubic", library="sphere", grains=1000, shapes=1,
                            contact_geometry="sdf", sdf_resolution=32, nodes_per_grain=512,
                            packing="simple cubic at 1.99 radii", timestep_s=1e-8, max_overlap_fraction=0.01,
@@ -144,6 +152,14 @@ class Workload:
                                np.ones(n))]
             self.rotations = np.tile(np.array([0, 0, 0, 1], np.float32), (n, 1))
             self.rates = np.zeros((1, 3))
+        elif name == "walled-10k":
+            from sand_atlas_dem_gb300.workloads import walled_lattice
+
+            case = walled_lattice(self.lib, round(self.config["grains"] ** (1 / 3)), self.config["solid_fraction"])
+            self.specimens = [(case["positions"], case["cell"], case["ids"], case["scales"])]
+            self.rotations = case["rotations"]
+            self.rates = np.zeros((1, 3))
+            self.planes = case["planes"]
         elif name == "uneven-50k":
             case = lattice_at(self.lib, round(self.config["grains"] ** (1 / 3)), self.config["solid_fraction"],
                               seed=5)
@@ -167,6 +183,9 @@ class Workload:
                                    pairs_per_particle=self.config["pairs_per_particle"],
                                    contacts_per_particle=self.config["contacts_per_particle"],
                                    max_overlap_fraction=self.config["max_overlap_fraction"])
+        elif name == "walled-10k":
+            self.spec = material_spec(self.lib, ids, scales, max_overlap_fraction=self.config["max_overlap_fraction"],
+                                      periodic=False, planes=self.planes, boundary_box=list(range(6)), **pairs)
         else:
             self.spec = material_spec(self.lib, ids, scales,
                                       max_overlap_fraction=self.config["max_overlap_fraction"], **pairs)

@@ -1194,19 +1194,31 @@ __device__ __forceinline__ float localWallDistance(const Res& r, uint32_t wall, 
     sum = wallAddDot(sum, xyz(r.wallRemainder[wall]), arm);
     return __fadd_rn(sum.hi, sum.lo);
 }
+// The per-(wall, grain) terms of the cluster bound (solver.slang:613-624):
+// the plane normal in the grain's scaled frame, the centre distance and the
+// grain-independent part of the FP32 pad.
+struct WallFrame {
+    f3 normal;
+    float normalLength, base, padBase;
+};
+__device__ __forceinline__ WallFrame wallFrame(const Res& r, uint32_t body, uint32_t wall, float base) {
+    float4 plane = r.wallPlane[wall];
+    WallFrame f;
+    f.normal = qinv(r.rotation[body], xyz(plane)) * r.body[body].x;
+    f.normalLength = length(f.normal);
+    f.base = base;
+    f.padBase = __fadd_rn(__fadd_rn(1.0f, fabsf(plane.w)), length(xyz(r.position[body])));
+    return f;
+}
 // solver.slang:613-624: whether any node of a sample cluster can reach
 // behind the plane (fixed-normal support bound with an FP32 pad).
-__device__ __forceinline__ bool wallClusterMayContact(const Res& r, uint32_t body, uint32_t wall, float base,
-                                                      uint32_t cluster) {
+__device__ __forceinline__ bool wallClusterMayContact(const Res& r, const WallFrame& f, uint32_t cluster) {
     f3 low = xyz(__ldg(&r.meshClusterMin[cluster])), high = xyz(__ldg(&r.meshClusterMax[cluster]));
-    float4 plane = r.wallPlane[wall];
-    f3 normal = qinv(r.rotation[body], xyz(plane)) * r.body[body].x;
     f3 center = 0.5f * (low + high), half = 0.5f * (high - low);
-    float support = __fsub_rn(dot(normal, center), dot(abs3(normal), half));
+    float support = __fsub_rn(dot(f.normal, center), dot(abs3(f.normal), half));
     float pad = __fmul_rn(__fmul_rn(64.0f, 1.1920928955078125e-7f),
-                          __fadd_rn(__fadd_rn(__fadd_rn(1.0f, fabsf(plane.w)), length(xyz(r.position[body]))),
-                                    __fmul_rn(length(normal), __fadd_rn(length(center), length(half)))));
-    return __fadd_rn(base, support) <= pad;
+                          __fadd_rn(f.padBase, __fmul_rn(f.normalLength, __fadd_rn(length(center), length(half)))));
+    return __fadd_rn(f.base, support) <= pad;
 }
 // solver.slang:625-638: node `node` of grain `body` behind the plane, with
 // its record (arm and depth; plane normal and node area).  `flag` raises the
@@ -1227,20 +1239,28 @@ __device__ __forceinline__ bool wallNode(const Res& r, const Config& c, uint32_t
     na = w4(xyz(r.wallPlane[wall]), __fmul_rn(__fmul_rn(point.w, b.x), b.x));
     return true;
 }
-// The plane contacts of one (wall, grain) item in the reference CPU
-// collector's order (cpu_scheduling.slang:133-154): the grain's nodes in
-// order (SDF geometry), or its sample clusters in preorder -- a cluster the
-// plane cannot reach skips its subtree -- and each visited cluster's nodes in
-// order (mesh geometry).  One warp, 32 nodes per round, order kept by ballot
-// ranks; counted, or written from `slot` on.  Returns the count.
-__device__ uint32_t wallItem(const Res& r, const Config& c, uint32_t item, bool emit, uint32_t slot) {
-    uint32_t body = item % c.N, wall = item / c.N, lane = laneId();
+// Whether grain `body` may reach behind plane `wall`: the centre-distance
+// early-out of collectWallContacts (solver.slang:642-653), one lane per item.
+__device__ __forceinline__ bool wallReach(const Res& r, uint32_t body, uint32_t wall, Sum2& centre) {
     float4 plane = r.wallPlane[wall];
-    Sum2 centre = wallCentreDistance(r, body, wall);
+    centre = wallCentreDistance(r, body, wall);
     float phi = __fadd_rn(centre.hi, centre.lo);
     float pad = __fmul_rn(__fmul_rn(64.0f, 1.1920928955078125e-7f),
                           __fadd_rn(__fadd_rn(1.0f, length(xyz(r.position[body]))), fabsf(plane.w)));
-    if (phi > __fadd_rn(r.body[body].z, pad)) return 0;
+    return !(phi > __fadd_rn(r.body[body].z, pad));
+}
+// The plane contacts of one (wall, grain) item that passed the early-out, in
+// the reference CPU collector's order (cpu_scheduling.slang:133-154): the
+// grain's nodes in order (SDF geometry), or its sample clusters in preorder
+// -- a cluster the plane cannot reach skips its subtree -- and each visited
+// cluster's nodes in order (mesh geometry).  One warp: the 32 clusters from
+// the walk's cursor are bounded at once (one per lane), then the walk
+// advances through them with the lanes' results; nodes are tested 32 per
+// round, order kept by ballot ranks.  Counted, or written from `slot` on.
+// Returns the count.
+__device__ uint32_t wallItem(const Res& r, const Config& c, uint32_t item, Sum2 centre, bool emit, uint32_t slot) {
+    uint32_t body = item % c.N, wall = item / c.N, lane = laneId();
+    float phi = __fadd_rn(centre.hi, centre.lo);
     uint32_t shape = r.shapeId[body], count = 0;
     auto visit = [&](bool valid, uint32_t node) {
         float4 pd, na;
@@ -1263,31 +1283,55 @@ __device__ uint32_t wallItem(const Res& r, const Config& c, uint32_t item, bool 
         for (uint32_t base = 0; base < nodes; base += WARP) visit(base + lane < nodes, base + lane);
         return count;
     }
+    WallFrame frame = wallFrame(r, body, wall, phi);
     uint4 info = __ldg(&r.meshClusterInfo[shape]);
-    uint32_t cluster = info.x;
-    // Escape links point forward, so each cluster is visited at most once.
-    for (uint32_t guard = 0; cluster < info.x + info.y && guard < info.y; ++guard) {
-        bool candidate = wallClusterMayContact(r, body, wall, phi, cluster);
-        uint4 range = __ldg(&r.meshClusterRanges[cluster]);
-        if (candidate)
-            for (uint32_t base = 0; base < range.y; base += WARP) {
-                uint32_t k = base + lane;
-                visit(k < range.y, k < range.y ? __ldg(&r.meshSampleIndices[range.x + k]) : 0u);
+    uint32_t end = info.x + info.y, cursor = info.x;
+    // Every window moves the cursor forward (escape links point forward; a
+    // link that does not ends the walk).
+    for (uint32_t guard = 0; cursor < end && guard < info.y; ++guard) {
+        uint32_t window = cursor, cl = window + lane;
+        bool candidate = cl < end && wallClusterMayContact(r, frame, cl);
+        uint4 range = cl < end ? __ldg(&r.meshClusterRanges[cl]) : make_uint4(0u, 0u, 0u, 0u);
+        uint32_t mask = __ballot_sync(0xffffffffu, candidate);
+        while (cursor < end && cursor - window < WARP) {
+            uint32_t k = cursor - window;
+            uint32_t x = __shfl_sync(0xffffffffu, range.x, int(k)), y = __shfl_sync(0xffffffffu, range.y, int(k));
+            uint32_t z = __shfl_sync(0xffffffffu, range.z, int(k));
+            if ((mask >> k) & 1u) {
+                for (uint32_t base = 0; base < y; base += WARP) {
+                    uint32_t n = base + lane;
+                    visit(n < y, n < y ? __ldg(&r.meshSampleIndices[x + n]) : 0u);
+                }
+                ++cursor;
+            } else {
+                cursor = z > cursor ? z : end;
             }
-        cluster = candidate ? cluster + 1 : range.z;
+        }
     }
     return count;
 }
-// Plane contacts per (wall, grain), wall-major; records where they start.
+// Plane contacts per (wall, grain), wall-major: each lane runs the early-out
+// of one item, then the warp collects its items that pass, one after the
+// other.  A warp's 32 items are a grid of warps apart: the grains near a wall
+// are runs of consecutive items, spread this way over many warps.  Records
+// where the plane contacts start.
 __global__ void k_wallCount(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
     if (r.control[0] != 0) return;
     if (gtid() == 0) r.work[W_WALL_BASE] = r.control[2];
-    uint32_t items = c.N * c.wallCount;
-    for (uint32_t item = warpGlobal(); item < items; item += warpStride()) {
-        uint32_t n = wallItem(r, c, item, false, 0);
-        if (laneId() == 0) r.wallCounts[item] = n;
+    uint32_t items = c.N * c.wallCount, lane = laneId(), stride = warpStride(), first = warpGlobal();
+    for (uint32_t base = 0; base < items; base += stride * WARP) {
+        uint32_t item = base + lane * stride + first;
+        Sum2 centre{0.f, 0.f};
+        bool reach = item < items && wallReach(r, item % c.N, item / c.N, centre);
+        if (item < items && !reach) r.wallCounts[item] = 0;
+        for (uint32_t mask = __ballot_sync(0xffffffffu, reach); mask; mask &= mask - 1u) {
+            uint32_t k = __ffs(mask) - 1u, it = base + k * stride + first;
+            Sum2 ck{__shfl_sync(0xffffffffu, centre.hi, int(k)), __shfl_sync(0xffffffffu, centre.lo, int(k))};
+            uint32_t n = wallItem(r, c, it, ck, false, 0);
+            if (lane == 0) r.wallCounts[it] = n;
+        }
     }
 }
 // The plane contacts appended after the grain-grain ones (gpu.py:544-545),
@@ -1296,15 +1340,22 @@ __global__ void k_wallEmit(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
     if (r.control[0] != 0) return;
-    uint32_t items = c.N * c.wallCount, base = r.work[W_WALL_BASE];
-    for (uint32_t i = gtid(); i <= items; i += gstride()) r.sideWallStart[i] = base + r.wallOffsets[i];
+    uint32_t items = c.N * c.wallCount, base0 = r.work[W_WALL_BASE], lane = laneId();
+    for (uint32_t i = gtid(); i <= items; i += gstride()) r.sideWallStart[i] = base0 + r.wallOffsets[i];
     if (gtid() == 0) {
-        uint32_t total = base + r.wallOffsets[items];
+        uint32_t total = base0 + r.wallOffsets[items];
         r.control[2] = total;
         if (total > c.contactCapacity) fail(r, F_CONTACT);
     }
-    for (uint32_t item = warpGlobal(); item < items; item += warpStride())
-        if (r.wallCounts[item] != 0) wallItem(r, c, item, true, base + r.wallOffsets[item]);
+    uint32_t stride = warpStride(), first = warpGlobal();
+    for (uint32_t base = 0; base < items; base += stride * WARP) {
+        uint32_t item = base + lane * stride + first;
+        bool some = item < items && r.wallCounts[item] != 0;
+        for (uint32_t mask = __ballot_sync(0xffffffffu, some); mask; mask &= mask - 1u) {
+            uint32_t it = base + (__ffs(mask) - 1u) * stride + first;
+            wallItem(r, c, it, wallCentreDistance(r, it % c.N, it / c.N), true, base0 + r.wallOffsets[it]);
+        }
+    }
 }
 // Within one (wall, grain) run, the order of a node's contact: its position in
 // the grain's cluster order (mesh) or its index (SDF).
@@ -1389,8 +1440,11 @@ __global__ void k_gatherWallRows(const __grid_constant__ Params P) {
     for (uint32_t item = gtid(); item < items; item += gstride()) {
         uint32_t body = item % c.N, wall = item / c.N;
         uint32_t lo = r.sideWallStart[item], hi = r.sideWallStart[item + 1];
-        f3 centre = xyz(r.position[body]) + xyz(r.positionRemainder[body]);
-        f3 velocity = xyz(r.wallVelocity[wall]);
+        f3 centre = mk(0.f, 0.f, 0.f), velocity = centre;
+        if (hi > lo) {
+            centre = xyz(r.position[body]) + xyz(r.positionRemainder[body]);
+            velocity = xyz(r.wallVelocity[wall]);
+        }
         f3 reaction = mk(0.f, 0.f, 0.f), moment = reaction;
         float power = 0.f;
         for (uint32_t k = hi; k > lo; --k) {

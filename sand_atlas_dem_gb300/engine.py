@@ -197,7 +197,8 @@ class GB300Device:
 
 
 class Engine:
-    """GPU-resident mesh-surface DEM engine (periodic, plane-free, mesh geometry)."""
+    """GPU-resident DEM engine: mesh or SDF contact geometry, periodic cells or
+    one nonperiodic specimen bounded by penalty planes."""
 
     @classmethod
     def batch(cls, library, spec, specimens, **kwargs):

@@ -3,6 +3,8 @@
 * :func:`contact_lattice` — grains on a cubic lattice slightly tighter than
   their equivalent diameter, so neighbours overlap shallowly: a small,
   contact-rich specimen for parity checks.
+* :func:`walled_lattice` — a jittered lattice in a nonperiodic domain boxed by six
+  moving penalty planes (the wall-stage benchmark).
 * :func:`lattice_assembly` — the reference's dilute starting lattice
   (``src/sand_atlas_dem/simulation.py:26-56``) with per-grain lognormal scales.
 * :func:`compress` — isotropic cell compression with drag on the GB300 engine
@@ -63,6 +65,31 @@ def lattice_at(library, side, solid_fraction, *, seed=3, scale_sigma=0.05):
     positions = (idx + 0.5) * step + rng.normal(0, 0.01 * l0, (n, 3))
     return dict(positions=positions, cell=np.full(3, side * step), ids=ids, scales=scales,
                 rotations=random_rotations(n, seed + 1))
+
+
+def walled_lattice(library, side, solid_fraction, *, seed=5, press=0.02, strain_rate=0.5, friction=0.3):
+    """``lattice_at`` grains in a nonperiodic domain one lattice step wider on
+    every side, boxed by six penalty planes (xmin, xmax, ..., zmax) placed
+    ``press`` median diameters inside the outer grains' nominal surfaces and
+    moving inward at ``strain_rate`` (1/s) of the box half-width each.  The
+    planes carry the grain material (kn 1e12, kt 5e11) and ``friction``."""
+    from .boundaries import BOX_NORMALS
+
+    case = lattice_at(library, side, solid_fraction, seed=seed)
+    step = case["cell"][0] / side
+    l0 = float(np.median([equivalent_diameter(s) for s in library.shapes]))
+    positions = case["positions"] + step
+    domain = case["cell"] + 2 * step
+    low = step + 0.5 * step - 0.5 * l0 + press * l0
+    high = step + (side - 0.5) * step + 0.5 * l0 - press * l0
+    speed = strain_rate * 0.5 * (high - low)
+    planes = [
+        dict(normal=n.tolist(), offset=float(low if k % 2 == 0 else -high), velocity=(speed * n).tolist(),
+             normal_stiffness=1e12, tangential_stiffness=5e11, friction=friction)
+        for k, n in enumerate(BOX_NORMALS.astype(float))
+    ]
+    return dict(positions=positions, cell=domain, ids=case["ids"], scales=case["scales"],
+                rotations=case["rotations"], planes=planes)
 
 
 def specimen_set(library, count=128, *, seed=11, grains=(500, 4000), solid_fraction=(0.55, 0.60),
