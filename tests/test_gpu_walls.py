@@ -268,3 +268,34 @@ def test_wall_checkpoint_round_trip(gpu_library, tmp_path):
     np.testing.assert_array_equal(a["meta"], b["meta"])
     for name in ("position", "velocity", "force", "slip", *WALL_STATE):
         assert np.allclose(a[name], b[name], rtol=2e-4, atol=3e-7), name
+
+
+@pytest.mark.parametrize("centre", [0.005, 5.0])
+@pytest.mark.parametrize("normal", [[0, 0, 1], [0.6, 0, 0.8], [1 / 3, 2 / 3, 2 / 3]])
+def test_shallow_contact_preserves_force_and_local_torque_under_translation(gpu_library, centre, normal):
+    """``tests/test_wall_local_frame.py:40-91`` on the GPU engine, and its
+    contact records bit for bit against the oracle."""
+    from tests.test_walls import translation_case
+
+    g = translation_case(Engine, centre, normal)
+    o = translation_case(OracleEngine, centre, normal)
+    for name in ("meta", "normalArea", "force", "torque"):
+        assert g[name].tobytes() == o[name].tobytes(), name
+
+
+def test_two_stage_wall_reduction_counts_reactions_and_moments(gpu_library):
+    """``tests/test_wall_reductions.py:33-72``: two reduction passes of the
+    (wall, grain) rows; the reduced rows bit for bit against the oracle."""
+    from tests.test_walls import two_stage_case
+
+    g, expected = two_stage_case(Engine)
+    row = g.diagnostics()
+    for w, (count, reaction, moment) in enumerate(expected):
+        value = row["walls"][w]
+        assert value["active_surface_contacts"] == count
+        assert np.linalg.norm(value["reaction"] - reaction) < np.linalg.norm(reaction) * 1e-4
+        assert np.linalg.norm(value["reaction_moment_origin"] - moment) < np.linalg.norm(reaction) * 0.04 * 1e-4
+    assert sum(w["active_surface_contacts"] for w in row["walls"]) == row["active_surface_contacts"]
+    o, _ = two_stage_case(OracleEngine)
+    rows = g.m.read_prefix(g._reduce_walls(), 24, np.float32, shape=(2, 3, 4))
+    assert rows.tobytes() == o.wall_rows().tobytes()

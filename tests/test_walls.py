@@ -1,6 +1,7 @@
 """Penalty planes (walls): the input contract and the CPU oracle against the
 reference's own closed-form wall checks (``tests/test_wall_boundaries.py``,
-``tests/test_wall_coulomb.py``), whose tolerances these tests keep."""
+``tests/test_wall_coulomb.py``, ``tests/test_wall_local_frame.py``,
+``tests/test_wall_reductions.py``), whose tolerances these tests keep."""
 
 import numpy as np
 import pytest
@@ -170,3 +171,73 @@ def test_oracle_box_walls_advance_and_invalid_gap_flag():
     after = e.state()
     for name, value in before.items():
         assert np.array_equal(np.asarray(value), np.asarray(after[name])), name
+
+
+def translation_case(engine_cls, centre, normal):
+    """``tests/test_wall_local_frame.py:40-91``: the six-node cube 0.1 um into
+    a plane with its centre at ``centre`` on every axis."""
+    from sand_atlas_dem_gb300.shapes import exact_cube
+
+    cube = exact_cube()
+    h, depth, kn = 1e-4, 1e-7, 1e12
+    p = np.full(3, centre)
+    n = np.array(normal, float)
+    offset = float(p @ n + min(cube.samples @ n) + depth)
+    wall = dict(normal=list(normal), offset=offset, velocity=[0, 0, 0], normal_stiffness=kn,
+                tangential_stiffness=kn / 2, friction=0)
+    spec = Experiment(periodic=False, particles=1, timestep=2e-9, planes=[wall], contacts_per_particle=64,
+                      pairs_per_particle=8, bin_capacity=16, max_overlap_fraction=0.1, contact_geometry="mesh")
+    e = engine_cls(ShapeLibrary([cube]), spec, [p], [max(0.01, 2 * centre)] * 3, [0], [1])
+    e.initialize()
+    state = e.state()
+    delta = np.maximum(0, offset - p @ n - cube.samples @ n)
+    forces = kn * (cube.areas * delta)[:, None] * n
+    expected = forces.sum(axis=0)
+    torque = np.cross(cube.samples, forces).sum(axis=0)
+    scale = np.linalg.norm(expected)
+    actual = state["force"][0, :3].astype(float) * e.force_unit
+    actual_torque = state["torque"][0, :3].astype(float) * e.force_unit * e.length_unit
+    assert np.linalg.norm(actual - expected) / scale <= 1e-4
+    assert np.linalg.norm(actual_torque - torque) / (scale * h) <= 1e-4
+    restored = (state["position"][0, :3].astype(float) + state["positionRemainder"][0, :3]) * e.length_unit
+    assert np.linalg.norm(restored - p) / h <= 1e-7
+    assert len(state["meta"]) == np.count_nonzero(delta)
+    return state
+
+
+@pytest.mark.parametrize("centre", [0.005, 5.0])
+@pytest.mark.parametrize("normal", [[0, 0, 1], [0.6, 0, 0.8], [1 / 3, 2 / 3, 2 / 3]])
+def test_oracle_shallow_contact_preserves_force_and_local_torque_under_translation(centre, normal):
+    translation_case(OracleEngine, centre, normal)
+
+
+def two_stage_case(engine_cls):
+    """``tests/test_wall_reductions.py:33-72``: 257 spheres between two planes
+    (two partial 256-row groups, then a second reduction pass)."""
+    shape = analytic_sphere(samples=2048)
+    n = 257
+    centres = np.array([[0.002 + (i % 17) * 0.002, 0.002 + (i // 17) * 0.002, 0.002] for i in range(n)])
+    walls = [plane([0, 0, 1], 0.00155), plane([0, 0, -1], -0.00245)]
+    spec = Experiment(periodic=False, particles=n, timestep=1e-8, max_overlap_fraction=0.1,
+                      contacts_per_particle=256, planes=walls)
+    e = engine_cls(ShapeLibrary([shape]), spec, centres, [0.04, 0.04, 0.006], [0] * n, [1] * n)
+    e.initialize()
+    expected = []
+    for wall in walls:
+        normal = np.array(wall["normal"], float)
+        depth = np.maximum(0, wall["offset"] - (shape.samples + centres[0]) @ normal)
+        forces = shape.areas[:, None] * 1e12 * depth[:, None] * normal
+        reaction = -n * forces.sum(0)
+        moment = -np.cross(shape.samples, forces).sum(0) * n - np.cross(centres, forces.sum(0)).sum(0)
+        expected.append((n * np.count_nonzero(depth), reaction, moment))
+    return e, expected
+
+
+def test_oracle_two_stage_wall_reduction_counts_reactions_and_moments():
+    e, expected = two_stage_case(OracleEngine)
+    rows = e.wall_rows()
+    for w, (count, reaction, moment) in enumerate(expected):
+        assert int(rows[w, 0, 3].view(np.uint32)) == count
+        assert np.linalg.norm(rows[w, 0, :3] * e.force_unit - reaction) < np.linalg.norm(reaction) * 1e-4
+        assert np.linalg.norm(rows[w, 1, :3] * e.energy_unit - moment) < np.linalg.norm(reaction) * 0.04 * 1e-4
+    assert sum(int(rows[w, 0, 3].view(np.uint32)) for w in range(2)) == e.state()["contacts"]
