@@ -71,3 +71,35 @@ def test_host_sizes_match_device_constants():
     grid = int(re.search(r"constexpr uint32_t GRID = (\d+);", text)[1])
     assert engine.WALK_BUCKETS == cells**3
     assert engine.DISTANCE_GRID == grid
+
+
+def test_plane_configurations_are_checked_before_any_launch(library):
+    """Planes bound one nonperiodic specimen, and their buffers must hold the
+    (wall, grain) rows: rejected in argument checking, with no device touched."""
+    lib = native.load()
+    count = len(BUFFER_ORDER)
+    pointers = (ct.c_void_p * count)()
+    config = dict.fromkeys(CONFIG_ORDER, 0.0)
+    config.update(N=10, shapes=1, pairCapacity=16, contactCapacity=16, binCapacity=4, binCount=1, bins0=1,
+                  bins1=1, bins2=1, hashSize=32, dt=1e-3, kn=1.0, wallCount=2, periodic=1.0)
+    extra = dict(leafWords=1.0, candidateCapacity=1.0, viscousCapture=0.0, specimens=1.0, cullerEnabled=0.0)
+
+    def dispatch(config, extra, sizes):
+        values = [config[k] for k in CONFIG_ORDER] + list(extra.values()) + [0.0] * len(TUNING_KEYS) + [1.0, 0.0, 0.0]
+        rc = lib.sdg_dispatch(b"step", 10, pointers, (ct.c_uint64 * count)(*sizes),
+                              (ct.c_double * len(values))(*values), len(values), None)
+        return rc, lib.sdg_last_error()
+
+    large = [1 << 40] * count
+    rc, message = dispatch(config, extra, large)
+    assert rc == 1 and b"planes" in message
+    rc, message = dispatch(dict(config, periodic=0.0), dict(extra, specimens=2.0), large)
+    assert rc == 1 and b"planes" in message
+    small = list(large)
+    small[BUFFER_ORDER.index("wallRows")] = 16
+    rc, message = dispatch(dict(config, periodic=0.0), extra, small)
+    assert rc == 1 and b"smaller than its configured capacity" in message
+    small = list(large)
+    small[BUFFER_ORDER.index("oldWallStart")] = 8
+    rc, message = dispatch(dict(config, periodic=0.0), extra, small)
+    assert rc == 1 and b"smaller than its configured capacity" in message
