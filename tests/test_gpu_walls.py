@@ -299,3 +299,33 @@ def test_two_stage_wall_reduction_counts_reactions_and_moments(gpu_library):
     o, _ = two_stage_case(OracleEngine)
     rows = g.m.read_prefix(g._reduce_walls(), 24, np.float32, shape=(2, 3, 4))
     assert rows.tobytes() == o.wall_rows().tobytes()
+
+
+def test_wall_and_grain_histories_coexist_and_wall_work_reduces_over_bodies(gpu_library):
+    """``tests/test_wall_reductions.py:97-151`` on the GPU engine."""
+    from sand_atlas_dem_gb300.model import f4
+
+    shape = analytic_sphere(samples=8192)
+    spec = Experiment(periodic=False, particles=2, timestep=1e-8, max_overlap_fraction=0.1,
+                      contacts_per_particle=4096, planes=[plane([0, 0, 1], 0.00155)])
+    engine = Engine(ShapeLibrary([shape]), spec, [[0.002] * 3, [0.002995, 0.002, 0.002]], [0.006] * 3, [0, 0], [1, 1])
+    engine.initialize()
+    engine.buffers["velocity"].copy_from_numpy(
+        f4(np.array([[0, 0.01, 0], [0, -0.01, 0]]) * engine.time_unit / engine.length_unit))
+    engine.advance(3, wall_velocities=[[0.1, 0, 0.1]])
+    row, state = engine.diagnostics(), engine.state()
+    assert row["active_grain_pairs"] == 1
+    wall_keys = state["meta"][:, 1] == 2
+    assert wall_keys.any() and (~wall_keys).any()
+    assert len({tuple(k[:3]) for k in state["meta"]}) == state["contacts"]
+    assert np.max(np.abs(state["slip"][wall_keys, :3])) > 0
+    assert np.max(np.abs(state["slip"][~wall_keys, :3])) > 0
+    scale = row["elastic_energy_proxy"]
+    assert abs(row["wall_work"] - row["walls"][0]["work"]) < scale * 1e-5
+    total_force = state["force"][:, :3].sum(0) * engine.force_unit
+    assert np.linalg.norm(total_force + row["walls"][0]["reaction"]) < np.linalg.norm(total_force) * 1e-5
+    centres = (state["position"][:, :3].astype(float) + state["positionRemainder"][:, :3]) * engine.length_unit
+    total_moment = np.cross(centres, state["force"][:, :3] * engine.force_unit).sum(0)
+    total_moment += state["torque"][:, :3].sum(0) * engine.energy_unit
+    assert np.linalg.norm(total_moment + row["walls"][0]["reaction_moment_origin"]) < np.linalg.norm(
+        total_force) * 0.006 * 1e-5

@@ -241,3 +241,37 @@ def test_oracle_two_stage_wall_reduction_counts_reactions_and_moments():
         assert np.linalg.norm(rows[w, 0, :3] * e.force_unit - reaction) < np.linalg.norm(reaction) * 1e-4
         assert np.linalg.norm(rows[w, 1, :3] * e.energy_unit - moment) < np.linalg.norm(reaction) * 0.04 * 1e-4
     assert sum(int(rows[w, 0, 3].view(np.uint32)) for w in range(2)) == e.state()["contacts"]
+
+
+def test_oracle_wall_and_grain_histories_coexist_and_wall_work_reduces_over_bodies():
+    """``tests/test_wall_reductions.py:97-151``: two spheres touching each
+    other and a moving plane keep both friction histories; the wall's
+    reaction and moment balance the grains."""
+    shape = analytic_sphere(samples=8192)
+    spec = Experiment(periodic=False, particles=2, timestep=1e-8, max_overlap_fraction=0.1,
+                      contacts_per_particle=4096, planes=[plane([0, 0, 1], 0.00155)])
+    e = OracleEngine(ShapeLibrary([shape]), spec, [[0.002] * 3, [0.002995, 0.002, 0.002]], [0.006] * 3, [0, 0],
+                     [1, 1])
+    e.initialize()
+    velocity = np.zeros((2, 4), np.float32)
+    velocity[:, :3] = np.array([[0, 0.01, 0], [0, -0.01, 0]]) * e.time_unit / e.length_unit
+    e.buffers["velocity"][...] = velocity
+    e.advance(3, wall_velocities=[[0.1, 0, 0.1]])
+    state = e.state()
+    data, fabric = e.diagnostic_rows()
+    walls = e.wall_rows()
+    assert round(float(fabric[1, 2])) == 1
+    wall_keys = state["meta"][:, 1] == 2
+    assert wall_keys.any() and (~wall_keys).any()
+    assert len({tuple(k[:3]) for k in state["meta"]}) == state["contacts"]
+    assert np.max(np.abs(state["slip"][wall_keys, :3])) > 0
+    assert np.max(np.abs(state["slip"][~wall_keys, :3])) > 0
+    scale = data[1, 3] * e.energy_unit
+    assert abs(data[6, 3] * e.energy_unit - walls[0, 2, 0] * e.energy_unit) < scale * 1e-5
+    total_force = state["force"][:, :3].sum(0) * e.force_unit
+    reaction = walls[0, 0, :3] * e.force_unit
+    assert np.linalg.norm(total_force + reaction) < np.linalg.norm(total_force) * 1e-5
+    centres = (state["position"][:, :3].astype(float) + state["positionRemainder"][:, :3]) * e.length_unit
+    total_moment = np.cross(centres, state["force"][:, :3] * e.force_unit).sum(0)
+    total_moment += state["torque"][:, :3].sum(0) * e.energy_unit
+    assert np.linalg.norm(total_moment + walls[0, 1, :3] * e.energy_unit) < np.linalg.norm(total_force) * 0.006 * 1e-5
