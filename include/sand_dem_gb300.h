@@ -157,10 +157,13 @@ int sdg_copy_buffers(void* const* dst, void* const* src, const uint64_t* bytes, 
  * buffers they were handed and no device allocator (a cgo, JNI or ctypes
  * stub), or whose device-memory budget is fixed after set-up.  The first call
  * on a device, with that device current, looks the array up; it must come
- * before any stream capture on that device.  n above SDG_SCAN_STATIC_MAX_N is
- * rejected (returns 1, text in sdg_last_error).  Nothing needs zeroing
- * beforehand.  Calls in flight at the same time on one device share the
- * array and race: issue them on one stream.
+ * before any stream capture on that device.  A device reset replaces the
+ * context, and the first call after it looks the array up again (the same
+ * rule applies to that call).  n above SDG_SCAN_STATIC_MAX_N is rejected
+ * (returns 1, text in sdg_last_error); so is a call made while an earlier,
+ * unrelated CUDA error is pending (it is reported, not cleared, and nothing
+ * is launched).  Nothing needs zeroing beforehand.  Calls in flight at the
+ * same time on one device share the array and race: issue them on one stream.
  */
 #define SDG_SCAN_STATIC_MAX_N (1u << 30)
 int sdg_exclusive_scan_static(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total, void* stream);

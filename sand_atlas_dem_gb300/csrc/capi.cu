@@ -73,6 +73,12 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
         g_error = "planes bound a single nonperiodic specimen";
         return 1;
     }
+    // The (wall, grain) items and their three rows are indexed in uint32
+    // (item = wall * N + grain, row = 3 * item + k).
+    if (uint64_t(c.wallCount) * c.N * 3 > uint64_t(UINT32_MAX)) {
+        g_error = "3 x planes x grains must stay below 2^32 (the (wall, grain) row index is 32-bit)";
+        return 1;
+    }
     if (c.meshGeometry == 0 && c.sourceSurfaceNormal != 0) {
         g_error = "the source-surface normal needs the mesh contact geometry";
         return 1;

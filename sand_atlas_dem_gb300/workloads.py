@@ -183,7 +183,7 @@ def material_spec(library, ids, scales, *, friction=0.5, damping_ratio=0.3, poli
 
 
 def dense_packing(library, n, target, *, seed=42, scale_sigma=0.2, speedup=3.0, rate=2000.0,
-                  max_steps=600_000, chunk=500, log=None, device=None, checkpoint=None):
+                  max_steps=600_000, chunk=500, log=None, device=None, checkpoint=None, start=None):
     """Seeded dense periodic packing prepared by GPU compression.
 
     Starts from :func:`dilute_lattice` with random orientations.  Phase 1
@@ -195,7 +195,8 @@ def dense_packing(library, n, target, *, seed=42, scale_sigma=0.2, speedup=3.0, 
     deepest overlap is below 0.5% of a diameter: the frictionless packing is
     below its jamming density, so overlaps relax.  Rejected chunks roll back
     and slow down.  Each phase is bounded by ``max_steps``; ``checkpoint``
-    (a callable) receives the engine after every 100 chunks.
+    (a callable) receives the engine after every 100 chunks; ``start`` (a
+    :func:`load_packing` record) resumes from a saved state.
     """
     from dataclasses import replace
 

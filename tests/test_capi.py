@@ -103,3 +103,6 @@ def test_plane_configurations_are_checked_before_any_launch(library):
     small[BUFFER_ORDER.index("oldWallStart")] = 8
     rc, message = dispatch(dict(config, periodic=0.0), extra, small)
     assert rc == 1 and b"smaller than its configured capacity" in message
+    # 3 x planes x grains rows must fit the 32-bit row index.
+    rc, message = dispatch(dict(config, periodic=0.0, N=float(1 << 30)), extra, large)
+    assert rc == 1 and b"2^32" in message

@@ -9,6 +9,7 @@ checkpoint format by a restart of the CPU oracle engine.
 """
 
 import json
+import os
 from pathlib import Path
 
 import numpy as np
@@ -18,7 +19,7 @@ from sand_atlas_dem_gb300 import checkpoint, hdf5
 from sand_atlas_dem_gb300.shapes import ShapeLibrary, analytic_sphere, exact_cube, with_sdf
 from tests.specimens import build, lattice_case
 
-ASSETS = Path("/root/reference/assets/generated")
+ASSETS = Path(os.environ.get("SAND_DEM_REFERENCE", "/root/reference")) / "assets" / "generated"
 
 
 @pytest.mark.skipif(not ASSETS.exists(), reason="the reference tree is not present")

@@ -50,6 +50,13 @@ def test_static_scan_matches_scratch_scan_twice(gpu_library):
         np.testing.assert_array_equal(got, (np.cumsum(values.astype(np.uint64)) - values).astype(np.uint32))
 
 
+def test_static_scan_of_nothing_has_total_zero(gpu_library):
+    import torch
+
+    got, total = _scan(gpu_library, torch, np.zeros(0, np.uint32), static=True)
+    assert got.size == 0 and total == 0
+
+
 def test_static_scan_rejects_oversized_input(gpu_library):
     lib = native.load()
     rc = lib.sdg_exclusive_scan_static(ct.c_void_p(16), ct.c_void_p(16), (1 << 30) + 1, None, None)
