@@ -338,6 +338,49 @@ class OracleEngine:
         fabric = tree_reduce(self.buffers["fabricRows"].reshape(self.pair_capacity, 2, 4))
         return rows, fabric
 
+    def diagnostics(self):
+        """The reference's diagnostics dictionary (``gpu.py:788-891``) from
+        the oracle's tree-reduced rows: stress tensors, p/q, strains, energies,
+        contact counts, coordination, fabric and sliding fraction.  Periodic
+        specimens (plane rows are :meth:`wall_rows`)."""
+        data, fabric_data = self.diagnostic_rows()
+        ctrl = self.check_errors()
+        active_pairs = round(float(fabric_data[1, 2]))
+        f = fabric_data.astype(float)
+        fabric = np.array([[f[0, 0], f[0, 3], f[1, 0]], [f[0, 3], f[0, 1], f[1, 1]],
+                           [f[1, 0], f[1, 1], f[0, 2]]]) / max(active_pairs, 1)
+        cell = self.buffers["cell"][:3]
+        box = cell[0, :3].astype(float) * self.length_unit
+        volume = float(box.prod())
+        energy = self.energy_unit
+        contact = data[:3, :3].astype(float) * energy / volume
+        kinetic = data[3:6, :3].astype(float) * energy / volume
+        total = contact + kinetic
+        sym = 0.5 * (total + total.T)
+        solid = sum(self.library.shapes[int(i)].volume * s**3 for i, s in zip(self.ids, self.scales))
+        initial = np.asarray(self.initial_cell, float)
+        return {
+            "step": self.step, "cell": box.tolist(), "stress": total.tolist(), "contact_stress": contact.tolist(),
+            "kinetic_stress": kinetic.tolist(),
+            "stress_antisymmetry": float(np.linalg.norm(total - total.T) / max(np.linalg.norm(total), 1e-30)),
+            "p": float(np.trace(sym) / 3), "q": float(sym[2, 2] - 0.5 * (sym[0, 0] + sym[1, 1])),
+            "axial_strain": float(1 - box[2] / initial[2]), "volumetric_strain": float(np.sum(1 - box / initial)),
+            "volume_ratio": float(volume / np.prod(initial)), "log_strain": (-np.log(box / initial)).tolist(),
+            "void_ratio": float(volume / solid - 1), "kinetic_energy": float(data[0, 3] * energy),
+            "elastic_energy_proxy": float(data[1, 3] * energy),
+            "unbalanced_force": float(data[2, 3] / max(data[3, 3], 1e-30)),
+            "max_overlap_fraction": float(data[4, 3]),
+            "friction_dissipation_last_step": float(data[5, 3] * energy),
+            "candidate_pairs": int(ctrl[1]), "active_surface_contacts": int(ctrl[2]),
+            "active_grain_pairs": active_pairs, "coordination": 2 * active_pairs / self.n,
+            "fabric": fabric.tolist(), "sliding_fraction": float(ctrl[6] / max(ctrl[2], 1)),
+            "cell_log_rate": (cell[1, :3] / self.time_unit).tolist(),
+            "friction_dissipation": float(data[6, 0] * energy), "drag_dissipation": float(data[6, 1] * energy),
+            "cell_work": float(data[6, 2] * energy), "wall_work": float(data[6, 3] * energy),
+            "normal_contact_dissipation": float(data[7, 0] * energy),
+            "normal_contact_power": float(data[7, 1] * energy / self.time_unit),
+        }
+
     def wall_rows(self):
         """Per-wall (reaction | count, moment | power, work) rows reduced over
         the grains in the reference tree order (``diagnostic.slang:33-49``)."""

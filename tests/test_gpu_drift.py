@@ -53,7 +53,7 @@ def test_thousand_step_horizon_against_oracle(gpu_library):
     print(json.dumps(rows))
     assert g.step == o.step == 1000
     assert all(r["contacts"] > 0 for r in rows)
-    assert rows[0]["same_contact_keys"]
+    assert all(r["same_contact_keys"] for r in rows), [r["step"] for r in rows if not r["same_contact_keys"]]
     # Drift bound over the horizon (a statement, not the per-step gate).
     assert max(r["centre_over_diameter"] for r in rows) < 1e-4
     assert max(r["rotation_component"] for r in rows) < 1e-4
