@@ -32,6 +32,16 @@ Data are synthetic (seeded); the reference's Hostun assets are not used.
 
 ``value``  : device throughput, CUDA events on the engine stream around each
              graph-replayed step, L2 flushed (256 MiB write) before each step.
+``amortized``: the workload's whole run after the headline steps (10,000
+             steps for dense-10k, the plain-method configuration's length;
+             2,000 otherwise), every step timed the same way, with the filter
+             builds and neighbour rebuilds its motion caused, the step-time
+             median, 99th percentile and maximum, and its kernel launches.
+``gpu_launches``: kernel launches of the timed steps: each captured step runs
+             its unconditional kernels; the neighbour-build and filter-build
+             bodies are conditional graph nodes that run only on the steps
+             whose device flag asks for them (counted from the device's
+             rebuild and build counters).
 ``e2e``    : the public API a caller uses (``Engine.advance`` chunks of 10
              steps plus ``diagnostics()``), host wall clock, including the
              host<->device traffic of those calls (counted by the engine).
@@ -57,6 +67,10 @@ METRIC = "grain-steps/s"
 COMMON = dict(shapes=64, friction=0.5, damping_ratio=0.3,
               dtype_note="FP32 state with compensated residuals; FP64 minimum image")
 WORKLOADS = {
+    "sparse-1k": dict(COMMON, workload="sparse-periodic-1k-icosphere-f4", library="f4", grains=1000,
+                      triangles_per_grain=320, nodes_per_grain=162, solid_fraction_target=0.35,
+                      initial_velocity_sigma_m_s=0.05, max_overlap_fraction=0.1, strain_rate_per_s=0.0,
+                      run_steps=2000),
     "dense-10k": dict(COMMON, workload="dense-periodic-10k-icosphere-f8", library="f8", grains=10_000,
                       triangles_per_grain=1280, nodes_per_grain=642, solid_fraction_target=0.58,
                       max_overlap_fraction=0.1, strain_rate_per_s=-0.5),
@@ -82,8 +96,14 @@ DATA = ROOT / "sand_atlas_dem_gb300" / "data"
 # k_nodeWalkSlow) from an ncu capture of the same workload
 # (profiles/walk-dense-10k.md); None where not captured.
 WALK_TRAFFIC = {"dense-10k": 74.51e6}
-# work[] counters of the stored node-filter results (csrc/dem_device.cuh).
-W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS, W_CERTIFIED = 8, 9, 10, 15
+# work[] counters (csrc/dem_device.cuh): the stored node-filter results and
+# the neighbour-list rebuilds.
+W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS, W_CERTIFIED, W_REBUILDS = 8, 9, 10, 15, 17
+# Steps of the long window timed after the headline steps: the length of the
+# workload's own run, so that the filter builds and neighbour rebuilds its
+# motion causes are inside it.
+WINDOW_STEPS = {"dense-10k": 10_000, "sparse-1k": 2_000, "uneven-50k": 2_000, "specimens-128": 2_000,
+                "walled-10k": 2_000, "sdf-spheres-1k": 2_000}
 
 
 def log(*args):
@@ -104,22 +124,22 @@ def library(kind):
     return synthetic_library(kind, 64)
 
 
-def packing(lib, grains, phi, seed=42):
-    """The prepared dense packing (committed record, else prepared here within
-    a bounded time and cached)."""
+def packing(lib, grains, phi, seed=42, kind="f8", name=None):
+    """The prepared packing (committed record, else prepared here within a
+    bounded time and cached)."""
     from sand_atlas_dem_gb300.workloads import descent_packing, load_packing, save_packing
 
-    name = f"packing-f8-{grains}.npz"
+    name = name or f"packing-{kind}-{grains}.npz"
     for path in (DATA / name, cache_dir() / name):
         if path.exists():
             return dict(load_packing(path), path=str(path))
     t = time.perf_counter()
     out = descent_packing(lib, grains, phi, seed=seed, max_seconds=600, log=lambda d: log("prepare", d))
-    meta = dict(library="f8", grains=grains, solid_fraction=phi, seed=seed, evaluations=out["evaluations"],
+    meta = dict(library=kind, grains=grains, solid_fraction=phi, seed=seed, evaluations=out["evaluations"],
                 seconds=round(time.perf_counter() - t, 1), achieved_solid_fraction=out["phi"],
-                max_overlap_fraction=out["overlap"])
+                max_overlap_fraction=out["overlap"], method="affine compression with frictionless force descent")
     save_packing(cache_dir() / name, out["engine"], out["ids"], out["scales"], meta)
-    return load_packing(cache_dir() / name)
+    return dict(load_packing(cache_dir() / name), path=str(cache_dir() / name))
 
 
 class Workload:
@@ -132,7 +152,20 @@ class Workload:
         self.name = name
         self.config = dict(WORKLOADS[name])
         self.lib = library(self.config["library"])
-        if name == "dense-10k":
+        self.velocities = None
+        if name == "sparse-1k":
+            # The plain-method CPU configuration: a loose packing at solid
+            # fraction 0.35 with random orientations and velocities N(0, 0.05 m/s).
+            pack = packing(self.lib, self.config["grains"], self.config["solid_fraction_target"], kind="f4",
+                           name="packing-f4-1000-phi035.npz")
+            self.specimens = [(pack["positions"], pack["cell"], pack["ids"], pack["scales"])]
+            self.rotations = pack["rotations"]
+            rng = np.random.default_rng(42 + 2)
+            self.velocities = rng.normal(0.0, self.config["initial_velocity_sigma_m_s"], (len(pack["ids"]), 3))
+            self.rates = np.zeros((1, 3))
+            self.config.update(packing_meta=pack["meta"],
+                               solid_fraction=pack["meta"].get("achieved_solid_fraction"))
+        elif name == "dense-10k":
             grains = grains or self.config["grains"]
             pack = packing(self.lib, grains, self.config["solid_fraction_target"])
             self.specimens = [(pack["positions"], pack["cell"], pack["ids"], pack["scales"])]
@@ -175,7 +208,7 @@ class Workload:
         scales = np.concatenate([s[3] for s in self.specimens])
         # Lattices have at most 26 neighbours in range: 16 pairs per grain
         # leave room, and the engine grows on overflow.
-        pairs = {} if name == "dense-10k" else dict(pairs_per_particle=16)
+        pairs = {} if name in ("dense-10k", "sparse-1k") else dict(pairs_per_particle=16)
         if name == "sdf-spheres-1k":
             from sand_atlas_dem_gb300.spec import Experiment
 
@@ -202,11 +235,18 @@ class Workload:
             e = cls.batch(self.lib, self.spec_for(chosen), [self.specimens[k] for k in chosen], **kwargs)
         rotations = np.concatenate([self.rotations[offsets[k]:offsets[k + 1]] for k in chosen])
         rotations = np.ascontiguousarray(rotations, np.float32)
-        buffer = e.buffers["rotation"]
-        if isinstance(buffer, np.ndarray):
-            buffer[...] = rotations
-        else:
-            buffer.copy_from_numpy(rotations)
+        uploads = {"rotation": rotations}
+        if self.velocities is not None:
+            v = np.zeros((e.n, 4), np.float32)
+            v[:, :3] = np.concatenate([self.velocities[offsets[k]:offsets[k + 1]] for k in chosen]) \
+                * e.time_unit / e.length_unit
+            uploads["velocity"] = v
+        for name, array in uploads.items():
+            buffer = e.buffers[name]
+            if isinstance(buffer, np.ndarray):
+                buffer[...] = array
+            else:
+                buffer.copy_from_numpy(array)
         e.initialize()
         return e
 
@@ -235,7 +275,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
-                 f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200"],
+                 f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -301,6 +341,37 @@ def algorithmic_bytes(n, pairs, contacts, items, nodes, survivors, kept, rebuild
     return step, query, walk
 
 
+def launches(e, steps, rebuilds, builds):
+    """Kernel launches of ``steps`` graph-replayed steps: the ones every step
+    runs, plus the neighbour-build body on rebuild steps and the filter-build
+    body on filter-build steps."""
+    lib, h = e.lib, e._native
+    return (lib.sdg_engine_kernels_per_step(h) * steps + lib.sdg_engine_branch_kernels(h, 0) * rebuilds
+            + lib.sdg_engine_branch_kernels(h, 1) * builds)
+
+
+def counters(e):
+    work = e.read("work", np.uint32, (64,))
+    return int(work[W_REBUILDS]), int(work[W_FILTER_BUILDS]), int(work[W_CERTIFIED])
+
+
+def long_window(e, w, steps, flush):
+    """The workload's whole run (``steps`` steps), each step timed on the
+    device with L2 flushed before it: the amortized throughput over every
+    filter build and neighbour rebuild the run's motion causes."""
+    before = counters(e)
+    ms = np.asarray(timed_steps(e, steps, flush))
+    after = counters(e)
+    rebuilds, builds = after[0] - before[0], after[1] - before[1]
+    return {"steps": steps, "value": w.grains * steps / (ms.sum() / 1e3), "unit": "grain-steps/s",
+            "ms_per_step": float(ms.mean()), "ms_median": float(np.median(ms)),
+            "ms_p99": float(np.percentile(ms, 99)), "ms_max": float(ms.max()),
+            "neighbour_rebuilds": rebuilds, "filter_builds": builds,
+            "certified_queries_per_step": (after[2] - before[2]) / steps,
+            "gpu_launches": launches(e, steps, rebuilds, builds),
+            "l2": "flushed before each step (256 MiB write)"}
+
+
 def timed_steps(e, steps, flush):
     """Device milliseconds of each of ``steps`` graph-replayed steps, L2 flushed before each."""
     import torch
@@ -340,18 +411,23 @@ def run_gb300(args, cpu=True):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=e.device)
     ctrl0 = e.check_errors()
     work0 = e.read("work", np.uint32, (64,))
+    window_steps = args.window if args.window is not None else WINDOW_STEPS[w.name]
     with ClockSampler() as clocks:
         step_ms = timed_steps(e, args.steps, flush)
+        work1 = e.read("work", np.uint32, (64,))
+        window = long_window(e, w, window_steps, flush) if window_steps else None
     ctrl = e.check_errors()
-    work1 = e.read("work", np.uint32, (64,))
+    timed_rebuilds = int(work1[W_REBUILDS] - work0[W_REBUILDS])
+    timed_builds = int(work1[W_FILTER_BUILDS] - work0[W_FILTER_BUILDS])
     filter_cache = {"margin": e.filter_margin,
                     "adapted_margin": float(work1[W_FILTER_MARGIN:W_FILTER_MARGIN + 1].view(np.float32)[0]),
-                    "builds_in_timed_steps": int(work1[W_FILTER_BUILDS] - work0[W_FILTER_BUILDS]),
+                    "builds_in_timed_steps": timed_builds,
+                    "neighbour_rebuilds_in_timed_steps": timed_rebuilds,
                     "timed_steps": int(work1[W_FILTER_STEPS] - work0[W_FILTER_STEPS]),
                     "certified_queries_per_step": float(work1[W_CERTIFIED] - work0[W_CERTIFIED]) / args.steps}
     device_s = sum(step_ms) / 1e3
     value = w.grains * args.steps / device_s
-    kernels = e.lib.sdg_engine_kernels_per_step(e._native)
+    kernel_count = launches(e, args.steps, timed_rebuilds, timed_builds)
     # Phase profile (cold L2 each), for the roofline of the dominant launch group.
     phases = []
     for _ in range(3):
@@ -425,7 +501,11 @@ def run_gb300(args, cpu=True):
                        dominant_phase=top, tuning=dict(e.tuning)),
         "e2e": {"value": e2e, "unit": "grain-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": f"Engine.advance({chunk}) + Engine.diagnostics() per chunk"},
-        "gpu_launches": int(kernels) * args.steps,
+        "gpu_launches": int(kernel_count),
+        "kernels_per_step": {"every_step": int(e.lib.sdg_engine_kernels_per_step(e._native)),
+                             "neighbour_build_body": int(e.lib.sdg_engine_branch_kernels(e._native, 0)),
+                             "filter_build_body": int(e.lib.sdg_engine_branch_kernels(e._native, 1))},
+        "amortized": window,
         "roofline": {
             "bound": "hbm",
             "kernel": kernel_name,
@@ -450,11 +530,52 @@ def run_gb300(args, cpu=True):
         line["plain_gpu_path"] = plain_comparison(w, args, flush)
     if args.culler:
         line["learned_culler"] = culler_comparison(w, args, flush)
+    if "run_steps" in w.config and cpu and not args.no_cpu_baseline:
+        line["full_run"] = full_run(w, args)
     if cpu and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args)
     if ctrl0[0] or ctrl[0]:
         line["solver_flags"] = int(ctrl[0])
     return line
+
+
+def full_run(w, args):
+    """The whole run of the configuration (``run_steps`` steps) from the
+    prepared start: on the GPU through the public API (one
+    ``Engine.advance`` call and ``diagnostics()``, host wall clock, host
+    copies included) and on the CPU oracle with every host thread; and how far
+    apart the two end states are."""
+    from oracle.engine import OracleEngine
+    from sand_atlas_dem_gb300.engine import Engine
+
+    steps = w.config["run_steps"]
+    g = w.engine(Engine)
+    g.synchronize()
+    t = time.perf_counter()
+    g.advance(steps, rate=w.rate())
+    g.diagnostics()
+    gpu_s = time.perf_counter() - t
+    o = w.engine(OracleEngine, threads=args.cpu_threads)
+    t = time.perf_counter()
+    o.advance(steps, rate=w.rate())
+    cpu_s = time.perf_counter() - t
+    sg, so = g.state(), o.state()
+    box = so["cell"][0, :3].astype(float)
+    d = (sg["position"][:, :3].astype(float) + sg["positionRemainder"][:, :3]) \
+        - (so["position"][:, :3].astype(float) + so["positionRemainder"][:, :3])
+    d -= np.round(d / box) * box
+    diameters = g.layout.body[:, 3].astype(float)
+    qg, qo = sg["rotation"].astype(float), so["rotation"].astype(float)
+    sign = np.where(np.einsum("ij,ij->i", qg, qo) < 0, -1.0, 1.0)
+    return {"steps": steps, "grain_steps": w.grains * steps,
+            "gpu_e2e_s": gpu_s, "gpu_e2e_value": w.grains * steps / gpu_s,
+            "cpu_oracle_s": cpu_s, "cpu_oracle_value": w.grains * steps / cpu_s, "cpu_threads": o.threads,
+            "gpu_over_cpu": cpu_s / gpu_s,
+            "same_contact_keys_at_end": bool(sg["contacts"] == so["contacts"]
+                                             and np.array_equal(sg["meta"], so["meta"])),
+            "contacts_at_end": int(sg["contacts"]),
+            "max_centre_deviation_diameters": float((np.linalg.norm(d, axis=1) / diameters).max()),
+            "max_quaternion_component_deviation": float(np.abs(sign[:, None] * qg - qo).max())}
 
 
 def plain_comparison(w, args, flush):
@@ -567,21 +688,25 @@ def cpu_sample(w):
     return [[0]] if len(w.specimens) == 1 else [[k] for k in range(8)]
 
 
-def cpu_baseline(w, args, steps=1):
-    """Oracle port of the reference CPU backend on this host's cores."""
+def cpu_baseline(w, args, budget_s=15.0, max_steps=200):
+    """Oracle port of the reference CPU backend on this host's cores: whole
+    steps of the workload (or of its sampled specimens), repeated until about
+    ``budget_s`` seconds of CPU work (at least 3 steps)."""
     from oracle.engine import OracleEngine
 
-    grains, seconds, threads = 0, 0.0, 1
-    for chosen in cpu_sample(w):
-        e = w.engine(OracleEngine, chosen, threads=args.cpu_threads)
-        threads = e.threads
-        t = time.perf_counter()
-        e.advance(steps, rate=w.rate(chosen))
-        seconds += time.perf_counter() - t
-        grains += e.n * steps
+    grains, seconds, threads, steps = 0, 0.0, 1, 0
+    engines = [(w.engine(OracleEngine, chosen, threads=args.cpu_threads), chosen) for chosen in cpu_sample(w)]
+    while steps < max_steps and (steps < 3 or seconds < budget_s):
+        for e, chosen in engines:
+            threads = e.threads
+            t = time.perf_counter()
+            e.advance(1, rate=w.rate(chosen))
+            seconds += time.perf_counter() - t
+            grains += e.n
+        steps += 1
     what = "the whole workload" if len(w.specimens) == 1 else f"specimens 0-7 ({grains // steps} grains)"
     return {"value": grains / seconds, "unit": "grain-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} full step(s) of {what}, {seconds:.2f} s"}
+            "sample": f"{steps} full steps of {what}, {seconds:.2f} s"}
 
 
 def run_reference(args):
@@ -625,6 +750,8 @@ def main():
     p.add_argument("--prepare-only", action="store_true")
     p.add_argument("--culler", action="store_true", help="also train the learned culler and compare")
     p.add_argument("--no-plain", action="store_true", help="skip the plain-path comparison")
+    p.add_argument("--window", type=int, default=None,
+                   help="steps of the long amortized window (default: the workload's run length; 0 skips it)")
     args = p.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

@@ -11,7 +11,7 @@
  *             (src/sand_atlas_dem/shaders/solver.slang:20-100) — the same
  *             order the reference CPU backend binds in its generated
  *             cpu_dispatch (src/sand_atlas_dem/cpu.py:189-300);
- *   [77, 134) this backend's extension buffers, in the order of
+ *   [77, 136) this backend's extension buffers, in the order of
  *             sand_atlas_dem_gb300.engine.EXTENSION_ORDER (leaf tables,
  *             node ranks, pair-by-second-grain runs, directed-pair branches,
  *             leaf masks, (directed pair, leaf) items and hit masks, contact
@@ -43,7 +43,10 @@
  *             the distance gap, and the triangle, and with planes the
  *             plane-contact count of each (wall, grain), wall-major, its
  *             exclusive scan, and the first contact of each (wall, grain)
- *             on the side being written and on the committed side).
+ *             on the side being written and on the committed side, and per
+ *             stored walk-list slot its node record -- source grain, target
+ *             grain, directed pair and packed sample index -- and its
+ *             (item, node slot)).
  * Value block (SDG_VALUE_COUNT doubles): the 25 reference Config scalars in
  * declaration order (solver.slang:12-19, normalized units as
  * src/sand_atlas_dem/gpu.py:490-518 builds them), then leaf mask words per
@@ -79,7 +82,7 @@
 extern "C" {
 #endif
 
-#define SDG_BUFFER_COUNT 134
+#define SDG_BUFFER_COUNT 136
 #define SDG_VALUE_COUNT 39
 #define SDG_PHASES 9
 
@@ -232,8 +235,20 @@ int sdg_culler_tile_eval(const void* params, const void* w1_bf16, const void* po
 int sdg_culler_inside_max(const void* points, const void* predictions, uint32_t shapes, uint32_t count,
                           void* keys, void* stream);
 
-/* Kernel launches per captured step (0 before the first capture). */
+/*
+ * Kernel launches of a captured step that skips both conditional bodies (0
+ * before the first capture).  The captured step holds the neighbour build
+ * and, with stored filter results, the filter build as conditional-node
+ * bodies keyed on device flags (the reference re-encodes the rebuild
+ * dispatches every step and lets them exit early, gpu.py:547-565).
+ */
 int sdg_engine_kernels_per_step(void* engine);
+/*
+ * Kernel launches inside conditional body `branch` of a captured step: 0 =
+ * the neighbour build (steps whose rebuild flag is set), 1 = the filter build
+ * (steps that build the stored filter results).  -1 for a bad argument.
+ */
+int sdg_engine_branch_kernels(void* engine, int branch);
 
 #ifdef __cplusplus
 }

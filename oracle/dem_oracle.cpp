@@ -12,7 +12,7 @@
 // FP32 operation order follows the Slang-generated C++ of the reference
 // (evidence/hostun424-cpu-pair-plane-counts-v1/.../instrumented-collector.cpp):
 // dot = ((0 + x0*y0) + x1*y1) + x2*y2, length = sqrtf(dot), min/max are the
-// ternaries a<b?a:b / a>b?a:b, literals are float.  Build with
+// ternaries a<b?a:b / a>b?a:b, literals are real.  Build with
 // -O3 -fno-fast-math -ffp-contract=off (cpu.py:323-334).
 //
 // ABI (mirrors the reference cpu_dispatch, cpu.py:189-300):
@@ -32,68 +32,81 @@
 #include <thread>
 #include <vector>
 
+// The arithmetic type: float (the restatement of the reference's FP32 step,
+// libdem_oracle.so) or, built with -DORACLE_FP64=1, double (the FP64 drift
+// oracle, libdem_oracle64.so: the same step with every float buffer and
+// every FP32 operation in double precision).
+#ifndef ORACLE_FP64
+#define ORACLE_FP64 0
+#endif
+#if ORACLE_FP64
+using real = double;
+#else
+using real = float;
+#endif
+
 namespace {
 
-struct float3 { float x, y, z; };
-struct float4 { float x, y, z, w; };
+struct vec3 { real x, y, z; };
+struct vec4 { real x, y, z, w; };
 struct uint4 { uint32_t x, y, z, w; };
 struct uint2 { uint32_t x, y; };
 struct double3 { double x, y, z; };
 
-inline float3 f3(float x, float y, float z) { return {x, y, z}; }
-inline float3 xyz(const float4& a) { return {a.x, a.y, a.z}; }
-inline float4 f4(const float3& a, float w) { return {a.x, a.y, a.z, w}; }
-inline float3 operator+(float3 a, float3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-inline float3 operator-(float3 a, float3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-inline float3 operator*(float3 a, float3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
-inline float3 operator/(float3 a, float3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
-inline float3 operator*(float s, float3 a) { return {s * a.x, s * a.y, s * a.z}; }
-inline float3 operator*(float3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
-inline float3 operator/(float3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
-inline float3 operator-(float3 a) { return {-a.x, -a.y, -a.z}; }
-inline float4 operator+(float4 a, float4 b) { return {a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
-inline float4 operator-(float4 a, float4 b) { return {a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w}; }
-inline float4 operator*(float4 a, float s) { return {a.x * s, a.y * s, a.z * s, a.w * s}; }
+inline vec3 f3(real x, real y, real z) { return {x, y, z}; }
+inline vec3 xyz(const vec4& a) { return {a.x, a.y, a.z}; }
+inline vec4 f4(const vec3& a, real w) { return {a.x, a.y, a.z, w}; }
+inline vec3 operator+(vec3 a, vec3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline vec3 operator-(vec3 a, vec3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline vec3 operator*(vec3 a, vec3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+inline vec3 operator/(vec3 a, vec3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+inline vec3 operator*(real s, vec3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline vec3 operator*(vec3 a, real s) { return {a.x * s, a.y * s, a.z * s}; }
+inline vec3 operator/(vec3 a, real s) { return {a.x / s, a.y / s, a.z / s}; }
+inline vec3 operator-(vec3 a) { return {-a.x, -a.y, -a.z}; }
+inline vec4 operator+(vec4 a, vec4 b) { return {a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+inline vec4 operator-(vec4 a, vec4 b) { return {a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w}; }
+inline vec4 operator*(vec4 a, real s) { return {a.x * s, a.y * s, a.z * s, a.w * s}; }
 
-inline float mn(float a, float b) { return a < b ? a : b; }
-inline float mx(float a, float b) { return a > b ? a : b; }
-inline float3 mn3(float3 a, float3 b) { return {mn(a.x, b.x), mn(a.y, b.y), mn(a.z, b.z)}; }
-inline float3 mx3(float3 a, float3 b) { return {mx(a.x, b.x), mx(a.y, b.y), mx(a.z, b.z)}; }
-inline float3 abs3(float3 a) { return {std::fabs(a.x), std::fabs(a.y), std::fabs(a.z)}; }
-inline float dot(float3 a, float3 b) {
-    float r = 0.0f;
+inline real mn(real a, real b) { return a < b ? a : b; }
+inline real mx(real a, real b) { return a > b ? a : b; }
+inline vec3 mn3(vec3 a, vec3 b) { return {mn(a.x, b.x), mn(a.y, b.y), mn(a.z, b.z)}; }
+inline vec3 mx3(vec3 a, vec3 b) { return {mx(a.x, b.x), mx(a.y, b.y), mx(a.z, b.z)}; }
+inline vec3 abs3(vec3 a) { return {std::fabs(a.x), std::fabs(a.y), std::fabs(a.z)}; }
+inline real dot(vec3 a, vec3 b) {
+    real r = 0.0f;
     r = r + a.x * b.x;
     r = r + a.y * b.y;
     r = r + a.z * b.z;
     return r;
 }
-inline float dot4(float4 a, float4 b) {
-    float r = 0.0f;
+inline real dot4(vec4 a, vec4 b) {
+    real r = 0.0f;
     r = r + a.x * b.x;
     r = r + a.y * b.y;
     r = r + a.z * b.z;
     r = r + a.w * b.w;
     return r;
 }
-inline float length(float3 a) { return std::sqrt(dot(a, a)); }
-inline float3 cross(float3 l, float3 r) {
+inline real length(vec3 a) { return std::sqrt(dot(a, a)); }
+inline vec3 cross(vec3 l, vec3 r) {
     return {l.y * r.z - l.z * r.y, l.z * r.x - l.x * r.z, l.x * r.y - l.y * r.x};
 }
-inline float comp(float3 a, uint32_t i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
-inline bool finite3(float3 a) { return std::isfinite(a.x) && std::isfinite(a.y) && std::isfinite(a.z); }
+inline real comp(vec3 a, uint32_t i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+inline bool finite3(vec3 a) { return std::isfinite(a.x) && std::isfinite(a.y) && std::isfinite(a.z); }
 
 // solver.slang:104-106
-inline float3 qrot(float4 q, float3 v) {
-    float3 u = xyz(q);
+inline vec3 qrot(vec4 q, vec3 v) {
+    vec3 u = xyz(q);
     return v + 2.0f * cross(u, cross(u, v) + q.w * v);
 }
-inline float3 qinv(float4 q, float3 v) { return qrot(float4{-q.x, -q.y, -q.z, q.w}, v); }
-inline float4 qmul(float4 a, float4 b) {
-    float3 v = (a.w * xyz(b) + b.w * xyz(a)) + cross(xyz(a), xyz(b));
+inline vec3 qinv(vec4 q, vec3 v) { return qrot(vec4{-q.x, -q.y, -q.z, q.w}, v); }
+inline vec4 qmul(vec4 a, vec4 b) {
+    vec3 v = (a.w * xyz(b) + b.w * xyz(a)) + cross(xyz(a), xyz(b));
     return f4(v, a.w * b.w - dot(xyz(a), xyz(b)));
 }
 // Slang normalize: x * rsqrt(dot(x, x)), rsqrt = 1 / sqrt.
-inline float4 normalize4(float4 q) { return q * (1.0f / std::sqrt(dot4(q, q))); }
+inline vec4 normalize4(vec4 q) { return q * (1.0f / std::sqrt(dot4(q, q))); }
 
 const uint32_t EMPTY = 0xffffffffu;
 
@@ -101,31 +114,31 @@ struct Config {
     uint32_t activeTimestep, N, shapes, pairCapacity, contactCapacity, binCapacity, binCount;
     uint32_t bins[3];
     uint32_t hashSize;
-    float dt, kn, kt, mu, normalViscosity, skin, drag, maxOverlap;
+    real dt, kn, kt, mu, normalViscosity, skin, drag, maxOverlap;
     uint32_t historyStep, meshGeometry, periodic, wallCount, wallBoxEnabled, sourceSurfaceNormal;
 };
 
 struct R {
     Config c;
-    uint32_t* control; float4* cell; float4* position; float4* positionRemainder;
-    float4* velocityRemainder; float4* momentumRemainder; float4* rotationRemainder;
-    float4* referencePositionRemainder; float4* cellLog; float4* accumulatedRemainder;
-    float4* velocity; float4* rotation; float4* momentum; float4* force; float4* torque;
-    float4* referencePosition; float4* referenceCell; uint32_t* shapeId; float4* body; float4* invI;
-    uint4* grids; uint4* sampleInfo; float4* gridOrigin; float* distance; float4* sample;
-    uint4* meshRoots; uint4* meshHullInfo; float4* meshPlanes; float4* meshMin; float4* meshMax;
-    uint4* meshLinks; float4* meshTriangles; float4* meshNormals; uint4* meshFrontier;
-    uint32_t* meshPairMask; float4* meshPairTransform; uint4* meshClusterInfo;
-    uint4* meshClusterRanges; float4* meshClusterMin; float4* meshClusterMax;
+    uint32_t* control; vec4* cell; vec4* position; vec4* positionRemainder;
+    vec4* velocityRemainder; vec4* momentumRemainder; vec4* rotationRemainder;
+    vec4* referencePositionRemainder; vec4* cellLog; vec4* accumulatedRemainder;
+    vec4* velocity; vec4* rotation; vec4* momentum; vec4* force; vec4* torque;
+    vec4* referencePosition; vec4* referenceCell; uint32_t* shapeId; vec4* body; vec4* invI;
+    uint4* grids; uint4* sampleInfo; vec4* gridOrigin; real* distance; vec4* sample;
+    uint4* meshRoots; uint4* meshHullInfo; vec4* meshPlanes; vec4* meshMin; vec4* meshMax;
+    uint4* meshLinks; vec4* meshTriangles; vec4* meshNormals; uint4* meshFrontier;
+    uint32_t* meshPairMask; vec4* meshPairTransform; uint4* meshClusterInfo;
+    uint4* meshClusterRanges; vec4* meshClusterMin; vec4* meshClusterMax;
     uint32_t* meshSampleIndices; uint32_t* binCounts; uint32_t* binParticles; uint32_t* pairCounts;
     uint32_t* pairOffsets; uint2* pairs; uint32_t* contactCounts; uint32_t* contactOffsets;
-    uint4* meta; float4* pointDepth; float4* normalArea; float4* slip; float4* contactForce;
-    float* normalLossPower; float4* normalDamping; float4* forceVelocity; float4* forceOmega;
-    uint4* oldMeta; float4* oldSlip; float4* oldNormal; uint32_t* oldHash; uint32_t* hash;
-    uint32_t* heads; uint32_t* next; float4* particleStress; float4* timestepRows;
-    float4* particleDiagnostic; float4* diagnosticRows; float4* accumulated; float4* fabricRows;
-    float4* wallPlane; float4* wallRemainder; float4* wallVelocity; float4* wallMaterial;
-    uint32_t* wallBoxIds; float4* wallRows; float4* wallAccumulated;
+    uint4* meta; vec4* pointDepth; vec4* normalArea; vec4* slip; vec4* contactForce;
+    real* normalLossPower; vec4* normalDamping; vec4* forceVelocity; vec4* forceOmega;
+    uint4* oldMeta; vec4* oldSlip; vec4* oldNormal; uint32_t* oldHash; uint32_t* hash;
+    uint32_t* heads; uint32_t* next; vec4* particleStress; vec4* timestepRows;
+    vec4* particleDiagnostic; vec4* diagnosticRows; vec4* accumulated; vec4* fabricRows;
+    vec4* wallPlane; vec4* wallRemainder; vec4* wallVelocity; vec4* wallMaterial;
+    uint32_t* wallBoxIds; vec4* wallRows; vec4* wallAccumulated;
     void** extra;      // entry-point uniform buffers
     const double* uni; // entry-point uniform scalars
 };
@@ -140,9 +153,9 @@ void bind(R& r, void** b, const double* v) {
     c.binCapacity = uint32_t(v[5]); c.binCount = uint32_t(v[6]);
     c.bins[0] = uint32_t(v[7]); c.bins[1] = uint32_t(v[8]); c.bins[2] = uint32_t(v[9]);
     c.hashSize = uint32_t(v[10]);
-    c.dt = float(v[11]); c.kn = float(v[12]); c.kt = float(v[13]); c.mu = float(v[14]);
-    c.normalViscosity = float(v[15]); c.skin = float(v[16]); c.drag = float(v[17]);
-    c.maxOverlap = float(v[18]);
+    c.dt = real(v[11]); c.kn = real(v[12]); c.kt = real(v[13]); c.mu = real(v[14]);
+    c.normalViscosity = real(v[15]); c.skin = real(v[16]); c.drag = real(v[17]);
+    c.maxOverlap = real(v[18]);
     c.historyStep = uint32_t(v[19]); c.meshGeometry = uint32_t(v[20]); c.periodic = uint32_t(v[21]);
     c.wallCount = uint32_t(v[22]); c.wallBoxEnabled = uint32_t(v[23]);
     c.sourceSurfaceNormal = uint32_t(v[24]);
@@ -152,44 +165,44 @@ void bind(R& r, void** b, const double* v) {
 inline void fail(R& r, uint32_t bit) { r.control[0] |= bit; }  // solver.slang:183, serial
 
 // solver.slang:111-118 (rounded3/4 are identities while control[15] is zero)
-inline void compensated3(float3& high, float3& low, float3 inc) {
-    float3 y = inc + low;
-    float3 nx = high + y;
-    float3 moved = nx - high;
+inline void compensated3(vec3& high, vec3& low, vec3 inc) {
+    vec3 y = inc + low;
+    vec3 nx = high + y;
+    vec3 moved = nx - high;
     low = y - moved;
     high = nx;
 }
-inline void compensated4(float4& high, float4& low, float4 inc) {
-    float4 y = inc + low;
-    float4 nx = high + y;
-    float4 moved = nx - high;
+inline void compensated4(vec4& high, vec4& low, vec4 inc) {
+    vec4 y = inc + low;
+    vec4 nx = high + y;
+    vec4 moved = nx - high;
     low = y - moved;
     high = nx;
 }
 // solver.slang:119-123
-inline float expm1Stable(float x) {
+inline real expm1Stable(real x) {
     if (std::fabs(x) < 0.01f)
         return x * (1.0f + x * (0.5f + x * (1.0f / 6.0f + x * (1.0f / 24.0f + x / 120.0f))));
     return std::exp(x) - 1.0f;
 }
-inline float3 expm1Stable3(float3 x) { return {expm1Stable(x.x), expm1Stable(x.y), expm1Stable(x.z)}; }
+inline vec3 expm1Stable3(vec3 x) { return {expm1Stable(x.x), expm1Stable(x.y), expm1Stable(x.z)}; }
 // solver.slang:124-129
-inline float4 rotationIncrement(float3 w, float dt, float4 q) {
-    float half = 0.5f * length(w) * dt;
-    float coefficient = std::fabs(half) < 0.001f ? 0.5f * dt * (1.0f - half * half / 6.0f)
+inline vec4 rotationIncrement(vec3 w, real dt, vec4 q) {
+    real half = 0.5f * length(w) * dt;
+    real coefficient = std::fabs(half) < 0.001f ? 0.5f * dt * (1.0f - half * half / 6.0f)
                                                  : std::sin(half) / length(w);
-    float cm1 = -2.0f * std::sin(0.5f * half) * std::sin(0.5f * half);
+    real cm1 = -2.0f * std::sin(0.5f * half) * std::sin(0.5f * half);
     return qmul(f4(coefficient * w, cm1), q);
 }
 // solver.slang:130-134
-inline void accumulate(R& r, uint32_t id, float4 inc) {
-    float4 high = r.accumulated[id], low = r.accumulatedRemainder[id];
+inline void accumulate(R& r, uint32_t id, vec4 inc) {
+    vec4 high = r.accumulated[id], low = r.accumulatedRemainder[id];
     compensated4(high, low, inc);
     r.accumulated[id] = high;
     r.accumulatedRemainder[id] = low;
 }
 // cpu_scheduling.slang:10-15 (FP64 branch, cast to FP32)
-inline float3 centerBranch(R& r, uint32_t i, uint32_t j) {
+inline vec3 centerBranch(R& r, uint32_t i, uint32_t j) {
     double3 box{double(r.cell[0].x), double(r.cell[0].y), double(r.cell[0].z)};
     double3 pj{double(r.position[j].x), double(r.position[j].y), double(r.position[j].z)};
     double3 pi{double(r.position[i].x), double(r.position[i].y), double(r.position[i].z)};
@@ -201,46 +214,46 @@ inline float3 centerBranch(R& r, uint32_t i, uint32_t j) {
         d.y = d.y - std::floor(d.y / box.y + 0.5) * box.y;
         d.z = d.z - std::floor(d.z / box.z + 0.5) * box.z;
     }
-    return {float(d.x), float(d.y), float(d.z)};
+    return {real(d.x), real(d.y), real(d.z)};
 }
 // solver.slang:154-158
-inline float3 omega(R& r, uint32_t i) {
-    float3 b = qinv(r.rotation[i], xyz(r.momentum[i]) + xyz(r.momentumRemainder[i]));
-    float3 w{dot(xyz(r.invI[3 * i]), b), dot(xyz(r.invI[3 * i + 1]), b), dot(xyz(r.invI[3 * i + 2]), b)};
+inline vec3 omega(R& r, uint32_t i) {
+    vec3 b = qinv(r.rotation[i], xyz(r.momentum[i]) + xyz(r.momentumRemainder[i]));
+    vec3 w{dot(xyz(r.invI[3 * i]), b), dot(xyz(r.invI[3 * i + 1]), b), dot(xyz(r.invI[3 * i + 2]), b)};
     return qrot(r.rotation[i], w);
 }
 // solver.slang:159-163
-inline float rotationalEnergy(R& r, uint32_t i, float3 l) {
-    float3 b = qinv(r.rotation[i], l);
-    float3 w{dot(xyz(r.invI[3 * i]), b), dot(xyz(r.invI[3 * i + 1]), b), dot(xyz(r.invI[3 * i + 2]), b)};
+inline real rotationalEnergy(R& r, uint32_t i, vec3 l) {
+    vec3 b = qinv(r.rotation[i], l);
+    vec3 w{dot(xyz(r.invI[3 * i]), b), dot(xyz(r.invI[3 * i + 1]), b), dot(xyz(r.invI[3 * i + 2]), b)};
     return 0.5f * dot(b, w);
 }
 // solver.slang:164-169
-inline void accumulateNormalLoss(R& r, uint32_t id, float dt) {
-    float4 value = r.normalDamping[id];
-    float3 high{value.x, 0, 0}, low{value.y, 0, 0};
+inline void accumulateNormalLoss(R& r, uint32_t id, real dt) {
+    vec4 value = r.normalDamping[id];
+    vec3 high{value.x, 0, 0}, low{value.y, 0, 0};
     compensated3(high, low, f3(value.z * dt, 0, 0));
     value.x = high.x;
     value.y = low.x;
     r.normalDamping[id] = value;
 }
 // solver.slang:176-180
-inline float cellPower(R& r, uint32_t i) {
-    float3 diagonal{r.particleStress[3 * i].x, r.particleStress[3 * i + 1].y, r.particleStress[3 * i + 2].z};
-    float3 v = xyz(r.velocity[i]);
+inline real cellPower(R& r, uint32_t i) {
+    vec3 diagonal{r.particleStress[3 * i].x, r.particleStress[3 * i + 1].y, r.particleStress[3 * i + 2].z};
+    vec3 v = xyz(r.velocity[i]);
     return -dot(diagonal + r.body[i].y * v * v, xyz(r.cell[1]));
 }
-inline float floorf_(float x) { return std::floor(x); }
+inline real floorf_(real x) { return std::floor(x); }
 // solver.slang:181-186
-inline float3 image(R& r, float3 d) {
-    float3 box = xyz(r.cell[0]);
+inline vec3 image(R& r, vec3 d) {
+    vec3 box = xyz(r.cell[0]);
     if (r.c.periodic == 0) return d;
     return d - f3(floorf_(d.x / box.x + 0.5f), floorf_(d.y / box.y + 0.5f), floorf_(d.z / box.z + 0.5f)) * box;
 }
 inline void binIndex(R& r, uint32_t i, uint32_t b[3]) {
-    float3 p = xyz(r.position[i]), box = xyz(r.cell[0]);
-    float g[3] = {floorf_(p.x / box.x * float(r.c.bins[0])), floorf_(p.y / box.y * float(r.c.bins[1])),
-                  floorf_(p.z / box.z * float(r.c.bins[2]))};
+    vec3 p = xyz(r.position[i]), box = xyz(r.cell[0]);
+    real g[3] = {floorf_(p.x / box.x * real(r.c.bins[0])), floorf_(p.y / box.y * real(r.c.bins[1])),
+                  floorf_(p.z / box.z * real(r.c.bins[2]))};
     for (int k = 0; k < 3; ++k) {
         uint32_t v = uint32_t(g[k]);
         b[k] = v < r.c.bins[k] - 1 ? v : r.c.bins[k] - 1;
@@ -250,46 +263,46 @@ inline uint32_t binFlat(R& r, const uint32_t b[3]) { return (b[0] * r.c.bins[1] 
 inline uint32_t modIndex(int a, uint32_t n) { return uint32_t((a % int(n) + int(n)) % int(n)); }
 
 // solver.slang:203-219
-float3 closestTriangle(float3 p, float3 a, float3 b, float3 c, uint32_t& feature) {
-    float3 ab = b - a, ac = c - a, ap = p - a;
-    float d1 = dot(ab, ap), d2 = dot(ac, ap);
+vec3 closestTriangle(vec3 p, vec3 a, vec3 b, vec3 c, uint32_t& feature) {
+    vec3 ab = b - a, ac = c - a, ap = p - a;
+    real d1 = dot(ab, ap), d2 = dot(ac, ap);
     feature = 4;
     if (d1 <= 0 && d2 <= 0) return a;
-    float3 bp = p - b;
-    float d3 = dot(ab, bp), d4 = dot(ac, bp);
+    vec3 bp = p - b;
+    real d3 = dot(ab, bp), d4 = dot(ac, bp);
     if (d3 >= 0 && d4 <= d3) { feature = 5; return b; }
-    float vc = d1 * d4 - d3 * d2;
+    real vc = d1 * d4 - d3 * d2;
     if (vc <= 0 && d1 >= 0 && d3 <= 0) { feature = 1; return a + (d1 / (d1 - d3)) * ab; }
-    float3 cp = p - c;
-    float d5 = dot(ab, cp), d6 = dot(ac, cp);
+    vec3 cp = p - c;
+    real d5 = dot(ab, cp), d6 = dot(ac, cp);
     if (d6 >= 0 && d5 <= d6) { feature = 6; return c; }
-    float vb = d5 * d2 - d1 * d6;
+    real vb = d5 * d2 - d1 * d6;
     if (vb <= 0 && d2 >= 0 && d6 <= 0) { feature = 3; return a + (d2 / (d2 - d6)) * ac; }
-    float va = d3 * d6 - d5 * d4;
+    real va = d3 * d6 - d5 * d4;
     if (va <= 0 && (d4 - d3) >= 0 && (d5 - d6) >= 0) {
         feature = 2;
         return b + ((d4 - d3) / ((d4 - d3) + (d5 - d6))) * (c - b);
     }
-    float inv = 1.0f / (va + vb + vc);
+    real inv = 1.0f / (va + vb + vc);
     feature = 0;
     return a + ab * (vb * inv) + ac * (vc * inv);
 }
 // solver.slang:220-223
-inline float meshBoxDistance(R& r, uint32_t node, float3 p) {
-    float3 d = mx3(mx3(xyz(r.meshMin[node]) - p, p - xyz(r.meshMax[node])), f3(0, 0, 0));
+inline real meshBoxDistance(R& r, uint32_t node, vec3 p) {
+    vec3 d = mx3(mx3(xyz(r.meshMin[node]) - p, p - xyz(r.meshMax[node])), f3(0, 0, 0));
     return dot(d, d);
 }
 // cpu_scheduling.slang:18-48 (cached pushed distances; same result as the
 // original solver.slang:224-252 walk)
-float4 meshDistance(R& r, uint32_t shape, float3 p, bool surfaceNormal) {
+vec4 meshDistance(R& r, uint32_t shape, vec3 p, bool surfaceNormal) {
     uint32_t root = r.meshRoots[shape].x;
     uint32_t pending[32];
-    float pendingDistance[32];
+    real pendingDistance[32];
     uint32_t top = 1;
     pending[0] = root;
     pendingDistance[0] = meshBoxDistance(r, root, p);
-    float best = 1e30f;
-    float3 nearest{0, 0, 0};
+    real best = 1e30f;
+    vec3 nearest{0, 0, 0};
     uint32_t nearestNormal = 0;
     bool found = false;
     while (top > 0) {
@@ -298,8 +311,8 @@ float4 meshDistance(R& r, uint32_t shape, float3 p, bool surfaceNormal) {
         uint4 link = r.meshLinks[node];
         if (link.z == 0) {
             uint32_t a = node + 1, b = r.meshLinks[a].x;
-            float da = meshBoxDistance(r, a, p), db = meshBoxDistance(r, b, p);
-            if (da < db) { uint32_t s = a; a = b; b = s; float ds = da; da = db; db = ds; }
+            real da = meshBoxDistance(r, a, p), db = meshBoxDistance(r, b, p);
+            if (da < db) { uint32_t s = a; a = b; b = s; real ds = da; da = db; db = ds; }
             if (top + 2 > 32) { fail(r, 1024); return {0, 0, 0, 1e20f}; }
             if (da <= best) { pending[top] = a; pendingDistance[top++] = da; }
             if (db <= best) { pending[top] = b; pendingDistance[top++] = db; }
@@ -307,62 +320,62 @@ float4 meshDistance(R& r, uint32_t shape, float3 p, bool surfaceNormal) {
         }
         for (uint32_t j = 0; j < link.z; ++j) {
             uint32_t triangle = link.y + j, feature;
-            float3 q = closestTriangle(p, xyz(r.meshTriangles[3 * triangle]), xyz(r.meshTriangles[3 * triangle + 1]),
+            vec3 q = closestTriangle(p, xyz(r.meshTriangles[3 * triangle]), xyz(r.meshTriangles[3 * triangle + 1]),
                                        xyz(r.meshTriangles[3 * triangle + 2]), feature);
-            float distance = dot(p - q, p - q);
+            real distance = dot(p - q, p - q);
             if (distance < best) { best = distance; nearest = q; nearestNormal = 7 * triangle + feature; found = true; }
         }
     }
-    float3 pseudo = found ? xyz(r.meshNormals[nearestNormal]) : f3(0, 0, 0);
-    float distance = std::sqrt(best);
-    float side = dot(p - nearest, pseudo) < 0 ? -1.0f : 1.0f;
-    float3 normal = surfaceNormal ? pseudo : (distance > 1e-12f ? (side * (p - nearest)) / distance : pseudo);
+    vec3 pseudo = found ? xyz(r.meshNormals[nearestNormal]) : f3(0, 0, 0);
+    real distance = std::sqrt(best);
+    real side = dot(p - nearest, pseudo) < 0 ? -1.0f : 1.0f;
+    vec3 normal = surfaceNormal ? pseudo : (distance > 1e-12f ? (side * (p - nearest)) / distance : pseudo);
     return f4(normal, side * distance);
 }
 // solver.slang:259-272
-bool meshMayContain(R& r, uint32_t shape, float3 p) {
+bool meshMayContain(R& r, uint32_t shape, vec3 p) {
     uint32_t root = r.meshRoots[shape].x;
-    float3 low = xyz(r.meshMin[root]), high = xyz(r.meshMax[root]);
+    vec3 low = xyz(r.meshMin[root]), high = xyz(r.meshMax[root]);
     if (p.x < low.x || p.y < low.y || p.z < low.z || p.x > high.x || p.y > high.y || p.z > high.z) return false;
-    float3 direction = (p - 0.5f * (low + high)) / (high - low);
-    float3 a = abs3(direction);
+    vec3 direction = (p - 0.5f * (low + high)) / (high - low);
+    vec3 a = abs3(direction);
     uint32_t axis = a.x >= a.y && a.x >= a.z ? 0 : (a.y >= a.z ? 1 : 2);
     uint32_t group = 2 * axis + (comp(direction, axis) >= 0 ? 1 : 0);
     uint4 info = r.meshHullInfo[6 * shape + group];
     for (uint32_t i = 0; i < info.y; ++i) {
-        float4 plane = r.meshPlanes[info.x + i];
+        vec4 plane = r.meshPlanes[info.x + i];
         if (dot(xyz(plane), p) + plane.w > 0) return false;
     }
     return true;
 }
 // solver.slang:274-288
-bool meshBoxMayContact(R& r, uint32_t shape, float3 low, float3 high) {
+bool meshBoxMayContact(R& r, uint32_t shape, vec3 low, vec3 high) {
     uint32_t root = r.meshRoots[shape].x;
-    float3 tl = xyz(r.meshMin[root]), th = xyz(r.meshMax[root]);
+    vec3 tl = xyz(r.meshMin[root]), th = xyz(r.meshMax[root]);
     if (high.x < tl.x || high.y < tl.y || high.z < tl.z || low.x > th.x || low.y > th.y || low.z > th.z) return false;
-    float3 center = 0.5f * (low + high), half = 0.5f * (high - low);
-    float3 direction = (center - 0.5f * (tl + th)) / (th - tl);
-    float3 a = abs3(direction);
+    vec3 center = 0.5f * (low + high), half = 0.5f * (high - low);
+    vec3 direction = (center - 0.5f * (tl + th)) / (th - tl);
+    vec3 a = abs3(direction);
     uint32_t axis = a.x >= a.y && a.x >= a.z ? 0 : (a.y >= a.z ? 1 : 2);
     uint32_t group = 2 * axis + (comp(direction, axis) >= 0 ? 1 : 0);
     uint4 info = r.meshHullInfo[6 * shape + group];
     for (uint32_t i = 0; i < info.y; ++i) {
-        float4 plane = r.meshPlanes[info.x + i];
+        vec4 plane = r.meshPlanes[info.x + i];
         if (dot(xyz(plane), center) + plane.w - dot(abs3(xyz(plane)), half) > 0) return false;
     }
     return true;
 }
 // solver.slang:290-305
 bool meshClusterMayContact(R& r, uint32_t src, uint32_t dst, uint32_t cluster) {
-    float3 sl = xyz(r.meshClusterMin[cluster]), sh = xyz(r.meshClusterMax[cluster]);
-    float3 branch = centerBranch(r, src, dst), low{1e30f, 1e30f, 1e30f}, high{-1e30f, -1e30f, -1e30f};
+    vec3 sl = xyz(r.meshClusterMin[cluster]), sh = xyz(r.meshClusterMax[cluster]);
+    vec3 branch = centerBranch(r, src, dst), low{1e30f, 1e30f, 1e30f}, high{-1e30f, -1e30f, -1e30f};
     for (uint32_t corner = 0; corner < 8; ++corner) {
-        float3 p{(corner & 1) ? sh.x : sl.x, (corner & 2) ? sh.y : sl.y, (corner & 4) ? sh.z : sl.z};
+        vec3 p{(corner & 1) ? sh.x : sl.x, (corner & 2) ? sh.y : sl.y, (corner & 4) ? sh.z : sl.z};
         p = qinv(r.rotation[dst], qrot(r.rotation[src], p * r.body[src].x) - branch) / r.body[dst].x;
         low = mn3(low, p);
         high = mx3(high, p);
     }
-    float pad = 0.00000762939453125f *
+    real pad = 0.00000762939453125f *
                 (1.0f + mx(mx(std::fabs(low.x), std::fabs(low.y)), std::fabs(low.z)) +
                  mx(mx(std::fabs(high.x), std::fabs(high.y)), std::fabs(high.z)) + length(branch) / r.body[dst].x);
     low = low - f3(pad, pad, pad);
@@ -370,18 +383,18 @@ bool meshClusterMayContact(R& r, uint32_t src, uint32_t dst, uint32_t cluster) {
     return meshBoxMayContact(r, r.shapeId[dst], low, high);
 }
 // solver.slang:404-417
-void meshPairBounds(R& r, uint32_t direction, uint32_t cluster, float3& low, float3& high) {
-    float3 center = 0.5f * (xyz(r.meshClusterMin[cluster]) + xyz(r.meshClusterMax[cluster]));
-    float3 half = 0.5f * (xyz(r.meshClusterMax[cluster]) - xyz(r.meshClusterMin[cluster]));
-    float c[3], e[3];
+void meshPairBounds(R& r, uint32_t direction, uint32_t cluster, vec3& low, vec3& high) {
+    vec3 center = 0.5f * (xyz(r.meshClusterMin[cluster]) + xyz(r.meshClusterMax[cluster]));
+    vec3 half = 0.5f * (xyz(r.meshClusterMax[cluster]) - xyz(r.meshClusterMin[cluster]));
+    real c[3], e[3];
     for (uint32_t axis = 0; axis < 3; ++axis) {
-        float4 row = r.meshPairTransform[4 * direction + axis];
+        vec4 row = r.meshPairTransform[4 * direction + axis];
         c[axis] = dot(xyz(row), center) + row.w;
         e[axis] = dot(abs3(xyz(row)), half);
     }
     low = f3(c[0], c[1], c[2]) - f3(e[0], e[1], e[2]);
     high = f3(c[0], c[1], c[2]) + f3(e[0], e[1], e[2]);
-    float pad = 0.000030517578125f *
+    real pad = 0.000030517578125f *
                 (1.0f + mx(mx(std::fabs(low.x), std::fabs(low.y)), std::fabs(low.z)) +
                  mx(mx(std::fabs(high.x), std::fabs(high.y)), std::fabs(high.z)) +
                  r.meshPairTransform[4 * direction + 3].x);
@@ -389,15 +402,15 @@ void meshPairBounds(R& r, uint32_t direction, uint32_t cluster, float3& low, flo
     high = high + f3(pad, pad, pad);
 }
 // solver.slang:319-343 with the CPU enclosure-plane prefilter (cpu.py:56-76)
-bool nodeContact(R& r, uint32_t src, uint32_t dst, uint32_t node, float4& pd, float4& na, float4 rejectionPlane) {
+bool nodeContact(R& r, uint32_t src, uint32_t dst, uint32_t node, vec4& pd, vec4& na, vec4 rejectionPlane) {
     uint32_t sid = r.shapeId[src];
-    float4 sp = r.sample[r.sampleInfo[sid].x + node];
-    float3 arm = qrot(r.rotation[src], xyz(sp) * r.body[src].x);
-    float3 branch = centerBranch(r, src, dst);
-    float3 local = qinv(r.rotation[dst], arm - branch) / r.body[dst].x;
+    vec4 sp = r.sample[r.sampleInfo[sid].x + node];
+    vec3 arm = qrot(r.rotation[src], xyz(sp) * r.body[src].x);
+    vec3 branch = centerBranch(r, src, dst);
+    vec3 local = qinv(r.rotation[dst], arm - branch) / r.body[dst].x;
     uint32_t targetShape = r.shapeId[dst];
-    float4 f;
-    float planePad = 0.00000762939453125f *
+    vec4 f;
+    real planePad = 0.00000762939453125f *
                      (1.0f + mx(mx(std::fabs(local.x), std::fabs(local.y)), std::fabs(local.z)));
     if (dot(xyz(rejectionPlane), local) + rejectionPlane.w > planePad) { pd = {0, 0, 0, 0}; na = {0, 0, 0, 0}; return false; }
     if (!meshMayContain(r, targetShape, local)) { pd = {0, 0, 0, 0}; na = {0, 0, 0, 0}; return false; }
@@ -405,10 +418,10 @@ bool nodeContact(R& r, uint32_t src, uint32_t dst, uint32_t node, float4& pd, fl
     pd = f4(arm, -f.w * r.body[dst].x);
     na = {0, 0, 0, 0};
     if (pd.w <= 0.0f) return false;
-    float3 grad = qrot(r.rotation[dst], xyz(f));
-    float len = length(grad);
+    vec3 grad = qrot(r.rotation[dst], xyz(f));
+    real len = length(grad);
     if (r.c.sourceSurfaceNormal != 0) {
-        float4 own = meshDistance(r, sid, xyz(sp), true);
+        vec4 own = meshDistance(r, sid, xyz(sp), true);
         if (std::fabs(own.w) > 0.00000999999974738f) { fail(r, 2); return false; }
         grad = -qrot(r.rotation[src], xyz(own));
         len = length(grad);
@@ -422,45 +435,45 @@ bool nodeContact(R& r, uint32_t src, uint32_t dst, uint32_t node, float4& pd, fl
 // solver.slang:188-200: trilinear signed distance and its gradient from the
 // shape's grid (FP32 order of the archived generated C++: lerp(x, y, s) =
 // x + (y - x) * s; products left to right).
-float4 sdf(R& r, uint32_t s, float3 p) {
+vec4 sdf(R& r, uint32_t s, vec3 p) {
     uint4 meta = r.grids[s];
-    float4 o = r.gridOrigin[s];
-    float3 g = (p - xyz(o)) / o.w;
+    vec4 o = r.gridOrigin[s];
+    vec3 g = (p - xyz(o)) / o.w;
     int32_t a[3] = {int32_t(std::floor(g.x)), int32_t(std::floor(g.y)), int32_t(std::floor(g.z))};
     int32_t dims[3] = {int32_t(meta.y), int32_t(meta.z), int32_t(meta.w)};
     for (int k = 0; k < 3; ++k)
         if (a[k] < 0 || a[k] >= dims[k] - 1) return {0.0f, 0.0f, 0.0f, 1.00000002004087734e+20f};
-    float3 t = g - f3(float(a[0]), float(a[1]), float(a[2]));
-    float3 u = f3(1.0f, 1.0f, 1.0f) - t;
-    float value = 0.0f;
-    float3 grad = f3(0.0f, 0.0f, 0.0f);
+    vec3 t = g - f3(real(a[0]), real(a[1]), real(a[2]));
+    vec3 u = f3(1.0f, 1.0f, 1.0f) - t;
+    real value = 0.0f;
+    vec3 grad = f3(0.0f, 0.0f, 0.0f);
     for (uint32_t i = 0; i < 2; ++i)
         for (uint32_t j = 0; j < 2; ++j)
             for (uint32_t k = 0; k < 2; ++k) {
-                float3 b = f3(float(i), float(j), float(k));
-                float3 w = u + (t - u) * b;
+                vec3 b = f3(real(i), real(j), real(k));
+                vec3 w = u + (t - u) * b;
                 uint32_t ix = uint32_t(a[0]) + i, iy = uint32_t(a[1]) + j, iz = uint32_t(a[2]) + k;
-                float f = r.distance[meta.x + (ix * meta.z + iy) * meta.w + iz];
+                real f = r.distance[meta.x + (ix * meta.z + iy) * meta.w + iz];
                 value = value + f * w.x * w.y * w.z;
-                float3 v = f3((2.0f * float(i) - 1.0f) * w.y * w.z, (2.0f * float(j) - 1.0f) * w.x * w.z,
-                              (2.0f * float(k) - 1.0f) * w.x * w.y);
+                vec3 v = f3((2.0f * real(i) - 1.0f) * w.y * w.z, (2.0f * real(j) - 1.0f) * w.x * w.z,
+                              (2.0f * real(k) - 1.0f) * w.x * w.y);
                 grad = grad + (f * v) / o.w;
             }
     return f4(grad, value);
 }
 // solver.slang:319-343 with the SDF geometry (meshGeometry == 0).
-bool nodeContactSdf(R& r, uint32_t src, uint32_t dst, uint32_t node, float4& pd, float4& na) {
+bool nodeContactSdf(R& r, uint32_t src, uint32_t dst, uint32_t node, vec4& pd, vec4& na) {
     uint32_t sid = r.shapeId[src];
-    float4 sp = r.sample[r.sampleInfo[sid].x + node];
-    float3 arm = qrot(r.rotation[src], xyz(sp) * r.body[src].x);
-    float3 branch = centerBranch(r, src, dst);
-    float3 local = qinv(r.rotation[dst], arm - branch) / r.body[dst].x;
-    float4 f = sdf(r, r.shapeId[dst], local);
+    vec4 sp = r.sample[r.sampleInfo[sid].x + node];
+    vec3 arm = qrot(r.rotation[src], xyz(sp) * r.body[src].x);
+    vec3 branch = centerBranch(r, src, dst);
+    vec3 local = qinv(r.rotation[dst], arm - branch) / r.body[dst].x;
+    vec4 f = sdf(r, r.shapeId[dst], local);
     pd = f4(arm, -f.w * r.body[dst].x);
     na = {0, 0, 0, 0};
     if (pd.w <= 0.0f) return false;
-    float3 grad = qrot(r.rotation[dst], xyz(f));
-    float len = length(grad);
+    vec3 grad = qrot(r.rotation[dst], xyz(f));
+    real len = length(grad);
     if (len < 1.00000001168609742e-07f || !std::isfinite(pd.w)) { fail(r, 2); return false; }
     na = f4(grad / len, sp.w * r.body[src].x * r.body[src].x);
     if (pd.w > r.c.maxOverlap * mn(r.body[src].w, r.body[dst].w)) fail(r, 4);
@@ -469,38 +482,38 @@ bool nodeContactSdf(R& r, uint32_t src, uint32_t dst, uint32_t node, float4& pd,
 
 // ---------------------------------------------------------------- kernels
 
-float wallStepWork(R& r, uint32_t id, float dt);
+real wallStepWork(R& r, uint32_t id, real dt);
 // solver.slang:858-888
 void beginStep(R& r, uint32_t id) {
     if (id >= r.c.N || r.control[0] != 0) return;
-    float dt = r.c.dt;
-    float3 rate = xyz(r.cell[1]);
+    real dt = r.c.dt;
+    vec3 rate = xyz(r.cell[1]);
     accumulateNormalLoss(r, id, 0.5f * dt);
-    float3 v = xyz(r.velocity[id]), vl = xyz(r.velocityRemainder[id]);
-    float3 l = xyz(r.momentum[id]), ll = xyz(r.momentumRemainder[id]);
+    vec3 v = xyz(r.velocity[id]), vl = xyz(r.velocityRemainder[id]);
+    vec3 l = xyz(r.momentum[id]), ll = xyz(r.momentumRemainder[id]);
     compensated3(v, vl, 0.5f * dt * xyz(r.force[id]) / r.body[id].y);
     compensated3(l, ll, 0.5f * dt * xyz(r.torque[id]));
-    float loss = -expm1Stable(-r.c.drag * dt) *
+    real loss = -expm1Stable(-r.c.drag * dt) *
                  (0.5f * r.body[id].y * dot(v + vl, v + vl) + rotationalEnergy(r, id, l + ll));
-    float cp = 0.5f * dt * cellPower(r, id);
-    accumulate(r, id, float4{0, loss, cp, wallStepWork(r, id, 0.5f * dt)});
-    float damping = expm1Stable(-0.5f * r.c.drag * dt);
+    real cp = 0.5f * dt * cellPower(r, id);
+    accumulate(r, id, vec4{0, loss, cp, wallStepWork(r, id, 0.5f * dt)});
+    real damping = expm1Stable(-0.5f * r.c.drag * dt);
     compensated3(v, vl, damping * (v + vl));
     compensated3(l, ll, damping * (l + ll));
     r.momentum[id] = f4(l, 0);
     r.momentumRemainder[id] = f4(ll, 0);
-    float4 q = r.rotation[id], ql = r.rotationRemainder[id];
-    float3 w = omega(r, id);
+    vec4 q = r.rotation[id], ql = r.rotationRemainder[id];
+    vec3 w = omega(r, id);
     r.rotation[id] = normalize4(q + rotationIncrement(w, 0.5f * dt, q));
     w = omega(r, id);
     compensated4(q, ql, rotationIncrement(w, dt, q));
     if (std::fabs(dot4(q, q) - 1.0f) > 2e-6f) { q = normalize4(q); ql = {0, 0, 0, 0}; }
     r.rotation[id] = q;
     r.rotationRemainder[id] = ql;
-    float3 logarithm = xyz(r.cellLog[0]), residual = xyz(r.cellLog[1]);
+    vec3 logarithm = xyz(r.cellLog[0]), residual = xyz(r.cellLog[1]);
     compensated3(logarithm, residual, rate * dt);
-    float3 box = xyz(r.cell[2]) * f3(std::exp(logarithm.x), std::exp(logarithm.y), std::exp(logarithm.z));
-    float3 p = xyz(r.position[id]), pl = xyz(r.positionRemainder[id]);
+    vec3 box = xyz(r.cell[2]) * f3(std::exp(logarithm.x), std::exp(logarithm.y), std::exp(logarithm.z));
+    vec3 p = xyz(r.position[id]), pl = xyz(r.positionRemainder[id]);
     compensated3(p, pl, expm1Stable3(rate * dt) * (p + pl) + dt * (v + vl));
     if (!finite3(p) || !finite3(pl)) { fail(r, 512); return; }
     if (r.c.periodic != 0) p = p - f3(floorf_(p.x / box.x), floorf_(p.y / box.y), floorf_(p.z / box.z)) * box;
@@ -515,7 +528,7 @@ void beginStep(R& r, uint32_t id) {
 // solver.slang:889-897
 void advanceCell(R& r) {
     if (r.control[0] != 0) return;
-    float3 logarithm = xyz(r.cellLog[0]), residual = xyz(r.cellLog[1]);
+    vec3 logarithm = xyz(r.cellLog[0]), residual = xyz(r.cellLog[1]);
     compensated3(logarithm, residual, xyz(r.cell[1]) * r.c.dt);
     r.cellLog[0] = f4(logarithm, 0);
     r.cellLog[1] = f4(residual, 0);
@@ -526,24 +539,24 @@ void advanceCell(R& r) {
 // solver.slang:898-904
 void checkRebuild(R& r, uint32_t id) {
     if (id >= r.c.N) return;
-    float3 d = image(r, (xyz(r.position[id]) - xyz(r.referencePosition[id])) +
+    vec3 d = image(r, (xyz(r.position[id]) - xyz(r.referencePosition[id])) +
                             (xyz(r.positionRemainder[id]) - xyz(r.referencePositionRemainder[id])));
-    float deformation = length(xyz(r.cell[0]) - xyz(r.referenceCell[0]));
+    real deformation = length(xyz(r.cell[0]) - xyz(r.referenceCell[0]));
     if (length(d) + deformation > 0.5f * r.c.skin) r.control[4] |= 1;
 }
 // solver.slang:905-920
 void finishStep(R& r, uint32_t id) {
     if (id >= r.c.N || r.control[0] != 0) return;
     accumulateNormalLoss(r, id, 0.5f * r.c.dt);
-    float3 v = xyz(r.velocity[id]), vl = xyz(r.velocityRemainder[id]);
-    float3 l = xyz(r.momentum[id]), ll = xyz(r.momentumRemainder[id]);
+    vec3 v = xyz(r.velocity[id]), vl = xyz(r.velocityRemainder[id]);
+    vec3 l = xyz(r.momentum[id]), ll = xyz(r.momentumRemainder[id]);
     compensated3(v, vl, 0.5f * r.c.dt * xyz(r.force[id]) / r.body[id].y);
     compensated3(l, ll, 0.5f * r.c.dt * xyz(r.torque[id]));
-    float loss = -expm1Stable(-r.c.drag * r.c.dt) *
+    real loss = -expm1Stable(-r.c.drag * r.c.dt) *
                  (0.5f * r.body[id].y * dot(v + vl, v + vl) + rotationalEnergy(r, id, l + ll));
-    float cp = 0.5f * r.c.dt * cellPower(r, id);
-    accumulate(r, id, float4{0, loss, cp, wallStepWork(r, id, 0.5f * r.c.dt)});
-    float damping = expm1Stable(-0.5f * r.c.drag * r.c.dt);
+    real cp = 0.5f * r.c.dt * cellPower(r, id);
+    accumulate(r, id, vec4{0, loss, cp, wallStepWork(r, id, 0.5f * r.c.dt)});
+    real damping = expm1Stable(-0.5f * r.c.drag * r.c.dt);
     compensated3(v, vl, damping * (v + vl));
     compensated3(l, ll, damping * (l + ll));
     if (!finite3(v) || !finite3(l)) { fail(r, 512); return; }
@@ -565,9 +578,9 @@ void clearBins(R& r, uint32_t id) {
 }
 void fillBins(R& r, uint32_t id) {
     if (id >= r.c.N || r.control[4] == 0) return;
-    float3 p = xyz(r.position[id]), pl = xyz(r.positionRemainder[id]);
+    vec3 p = xyz(r.position[id]), pl = xyz(r.positionRemainder[id]);
     if (!finite3(p) || !finite3(pl)) { fail(r, 512); return; }
-    float3 box = xyz(r.cell[0]);
+    vec3 box = xyz(r.cell[0]);
     if (r.c.periodic == 0 && (p.x + pl.x < 0 || p.y + pl.y < 0 || p.z + pl.z < 0 || (p.x - box.x) + pl.x >= 0 ||
                               (p.y - box.y) + pl.y >= 0 || (p.z - box.z) + pl.z >= 0)) { fail(r, 2048); return; }
     uint32_t b[3];
@@ -581,12 +594,12 @@ void fillBins(R& r, uint32_t id) {
 uint32_t findPairs(R& r, uint32_t id, bool emit) {
     uint32_t b[3];
     binIndex(r, id, b);
-    float cutoff = r.referenceCell[1].w;
+    real cutoff = r.referenceCell[1].w;
     int reach[3], low[3], high[3];
     uint32_t width[3];
-    float box[3] = {r.cell[0].x, r.cell[0].y, r.cell[0].z};
+    real box[3] = {r.cell[0].x, r.cell[0].y, r.cell[0].z};
     for (int k = 0; k < 3; ++k) {
-        reach[k] = int(std::ceil(cutoff / box[k] * float(r.c.bins[k])));
+        reach[k] = int(std::ceil(cutoff / box[k] * real(r.c.bins[k])));
         low[k] = int(b[k]) - reach[k] > 0 ? int(b[k]) - reach[k] : 0;
         high[k] = int(b[k]) + reach[k] < int(r.c.bins[k]) - 1 ? int(b[k]) + reach[k] : int(r.c.bins[k]) - 1;
         uint32_t w = uint32_t(2 * reach[k] + 1);
@@ -605,9 +618,9 @@ uint32_t findPairs(R& r, uint32_t id, bool emit) {
                 for (uint32_t slot = 0; slot < occupancy; ++slot) {
                     uint32_t j = r.binParticles[bi * r.c.binCapacity + slot];
                     if (j <= id) continue;
-                    float3 d = centerBranch(r, id, j);
+                    vec3 d = centerBranch(r, id, j);
                     if (r.c.sourceSurfaceNormal != 0 && dot(d, d) < 1e-12f) { fail(r, 16384); continue; }
-                    float range = r.body[id].z + r.body[j].z + r.c.skin;
+                    real range = r.body[id].z + r.body[j].z + r.c.skin;
                     if (dot(d, d) > range * range) continue;
                     if (emit) {
                         uint32_t index = r.pairOffsets[id] + count;
@@ -652,7 +665,7 @@ void countContacts(R& r, uint32_t pair) {
         uint2 ij = r.pairs[pair];
         uint32_t a, total = sdfNodes(r, ij, a);
         for (uint32_t s = 0; s < total; ++s) {
-            float4 pd, na;
+            vec4 pd, na;
             if (nodeContactSdf(r, s < a ? ij.x : ij.y, s < a ? ij.y : ij.x, s < a ? s : s - a, pd, na)) count++;
         }
     }
@@ -680,7 +693,7 @@ void emitContacts(R& r, uint32_t pair) {
     for (uint32_t lane = 0; lane < 64; ++lane)
         for (uint32_t s = lane; s < total; s += 64) {
             uint32_t i = s < a ? ij.x : ij.y, j = s < a ? ij.y : ij.x, node = s < a ? s : s - a;
-            float4 pd, na;
+            vec4 pd, na;
             if (nodeContactSdf(r, i, j, node, pd, na)) {
                 if (offset >= r.c.contactCapacity) { fail(r, 32); break; }
                 r.meta[offset] = uint4{i, j, node, 0};
@@ -707,16 +720,16 @@ void prepareMeshPairs(R& r, uint32_t id) {
     for (uint32_t pass = 0; pass < 2; ++pass) {
         if ((mask & (1u << pass)) == 0) continue;
         uint32_t i = pass == 0 ? ij.x : ij.y, j = pass == 0 ? ij.y : ij.x;
-        float ratio = r.body[i].x / r.body[j].x;
-        float3 a = qinv(r.rotation[j], qrot(r.rotation[i], f3(ratio, 0, 0)));
-        float3 b = qinv(r.rotation[j], qrot(r.rotation[i], f3(0, ratio, 0)));
-        float3 c = qinv(r.rotation[j], qrot(r.rotation[i], f3(0, 0, ratio)));
-        float3 branch = centerBranch(r, i, j), offset = qinv(r.rotation[j], -branch) / r.body[j].x;
+        real ratio = r.body[i].x / r.body[j].x;
+        vec3 a = qinv(r.rotation[j], qrot(r.rotation[i], f3(ratio, 0, 0)));
+        vec3 b = qinv(r.rotation[j], qrot(r.rotation[i], f3(0, ratio, 0)));
+        vec3 c = qinv(r.rotation[j], qrot(r.rotation[i], f3(0, 0, ratio)));
+        vec3 branch = centerBranch(r, i, j), offset = qinv(r.rotation[j], -branch) / r.body[j].x;
         uint32_t base = 4 * (2 * id + pass);
-        r.meshPairTransform[base] = float4{a.x, b.x, c.x, offset.x};
-        r.meshPairTransform[base + 1] = float4{a.y, b.y, c.y, offset.y};
-        r.meshPairTransform[base + 2] = float4{a.z, b.z, c.z, offset.z};
-        r.meshPairTransform[base + 3] = float4{length(branch) / r.body[j].x, 0, 0, 0};
+        r.meshPairTransform[base] = vec4{a.x, b.x, c.x, offset.x};
+        r.meshPairTransform[base + 1] = vec4{a.y, b.y, c.y, offset.y};
+        r.meshPairTransform[base + 2] = vec4{a.z, b.z, c.z, offset.z};
+        r.meshPairTransform[base + 3] = vec4{length(branch) / r.body[j].x, 0, 0, 0};
     }
     r.meshPairMask[id] = mask;
 }
@@ -726,14 +739,14 @@ void cpuCollectMesh(R& r, uint32_t pair) {
     uint2 ij = r.pairs[pair];
     for (uint32_t pass = 0; pass < 2; ++pass) {
         uint32_t i = pass == 0 ? ij.x : ij.y, j = pass == 0 ? ij.y : ij.x;
-        float3 sourceCentre = -qinv(r.rotation[j], centerBranch(r, i, j)) / r.body[j].x;
-        float4 rejectionPlane{0, 0, 0, 0};
-        float largest = -1e30f;
+        vec3 sourceCentre = -qinv(r.rotation[j], centerBranch(r, i, j)) / r.body[j].x;
+        vec4 rejectionPlane{0, 0, 0, 0};
+        real largest = -1e30f;
         for (uint32_t group = 0; group < 6; ++group) {
             uint4 hull = r.meshHullInfo[6 * r.shapeId[j] + group];
             for (uint32_t plane = 0; plane < hull.y; ++plane) {
-                float4 enclosure = r.meshPlanes[hull.x + plane];
-                float violation = dot(xyz(enclosure), sourceCentre) + enclosure.w;
+                vec4 enclosure = r.meshPlanes[hull.x + plane];
+                real violation = dot(xyz(enclosure), sourceCentre) + enclosure.w;
                 if (violation > largest) { largest = violation; rejectionPlane = enclosure; }
             }
         }
@@ -745,7 +758,7 @@ void cpuCollectMesh(R& r, uint32_t pair) {
             if (candidate) {
                 for (uint32_t lane = 0; lane < range.y; ++lane) {
                     uint32_t node = r.meshSampleIndices[range.x + lane];
-                    float4 pd, na;
+                    vec4 pd, na;
                     if (nodeContact(r, i, j, node, pd, na, rejectionPlane)) {
                         uint32_t offset = r.control[2]++;
                         if (offset >= r.c.contactCapacity) { fail(r, 32); return; }
@@ -770,14 +783,14 @@ void collectParallel(R& r, uint32_t pairs, uint32_t threads) {
         return;
     }
     std::vector<std::vector<uint4>> meta(pairs);
-    std::vector<std::vector<float4>> point(pairs), normal(pairs);
+    std::vector<std::vector<vec4>> point(pairs), normal(pairs);
     std::vector<uint32_t> flags(pairs, 0), counts(pairs, 0);
     std::atomic<uint32_t> next{0};
     auto worker = [&]() {
         R local = r;
         uint32_t control[16];
         std::vector<uint4> m;
-        std::vector<float4> pd, na;
+        std::vector<vec4> pd, na;
         for (;;) {
             uint32_t pair = next.fetch_add(1, std::memory_order_relaxed);
             if (pair >= pairs) return;
@@ -817,8 +830,8 @@ void collectParallel(R& r, uint32_t pairs, uint32_t threads) {
         size_t k = meta[p].size();
         if (k) {
             std::memcpy(r.meta + offset, meta[p].data(), k * sizeof(uint4));
-            std::memcpy(r.pointDepth + offset, point[p].data(), k * sizeof(float4));
-            std::memcpy(r.normalArea + offset, normal[p].data(), k * sizeof(float4));
+            std::memcpy(r.pointDepth + offset, point[p].data(), k * sizeof(vec4));
+            std::memcpy(r.normalArea + offset, normal[p].data(), k * sizeof(vec4));
         }
         r.contactCounts[p] = uint32_t(k);
         offset += k;
@@ -828,14 +841,14 @@ void collectParallel(R& r, uint32_t pairs, uint32_t threads) {
 // (count, scan, total, emit); every node of both grains, no cull.
 void exhaustiveContacts(R& r) {
     uint32_t pairs = activePairs(r);
-    float4 none{0, 0, 0, 0};
+    vec4 none{0, 0, 0, 0};
     std::vector<uint32_t> counts(r.c.pairCapacity, 0);
     if (r.control[0] == 0) {
         for (uint32_t pair = 0; pair < pairs; ++pair) {
             uint2 ij = r.pairs[pair];
             uint32_t a = r.sampleInfo[r.shapeId[ij.x]].y, total = a + r.sampleInfo[r.shapeId[ij.y]].y;
             for (uint32_t s = 0; s < total; ++s) {
-                float4 pd, na;
+                vec4 pd, na;
                 if (nodeContact(r, s < a ? ij.x : ij.y, s < a ? ij.y : ij.x, s < a ? s : s - a, pd, na, none)) counts[pair]++;
             }
         }
@@ -851,7 +864,7 @@ void exhaustiveContacts(R& r) {
         uint32_t a = r.sampleInfo[r.shapeId[ij.x]].y, total = a + r.sampleInfo[r.shapeId[ij.y]].y, o = r.contactOffsets[pair];
         for (uint32_t s = 0; s < total; ++s) {
             uint32_t i = s < a ? ij.x : ij.y, j = s < a ? ij.y : ij.x, node = s < a ? s : s - a;
-            float4 pd, na;
+            vec4 pd, na;
             if (nodeContact(r, i, j, node, pd, na, none)) {
                 if (o >= r.c.contactCapacity) { fail(r, 32); break; }
                 r.meta[o] = uint4{i, j, node, 0};
@@ -865,19 +878,19 @@ void exhaustiveContacts(R& r) {
 // ------------------------------------------------------------------ planes
 // solver.slang:578-595: error-free two-sums (the materialisation mask
 // rounded1 is the identity while control[15] is zero).
-struct Sum2 { float hi, lo; };
-inline Sum2 wallTwoSum(float a, float b) {
-    float high = a + b, v = high - a;
-    float low = (a - (high - v)) + (b - v);
+struct Sum2 { real hi, lo; };
+inline Sum2 wallTwoSum(real a, real b) {
+    real high = a + b, v = high - a;
+    real low = (a - (high - v)) + (b - v);
     return {high, low};
 }
-inline Sum2 wallAdd(Sum2 a, float b) {
+inline Sum2 wallAdd(Sum2 a, real b) {
     Sum2 sum = wallTwoSum(a.hi, b);
     return wallTwoSum(sum.hi, sum.lo + a.lo);
 }
-inline Sum2 wallAddDot(Sum2 sum, float3 a, float3 b) {
-    float3 product = a * b;
-    float3 error{std::fma(a.x, b.x, -product.x), std::fma(a.y, b.y, -product.y), std::fma(a.z, b.z, -product.z)};
+inline Sum2 wallAddDot(Sum2 sum, vec3 a, vec3 b) {
+    vec3 product = a * b;
+    vec3 error{std::fma(a.x, b.x, -product.x), std::fma(a.y, b.y, -product.y), std::fma(a.z, b.z, -product.z)};
     for (uint32_t axis = 0; axis < 3; ++axis) {
         sum = wallAdd(sum, comp(product, axis));
         sum = wallAdd(sum, comp(error, axis));
@@ -886,8 +899,8 @@ inline Sum2 wallAddDot(Sum2 sum, float3 a, float3 b) {
 }
 // solver.slang:596-604: the plane's signed offset at the grain centre.
 Sum2 wallCentreDistance(R& r, uint32_t body, uint32_t wall) {
-    float4 plane = r.wallPlane[wall], low = r.wallRemainder[wall];
-    float3 p = xyz(r.position[body]), pl = xyz(r.positionRemainder[body]);
+    vec4 plane = r.wallPlane[wall], low = r.wallRemainder[wall];
+    vec3 p = xyz(r.position[body]), pl = xyz(r.positionRemainder[body]);
     Sum2 sum{-plane.w, -low.w};
     sum = wallAddDot(sum, xyz(plane), p);
     sum = wallAddDot(sum, xyz(plane), pl);
@@ -895,7 +908,7 @@ Sum2 wallCentreDistance(R& r, uint32_t body, uint32_t wall) {
     return wallAddDot(sum, xyz(low), pl);
 }
 // solver.slang:605-610
-float localWallDistance(R& r, uint32_t body, uint32_t wall, float3 arm) {
+real localWallDistance(R& r, uint32_t body, uint32_t wall, vec3 arm) {
     Sum2 sum = wallCentreDistance(r, body, wall);
     sum = wallAddDot(sum, xyz(r.wallPlane[wall]), arm);
     sum = wallAddDot(sum, xyz(r.wallRemainder[wall]), arm);
@@ -903,24 +916,24 @@ float localWallDistance(R& r, uint32_t body, uint32_t wall, float3 arm) {
 }
 // solver.slang:613-624
 bool wallClusterMayContact(R& r, uint32_t body, uint32_t wall, uint32_t cluster) {
-    float3 low = xyz(r.meshClusterMin[cluster]), high = xyz(r.meshClusterMax[cluster]);
-    float4 plane = r.wallPlane[wall];
-    float3 normal = qinv(r.rotation[body], xyz(plane)) * r.body[body].x;
-    float3 center = 0.5f * (low + high), half = 0.5f * (high - low);
+    vec3 low = xyz(r.meshClusterMin[cluster]), high = xyz(r.meshClusterMax[cluster]);
+    vec4 plane = r.wallPlane[wall];
+    vec3 normal = qinv(r.rotation[body], xyz(plane)) * r.body[body].x;
+    vec3 center = 0.5f * (low + high), half = 0.5f * (high - low);
     Sum2 centreDistance = wallCentreDistance(r, body, wall);
-    float base = centreDistance.hi + centreDistance.lo;
-    float support = dot(normal, center) - dot(abs3(normal), half);
-    float pad = 64.0f * 1.1920928955078125e-7f *
+    real base = centreDistance.hi + centreDistance.lo;
+    real support = dot(normal, center) - dot(abs3(normal), half);
+    real pad = 64.0f * 1.1920928955078125e-7f *
                 (((1.0f + std::fabs(plane.w)) + length(xyz(r.position[body]))) +
                  length(normal) * (length(center) + length(half)));
     return base + support <= pad;
 }
 // solver.slang:625-638 (serial append)
 void appendWallContact(R& r, uint32_t body, uint32_t wall, uint32_t node) {
-    float4 point = r.sample[r.sampleInfo[r.shapeId[body]].x + node];
-    float3 arm = qrot(r.rotation[body], xyz(point) * r.body[body].x);
-    float4 plane = r.wallPlane[wall];
-    float phi = localWallDistance(r, body, wall, arm);
+    vec4 point = r.sample[r.sampleInfo[r.shapeId[body]].x + node];
+    vec3 arm = qrot(r.rotation[body], xyz(point) * r.body[body].x);
+    vec4 plane = r.wallPlane[wall];
+    real phi = localWallDistance(r, body, wall, arm);
     if (!std::isfinite(phi)) { fail(r, 512); return; }
     if (phi >= 0) return;
     if (-phi > r.c.maxOverlap * r.body[body].w) fail(r, 4);
@@ -935,10 +948,10 @@ void appendWallContact(R& r, uint32_t body, uint32_t wall, uint32_t node) {
 void collectWallContacts(R& r, uint32_t id) {
     uint32_t body = id % r.c.N, wall = id / r.c.N;
     if (wall >= r.c.wallCount || r.control[0] != 0) return;
-    float4 plane = r.wallPlane[wall];
+    vec4 plane = r.wallPlane[wall];
     Sum2 centreDistance = wallCentreDistance(r, body, wall);
-    float phi = centreDistance.hi + centreDistance.lo;
-    float pad = 64.0f * 1.1920928955078125e-7f * ((1.0f + length(xyz(r.position[body]))) + std::fabs(plane.w));
+    real phi = centreDistance.hi + centreDistance.lo;
+    real pad = 64.0f * 1.1920928955078125e-7f * ((1.0f + length(xyz(r.position[body]))) + std::fabs(plane.w));
     if (phi > r.body[body].z + pad) return;
     if (r.c.meshGeometry == 0) {
         uint32_t count = r.sampleInfo[r.shapeId[body]].y;
@@ -960,8 +973,8 @@ void collectWallContacts(R& r, uint32_t id) {
 void advanceWalls(R& r) {
     if (r.control[0] != 0) return;
     for (uint32_t w = 0; w < r.c.wallCount; ++w) {
-        float4 plane = r.wallPlane[w], residual = r.wallRemainder[w];
-        float3 high{plane.w, 0, 0}, low{residual.w, 0, 0};
+        vec4 plane = r.wallPlane[w], residual = r.wallRemainder[w];
+        vec3 high{plane.w, 0, 0}, low{residual.w, 0, 0};
         compensated3(high, low, f3(dot(xyz(plane), xyz(r.wallVelocity[w])) * r.c.dt, 0, 0));
         plane.w = high.x;
         residual.w = low.x;
@@ -972,23 +985,23 @@ void advanceWalls(R& r) {
     if (r.c.wallBoxEnabled != 0) {
         for (uint32_t axis = 0; axis < 3; ++axis) {
             uint32_t lo = r.wallBoxIds[2 * axis], hi = r.wallBoxIds[2 * axis + 1];
-            float low = r.wallPlane[lo].w + r.wallRemainder[lo].w;
-            float high = -(r.wallPlane[hi].w + r.wallRemainder[hi].w);
+            real low = r.wallPlane[lo].w + r.wallRemainder[lo].w;
+            real high = -(r.wallPlane[hi].w + r.wallRemainder[hi].w);
             if (low < 0 || high > comp(xyz(r.cell[0]), axis) || high <= low) fail(r, 4096);
         }
     }
 }
 // solver.slang:135-146: half-step wall work per (wall, grain) row.
-float wallStepWork(R& r, uint32_t id, float dt) {
-    float total = 0;
+real wallStepWork(R& r, uint32_t id, real dt) {
+    real total = 0;
     for (uint32_t w = 0; w < r.c.wallCount; ++w) {
         uint32_t index = w * r.c.N + id;
-        float increment = dt * r.wallRows[3 * index + 1].w;
-        float4 state = r.wallAccumulated[index];
-        float3 high{state.x, 0, 0}, low{state.y, 0, 0};
+        real increment = dt * r.wallRows[3 * index + 1].w;
+        vec4 state = r.wallAccumulated[index];
+        vec3 high{state.x, 0, 0}, low{state.y, 0, 0};
         compensated3(high, low, f3(increment, 0, 0));
-        r.wallAccumulated[index] = float4{high.x, low.x, 0, 0};
-        r.wallRows[3 * index + 2] = float4{high.x + low.x, 0, 0, 0};
+        r.wallAccumulated[index] = vec4{high.x, low.x, 0, 0};
+        r.wallRows[3 * index + 2] = vec4{high.x + low.x, 0, 0, 0};
         total = total + increment;
     }
     return total;
@@ -997,15 +1010,15 @@ float wallStepWork(R& r, uint32_t id, float dt) {
 void gatherWallRows(R& r, uint32_t index) {
     if (index >= r.c.N * r.c.wallCount || r.control[0] != 0) return;
     uint32_t body = index % r.c.N, wall = index / r.c.N, count = 0, visited = 0;
-    float3 reaction{0, 0, 0}, moment{0, 0, 0};
-    float power = 0;
+    vec3 reaction{0, 0, 0}, moment{0, 0, 0};
+    real power = 0;
     uint32_t entry = r.heads[body];
     while (entry != EMPTY) {
         if (visited++ > 2 * r.c.contactCapacity) { fail(r, 128); return; }
         uint32_t contact = entry / 2;
         if (r.meta[contact].y == r.c.N + wall) {
-            float3 force = xyz(r.contactForce[contact]);
-            float3 point = (xyz(r.position[body]) + xyz(r.positionRemainder[body])) + xyz(r.pointDepth[contact]);
+            vec3 force = xyz(r.contactForce[contact]);
+            vec3 point = (xyz(r.position[body]) + xyz(r.positionRemainder[body])) + xyz(r.pointDepth[contact]);
             reaction = reaction - force;
             moment = moment - cross(point, force);
             power = power + dot(force, xyz(r.wallVelocity[wall]));
@@ -1013,17 +1026,23 @@ void gatherWallRows(R& r, uint32_t index) {
         }
         entry = r.next[entry];
     }
-    float4 work = r.wallAccumulated[index];
-    float bits;
+    vec4 work = r.wallAccumulated[index];
+    // The contact count travels in the row's w as an integer bit pattern;
+    // the FP64 build (a drift oracle without planes) stores its value.
+#if ORACLE_FP64
+    real bits = real(count);
+#else
+    real bits;
     std::memcpy(&bits, &count, 4);
+#endif
     r.wallRows[3 * index] = f4(reaction, bits);
     r.wallRows[3 * index + 1] = f4(moment, power);
-    r.wallRows[3 * index + 2] = float4{work.x + work.y, 0, 0, 0};
+    r.wallRows[3 * index + 2] = vec4{work.x + work.y, 0, 0, 0};
 }
 // solver.slang:950-955
 void refreshWallPower(R& r, uint32_t index) {
     if (index >= r.c.N * r.c.wallCount) return;
-    float4 value = r.wallRows[3 * index + 1];
+    vec4 value = r.wallRows[3 * index + 1];
     value.w = -dot(xyz(r.wallRows[3 * index]), xyz(r.wallVelocity[index / r.c.N]));
     r.wallRows[3 * index + 1] = value;
 }
@@ -1034,39 +1053,39 @@ inline uint32_t hashKey(R& r, uint4 key) {
     h ^= h >> 16;
     return h & (r.c.hashSize - 1);
 }
-float3 transported(float3 x, float3 a, float3 b, float spin) {
-    float c = mn(mx(dot(a, b), -1.0f), 1.0f);
+vec3 transported(vec3 x, vec3 a, vec3 b, real spin) {
+    real c = mn(mx(dot(a, b), -1.0f), 1.0f);
     if (c < -0.999999f) return {0, 0, 0};
-    float3 v = cross(a, b);
-    float3 out = x + cross(v, x) + cross(v, cross(v, x)) / (1.0f + c);
+    vec3 v = cross(a, b);
+    vec3 out = x + cross(v, x) + cross(v, cross(v, x)) / (1.0f + c);
     out = out * std::cos(spin) + cross(b, out) * std::sin(spin) + b * dot(b, out) * (1.0f - std::cos(spin));
     return out - b * dot(out, b);
 }
 // normal.slang:2-11
-struct NormalResponse { float force, lossPower; };
-NormalResponse normalResponse(float depth, float area, float normalVelocity, float stiffness, float viscosity, float weight) {
+struct NormalResponse { real force, lossPower; };
+NormalResponse normalResponse(real depth, real area, real normalVelocity, real stiffness, real viscosity, real weight) {
     NormalResponse value{0, 0};
     if (depth <= 0) return value;
-    float elastic = weight * stiffness * area * depth;
+    real elastic = weight * stiffness * area * depth;
     value.force = viscosity == 0 ? elastic : mx(0.0f, elastic - weight * viscosity * area * normalVelocity);
     value.lossPower = mx(0.0f, (elastic - value.force) * normalVelocity);
     return value;
 }
 // plane.slang:6-36: one-sided penalty plane with Coulomb slip.
-struct PlaneResponse { float4 forceEnergy, slipLoss; bool sliding; float normalLossPower; };
-PlaneResponse planeViscousResponse(float3 normal, float signedDistance, float area, float3 relativeVelocity,
-                                   float3 oldSlip, float kn, float kt, float mu, float viscosity, float dt) {
+struct PlaneResponse { vec4 forceEnergy, slipLoss; bool sliding; real normalLossPower; };
+PlaneResponse planeViscousResponse(vec3 normal, real signedDistance, real area, vec3 relativeVelocity,
+                                   vec3 oldSlip, real kn, real kt, real mu, real viscosity, real dt) {
     PlaneResponse value{{0, 0, 0, 0}, {0, 0, 0, 0}, false, 0};
     if (signedDistance >= 0) return value;
-    float depth = -signedDistance;
-    float3 tangent = relativeVelocity - normal * dot(relativeVelocity, normal);
-    float3 trial = oldSlip - normal * dot(oldSlip, normal) + dt * tangent;
-    float3 slip = trial;
+    real depth = -signedDistance;
+    vec3 tangent = relativeVelocity - normal * dot(relativeVelocity, normal);
+    vec3 trial = oldSlip - normal * dot(oldSlip, normal) + dt * tangent;
+    vec3 slip = trial;
     NormalResponse response = normalResponse(depth, area, dot(relativeVelocity, normal), kn, viscosity, 1.0f);
-    float fn = response.force;
+    real fn = response.force;
     value.normalLossPower = response.lossPower;
-    float3 ft = -kt * area * slip;
-    float magnitude = length(ft);
+    vec3 ft = -kt * area * slip;
+    real magnitude = length(ft);
     if (magnitude > mu * fn && magnitude > 0) {
         value.sliding = true;
         ft = ft * (mu * fn / magnitude);
@@ -1087,13 +1106,13 @@ void resolveContacts(R& r, uint32_t id) {
     if (id >= activeContacts(r) || r.control[0] != 0) return;
     uint4 key = r.meta[id];
     uint32_t i = key.x, j = key.y;
-    float3 n = xyz(r.normalArea[id]);
+    vec3 n = xyz(r.normalArea[id]);
     bool wall = j >= r.c.N;
-    float viscosity = r.c.normalViscosity;
+    real viscosity = r.c.normalViscosity;
     if (wall) viscosity = r.wallMaterial[j - r.c.N].w;
-    float3 wi = viscosity > 0 ? xyz(r.forceOmega[i]) : omega(r, i), wj{0, 0, 0};
+    vec3 wi = viscosity > 0 ? xyz(r.forceOmega[i]) : omega(r, i), wj{0, 0, 0};
     if (!wall) wj = viscosity > 0 ? xyz(r.forceOmega[j]) : omega(r, j);
-    float3 elastic{0, 0, 0};
+    vec3 elastic{0, 0, 0};
     uint32_t slot = hashKey(r, key);
     if (r.c.historyStep != 0) {
         for (uint32_t probe = 0; probe < r.c.hashSize; ++probe) {
@@ -1107,18 +1126,18 @@ void resolveContacts(R& r, uint32_t id) {
             slot = (slot + 1) & (r.c.hashSize - 1);
         }
     }
-    float3 arm = xyz(r.pointDepth[id]);
+    vec3 arm = xyz(r.pointDepth[id]);
     if (wall) {
         uint32_t w = j - r.c.N;
-        float4 material = r.wallMaterial[w];
-        float3 v = viscosity > 0 ? xyz(r.forceVelocity[i]) : xyz(r.velocity[i]) + xyz(r.velocityRemainder[i]);
-        float3 rv = v + cross(wi, arm) - xyz(r.wallVelocity[w]);
+        vec4 material = r.wallMaterial[w];
+        vec3 v = viscosity > 0 ? xyz(r.forceVelocity[i]) : xyz(r.velocity[i]) + xyz(r.velocityRemainder[i]);
+        vec3 rv = v + cross(wi, arm) - xyz(r.wallVelocity[w]);
         PlaneResponse response = planeViscousResponse(n, -r.pointDepth[id].w, r.normalArea[id].w, rv, elastic,
                                                       material.x, material.y, material.z, material.w, r.c.dt);
         r.slip[id] = response.slipLoss;
         r.contactForce[id] = response.forceEnergy;
         r.normalLossPower[id] = response.normalLossPower;
-        float4 fe = response.forceEnergy;
+        vec4 fe = response.forceEnergy;
         if (!std::isfinite(fe.x) || !std::isfinite(fe.y) || !std::isfinite(fe.z) || !std::isfinite(fe.w) ||
             !std::isfinite(response.normalLossPower)) { fail(r, 512); return; }
         if (response.sliding) r.control[6]++;
@@ -1128,25 +1147,25 @@ void resolveContacts(R& r, uint32_t id) {
         r.next[2 * id + 1] = EMPTY;
         return;
     }
-    float3 branch = centerBranch(r, i, j);
-    float3 translation = xyz(r.velocity[i]) - xyz(r.velocity[j]);
+    vec3 branch = centerBranch(r, i, j);
+    vec3 translation = xyz(r.velocity[i]) - xyz(r.velocity[j]);
     if (viscosity > 0) translation = xyz(r.forceVelocity[i]) - xyz(r.forceVelocity[j]);
-    float3 rv = translation - xyz(r.cell[1]) * branch + cross(wi, arm) - cross(wj, arm - branch);
+    vec3 rv = translation - xyz(r.cell[1]) * branch + cross(wi, arm) - cross(wj, arm - branch);
     elastic = elastic + (rv - n * dot(rv, n)) * r.c.dt;
-    float3 trial = elastic;
-    float area = r.normalArea[id].w, depth = r.pointDepth[id].w;
+    vec3 trial = elastic;
+    real area = r.normalArea[id].w, depth = r.pointDepth[id].w;
     NormalResponse response = normalResponse(depth, area, dot(rv, n), r.c.kn, viscosity, 0.5f);
-    float fn = response.force;
+    real fn = response.force;
     r.normalLossPower[id] = response.lossPower;
-    float3 ft = -0.5f * r.c.kt * area * elastic;
-    float magnitude = length(ft);
+    vec3 ft = -0.5f * r.c.kt * area * elastic;
+    real magnitude = length(ft);
     if (magnitude > r.c.mu * fn && magnitude > 0) {
         ft = ft * (r.c.mu * fn / magnitude);
         elastic = -ft / (0.5f * r.c.kt * area);
         r.control[6]++;
     }
     r.slip[id] = f4(elastic, mx(0.0f, -dot(ft, trial - elastic)));
-    float4 cf = f4(fn * n + ft, 0.25f * area * (r.c.kn * depth * depth + r.c.kt * dot(elastic, elastic)));
+    vec4 cf = f4(fn * n + ft, 0.25f * area * (r.c.kn * depth * depth + r.c.kt * dot(elastic, elastic)));
     r.contactForce[id] = cf;
     if (!std::isfinite(cf.x) || !std::isfinite(cf.y) || !std::isfinite(cf.z) || !std::isfinite(cf.w) ||
         !std::isfinite(response.lossPower)) { fail(r, 512); return; }
@@ -1170,12 +1189,12 @@ void buildHistoryHash(R& r, uint32_t id) {
 // solver.slang:760-811
 void gather(R& r, uint32_t id) {
     if (id >= r.c.N || r.control[0] != 0) return;
-    float3 f{0, 0, 0}, t{0, 0, 0}, fLow{0, 0, 0}, tLow{0, 0, 0};
-    float3 stress0{0, 0, 0}, stress1{0, 0, 0}, stress2{0, 0, 0};
-    float energy = 0, denom = 0, maxDepth = 0, dissipation = 0, normalPower = 0;
-    float stiffnessRate = 0, viscousRate = 0;
-    float3 one{1, 1, 1};
-    float inverseInertia = mx(mx(dot(abs3(xyz(r.invI[3 * id])), one), dot(abs3(xyz(r.invI[3 * id + 1])), one)),
+    vec3 f{0, 0, 0}, t{0, 0, 0}, fLow{0, 0, 0}, tLow{0, 0, 0};
+    vec3 stress0{0, 0, 0}, stress1{0, 0, 0}, stress2{0, 0, 0};
+    real energy = 0, denom = 0, maxDepth = 0, dissipation = 0, normalPower = 0;
+    real stiffnessRate = 0, viscousRate = 0;
+    vec3 one{1, 1, 1};
+    real inverseInertia = mx(mx(dot(abs3(xyz(r.invI[3 * id])), one), dot(abs3(xyz(r.invI[3 * id + 1])), one)),
                               dot(abs3(xyz(r.invI[3 * id + 2])), one));
     uint32_t entry = r.heads[id], visited = 0;
     while (entry != EMPTY) {
@@ -1183,16 +1202,16 @@ void gather(R& r, uint32_t id) {
         uint32_t contact = entry / 2;
         bool source = (entry & 1) == 0;
         uint4 key = r.meta[contact];
-        float3 force = xyz(r.contactForce[contact]);
-        float3 arm = xyz(r.pointDepth[contact]);
+        vec3 force = xyz(r.contactForce[contact]);
+        vec3 arm = xyz(r.pointDepth[contact]);
         if (r.c.activeTimestep != 0) {
             bool wall = key.y >= r.c.N;
-            float3 localArm = source ? arm : arm - centerBranch(r, key.x, key.y);
-            float mobility = 1.0f / r.body[id].y + dot(localArm, localArm) * inverseInertia;
-            float4 material{r.c.kn, r.c.kt, r.c.mu, r.c.normalViscosity};
+            vec3 localArm = source ? arm : arm - centerBranch(r, key.x, key.y);
+            real mobility = 1.0f / r.body[id].y + dot(localArm, localArm) * inverseInertia;
+            vec4 material{r.c.kn, r.c.kt, r.c.mu, r.c.normalViscosity};
             if (wall) material = r.wallMaterial[key.y - r.c.N];
-            float area = r.normalArea[contact].w * (wall ? 1.0f : 0.5f);
-            float coupling = wall ? 1.0f : 2.0f;
+            real area = r.normalArea[contact].w * (wall ? 1.0f : 0.5f);
+            real coupling = wall ? 1.0f : 2.0f;
             stiffnessRate = stiffnessRate + coupling * area * (material.x * (1.0f + material.z) + material.y) * mobility;
             viscousRate = viscousRate + coupling * area * material.w * (1.0f + material.z) * mobility;
         }
@@ -1210,7 +1229,7 @@ void gather(R& r, uint32_t id) {
             entry = r.next[entry];
             continue;
         }
-        float3 branch = centerBranch(r, key.x, key.y);
+        vec3 branch = centerBranch(r, key.x, key.y);
         compensated3(f, fLow, source ? force : -force);
         compensated3(t, tLow, source ? cross(arm, force) : cross(arm - branch, -force));
         stress0 = stress0 - 0.5f * force.x * branch;
@@ -1225,8 +1244,8 @@ void gather(R& r, uint32_t id) {
     }
     f = f + fLow;
     t = t + tLow;
-    r.timestepRows[id] = float4{stiffnessRate, viscousRate, 0, 0};
-    float4 normalState = r.normalDamping[id];
+    r.timestepRows[id] = vec4{stiffnessRate, viscousRate, 0, 0};
+    vec4 normalState = r.normalDamping[id];
     normalState.z = normalPower;
     r.normalDamping[id] = normalState;
     r.force[id] = f4(f, maxDepth);
@@ -1234,38 +1253,38 @@ void gather(R& r, uint32_t id) {
     r.particleStress[3 * id] = f4(stress0, 0);
     r.particleStress[3 * id + 1] = f4(stress1, 0);
     r.particleStress[3 * id + 2] = f4(stress2, 0);
-    float3 v = xyz(r.velocity[id]);
-    float kinetic = 0.5f * (r.body[id].y * dot(v, v) + dot(xyz(r.momentum[id]), omega(r, id)));
-    r.particleDiagnostic[id] = float4{kinetic, energy, length(f), denom};
-    accumulate(r, id, float4{dissipation, 0, 0, 0});
+    vec3 v = xyz(r.velocity[id]);
+    real kinetic = 0.5f * (r.body[id].y * dot(v, v) + dot(xyz(r.momentum[id]), omega(r, id)));
+    r.particleDiagnostic[id] = vec4{kinetic, energy, length(f), denom};
+    accumulate(r, id, vec4{dissipation, 0, 0, 0});
 }
 // solver.slang:815-832
 void checkContactTimestep(R& r, uint32_t id) {
     if (id >= r.c.N || r.control[0] != 0 || r.c.dt == 0) return;
-    float dt = r.c.dt;
-    float rx = r.timestepRows[id].x, ry = r.timestepRows[id].y;
-    float3 v = xyz(r.velocity[id]) + xyz(r.velocityRemainder[id]);
-    float speed = length(v) + dt * length(xyz(r.force[id])) / r.body[id].y;
-    float3 one{1, 1, 1};
-    float inverseInertia = mx(mx(dot(abs3(xyz(r.invI[3 * id])), one), dot(abs3(xyz(r.invI[3 * id + 1])), one)),
+    real dt = r.c.dt;
+    real rx = r.timestepRows[id].x, ry = r.timestepRows[id].y;
+    vec3 v = xyz(r.velocity[id]) + xyz(r.velocityRemainder[id]);
+    real speed = length(v) + dt * length(xyz(r.force[id])) / r.body[id].y;
+    vec3 one{1, 1, 1};
+    real inverseInertia = mx(mx(dot(abs3(xyz(r.invI[3 * id])), one), dot(abs3(xyz(r.invI[3 * id + 1])), one)),
                               dot(abs3(xyz(r.invI[3 * id + 2])), one));
-    float spin = inverseInertia * (length(xyz(r.momentum[id]) + xyz(r.momentumRemainder[id])) + dt * length(xyz(r.torque[id])));
-    float wallSpeed = 0;
+    real spin = inverseInertia * (length(xyz(r.momentum[id]) + xyz(r.momentumRemainder[id])) + dt * length(xyz(r.torque[id])));
+    real wallSpeed = 0;
     for (uint32_t w = 0; w < r.c.wallCount; ++w) wallSpeed = mx(wallSpeed, length(xyz(r.wallVelocity[w])));
-    float motion = dt * (speed + r.body[id].z * spin + wallSpeed);
+    real motion = dt * (speed + r.body[id].z * spin + wallSpeed);
     bool finite = std::isfinite(rx) && std::isfinite(ry) && std::isfinite(motion) && std::isfinite(spin);
     if (!finite) { fail(r, 512); return; }
-    float3 rate = abs3(xyz(r.cell[1]));
+    vec3 rate = abs3(xyz(r.cell[1]));
     if (dt * std::sqrt(rx) > 0.1f || dt * ry > 0.1f || dt * spin > 0.01f || motion > 0.25f * r.c.skin ||
         rate.x * dt > 0.01f || rate.y * dt > 0.01f || rate.z * dt > 0.01f) fail(r, 8192);
 }
 // solver.slang:922-936
 void diagnosticRows(R& r, uint32_t id) {
     if (id >= r.c.N) return;
-    float3 v = xyz(r.velocity[id]);
-    float m = r.body[id].y;
-    float kinetic = 0.5f * (m * dot(v, v) + dot(xyz(r.momentum[id]), omega(r, id)));
-    float4* row = r.diagnosticRows + 8 * size_t(id);
+    vec3 v = xyz(r.velocity[id]);
+    real m = r.body[id].y;
+    real kinetic = 0.5f * (m * dot(v, v) + dot(xyz(r.momentum[id]), omega(r, id)));
+    vec4* row = r.diagnosticRows + 8 * size_t(id);
     row[0] = f4(xyz(r.particleStress[3 * id]), kinetic);
     row[1] = f4(xyz(r.particleStress[3 * id + 1]), r.particleDiagnostic[id].y);
     row[2] = f4(xyz(r.particleStress[3 * id + 2]), length(xyz(r.force[id])));
@@ -1273,19 +1292,19 @@ void diagnosticRows(R& r, uint32_t id) {
     row[4] = f4(m * v.y * v, r.force[id].w);
     row[5] = f4(m * v.z * v, r.torque[id].w);
     row[6] = r.accumulated[id];
-    float4 ns = r.normalDamping[id];
-    row[7] = float4{ns.x + ns.y, ns.z, 0, 0};
+    vec4 ns = r.normalDamping[id];
+    row[7] = vec4{ns.x + ns.y, ns.z, 0, 0};
 }
 // solver.slang:938-947
 void fabricRows(R& r, uint32_t id) {
     if (id >= r.c.pairCapacity) return;
-    float4 a{0, 0, 0, 0}, b{0, 0, 0, 0};
+    vec4 a{0, 0, 0, 0}, b{0, 0, 0, 0};
     if (id < r.control[1] && r.contactCounts[id] > 0) {
         uint2 ij = r.pairs[id];
-        float3 d = centerBranch(r, ij.x, ij.y);
-        float3 n = d * (1.0f / std::sqrt(dot(d, d)));
-        a = float4{n.x * n.x, n.y * n.y, n.z * n.z, n.x * n.y};
-        b = float4{n.x * n.z, n.y * n.z, 1, 0};
+        vec3 d = centerBranch(r, ij.x, ij.y);
+        vec3 n = d * (1.0f / std::sqrt(dot(d, d)));
+        a = vec4{n.x * n.x, n.y * n.y, n.z * n.z, n.x * n.y};
+        b = vec4{n.x * n.z, n.y * n.z, 1, 0};
     }
     r.fabricRows[2 * id] = a;
     r.fabricRows[2 * id + 1] = b;
@@ -1332,12 +1351,12 @@ extern "C" int oracle_dispatch(const char* name, uint32_t count, void** buffers,
     // Probes (entry-point uniforms after the Config scalars).
     else if (k == "meshProbe") {  // solver.slang:253-257: uniform shape; points, result
         uint32_t shape = uint32_t(r.uni[1]);
-        float4* points = static_cast<float4*>(r.extra[0]);
-        float4* result = static_cast<float4*>(r.extra[1]);
+        vec4* points = static_cast<vec4*>(r.extra[0]);
+        vec4* result = static_cast<vec4*>(r.extra[1]);
         for (uint32_t id = 0; id < count; ++id) result[id] = meshDistance(r, shape, xyz(points[id]), false);
     } else if (k == "meshCullProbe") {  // solver.slang:314-318
         uint32_t shape = uint32_t(r.uni[1]);
-        float4* points = static_cast<float4*>(r.extra[0]);
+        vec4* points = static_cast<vec4*>(r.extra[0]);
         uint32_t* result = static_cast<uint32_t*>(r.extra[1]);
         for (uint32_t id = 0; id < count; ++id) result[id] = meshMayContain(r, shape, xyz(points[id])) ? 1 : 0;
     } else if (k == "meshClusterProbe") {  // solver.slang:306-313: src, dst
@@ -1347,27 +1366,27 @@ extern "C" int oracle_dispatch(const char* name, uint32_t count, void** buffers,
             result[id] = meshClusterMayContact(r, src, dst, r.meshClusterInfo[r.shapeId[src]].x + id) ? 1 : 0;
     } else if (k == "meshPairBoundsProbe") {  // solver.slang:418-424: direction, first
         uint32_t direction = uint32_t(r.uni[1]), first = uint32_t(r.uni[2]);
-        float4* result = static_cast<float4*>(r.extra[0]);
+        vec4* result = static_cast<vec4*>(r.extra[0]);
         for (uint32_t id = 0; id < count; ++id) {
-            float3 lo, hi;
+            vec3 lo, hi;
             meshPairBounds(r, direction, first + id, lo, hi);
             result[2 * id] = f4(lo, 0);
             result[2 * id + 1] = f4(hi, 0);
         }
     } else if (k == "planeProbe") {  // plane.slang:44-64: N; normal; offset, kn, kt, mu, dt
-        float3 normal{float(r.uni[1]), float(r.uni[2]), float(r.uni[3])};
-        float offset = float(r.uni[4]), kn = float(r.uni[5]), kt = float(r.uni[6]), mu = float(r.uni[7]);
-        float dt = float(r.uni[8]);
-        float4* pointArea = static_cast<float4*>(r.extra[0]);
-        float4* relativeVelocity = static_cast<float4*>(r.extra[1]);
-        float4* oldSlipActive = static_cast<float4*>(r.extra[2]);
-        float4* forceEnergy = static_cast<float4*>(r.extra[3]);
-        float4* slipLoss = static_cast<float4*>(r.extra[4]);
-        float4* torqueActive = static_cast<float4*>(r.extra[5]);
+        vec3 normal{real(r.uni[1]), real(r.uni[2]), real(r.uni[3])};
+        real offset = real(r.uni[4]), kn = real(r.uni[5]), kt = real(r.uni[6]), mu = real(r.uni[7]);
+        real dt = real(r.uni[8]);
+        vec4* pointArea = static_cast<vec4*>(r.extra[0]);
+        vec4* relativeVelocity = static_cast<vec4*>(r.extra[1]);
+        vec4* oldSlipActive = static_cast<vec4*>(r.extra[2]);
+        vec4* forceEnergy = static_cast<vec4*>(r.extra[3]);
+        vec4* slipLoss = static_cast<vec4*>(r.extra[4]);
+        vec4* torqueActive = static_cast<vec4*>(r.extra[5]);
         for (uint32_t id = 0; id < count; ++id) {
-            float4 point = pointArea[id];
-            float phi = dot(normal, xyz(point)) - offset;
-            float3 old = oldSlipActive[id].w != 0 ? xyz(oldSlipActive[id]) : float3{0, 0, 0};
+            vec4 point = pointArea[id];
+            real phi = dot(normal, xyz(point)) - offset;
+            vec3 old = oldSlipActive[id].w != 0 ? xyz(oldSlipActive[id]) : vec3{0, 0, 0};
             PlaneResponse value = planeViscousResponse(normal, phi, point.w, xyz(relativeVelocity[id]), old, kn, kt,
                                                        mu, 0.0f, dt);
             forceEnergy[id] = value.forceEnergy;
@@ -1375,12 +1394,12 @@ extern "C" int oracle_dispatch(const char* name, uint32_t count, void** buffers,
             torqueActive[id] = f4(cross(xyz(point), xyz(value.forceEnergy)), phi < 0 ? 1.0f : 0.0f);
         }
     } else if (k == "normalProbe") {  // normal.slang:166-174: stiffness, viscosity, weight
-        float stiffness = float(r.uni[1]), viscosity = float(r.uni[2]), weight = float(r.uni[3]);
-        float4* input = static_cast<float4*>(r.extra[0]);
-        float4* output = static_cast<float4*>(r.extra[1]);
+        real stiffness = real(r.uni[1]), viscosity = real(r.uni[2]), weight = real(r.uni[3]);
+        vec4* input = static_cast<vec4*>(r.extra[0]);
+        vec4* output = static_cast<vec4*>(r.extra[1]);
         for (uint32_t id = 0; id < count; ++id) {
             NormalResponse v = normalResponse(input[id].x, input[id].y, input[id].z, stiffness, viscosity, weight);
-            output[id] = float4{v.force, v.lossPower, 0, 0};
+            output[id] = vec4{v.force, v.lossPower, 0, 0};
         }
     } else return -1;
     return 0;

@@ -31,6 +31,8 @@ from sand_atlas_dem_gb300.model import (
 
 HERE = Path(__file__).resolve().parent
 ORACLE_LIB = HERE / "_build" / "libdem_oracle.so"
+# The same source built in double precision: the FP64 drift oracle.
+ORACLE_LIB64 = HERE / "_build" / "libdem_oracle64.so"
 REF_LIB = HERE / "_ref" / "collector_ref.so"
 
 
@@ -39,22 +41,22 @@ def build():
     return ORACLE_LIB
 
 
-_LIB = None
+_LIBS = {}
 
 
-def library():
-    global _LIB
-    if _LIB is None:
-        if not ORACLE_LIB.exists():
+def library(precision="fp32"):
+    if precision not in _LIBS:
+        path = ORACLE_LIB64 if precision == "fp64" else ORACLE_LIB
+        if not path.exists():
             build()
-        lib = ct.CDLL(str(ORACLE_LIB))
+        lib = ct.CDLL(str(path))
         lib.oracle_dispatch.argtypes = [
             ct.c_char_p, ct.c_uint32, ct.POINTER(ct.c_void_p), ct.POINTER(ct.c_uint64),
             ct.POINTER(ct.c_double), ct.c_uint32,
         ]
         lib.oracle_dispatch.restype = ct.c_int
-        _LIB = lib
-    return _LIB
+        _LIBS[precision] = lib
+    return _LIBS[precision]
 
 
 class ReferenceCollector:
@@ -82,14 +84,26 @@ class ReferenceCollector:
             raise RuntimeError("reference collector failed")
 
 
-def _zeros4(rows):
-    return np.zeros((max(1, rows), 4), np.float32)
+def _zeros4(rows, dtype=np.float32):
+    return np.zeros((max(1, rows), 4), dtype)
 
 
 class OracleEngine:
-    """Reference-order CPU engine over the restated kernels."""
+    """Reference-order CPU engine over the restated kernels.
 
-    def __init__(self, library_, spec, positions, cell, shape_ids, scales, *, collector=None, threads=1):
+    ``precision="fp64"`` runs the same kernels in double precision (every
+    float buffer float64, every FP32 operation in double): the FP64 drift
+    oracle.  Its state arrays are float64; a position is held whole in
+    ``position`` (its remainder row stays zero)."""
+
+    def __init__(self, library_, spec, positions, cell, shape_ids, scales, *, collector=None, threads=1,
+                 precision="fp32"):
+        if precision not in ("fp32", "fp64"):
+            raise ValueError("precision is fp32 or fp64")
+        if precision == "fp64" and collector is not None:
+            raise ValueError("the reference's compiled collector is FP32 only")
+        self.precision = precision
+        real = np.float64 if precision == "fp64" else np.float32
         self.layout = h = HostLayout(library_, spec, positions, cell, shape_ids, scales)
         self.spec, self.library, self.n = spec, library_, h.n
         self.viscous = spec.viscous
@@ -104,27 +118,33 @@ class OracleEngine:
             setattr(self, name, getattr(h, name))
         b = dict(h.geometry)
         b.update(h.initial_state())
+        if precision == "fp64":
+            b = {k: (v.astype(np.float64) if v.dtype == np.float32 else v) for k, v in b.items()}
+            # The whole FP64 centre in one value (hi + lo is exact in double).
+            b["position"] = b["position"] + b["positionRemainder"]
+            b["positionRemainder"][...] = 0
+            b["position"][:, :3] = np.asarray(h.normalized_position, np.float64)
         pc, cc, n = h.pair_capacity, h.contact_capacity, h.n
         b["meshPairMask"] = np.zeros(pc, np.uint32)
-        b["meshPairTransform"] = _zeros4(8 * pc)
-        b["fabricRows"] = _zeros4(2 * pc)
+        b["meshPairTransform"] = _zeros4(8 * pc, real)
+        b["fabricRows"] = _zeros4(2 * pc, real)
         b["binCounts"] = np.zeros(h.bin_count, np.uint32)
         b["binParticles"] = np.zeros(h.bin_count * h.bin_capacity, np.uint32)
         for name, count in (("pairCounts", n), ("pairOffsets", n), ("contactCounts", pc),
                             ("contactOffsets", pc), ("heads", n), ("next", 2 * cc)):
             b[name] = np.zeros(count, np.uint32)
         b["pairs"] = np.zeros((pc, 2), np.uint32)
-        b["pointDepth"] = _zeros4(cc)
-        b["contactForce"] = _zeros4(cc)
-        b["normalLossPower"] = np.zeros(cc, np.float32)
+        b["pointDepth"] = _zeros4(cc, real)
+        b["contactForce"] = _zeros4(cc, real)
+        b["normalLossPower"] = np.zeros(cc, real)
         self.wall_count = h.wall_count
-        b.update({k: v.copy() for k, v in h.walls.items()})
+        b.update({k: (v.astype(real) if v.dtype == np.float32 else v.copy()) for k, v in h.walls.items()})
         self.buffers = b
         self.sides = [
             {
                 "meta": np.zeros((cc, 4), np.uint32),
-                "slip": _zeros4(cc),
-                "normalArea": _zeros4(cc),
+                "slip": _zeros4(cc, real),
+                "normalArea": _zeros4(cc, real),
                 "hash": np.full(h.hash_size, 0xFFFFFFFF, np.uint32),
             }
             for _ in (0, 1)
@@ -158,7 +178,7 @@ class OracleEngine:
                 return
             values.append(float(self.threads))
         vals = (ct.c_double * len(values))(*values)
-        if library().oracle_dispatch(name.encode(), int(count), pointers, sizes, vals, len(values)):
+        if library(self.precision).oracle_dispatch(name.encode(), int(count), pointers, sizes, vals, len(values)):
             raise ValueError(f"oracle has no kernel {name}")
 
     # -- the reference step ---------------------------------------------
@@ -346,7 +366,8 @@ class OracleEngine:
         data, fabric_data = self.diagnostic_rows()
         ctrl = self.check_errors()
         active_pairs = round(float(fabric_data[1, 2]))
-        f = fabric_data.astype(float)
+        # FP32 rows divided in FP32, as the reference's numpy expression does.
+        f = fabric_data
         fabric = np.array([[f[0, 0], f[0, 3], f[1, 0]], [f[0, 3], f[0, 1], f[1, 1]],
                            [f[1, 0], f[1, 1], f[0, 2]]]) / max(active_pairs, 1)
         cell = self.buffers["cell"][:3]

@@ -104,6 +104,7 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
             bytes[77 + 49] < (uint64_t(c.shapes) * WALK_BUCKETS + 1) * 4 ||
             (c.meshGeometry == 0 && bytes[77 + 50] < uint64_t(c.pairCapacity) * 32 * 4) ||
             bytes[77 + 51] < uint64_t(c.survivorCapacity) * 16 || bytes[77 + 52] < uint64_t(c.survivorCapacity) * 4 ||
+            bytes[77 + 57] < uint64_t(c.survivorCapacity) * 16 || bytes[77 + 58] < uint64_t(c.survivorCapacity) * 8 ||
             (c.wallCount != 0 &&
              (bytes[70] < uint64_t(c.wallCount) * 16 || bytes[71] < uint64_t(c.wallCount) * 16 ||
               bytes[72] < uint64_t(c.wallCount) * 16 || bytes[73] < uint64_t(c.wallCount) * 16 ||
@@ -136,9 +137,21 @@ void launch_forces(const Params& P, cudaStream_t s, bool captureKinematics) {
     if (c.activeTimestep) launch_state("checkContactTimestep", P, c.N, s);
 }
 
+// Whether the filter results (items, survivor and exact-query lists) are
+// stored and rebuilt only on the steps whose motion check asks for it.
+static bool storedFilters(const Config& c) {
+    return c.meshGeometry != 0 && c.filterMargin > 0.0f && c.cullerEnabled == 0;
+}
+
 // One step of Engine._advance_once (gpu.py:714-724); captureContactKinematics
-// is fused into beginStep when the normal law is viscous.
-void launch_step(const Params& P, cudaStream_t s) {
+// is fused into beginStep when the normal law is viscous.  The two parts that
+// most steps skip -- the neighbour build (device flag control[4], set by
+// checkRebuild) and the filter build (work[W_FILTER], set by the pair set-up's
+// motion check) -- go through `branch(flag, body)`: plain launches run the
+// body on s (its kernels return at once when the flag is clear); graph
+// capture makes it the body of a conditional node keyed on the flag.
+template <class Branch>
+static void stepSequence(const Params& P, cudaStream_t s, Branch&& branch) {
     const Config& c = P.c;
     if (c.activeTimestep) launch_state("checkContactTimestep", P, c.N, s);
     Params B = P;
@@ -147,8 +160,28 @@ void launch_step(const Params& P, cudaStream_t s) {
     launch_state("advanceCell", P, c.specimens, s);
     if (c.wallCount) launch_state("advanceWalls", P, 1, s);
     launch_state("checkRebuild", P, c.N, s);
-    launch_forces(P, s, false);
+    branch(P.r.control + 4, [&](cudaStream_t b) { launch_contacts("neighbours", P, c.N, b); });
+    if (storedFilters(c)) {
+        launch_contacts("collectHead", P, 0, s);
+        branch(P.r.work + W_FILTER, [&](cudaStream_t b) { launch_contacts("collectBuild", P, 0, b); });
+        launch_contacts("collectTail", P, 0, s);
+    } else {
+        launch_contacts("collect", P, 0, s);
+    }
+    launch_contacts("resolveContacts", P, 0, s);
+    launch_contacts("gather", P, c.N, s);
+    launch_contacts("gatherWallRows", P, c.N, s);
+    if (c.activeTimestep) launch_state("checkContactTimestep", P, c.N, s);
     launch_state("finishStep", P, c.N, s);
+}
+
+void launch_step(const Params& P, cudaStream_t s) {
+    stepSequence(P, s, [&](const uint32_t*, auto&& body) { body(s); });
+}
+
+// Sets a conditional node's value from a device flag (graph replay).
+__global__ void k_setCondition(cudaGraphConditionalHandle handle, const uint32_t* flag) {
+    cudaGraphSetConditional(handle, *flag != 0u ? 1u : 0u);
 }
 
 // Committed/new history sides swap every step (gpu.py:725).
@@ -166,27 +199,33 @@ static Params swapSides(const Params& P) {
     return Q;
 }
 
+// Kernel launches of a captured step: those every step runs, and those of
+// the neighbour-build and filter-build bodies (run only on steps whose flag
+// is set).
+struct StepKernels {
+    uint32_t always = 0, branch[2] = {0, 0};
+};
+
 // Captured one-step graphs for the two history-side orientations of a
 // buffer/config set, keyed on the orientation-independent parameter pair.
 struct Engine {
     std::vector<unsigned char> key;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
-    uint32_t kernels = 0;  // kernel nodes per captured step
-    ~Engine() { reset(); }
+    StepKernels kernels;
+    cudaStream_t aux = nullptr;  // captures the conditional bodies
+    ~Engine() {
+        reset();
+        if (aux) cudaStreamDestroy(aux);
+    }
     void reset() {
         for (auto& e : exec)
             if (e) { cudaGraphExecDestroy(e); e = nullptr; }
         key.clear();
+        kernels = StepKernels{};
     }
 };
 
-static int capture(const Params& P, cudaStream_t s, cudaGraphExec_t* out, uint32_t* kernels) {
-    cudaGraph_t graph = nullptr;
-    int rc = record(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
-    if (rc) return rc;
-    launch_step(P, s);
-    rc = record(cudaStreamEndCapture(s, &graph), "end capture");
-    if (rc) return rc;
+static uint32_t kernelNodes(cudaGraph_t graph) {
     size_t count = 0;
     cudaGraphGetNodes(graph, nullptr, &count);
     std::vector<cudaGraphNode_t> nodes(count);
@@ -197,9 +236,66 @@ static int capture(const Params& P, cudaStream_t s, cudaGraphExec_t* out, uint32
         cudaGraphNodeGetType(n, &t);
         k += t == cudaGraphNodeTypeKernel;
     }
-    *kernels = k;
-    rc = record(cudaGraphInstantiate(out, graph, 0), "instantiate");
+    return k;
+}
+
+// One step as a graph: the step sequence captured on s, each branch an IF
+// node whose condition a one-thread kernel sets from the branch's device
+// flag just before it (the condition defaults to 1 -- run -- on every
+// launch), its body captured on aux into the node's body graph.
+static int capture(const Params& P, cudaStream_t s, cudaStream_t aux, cudaGraphExec_t* out, StepKernels* kernels) {
+    cudaGraph_t graph = nullptr;
+    int rc = record(cudaGraphCreate(&graph, 0), "graph create");
+    if (rc) return rc;
+    rc = record(cudaStreamBeginCaptureToGraph(s, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                "begin capture");
+    if (rc) { cudaGraphDestroy(graph); return rc; }
+    StepKernels counted;
+    int branches = 0;
+    stepSequence(P, s, [&](const uint32_t* flag, auto&& body) {
+        int index = branches++;
+        if (rc) return;
+        cudaGraphConditionalHandle handle;
+        rc = record(cudaGraphConditionalHandleCreate(&handle, graph, 1u, cudaGraphCondAssignDefault),
+                    "conditional handle");
+        if (rc) return;
+        k_setCondition<<<1, 1, 0, s>>>(handle, flag);
+        cudaStreamCaptureStatus status;
+        cudaGraph_t target = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        const cudaGraphEdgeData* edges = nullptr;
+        size_t count = 0;
+        rc = record(cudaStreamGetCaptureInfo(s, &status, nullptr, &target, &deps, &edges, &count), "capture info");
+        if (rc) return;
+        cudaGraphNodeParams params = {};
+        params.type = cudaGraphNodeTypeConditional;
+        params.conditional.handle = handle;
+        params.conditional.type = cudaGraphCondTypeIf;
+        params.conditional.size = 1;
+        cudaGraphNode_t node;
+        rc = record(cudaGraphAddNode(&node, target, deps, edges, count, &params), "conditional node");
+        if (rc) return;
+        cudaGraph_t bodyGraph = params.conditional.phGraph_out[0];
+        rc = record(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies),
+                    "capture dependencies");
+        if (rc) return;
+        rc = record(cudaStreamBeginCaptureToGraph(aux, bodyGraph, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal), "begin body capture");
+        if (rc) return;
+        body(aux);
+        cudaGraph_t done = nullptr;
+        rc = record(cudaStreamEndCapture(aux, &done), "end body capture");
+        if (!rc && index < 2) counted.branch[index] = kernelNodes(bodyGraph);
+    });
+    cudaGraph_t captured = nullptr;
+    int end = record(cudaStreamEndCapture(s, &captured), "end capture");
+    rc = rc ? rc : end;
+    if (!rc) {
+        counted.always = kernelNodes(graph);
+        rc = record(cudaGraphInstantiate(out, graph, 0), "instantiate");
+    }
     cudaGraphDestroy(graph);
+    if (!rc) *kernels = counted;
     return rc;
 }
 
@@ -350,9 +446,11 @@ int sdg_engine_advance(void* engine, void* const* buffers, const uint64_t* bytes
     std::memcpy(key.data() + sizeof(Params), &second, sizeof(Params));
     if (key != e->key) {
         e->reset();
-        uint32_t kernels = 0;
-        if (int rc = capture(first, s, &e->exec[0], &kernels)) { e->reset(); return rc; }
-        if (int rc = capture(second, s, &e->exec[1], &kernels)) { e->reset(); return rc; }
+        if (!e->aux)
+            if (int rc = record(cudaStreamCreateWithFlags(&e->aux, cudaStreamNonBlocking), "capture stream")) return rc;
+        StepKernels kernels;
+        if (int rc = capture(first, s, e->aux, &e->exec[0], &kernels)) { e->reset(); return rc; }
+        if (int rc = capture(second, s, e->aux, &e->exec[1], &kernels)) { e->reset(); return rc; }
         e->kernels = kernels;
         e->key = key;
     }
@@ -362,10 +460,20 @@ int sdg_engine_advance(void* engine, void* const* buffers, const uint64_t* bytes
     return 0;
 }
 
-// Kernel launches per captured step (0 before the first graph capture).
+// Kernel launches of a captured step that skips both conditional bodies (0
+// before the first graph capture).
 int sdg_engine_kernels_per_step(void* engine) {
     Engine* e = static_cast<Engine*>(engine);
-    return e ? int(e->kernels) : -1;
+    return e ? int(e->kernels.always) : -1;
+}
+
+// Kernel launches inside conditional body `branch` of a captured step: 0 =
+// the neighbour build (run on rebuild steps), 1 = the filter build (run on
+// steps that build the stored filter results; absent without them).
+int sdg_engine_branch_kernels(void* engine, int branch) {
+    Engine* e = static_cast<Engine*>(engine);
+    if (!e || branch < 0 || branch > 1) return -1;
+    return int(e->kernels.branch[branch]);
 }
 
 }  // extern "C"

@@ -136,8 +136,10 @@ struct Res {
     uint32_t* wallOffsets;            // wallCount x N + 1: their exclusive scan
     uint32_t* sideWallStart;          // wallCount x N + 1: first contact of each (wall, grain), side being written
     const uint32_t* oldWallStart;     // wallCount x N + 1: the same on the committed side
+    uint4* walkNode;                  // survivorCapacity: per stored walk slot (source, target, directed pair, packed sample)
+    uint2* walkItem;                  // survivorCapacity: per stored walk slot (item, node slot)
 };
-constexpr int EXTENSION_COUNT = 57;
+constexpr int EXTENSION_COUNT = 59;
 constexpr uint32_t WALK_CELLS = 24;  // coarse cells per axis of a shape's grid box for the walk order
 constexpr uint32_t WALK_BUCKETS = WALK_CELLS * WALK_CELLS * WALK_CELLS;
 constexpr uint32_t GRID = 48;  // cells per axis of each shape's distance-bound grid
@@ -162,6 +164,7 @@ constexpr int W_FILTER_BASE = 13;   // configured margin they were built under (
 constexpr int W_SLOW = 14;          // stored walk slots left for a full walk this step
 constexpr int W_CERTIFIED = 15;     // exact queries answered by a certificate (counter)
 constexpr int W_WALL_BASE = 16;     // first plane contact: the grain-grain contact total
+constexpr int W_REBUILDS = 17;      // steps that rebuilt the neighbour list (counter)
 
 struct Params {
     Config c;
@@ -484,10 +487,10 @@ __device__ __forceinline__ float4 meshDistanceCertified(const Res& r, uint32_t s
 // other: the same closest point, squared distance and feature the walk
 // records -- the partner's only where it is strictly nearer, as the leaf's
 // triangles are taken in order.
-__device__ __forceinline__ float4 meshDistanceAt(const Res& r, f3 p, uint32_t certified) {
+// `a`, `b`, `c` are the certified triangle's vertices (loaded by the caller).
+__device__ __forceinline__ float4 meshDistanceAt(const Res& r, f3 p, uint32_t certified, float4 a, float4 b, float4 c) {
     uint32_t triangle = certified & 0x3FFFFFFFu, partner = certified >> 30, feature;
-    f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * triangle])), xyz(__ldg(&r.meshTriangles[3 * triangle + 1])),
-                           xyz(__ldg(&r.meshTriangles[3 * triangle + 2])), feature);
+    f3 q = closestTriangle(p, xyz(a), xyz(b), xyz(c), feature);
     f3 dq = p - q;
     float best = dot(dq, dq);
     uint32_t normal = 7 * triangle + feature;
@@ -631,17 +634,17 @@ __device__ __forceinline__ bool nodePrefilter(const Res& r, uint32_t src, uint32
     return nodeTests(r, r.shapeId[dst], plane, local, grow);
 }
 // The contact record from the target's signed distance f at the node.
-__device__ __forceinline__ bool nodeContactFrom(const Res& r, const Config& c, uint32_t src, uint32_t dst,
-                                                uint32_t node, f3 arm, float4 f, float4& pd, float4& na) {
-    uint32_t sid = r.shapeId[src];
-    float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[sid].x) + node]);
-    float4 bs = r.body[src], bd = r.body[dst];
+// The contact record of a node whose target-frame query gave f, from the
+// node's sample `sp`, both grains' body rows and the target's rotation
+// (loaded by the caller); `src` is read only for the source-surface normal.
+__device__ __forceinline__ bool nodeContactWith(const Res& r, const Config& c, uint32_t src, float4 sp, float4 bs,
+                                                float4 bd, float4 qd, f3 arm, float4 f, float4& pd, float4& na) {
     pd = w4(arm, __fmul_rn(-f.w, bd.x));
     if (pd.w <= 0.0f) return false;
-    f3 grad = qrot(r.rotation[dst], xyz(f));
+    f3 grad = qrot(qd, xyz(f));
     float len = length(grad);
     if (c.sourceSurfaceNormal != 0) {
-        float4 own = meshDistance(r, sid, xyz(sp), true);
+        float4 own = meshDistance(r, r.shapeId[src], xyz(sp), true);
         if (fabsf(own.w) > 0.00000999999974738f) { fail(r, F_DEGENERATE); return false; }
         grad = -qrot(r.rotation[src], xyz(own));
         len = length(grad);
@@ -650,6 +653,12 @@ __device__ __forceinline__ bool nodeContactFrom(const Res& r, const Config& c, u
     na = w4(grad / len, __fmul_rn(__fmul_rn(sp.w, bs.x), bs.x));
     if (pd.w > __fmul_rn(c.maxOverlap, mn(bs.w, bd.w))) fail(r, F_PENETRATION);
     return true;
+}
+__device__ __forceinline__ bool nodeContactFrom(const Res& r, const Config& c, uint32_t src, uint32_t dst,
+                                                uint32_t node, f3 arm, float4 f, float4& pd, float4& na) {
+    uint32_t sid = r.shapeId[src];
+    float4 sp = __ldg(&r.sample[__ldg(&r.sampleInfo[sid].x) + node]);
+    return nodeContactWith(r, c, src, sp, r.body[src], r.body[dst], r.rotation[dst], arm, f, pd, na);
 }
 __device__ __forceinline__ bool nodeExact(const Res& r, const Config& c, uint32_t src, uint32_t dst, uint32_t node,
                                           f3 arm, f3 local, float4& pd, float4& na, uint32_t seed = 0xFFFFFFFFu) {

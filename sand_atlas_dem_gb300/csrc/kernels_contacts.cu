@@ -255,6 +255,7 @@ __global__ void k_pairsEmit(const __grid_constant__ Params P) {
     const Res& r = P.r;
     uint32_t id = gtid();
     if (id >= P.c.N || r.control[4] == 0) return;
+    if (id == 0) r.work[W_REBUILDS] += 1u;
     findPairs(r, P.c, id, true);
     r.referencePosition[id] = r.position[id];
     r.referencePositionRemainder[id] = r.positionRemainder[id];
@@ -624,15 +625,9 @@ __global__ void __launch_bounds__(256) k_nodeFilter(const __grid_constant__ Para
     const Res& r = P.r;
     const Config& c = P.c;
     uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
-    if (r.work[W_FILTER] == 0) {
-        // Stored survivors serve this step: only the hit masks start afresh.
-        if (r.control[0] != 0) return;
-        for (uint32_t item = gtid(); item < n; item += gstride()) {
-            r.candHitMask[item] = make_uint2(0u, 0u);
-            r.candHitCount[item] = 0;
-        }
-        return;
-    }
+    // Stored survivors serve this step (their hit masks were cleared by the
+    // previous step's emit).
+    if (r.work[W_FILTER] == 0) return;
     float grow = __fmul_rn(1.001f, buildMargin(r, c));
     // Two items per warp, one per half-warp, four node slots per lane
     // (slot = lane in half + 16 j): twice the loads in flight per instruction.
@@ -821,6 +816,15 @@ __global__ void k_walkList(const __grid_constant__ Params P) {
             uint32_t slot = r.walkBucketOffset[bucket] + atomicSub(&r.walkBucketCount[bucket], 1u) - 1u;
             r.walkList[slot] = s;
             r.walkCertTriangle[slot] = EMPTY;
+            // The slot's node record: what its exact query reads every step
+            // (one load instead of the survivor -> item -> pair -> sample chain).
+            uint2 sv = r.survivors[s];
+            uint2 cd = r.candidates[sv.x];
+            uint2 ij = r.pairs[cd.x >> 1];
+            uint32_t src = (cd.x & 1) ? ij.y : ij.x, dst = (cd.x & 1) ? ij.x : ij.y;
+            uint32_t node = __ldg(&r.meshSampleIndices[__ldg(&r.meshClusterRanges[cd.y]).x + sv.y]);
+            r.walkNode[slot] = make_uint4(src, dst, cd.x, __ldg(&r.sampleInfo[r.shapeId[src]].x) + node);
+            r.walkItem[slot] = sv;
         } else {
             r.walkList[r.keepOffset[s]] = s;
         }
@@ -851,11 +855,35 @@ __global__ void k_survivorList(const __grid_constant__ Params P) {
     }
 }
 // Exact query, one thread per kept survivor.
-__device__ __forceinline__ void recordHit(const Res& r, uint32_t s, const SurvivorNode& v, float4 pd, float4 na) {
+__device__ __forceinline__ void recordHitAt(const Res& r, uint32_t s, uint32_t item, uint32_t slot, float4 pd,
+                                            float4 na) {
     r.hitScratch[2 * s] = pd;
     r.hitScratch[2 * s + 1] = na;
-    atomicOr(v.slot < WARP ? &r.candHitMask[v.item].x : &r.candHitMask[v.item].y, 1u << (v.slot & 31u));
-    atomicAdd(&r.candHitCount[v.item], 1u);
+    atomicOr(slot < WARP ? &r.candHitMask[item].x : &r.candHitMask[item].y, 1u << (slot & 31u));
+    atomicAdd(&r.candHitCount[item], 1u);
+}
+__device__ __forceinline__ void recordHit(const Res& r, uint32_t s, const SurvivorNode& v, float4 pd, float4 na) {
+    recordHitAt(r, s, v.item, v.slot, pd, na);
+}
+// A stored walk slot's node, placed in the target frame from its record:
+// the same expressions as survivorNode (the same arm and local bits).
+struct WalkNode {
+    uint4 rec;  // source, target, directed pair, packed sample
+    float4 sp, bs, bd, qd;
+    f3 arm, local;
+};
+__device__ __forceinline__ WalkNode walkNode(const Res& r, uint32_t t) {
+    WalkNode w;
+    w.rec = r.walkNode[t];
+    w.sp = __ldg(&r.sample[w.rec.w]);
+    w.bs = r.body[w.rec.x];
+    w.bd = r.body[w.rec.y];
+    w.qd = r.rotation[w.rec.y];
+    float4 qs = r.rotation[w.rec.x];
+    f3 branch = xyz(r.dpairBranch[w.rec.z]);
+    w.arm = qrot(qs, xyz(w.sp) * w.bs.x);
+    w.local = qinv(w.qd, w.arm - branch) / w.bd.x;
+    return w;
 }
 // Exact queries of a list built every step (margin 0 or the learned culler):
 // one seeded walk per node.
@@ -894,16 +922,22 @@ __global__ void __launch_bounds__(256) k_nodeWalkKnown(const __grid_constant__ P
         uint32_t triangle = r.walkCertTriangle[t];
         bool known = false;
         if (triangle != EMPTY) {
-            uint32_t s = r.walkList[t];
-            SurvivorNode v = survivorNode(r, s);
+            // Every load below depends only on the slot: they issue together.
+            uint32_t base = 3 * (triangle & 0x3FFFFFFFu);
+            float4 ta = __ldg(&r.meshTriangles[base]), tb = __ldg(&r.meshTriangles[base + 1]),
+                   tc = __ldg(&r.meshTriangles[base + 2]);
             float4 cp = r.walkCertPoint[t];
-            float slack = __fmul_rn(1e-5f, __fadd_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(v.local.x), fabsf(v.local.y)),
-                                                                    fabsf(v.local.z))));
-            known = __fadd_rn(__fmul_rn(2.002f, length(v.local - xyz(cp))), slack) < cp.w;
+            WalkNode w = walkNode(r, t);
+            float slack = __fmul_rn(1e-5f, __fadd_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(w.local.x), fabsf(w.local.y)),
+                                                                    fabsf(w.local.z))));
+            known = __fadd_rn(__fmul_rn(2.002f, length(w.local - xyz(cp))), slack) < cp.w;
             if (known) {
                 float4 pd, na;
-                float4 f = meshDistanceAt(r, v.local, triangle);
-                if (nodeContactFrom(r, c, v.src, v.dst, v.node, v.arm, f, pd, na)) recordHit(r, s, v, pd, na);
+                float4 f = meshDistanceAt(r, w.local, triangle, ta, tb, tc);
+                if (nodeContactWith(r, c, w.rec.x, w.sp, w.bs, w.bd, w.qd, w.arm, f, pd, na)) {
+                    uint2 it = r.walkItem[t];
+                    recordHitAt(r, r.walkList[t], it.x, it.y, pd, na);
+                }
             }
         }
         r.survKeep[t] = known ? 0u : 1u;
@@ -928,47 +962,71 @@ __global__ void __launch_bounds__(256) k_nodeWalkSlow(const __grid_constant__ Pa
     float reach = __fadd_rn(__fmul_rn(2.01f, __uint_as_float(r.work[W_FILTER_MARGIN])), 1e-4f);
     for (uint32_t i = gtid(); i < n; i += gstride()) {
         uint32_t t = r.walkKey[i];
-        uint32_t s = r.walkList[t];
-        SurvivorNode v = survivorNode(r, s);
-        uint32_t shape = r.shapeId[v.dst], triangle;
+        WalkNode w = walkNode(r, t);
+        uint32_t shape = r.shapeId[w.rec.y], triangle;
         float gap;
         float4 pd, na;
-        float4 f = meshDistanceCertified(r, shape, v.local, gridSeed(r, shape, v.local), reach, triangle, gap);
+        float4 f = meshDistanceCertified(r, shape, w.local, gridSeed(r, shape, w.local), reach, triangle, gap);
         r.walkCertTriangle[t] = triangle;
-        r.walkCertPoint[t] = w4(v.local, gap);
-        if (nodeContactFrom(r, c, v.src, v.dst, v.node, v.arm, f, pd, na)) recordHit(r, s, v, pd, na);
+        r.walkCertPoint[t] = w4(w.local, gap);
+        if (nodeContactWith(r, c, w.rec.x, w.sp, w.bs, w.bd, w.qd, w.arm, f, pd, na)) {
+            uint2 it = r.walkItem[t];
+            recordHitAt(r, r.walkList[t], it.x, it.y, pd, na);
+        }
+    }
+}
+// Emits one item's hits (the warp, lane per node slot of each 32-slot half).
+__device__ __forceinline__ void emitItem(const Res& r, const Config& c, uint32_t item, uint2 m) {
+    uint2 cd = r.candidates[item];
+    uint32_t d = cd.x, p = d >> 1, pass = d & 1;
+    uint2 ij = r.pairs[p];
+    uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
+    uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
+    uint2 sm = r.candSurvMask[item];
+    uint32_t out = r.candHitOffset[item], in = r.candSurvOffset[item];
+#pragma unroll
+    for (uint32_t half = 0; half < 2; ++half) {
+        uint32_t word = half ? m.y : m.x;
+        if (!((word >> laneId()) & 1u)) continue;
+        uint32_t rank = (half ? __popc(m.x) : 0) + __popc(word & lanesBelow());
+        uint32_t survivorRank = (half ? __popc(sm.x) : 0) + __popc((half ? sm.y : sm.x) & lanesBelow());
+        uint32_t slot = out + rank, from = in + survivorRank;
+        if (slot >= c.contactCapacity || from >= c.survivorCapacity) { fail(r, F_CONTACT); continue; }
+        uint32_t node = __ldg(&r.meshSampleIndices[range.x + laneId() + half * WARP]);
+        r.meta[slot] = make_uint4(src, dst, node, 0);
+        r.pointDepth[slot] = r.hitScratch[2 * from];
+        r.normalArea[slot] = r.hitScratch[2 * from + 1];
+        r.contactPair[slot] = p;
     }
 }
 // Copies the hits of each item from their survivor slots to their canonical
-// offsets.
+// offsets, and clears the item's hit mask and count for the next step (also
+// on a failed step, whose walks may have set bits before the failure: the
+// masks are all zero whenever a step starts, so a step that reuses the
+// stored survivors needs no clearing pass).
 __global__ void __launch_bounds__(256) k_nodeEmit(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
-    if (r.control[0] != 0) return;
+    bool live = r.control[0] == 0;
     uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
-    for (uint32_t item = warpGlobal(); item < n; item += warpStride()) {
-        uint2 m = r.candHitMask[item];
-        if ((m.x | m.y) == 0) continue;
-        uint2 cd = r.candidates[item];
-        uint32_t d = cd.x, p = d >> 1, pass = d & 1;
-        uint2 ij = r.pairs[p];
-        uint32_t src = pass ? ij.y : ij.x, dst = pass ? ij.x : ij.y;
-        uint4 range = __ldg(&r.meshClusterRanges[cd.y]);
-        uint2 sm = r.candSurvMask[item];
-        uint32_t out = r.candHitOffset[item], in = r.candSurvOffset[item];
-#pragma unroll
-        for (uint32_t half = 0; half < 2; ++half) {
-            uint32_t word = half ? m.y : m.x;
-            if (!((word >> laneId()) & 1u)) continue;
-            uint32_t rank = (half ? __popc(m.x) : 0) + __popc(word & lanesBelow());
-            uint32_t survivorRank = (half ? __popc(sm.x) : 0) + __popc((half ? sm.y : sm.x) & lanesBelow());
-            uint32_t slot = out + rank, from = in + survivorRank;
-            if (slot >= c.contactCapacity || from >= c.survivorCapacity) { fail(r, F_CONTACT); continue; }
-            uint32_t node = __ldg(&r.meshSampleIndices[range.x + laneId() + half * WARP]);
-            r.meta[slot] = make_uint4(src, dst, node, 0);
-            r.pointDepth[slot] = r.hitScratch[2 * from];
-            r.normalArea[slot] = r.hitScratch[2 * from + 1];
-            r.contactPair[slot] = p;
+    // Lane per item: read and clear the masks of 32 items, then the warp
+    // emits the items with hits one after the other.
+    for (uint32_t first = WARP * warpGlobal(); first < n; first += WARP * warpStride()) {
+        uint32_t mine = first + laneId();
+        uint2 own = mine < n ? r.candHitMask[mine] : make_uint2(0u, 0u);
+        bool any = (own.x | own.y) != 0;
+        if (any) {
+            r.candHitMask[mine] = make_uint2(0u, 0u);
+            r.candHitCount[mine] = 0;
+        }
+        uint32_t pending = __ballot_sync(0xffffffffu, any);
+        if (!live) continue;
+        while (pending) {
+            uint32_t lane = __ffs(pending) - 1;
+            pending &= pending - 1;
+            uint32_t item = first + lane;
+            uint2 m = make_uint2(__shfl_sync(0xffffffffu, own.x, lane), __shfl_sync(0xffffffffu, own.y, lane));
+            emitItem(r, c, item, m);
         }
     }
 }
@@ -1801,26 +1859,38 @@ static void neighbours(const Params& P, cudaStream_t s) {
     k_byJSort<<<blocks(c.N, T), T, 0, s>>>(P);
 }
 
-// Pair set-up, leaf cull and the (directed pair, leaf) item list; with the
-// SDF geometry, pair set-up, contact counts and their scan.
-static void collectCull(const Params& P, cudaStream_t s) {
+// Pair set-up (branches, the stored-filter motion check); with the SDF
+// geometry also the contact counts and their scan.
+static void collectHead(const Params& P, cudaStream_t s) {
     const Res& r = P.r;
     const Config& c = P.c;
     uint32_t T = 256;
     k_resetContacts<<<1, 1, 0, s>>>(P);
-    uint32_t g = grid(c.cullBlocksPerSM, 8);
-    k_pairSetup<<<g, T, 0, s>>>(P);
+    k_pairSetup<<<grid(c.cullBlocksPerSM, 8), T, 0, s>>>(P);
     if (c.meshGeometry == 0) {
         k_sdfCount<<<grid(c.queryBlocksPerSM, 8), T, 0, s>>>(P);
         launch_scan(r.contactCounts, r.contactOffsets, ScanCount{r.control + 1, c.pairCapacity, 1, 0}, false,
                     r.control + 2, nullptr, r.scanPartials, s);
-        return;
     }
+}
+// Root masks, leaf cull and the (directed pair, leaf) item list: steps that
+// build the filter results (every kernel returns at once on the others).
+static void cullBuild(const Params& P, cudaStream_t s) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (c.meshGeometry == 0) return;
+    uint32_t T = 256, g = grid(c.cullBlocksPerSM, 8);
     k_pairMasks<<<g, T, 0, s>>>(P);
     k_leafCull<<<g, T, 0, s>>>(P);
     launch_scan(r.dpairLeafCount, r.dpairCandOffset, ScanCount{r.control + 1, c.pairCapacity, 2, 0}, true,
                 r.work + W_CANDIDATES, r.work + W_FILTER, r.scanPartials, s);
     k_leafEmit<<<g, T, 0, s>>>(P);
+}
+// Pair set-up, leaf cull and the (directed pair, leaf) item list; with the
+// SDF geometry, pair set-up, contact counts and their scan.
+static void collectCull(const Params& P, cudaStream_t s) {
+    collectHead(P, s);
+    cullBuild(P, s);
 }
 // Node filter, survivor list and (with the learned culler) the kept list.
 static void collectFilter(const Params& P, cudaStream_t s) {
@@ -1903,6 +1973,13 @@ static void contacts(const Params& P, cudaStream_t s) {
     collectEmit(P, s);
     collectWalls(P, s);
 }
+// The exact queries, contact emit and plane contacts: the part of the
+// collector every step runs once the filter results are in place.
+static void collectTail(const Params& P, cudaStream_t s) {
+    collectWalk(P, s);
+    collectEmit(P, s);
+    collectWalls(P, s);
+}
 
 int launch_contacts(const std::string_view& name, const Params& P, uint32_t count, cudaStream_t s) {
     const Config& c = P.c;
@@ -1910,6 +1987,9 @@ int launch_contacts(const std::string_view& name, const Params& P, uint32_t coun
     if (name == "neighbours") neighbours(P, s);
     else if (name == "collect") contacts(P, s);
     else if (name == "collectCull") collectCull(P, s);
+    else if (name == "collectHead") collectHead(P, s);
+    else if (name == "collectBuild") { cullBuild(P, s); collectFilter(P, s); }
+    else if (name == "collectTail") collectTail(P, s);
     else if (name == "collectQuery") collectQuery(P, s);
     else if (name == "collectFilter") collectFilter(P, s);
     else if (name == "collectWalk") collectWalk(P, s);

@@ -46,7 +46,7 @@ EXTENSION_ORDER = (
     "walkList", "dpairSourcePlane", "meshChildren", "distanceGrid", "distanceGridInfo", "distanceGridTriangle",
     "filterRefRotation", "filterRefBranch", "filterRefPairs", "walkKey", "walkBucketCount", "walkBucketOffset",
     "sdfLaneCounts", "walkCertPoint", "walkCertTriangle", "wallCounts", "wallOffsets", "sideWallStart",
-    "oldWallStart",
+    "oldWallStart", "walkNode", "walkItem",
 )
 DISTANCE_GRID = 48  # cells per axis of each shape's distance-bound grid (csrc GRID)
 WALK_BUCKETS = 24**3  # walk-order buckets per shape (csrc WALK_BUCKETS)
@@ -308,6 +308,7 @@ class Engine:
             "walkBucketOffset": 4 * (len(library.shapes) * WALK_BUCKETS + 1),
             "sdfLaneCounts": 4 * 32 * pc if spec.contact_geometry == "sdf" else 16,
             "walkCertPoint": 16 * self.survivor_capacity, "walkCertTriangle": 4 * self.survivor_capacity,
+            "walkNode": 16 * self.survivor_capacity, "walkItem": 8 * self.survivor_capacity,
             "wallCounts": 4 * walls, "wallOffsets": 4 * (walls + 1),
         }
         for name, nbytes in sizes.items():

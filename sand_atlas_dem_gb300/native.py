@@ -118,6 +118,8 @@ def load():
         fn.restype = ct.c_int
     lib.sdg_engine_kernels_per_step.argtypes = [ct.c_void_p]
     lib.sdg_engine_kernels_per_step.restype = ct.c_int
+    lib.sdg_engine_branch_kernels.argtypes = [ct.c_void_p, ct.c_int]
+    lib.sdg_engine_branch_kernels.restype = ct.c_int
     _LIB = lib
     return lib
 
@@ -140,6 +142,7 @@ EXPORTS = (
     "sdg_engine_advance",
     "sdg_engine_profile",
     "sdg_engine_kernels_per_step",
+    "sdg_engine_branch_kernels",
     "sdg_exclusive_scan",
     "sdg_scan_partials",
     "sdg_copy_buffers",

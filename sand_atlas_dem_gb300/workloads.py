@@ -489,6 +489,8 @@ def main(argv=None):
     p.add_argument("--resume", help="continue from a saved (partial) packing record")
     p.add_argument("--max-evaluations", type=int, default=40_000)
     p.add_argument("--max-seconds", type=float, default=None)
+    p.add_argument("--overlap", type=float, default=0.05,
+                   help="deepest overlap (fraction of a diameter) each relaxation must reach")
     args = p.parse_args(argv)
     library = synthetic_library(args.library)
     start = time.perf_counter()
@@ -497,7 +499,7 @@ def main(argv=None):
     resume = load_packing(args.resume) if args.resume else None
     before = resume["meta"] if resume else {}
     out = descent_packing(library, args.grains, args.solid_fraction, seed=args.seed, start=resume,
-                          max_evaluations=args.max_evaluations, max_seconds=args.max_seconds,
+                          overlap=args.overlap, max_evaluations=args.max_evaluations, max_seconds=args.max_seconds,
                           log=lambda row: print(json.dumps(row), file=sys.stderr, flush=True))
     meta.update(method="affine compression with frictionless force descent",
                 evaluations=out["evaluations"] + before.get("evaluations", 0),
