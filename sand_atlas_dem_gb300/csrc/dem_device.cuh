@@ -278,6 +278,21 @@ __device__ __forceinline__ float4 rotationIncrement(f3 w, float dt, float4 q) {
 // referenceCell rows at [2s].  A single specimen is s = 0 throughout.
 __device__ __forceinline__ uint32_t specimenOf(const Res& r, uint32_t i) { return r.grainSpecimen[i]; }
 
+// The periodic image shift floor(d / box + 0.5) of a raw separation d.
+// Where |d| <= 0.45 box it is 0 and where 0.55 box <= |d| <= 1.45 box it is
+// +-1: d / box + 0.5 lies in [0.05, 0.95] or [1.05, 1.95] (mirrored for
+// d < 0), whatever the rounding of the FP64 division.  An FP32 comparison
+// (relative error 1e-7) cannot move |d| across those margins, so it picks the
+// very value the FP64 expression takes; only near |d| = box / 2 (and beyond
+// 1.45 box) is the FP64 expression evaluated.  That spares nearly every
+// pair the FP64 division, a few dozen instructions on GB300's narrow FP64
+// pipe.
+__device__ __forceinline__ double imageShift(double d, double box) {
+    float ad = fabsf(__double2float_rn(d)), fb = __double2float_rn(box);
+    if (ad <= __fmul_rn(0.45f, fb)) return 0.0;
+    if (ad >= __fmul_rn(0.55f, fb) && ad <= __fmul_rn(1.45f, fb)) return d > 0.0 ? 1.0 : -1.0;
+    return floor(__dadd_rn(__ddiv_rn(d, box), 0.5));
+}
 // Minimum-image branch j - i in FP64, cast to FP32 (cpu_scheduling.slang:10-15).
 __device__ __forceinline__ f3 centerBranch64(const Res& r, const Config& c, uint32_t i, uint32_t j) {
     float4 pi = r.position[i], pj = r.position[j], li = r.positionRemainder[i], lj = r.positionRemainder[j];
@@ -287,9 +302,9 @@ __device__ __forceinline__ f3 centerBranch64(const Res& r, const Config& c, uint
     double dz = __dadd_rn(__dsub_rn((double)pj.z, (double)pi.z), __dsub_rn((double)lj.z, (double)li.z));
     if (c.periodic != 0) {
         double bx = cell.x, by = cell.y, bz = cell.z;
-        dx = __dsub_rn(dx, __dmul_rn(floor(__dadd_rn(__ddiv_rn(dx, bx), 0.5)), bx));
-        dy = __dsub_rn(dy, __dmul_rn(floor(__dadd_rn(__ddiv_rn(dy, by), 0.5)), by));
-        dz = __dsub_rn(dz, __dmul_rn(floor(__dadd_rn(__ddiv_rn(dz, bz), 0.5)), bz));
+        dx = __dsub_rn(dx, __dmul_rn(imageShift(dx, bx), bx));
+        dy = __dsub_rn(dy, __dmul_rn(imageShift(dy, by), by));
+        dz = __dsub_rn(dz, __dmul_rn(imageShift(dz, bz), bz));
     }
     return {__double2float_rn(dx), __double2float_rn(dy), __double2float_rn(dz)};
 }
