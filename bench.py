@@ -98,7 +98,7 @@ DATA = ROOT / "sand_atlas_dem_gb300" / "data"
 WALK_TRAFFIC = {"dense-10k": 74.51e6}
 # work[] counters (csrc/dem_device.cuh): the stored node-filter results and
 # the neighbour-list rebuilds.
-W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS, W_CERTIFIED, W_REBUILDS = 8, 9, 10, 15, 17
+W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS, W_CERTIFIED, W_REBUILDS, W_DORMANT = 8, 9, 10, 15, 17, 18
 # Steps of the long window timed after the headline steps: the length of the
 # workload's own run, so that the filter builds and neighbour rebuilds its
 # motion causes are inside it.
@@ -321,7 +321,7 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def algorithmic_bytes(n, pairs, contacts, items, nodes, survivors, kept, rebuild, library_bytes):
+def algorithmic_bytes(n, pairs, contacts, items, nodes, survivors, kept, rebuild, library_bytes, dormant=0):
     """Per-step algorithmic HBM bytes of the whole step and of the node query.
 
     Step: 516 B/grain + 264 B/pair + 272 B/contact + 88 B/grain on rebuild
@@ -332,12 +332,14 @@ def algorithmic_bytes(n, pairs, contacts, items, nodes, survivors, kept, rebuild
     sample index and sample (20 B); each survivor of the one-dot test is
     listed and read back, and its keep flag written and scanned (24 B); each
     exact query reads its list entry, item record, pair, branch, sample and
-    both grains' rotation and body, and a hit writes its record (132 B); the
+    both grains' rotation and body, and a hit writes its record (132 B); a
+    dormant slot of a stored list (its node proven out of reach until the
+    next build) reads its 8-byte certificate word and is not queried; the
     packed library is read once (it stays in L2).
     """
     step = 516 * n + 264 * pairs + 272 * contacts + 88 * n * rebuild + library_bytes
     query = 88 * items + 20 * nodes + 24 * survivors + 132 * kept + library_bytes
-    walk = 132 * kept + library_bytes
+    walk = 132 * (kept - dormant) + 8 * dormant + library_bytes
     return step, query, walk
 
 
@@ -352,7 +354,7 @@ def launches(e, steps, rebuilds, builds):
 
 def counters(e):
     work = e.read("work", np.uint32, (64,))
-    return int(work[W_REBUILDS]), int(work[W_FILTER_BUILDS]), int(work[W_CERTIFIED])
+    return int(work[W_REBUILDS]), int(work[W_FILTER_BUILDS]), int(work[W_CERTIFIED]), int(work[W_DORMANT])
 
 
 def long_window(e, w, steps, flush):
@@ -368,6 +370,7 @@ def long_window(e, w, steps, flush):
             "ms_p99": float(np.percentile(ms, 99)), "ms_max": float(ms.max()),
             "neighbour_rebuilds": rebuilds, "filter_builds": builds,
             "certified_queries_per_step": (after[2] - before[2]) / steps,
+            "dormant_slots_at_end": after[3],
             "gpu_launches": launches(e, steps, rebuilds, builds),
             "l2": "flushed before each step (256 MiB write)"}
 
@@ -403,7 +406,7 @@ def run_gb300(args, cpu=True):
     from sand_atlas_dem_gb300.engine import Engine
 
     w = Workload(args.workload, args.grains)
-    e = w.engine(Engine)
+    e = w.engine(Engine, use_graph=not args.no_graph)
     rate = w.rate()
     # Warm-up (graph capture happens in the first call).
     e.advance(max(3, args.warmup), rate=rate)
@@ -424,7 +427,8 @@ def run_gb300(args, cpu=True):
                     "builds_in_timed_steps": timed_builds,
                     "neighbour_rebuilds_in_timed_steps": timed_rebuilds,
                     "timed_steps": int(work1[W_FILTER_STEPS] - work0[W_FILTER_STEPS]),
-                    "certified_queries_per_step": float(work1[W_CERTIFIED] - work0[W_CERTIFIED]) / args.steps}
+                    "certified_queries_per_step": float(work1[W_CERTIFIED] - work0[W_CERTIFIED]) / args.steps,
+                    "dormant_slots": int(work1[W_DORMANT])}
     device_s = sum(step_ms) / 1e3
     value = w.grains * args.steps / device_s
     kernel_count = launches(e, args.steps, timed_rebuilds, timed_builds)
@@ -443,8 +447,9 @@ def run_gb300(args, cpu=True):
     cand = e.read("candidates", np.uint32, (e.candidate_capacity, 2))[:items]
     nodes = int(leaf_nodes[cand[:, 1]].sum()) if items else 0
     lib_bytes = sum(a.nbytes for k, a in e.layout.geometry.items() if k.startswith("mesh") or k == "sample")
+    dormant = filter_cache["dormant_slots"]
     step_bytes, query_bytes, walk_bytes = algorithmic_bytes(w.grains, pairs, contacts, items, nodes, survivors,
-                                                            kept, 0, lib_bytes)
+                                                            kept, 0, lib_bytes, dormant)
     kernel_name = ("k_nodeWalkKnown + k_nodeWalkSlow (exact queries: certified triangles, then full BVH walks)"
                    if e.filter_margin > 0 and e.culler is None else "k_nodeWalk (exact BVH queries, one thread per kept node)")
     group_name = "k_nodeFilter, k_survivorList, k_survivorPrefilter, k_walkList, k_nodeWalk + scans"
@@ -749,6 +754,11 @@ def main():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--prepare-only", action="store_true")
     p.add_argument("--culler", action="store_true", help="also train the learned culler and compare")
+    p.add_argument("--no-graph", action="store_true",
+                   help="launch each step's kernels one by one instead of replaying the captured graph "
+                        "(for per-kernel profilers, which do not list the kernels of conditional graph nodes; "
+                        "the neighbour-build and filter-build kernels then launch and return at once on the "
+                        "steps that skip them)")
     p.add_argument("--no-plain", action="store_true", help="skip the plain-path comparison")
     p.add_argument("--window", type=int, default=None,
                    help="steps of the long amortized window (default: the workload's run length; 0 skips it)")

@@ -40,7 +40,8 @@
  *             contact counts per virtual lane of the reference's 64-lane
  *             group, 32 words per pair, and per stored walk-list slot its
  *             nearest-triangle certificate: the point it was taken at with
- *             the distance gap, and the triangle, and with planes the
+ *             the distance gap, and the triangle with a tying triangle of
+ *             another leaf (two words; or a dormant mark), and with planes the
  *             plane-contact count of each (wall, grain), wall-major, its
  *             exclusive scan, and the first contact of each (wall, grain)
  *             on the side being written and on the committed side, and per

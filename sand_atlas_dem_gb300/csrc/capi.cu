@@ -7,6 +7,7 @@
 // sizes only.  Entry points return 0 on success, nonzero on a CUDA or argument
 // error (text via sdg_last_error); solver failures are reported in control[0]
 // exactly as the reference does.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -54,6 +55,12 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
     c.survivorCapacity = uint32_t(v[36]);
     c.distanceGridEnabled = uint32_t(v[37]);
     c.filterMargin = float(v[38]);
+    {
+        // meshChildren, meshTriangles, meshNormals, sample (buffer order).
+        const int library[4] = {77 + 40, 31, 32, 24};
+        for (int k = 0; k < 4; ++k)
+            c.library16[k] = bytes ? uint32_t(std::min<uint64_t>(bytes[library[k]] / 16, 0xFFFFFFFFu)) : 0u;
+    }
     if (!(c.filterMargin >= 0.0f) || c.filterMargin > 1.0f) {
         g_error = "filter margin must lie in [0, 1] (target shape frame)";
         return 1;
@@ -103,7 +110,7 @@ static int unpack(void* const* buffers, const uint64_t* bytes, const double* val
             bytes[77 + 48] < (uint64_t(c.shapes) * WALK_BUCKETS + 1) * 4 ||
             bytes[77 + 49] < (uint64_t(c.shapes) * WALK_BUCKETS + 1) * 4 ||
             (c.meshGeometry == 0 && bytes[77 + 50] < uint64_t(c.pairCapacity) * 32 * 4) ||
-            bytes[77 + 51] < uint64_t(c.survivorCapacity) * 16 || bytes[77 + 52] < uint64_t(c.survivorCapacity) * 4 ||
+            bytes[77 + 51] < uint64_t(c.survivorCapacity) * 16 || bytes[77 + 52] < uint64_t(c.survivorCapacity) * 8 ||
             bytes[77 + 57] < uint64_t(c.survivorCapacity) * 16 || bytes[77 + 58] < uint64_t(c.survivorCapacity) * 8 ||
             (c.wallCount != 0 &&
              (bytes[70] < uint64_t(c.wallCount) * 16 || bytes[71] < uint64_t(c.wallCount) * 16 ||
@@ -154,6 +161,7 @@ template <class Branch>
 static void stepSequence(const Params& P, cudaStream_t s, Branch&& branch) {
     const Config& c = P.c;
     if (c.activeTimestep) launch_state("checkContactTimestep", P, c.N, s);
+    launch_contacts("prefetch", P, 0, s);
     Params B = P;
     B.c.viscousCapture = c.normalViscosity > 0 ? 1u : 0u;
     launch_state("beginStep", B, c.N, s);

@@ -15,6 +15,9 @@
 namespace sdg {
 
 constexpr uint32_t EMPTY = 0xffffffffu;
+// A stored walk slot whose node was found farther outside its target than
+// any motion the stored filter results allow before their next build.
+constexpr uint32_t DORMANT = 0xfffffffeu;
 constexpr int RESOURCE_COUNT = 77;
 
 // Solver flags (src/sand_atlas_dem/gpu.py:11-26) plus one for bounded waits.
@@ -52,6 +55,10 @@ struct Config {
     // distance and their survivors are reused while no node has moved that far
     // relative to its partner (0 = run the filters every step).
     float filterMargin;
+    // Sizes (16-byte units, from the caller's buffer sizes; 0 = unknown) of
+    // the library arrays the exact queries read: meshChildren, meshTriangles,
+    // meshNormals, sample.  The step prefetches them into L2.
+    uint32_t library16[4];
 };
 
 // Buffers: the reference Resources block (solver.slang:20-100) in declaration
@@ -131,7 +138,9 @@ struct Res {
     uint32_t* walkBucketOffset;       // shapes x WALK_BUCKETS + 1: first walk-list slot of each bucket
     uint32_t* sdfLaneCounts;          // SDF geometry, 32 x pairCapacity: contacts of virtual lanes l and l + 32
     float4* walkCertPoint;            // survivorCapacity: per stored walk slot, where its certificate was taken, and the gap
-    uint32_t* walkCertTriangle;       // survivorCapacity: its certified nearest triangle (EMPTY: none)
+    uint2* walkCertTriangle;          // survivorCapacity: x its certified nearest triangle (EMPTY: none; DORMANT:
+                                      // cannot touch before the next build), y a triangle of another leaf tying it
+                                      // with the same result (EMPTY: none)
     uint32_t* wallCounts;             // wallCount x N: plane contacts of each (wall, grain), wall-major
     uint32_t* wallOffsets;            // wallCount x N + 1: their exclusive scan
     uint32_t* sideWallStart;          // wallCount x N + 1: first contact of each (wall, grain), side being written
@@ -165,6 +174,7 @@ constexpr int W_SLOW = 14;          // stored walk slots left for a full walk th
 constexpr int W_CERTIFIED = 15;     // exact queries answered by a certificate (counter)
 constexpr int W_WALL_BASE = 16;     // first plane contact: the grain-grain contact total
 constexpr int W_REBUILDS = 17;      // steps that rebuilt the neighbour list (counter)
+constexpr int W_DORMANT = 18;       // dormant slots in the stored exact-query list
 
 struct Params {
     Config c;
@@ -436,9 +446,31 @@ __device__ __forceinline__ float4 meshDistance(const Res& r, uint32_t shape, f3 
 // triangle that ties it exactly in the same BVH leaf (two faces meeting at
 // an edge) is not counted against the gap but returned as a partner, in the
 // top two bits (its offset after it in the leaf): between the two, the walk
-// records the partner only where it is strictly nearer.
-__device__ __forceinline__ float4 meshDistanceCertified(const Res& r, uint32_t shape, f3 p, uint32_t seed, float reach,
-                                                        uint32_t& triangle, float& gap) {
+// records the partner only where it is strictly nearer.  A triangle of
+// another leaf whose result ties it bit for bit -- the same squared
+// distance, closest point and pseudonormal, as the two faces of an edge
+// give when both compute the edge point from the same endpoints -- is not
+// counted against the gap either but returned in `tie`: whichever of the two
+// a walk records, its result is the same.
+__device__ __forceinline__ bool sameResult(const Res& r, f3 q, uint32_t normal, f3 q2, uint32_t normal2) {
+    float4 n = __ldg(&r.meshNormals[normal]), n2 = __ldg(&r.meshNormals[normal2]);
+    return __float_as_uint(q.x) == __float_as_uint(q2.x) && __float_as_uint(q.y) == __float_as_uint(q2.y) &&
+           __float_as_uint(q.z) == __float_as_uint(q2.z) && __float_as_uint(n.x) == __float_as_uint(n2.x) &&
+           __float_as_uint(n.y) == __float_as_uint(n2.y) && __float_as_uint(n.z) == __float_as_uint(n2.z);
+}
+// `Warp`: the whole warp runs one walk (p, shape, seed and reach the same on
+// every lane).  Every lane then holds the same stack and takes the same
+// decisions; the lanes evaluate a leaf's triangles together and its results
+// are taken in triangle order, so the walk and its result are the
+// one-thread walk's.  A few walks fill a warp each, instead of one lane of a
+// diverging warp each.
+// `children`/`nodeBase`: where the walk reads node n's record --
+// children + 4 (n - nodeBase): the library's meshChildren (base 0) or the
+// shape's records staged in shared memory (base: its first node).
+template <bool Warp>
+__device__ __forceinline__ float4 meshDistanceCertifiedT(const Res& r, uint32_t shape, f3 p, uint32_t seed,
+                                                         float reach, uint32_t& triangle, uint32_t& tie, float& gap,
+                                                         const float4* children, uint32_t nodeBase) {
     uint32_t root = __ldg(&r.meshRoots[shape].x);
     uint32_t pending[32];
     float pendingDistance[32];
@@ -456,54 +488,97 @@ __device__ __forceinline__ float4 meshDistanceCertified(const Res& r, uint32_t s
     }
     float best = cap, second = cap;
     f3 nearest = mk(0.f, 0.f, 0.f);
-    uint32_t nearestNormal = 0, bestNode = 0xFFFFFFFFu, partner = 0;
+    uint32_t nearestNormal = 0, bestNode = 0xFFFFFFFFu, partner = 0, tied = EMPTY;
     bool found = false;
+    // One leaf triangle's result, in the walk's order.
+    auto take = [&](uint32_t node, uint32_t t, f3 q, uint32_t feature, float distance) {
+        if (distance < best) {
+            second = best;
+            best = distance; nearest = q; nearestNormal = 7 * t + feature; found = true;
+            bestNode = node;
+            partner = 0;
+            tied = EMPTY;
+        } else if (distance == best && found && node == bestNode && partner == 0) {
+            partner = t - nearestNormal / 7;  // 1..3: later in the same leaf
+        } else if (distance == best && found && node != bestNode && tied == EMPTY &&
+                   sameResult(r, q, 7 * t + feature, nearest, nearestNormal)) {
+            tied = t;
+        } else if (distance < second) {
+            second = distance;
+        }
+    };
     while (top > 0) {
         uint32_t slot = --top, node = pending[slot];
         float limit = __fmul_rn(second, 1.00000095367431640625f);
         if (pendingDistance[slot] > limit) continue;
-        const float4* record = r.meshChildren + 4 * size_t(node);
-        float4 r0 = __ldg(record), r1 = __ldg(record + 1);
+        const float4* record = children + 4 * size_t(node - nodeBase);
+        float4 r0 = record[0], r1 = record[1];
         if (__float_as_uint(r0.w) != LEAF_MARK) {
-            float4 r2 = __ldg(record + 2), r3 = __ldg(record + 3);
+            float4 r2 = record[2], r3 = record[3];
             uint32_t a = node + 1, b = __float_as_uint(r0.w);
             float da = boxDistance(xyz(r0), xyz(r1), p), db = boxDistance(xyz(r2), xyz(r3), p);
             if (da < db) { uint32_t s = a; a = b; b = s; float ds = da; da = db; db = ds; }
-            if (top + 2 > 32) { fail(r, F_STACK); triangle = 0xFFFFFFFFu; gap = 0.f; return make_float4(0.f, 0.f, 0.f, 1e20f); }
+            if (top + 2 > 32) {
+                fail(r, F_STACK);
+                triangle = tie = EMPTY;
+                gap = 0.f;
+                return make_float4(0.f, 0.f, 0.f, 1e20f);
+            }
             if (da <= limit) { pending[top] = a; pendingDistance[top++] = da; }
             if (db <= limit) { pending[top] = b; pendingDistance[top++] = db; }
             continue;
         }
         uint32_t first = __float_as_uint(r0.x), count = __float_as_uint(r0.y);
-        for (uint32_t k = 0; k < count; ++k) {
-            uint32_t t = first + k, feature;
-            f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * t])), xyz(__ldg(&r.meshTriangles[3 * t + 1])),
-                                   xyz(__ldg(&r.meshTriangles[3 * t + 2])), feature);
-            f3 dq = p - q;
-            float distance = dot(dq, dq);
-            if (distance < best) {
-                second = best;
-                best = distance; nearest = q; nearestNormal = 7 * t + feature; found = true;
-                bestNode = node;
-                partner = 0;
-            } else if (distance == best && found && node == bestNode && partner == 0) {
-                partner = t - nearestNormal / 7;  // 1..3: later in the same leaf
-            } else if (distance < second) {
-                second = distance;
+        if constexpr (Warp) {
+            const uint32_t lane = threadIdx.x & 31u;
+            for (uint32_t k0 = 0; k0 < count; k0 += 32) {
+                uint32_t t = first + k0 + lane, feature = 0;
+                f3 q = mk(0.f, 0.f, 0.f);
+                float distance = 0.f;
+                if (k0 + lane < count) {
+                    q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * t])), xyz(__ldg(&r.meshTriangles[3 * t + 1])),
+                                        xyz(__ldg(&r.meshTriangles[3 * t + 2])), feature);
+                    f3 dq = p - q;
+                    distance = dot(dq, dq);
+                }
+                uint32_t m = min(32u, count - k0);
+                for (uint32_t j = 0; j < m; ++j) {
+                    f3 qj = mk(__shfl_sync(0xffffffffu, q.x, j), __shfl_sync(0xffffffffu, q.y, j),
+                               __shfl_sync(0xffffffffu, q.z, j));
+                    take(node, first + k0 + j, qj, __shfl_sync(0xffffffffu, feature, j),
+                         __shfl_sync(0xffffffffu, distance, j));
+                }
+            }
+        } else {
+            for (uint32_t k = 0; k < count; ++k) {
+                uint32_t t = first + k, feature;
+                f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * t])), xyz(__ldg(&r.meshTriangles[3 * t + 1])),
+                                       xyz(__ldg(&r.meshTriangles[3 * t + 2])), feature);
+                f3 dq = p - q;
+                take(node, t, q, feature, dot(dq, dq));
             }
         }
     }
     triangle = found ? (nearestNormal / 7) | (partner << 30) : 0xFFFFFFFFu;
+    tie = found ? tied : EMPTY;
     gap = found ? __fsub_rn(__fsqrt_rn(second), __fsqrt_rn(best)) : 0.f;
     return distanceResult(r, p, best, nearest, nearestNormal, found, false);
 }
+__device__ __forceinline__ float4 meshDistanceCertified(const Res& r, uint32_t shape, f3 p, uint32_t seed, float reach,
+                                                        uint32_t& triangle, uint32_t& tie, float& gap) {
+    return meshDistanceCertifiedT<false>(r, shape, p, seed, reach, triangle, tie, gap, r.meshChildren, 0u);
+}
 // The walk's result when the certified triangle (and its same-leaf partner,
-// encoded as by meshDistanceCertified) are known to be nearer than every
-// other: the same closest point, squared distance and feature the walk
-// records -- the partner's only where it is strictly nearer, as the leaf's
-// triangles are taken in order.
+// encoded as by meshDistanceCertified, and its tie of another leaf) are
+// known to be nearer than every other: the same closest point, squared
+// distance and feature the walk records -- the partner's only where it is
+// strictly nearer, as the leaf's triangles are taken in order.  With a tie
+// (EMPTY: none) the result stands only where the tie gives the same result
+// bit for bit (the walk may reach either leaf first); `same` is cleared
+// otherwise, and the caller walks.
 // `a`, `b`, `c` are the certified triangle's vertices (loaded by the caller).
-__device__ __forceinline__ float4 meshDistanceAt(const Res& r, f3 p, uint32_t certified, float4 a, float4 b, float4 c) {
+__device__ __forceinline__ float4 meshDistanceAt(const Res& r, f3 p, uint32_t certified, uint32_t tie, float4 a,
+                                                 float4 b, float4 c, bool& same) {
     uint32_t triangle = certified & 0x3FFFFFFFu, partner = certified >> 30, feature;
     f3 q = closestTriangle(p, xyz(a), xyz(b), xyz(c), feature);
     f3 dq = p - q;
@@ -516,6 +591,14 @@ __device__ __forceinline__ float4 meshDistanceAt(const Res& r, f3 p, uint32_t ce
         f3 dq2 = p - q2;
         float d2 = dot(dq2, dq2);
         if (d2 < best) { best = d2; q = q2; normal = 7 * other + otherFeature; }
+    }
+    same = true;
+    if (tie != EMPTY) {
+        uint32_t tieFeature;
+        f3 q3 = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * tie])), xyz(__ldg(&r.meshTriangles[3 * tie + 1])),
+                                xyz(__ldg(&r.meshTriangles[3 * tie + 2])), tieFeature);
+        f3 dq3 = p - q3;
+        same = __float_as_uint(dot(dq3, dq3)) == __float_as_uint(best) && sameResult(r, q3, 7 * tie + tieFeature, q, normal);
     }
     return distanceResult(r, p, best, q, normal, true, false);
 }

@@ -809,13 +809,14 @@ __global__ void k_walkList(const __grid_constant__ Params P) {
     bool stored = storedKeep(c);
     if (r.control[0] != 0 || (stored && r.work[W_FILTER] == 0)) return;
     uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
+    if (stored && gtid() == 0) r.work[W_DORMANT] = 0;  // a new list: no slot sleeps yet
     for (uint32_t s = gtid(); s < n; s += gstride()) {
         if (!r.survKeep[s]) continue;
         if (stored) {
             uint32_t bucket = r.walkKey[s];
             uint32_t slot = r.walkBucketOffset[bucket] + atomicSub(&r.walkBucketCount[bucket], 1u) - 1u;
             r.walkList[slot] = s;
-            r.walkCertTriangle[slot] = EMPTY;
+            r.walkCertTriangle[slot] = make_uint2(EMPTY, EMPTY);
             // The slot's node record: what its exact query reads every step
             // (one load instead of the survivor -> item -> pair -> sample chain).
             uint2 sv = r.survivors[s];
@@ -908,8 +909,10 @@ __global__ void __launch_bounds__(256) k_nodeWalk(const __grid_constant__ Params
 // triangle's distance lies above T's.  Distances are 1-Lipschitz in the
 // point, so while 2 |p - p0| + slack < g, T is still the unique nearest
 // triangle at p and the walk would record it with the values closestTriangle
-// gives for it: the step evaluates T alone.  The slack, 1e-5 (1 + |p|_1),
-// covers the FP32 rounding of the distances.  The other slots are flagged
+// gives for it: the step evaluates T alone (with its partner or tie, where it
+// has one).  The slack, 1e-5 (1 + |p|_1), covers the FP32 rounding of the
+// distances.  A dormant slot is skipped: its node cannot touch the target
+// before the stored results are built again.  The other slots are flagged
 // (survKeep, unused by a stored list while it is walked), listed in slot
 // order -- the walk-bucket order, so that a warp's walks stay coherent -- and
 // walked by k_nodeWalkSlow in full warps.
@@ -919,9 +922,12 @@ __global__ void __launch_bounds__(256) k_nodeWalkKnown(const __grid_constant__ P
     if (r.control[0] != 0) return;
     uint32_t n = min(r.work[W_KEPT], c.survivorCapacity);
     for (uint32_t t = gtid(); t < n; t += gstride()) {
-        uint32_t triangle = r.walkCertTriangle[t];
+        uint2 cert = r.walkCertTriangle[t];
+        uint32_t triangle = cert.x;
         bool known = false;
-        if (triangle != EMPTY) {
+        if (triangle == DORMANT) {
+            known = true;
+        } else if (triangle != EMPTY) {
             // Every load below depends only on the slot: they issue together.
             uint32_t base = 3 * (triangle & 0x3FFFFFFFu);
             float4 ta = __ldg(&r.meshTriangles[base]), tb = __ldg(&r.meshTriangles[base + 1]),
@@ -933,8 +939,8 @@ __global__ void __launch_bounds__(256) k_nodeWalkKnown(const __grid_constant__ P
             known = __fadd_rn(__fmul_rn(2.002f, length(w.local - xyz(cp))), slack) < cp.w;
             if (known) {
                 float4 pd, na;
-                float4 f = meshDistanceAt(r, w.local, triangle, ta, tb, tc);
-                if (nodeContactWith(r, c, w.rec.x, w.sp, w.bs, w.bd, w.qd, w.arm, f, pd, na)) {
+                float4 f = meshDistanceAt(r, w.local, triangle, cert.y, ta, tb, tc, known);
+                if (known && nodeContactWith(r, c, w.rec.x, w.sp, w.bs, w.bd, w.qd, w.arm, f, pd, na)) {
                     uint2 it = r.walkItem[t];
                     recordHitAt(r, r.walkList[t], it.x, it.y, pd, na);
                 }
@@ -952,27 +958,243 @@ __global__ void k_slowList(const __grid_constant__ Params P) {
     for (uint32_t t = gtid(); t < n; t += gstride())
         if (r.survKeep[t]) r.walkKey[r.keepOffset[t]] = t;
 }
+// Dormant slots.  Until the next build, the motion check of k_pairSetup
+// bounds chord_i r_i + |d branch| + chord_j r_j by m s_j (chord: of a
+// grain's rotation since the build; r: bounding radius; s: scale), so a node
+// inside the target's bounding sphere -- as every node touching it is --
+// lies within m (target frame, unscaled) of where it was at the build, and
+// a node at distance |v| from the target's centre now lies within
+// m max(1, |v| / r_j) of it.  A node farther outside than the sum (times
+// 1.001, plus the distance rounding slack) cannot touch the target before
+// the next build, and its slot sleeps.
+// One slot's certifying walk (by its warp when `Warp`; lane 0 records).
+template <bool Warp>
+__device__ __forceinline__ void certifySlot(const Res& r, const Config& c, uint32_t t, float margin, float reach,
+                                            const float4* children, uint32_t nodeBase) {
+    WalkNode w = walkNode(r, t);
+    uint32_t shape = r.shapeId[w.rec.y], triangle, tie;
+    float gap;
+    float4 f = meshDistanceCertifiedT<Warp>(r, shape, w.local, gridSeed(r, shape, w.local), reach, triangle, tie, gap,
+                                            children, nodeBase);
+    if (Warp && laneId() != 0) return;
+    float slack = __fmul_rn(2e-5f, __fadd_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(w.local.x), fabsf(w.local.y)),
+                                                             fabsf(w.local.z))));
+    float reachNow = fmaxf(1.0f, __fdiv_rn(__fmul_rn(length(w.local), w.bd.x), w.bd.z));
+    float sleep = __fmul_rn(__fmul_rn(1.001f, margin), __fadd_rn(1.0f, reachNow));
+    bool dormant = triangle != EMPTY && f.w > __fadd_rn(sleep, slack);
+    if (dormant) {
+        // One count per group of lanes marking slots together.
+        uint32_t group = __activemask();
+        if (laneId() == uint32_t(__ffs(group) - 1)) atomicAdd(&r.work[W_DORMANT], uint32_t(__popc(group)));
+    }
+    r.walkCertTriangle[t] = dormant ? make_uint2(DORMANT, EMPTY) : make_uint2(triangle, tie);
+    r.walkCertPoint[t] = w4(w.local, gap);
+    float4 pd, na;
+    if (nodeContactWith(r, c, w.rec.x, w.sp, w.bs, w.bd, w.qd, w.arm, f, pd, na)) {
+        uint2 it = r.walkItem[t];
+        recordHitAt(r, r.walkList[t], it.x, it.y, pd, na);
+    }
+}
 // A certifying walk for each listed slot, recording its new certificate.
+// Few walks (up to two per warp of the grid) run a warp each; more run a
+// lane each, in 32-slot runs of the list (coherent walks) dealt to the
+// blocks in turn, so that either way they spread over every SM.
 __global__ void __launch_bounds__(256) k_nodeWalkSlow(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
     if (r.control[0] != 0) return;
     uint32_t n = min(r.work[W_SLOW], c.survivorCapacity);
     if (gtid() == 0) r.work[W_CERTIFIED] += min(r.work[W_KEPT], c.survivorCapacity) - n;
-    float reach = __fadd_rn(__fmul_rn(2.01f, __uint_as_float(r.work[W_FILTER_MARGIN])), 1e-4f);
-    for (uint32_t i = gtid(); i < n; i += gstride()) {
-        uint32_t t = r.walkKey[i];
-        WalkNode w = walkNode(r, t);
-        uint32_t shape = r.shapeId[w.rec.y], triangle;
-        float gap;
-        float4 pd, na;
-        float4 f = meshDistanceCertified(r, shape, w.local, gridSeed(r, shape, w.local), reach, triangle, gap);
-        r.walkCertTriangle[t] = triangle;
-        r.walkCertPoint[t] = w4(w.local, gap);
-        if (nodeContactWith(r, c, w.rec.x, w.sp, w.bs, w.bd, w.qd, w.arm, f, pd, na)) {
-            uint2 it = r.walkItem[t];
-            recordHitAt(r, r.walkList[t], it.x, it.y, pd, na);
+    float margin = __uint_as_float(r.work[W_FILTER_MARGIN]);
+    float reach = __fadd_rn(__fmul_rn(2.01f, margin), 1e-4f);
+    uint32_t warps = gridDim.x * (blockDim.x >> 5), warp = blockIdx.x + gridDim.x * (threadIdx.x >> 5);
+    if (n <= 2 * warps) {
+        for (uint32_t i = warp; i < n; i += warps)
+            certifySlot<true>(r, c, r.walkKey[i], margin, reach, r.meshChildren, 0u);
+    } else {
+        for (uint32_t i = 32 * warp + laneId(); i < n; i += 32 * warps)
+            certifySlot<false>(r, c, r.walkKey[i], margin, reach, r.meshChildren, 0u);
+    }
+}
+// The same walks with each target shape's BVH node records staged in shared
+// memory.  The slow list is in walk-bucket order, so each shape's walks form
+// one run of it (from the scan of the flags at the shape's first bucket to
+// the scan at the next shape's); the runs are cut into units of one shape,
+// dealt to the CTAs in turn.  A CTA copies its unit's shape records (one
+// 64-byte record per node, up to STAGE_BYTES) into shared memory by bulk
+// asynchronous copies completing on an mbarrier -- once per change of shape
+// -- and walks the unit: a warp per walk when the step has few walks, a lane
+// per walk otherwise.  Internal node visits then read shared memory instead
+// of L2; leaves read their triangles from the library as before.  A shape
+// whose records exceed the stage is walked from the library by the same CTA.
+constexpr uint32_t STAGE_THREADS = 512;
+constexpr uint32_t STAGE_BYTES = 192u << 10;
+constexpr uint32_t STAGE_MAX_SHAPES = 4096;
+constexpr uint32_t STAGE_CHUNK = 16u << 10;
+__device__ __forceinline__ uint32_t smemAddress(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ bool mbarrierWait(uint32_t bar, uint32_t parity) {
+    // Bounded: about 2^22 polls (far beyond a 192 KB copy), then give up.
+    for (uint32_t k = 0; k < (1u << 22); ++k) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__global__ void __launch_bounds__(STAGE_THREADS, 1) k_nodeWalkStaged(const __grid_constant__ Params P) {
+    extern __shared__ __align__(128) unsigned char stageMemory[];
+    float4* stage = reinterpret_cast<float4*>(stageMemory);
+    uint32_t* unitStart = reinterpret_cast<uint32_t*>(stageMemory + STAGE_BYTES);  // shapes + 1
+    __shared__ __align__(8) uint64_t barrier;
+    __shared__ uint32_t warpTotals[STAGE_THREADS / 32], carry, liveFlag;
+    const Res& r = P.r;
+    const Config& c = P.c;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warpId = tid >> 5, warps = STAGE_THREADS / 32;
+    if (tid == 0) liveFlag = r.control[0] == 0 ? 1u : 0u;
+    __syncthreads();
+    if (!liveFlag) return;  // block-uniform
+    uint32_t n = min(r.work[W_SLOW], c.survivorCapacity);
+    if (blockIdx.x == 0 && tid == 0) r.work[W_CERTIFIED] += min(r.work[W_KEPT], c.survivorCapacity) - n;
+    if (n == 0) return;
+    float margin = __uint_as_float(r.work[W_FILTER_MARGIN]);
+    float reach = __fadd_rn(__fmul_rn(2.01f, margin), 1e-4f);
+    bool warpMode = n <= 2u * gridDim.x * warps;
+    uint32_t per = warpMode ? 2u * warps : 4u * STAGE_THREADS;  // walks per unit
+    // Units per shape, scanned into unitStart (exclusive; unitStart[shapes] = total).
+    if (tid == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < c.shapes; base += STAGE_THREADS) {
+        uint32_t s = base + tid, units = 0;
+        if (s < c.shapes) {
+            uint32_t lo = r.keepOffset[r.walkBucketOffset[s * WALK_BUCKETS]];
+            uint32_t hi = r.keepOffset[r.walkBucketOffset[(s + 1) * WALK_BUCKETS]];
+            units = (hi - lo + per - 1) / per;
         }
+        uint32_t x = units;
+#pragma unroll
+        for (uint32_t d = 1; d < 32; d <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += y;
+        }
+        if (lane == 31) warpTotals[warpId] = x;
+        __syncthreads();
+        if (warpId == 0) {
+            uint32_t t = lane < warps ? warpTotals[lane] : 0u;
+#pragma unroll
+            for (uint32_t d = 1; d < 32; d <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, t, d);
+                if (lane >= d) t += y;
+            }
+            if (lane < warps) warpTotals[lane] = t;  // inclusive over warps
+        }
+        __syncthreads();
+        uint32_t before = carry + (warpId ? warpTotals[warpId - 1] : 0u) + x - units;
+        if (s < c.shapes) unitStart[s] = before;
+        __syncthreads();
+        if (tid == 0) carry += warpTotals[warps - 1];
+        __syncthreads();
+    }
+    if (tid == 0) unitStart[c.shapes] = carry;
+    uint32_t bar = smemAddress(&barrier);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    uint32_t total = unitStart[c.shapes], phase = 0, staged = EMPTY;
+    bool stalled = false;
+    for (uint32_t u = blockIdx.x; u < total && !stalled; u += gridDim.x) {
+        // The unit's shape: the last s with unitStart[s] <= u.
+        uint32_t lo = 0, hi = c.shapes;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (unitStart[mid] <= u) lo = mid; else hi = mid;
+        }
+        uint32_t shape = lo;
+        uint32_t first = r.keepOffset[r.walkBucketOffset[shape * WALK_BUCKETS]] + (u - unitStart[shape]) * per;
+        uint32_t last = min(first + per, r.keepOffset[r.walkBucketOffset[(shape + 1) * WALK_BUCKETS]]);
+        uint4 nodes = __ldg(&r.meshRoots[shape]);
+        uint32_t bytes = (nodes.y - nodes.x) * 64u;
+        bool fits = bytes <= STAGE_BYTES;
+        if (fits && staged != shape) {
+            __syncthreads();  // every warp is done with the staged shape
+            if (tid == 0) {
+                // The async proxy overwrites what the generic proxy read.
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+                const char* from = reinterpret_cast<const char*>(r.meshChildren + 4 * size_t(nodes.x));
+                uint32_t to = smemAddress(stage);
+                for (uint32_t off = 0; off < bytes; off += STAGE_CHUNK) {
+                    uint32_t size = min(STAGE_CHUNK, bytes - off);
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                        ::"r"(to + off), "l"(from + off), "r"(size), "r"(bar)
+                        : "memory");
+                }
+            }
+            if (!mbarrierWait(bar, phase)) {
+                fail(r, F_WAIT);
+                stalled = true;  // block-uniform only if every thread timed out: re-checked below
+            }
+            phase ^= 1u;
+            staged = shape;
+            // Every thread leaves together if any thread gave up.
+            stalled = __syncthreads_or(stalled);
+            if (stalled) break;
+        }
+        const float4* children = fits ? stage : r.meshChildren;
+        uint32_t base = fits ? nodes.x : 0u;
+        if (warpMode) {
+            for (uint32_t i = first + warpId; i < last; i += warps)
+                certifySlot<true>(r, c, r.walkKey[i], margin, reach, children, base);
+        } else {
+            for (uint32_t i = first + tid; i < last; i += STAGE_THREADS)
+                certifySlot<false>(r, c, r.walkKey[i], margin, reach, children, base);
+        }
+    }
+    if (stalled && tid == 0) {
+        // A copy may still be landing: wait for it (bounded) before the
+        // shared memory is released.
+        mbarrierWait(bar, phase ^ 1u);
+    }
+}
+// L2 prefetch, first in a step, of what the step's exact queries read
+// through chains of dependent loads: the packed library (BVH node records,
+// triangles, pseudonormals, node samples) and, with a stored exact-query
+// list, its per-slot certificates and node records.  One bulk copy-engine
+// prefetch (cp.async.bulk.prefetch.L2) per 16 KB, from two CTAs per SM: the
+// lines arrive while the drift, neighbour and pair kernels run, instead of
+// one latency at a time inside the walks (64 KB pieces from four CTAs took
+// longer than the walks saved).  A hint only: nothing waits for it and no result
+// depends on it.  Every range starts 16-byte aligned (float4/uint4/uint2
+// arrays from the allocator) and is cut to a multiple of 16 bytes.
+__global__ void k_prefetch(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    constexpr uint32_t CHUNK = 16u << 10;
+    uint32_t kept = storedKeep(c) ? min(r.work[W_KEPT], c.survivorCapacity) : 0u;
+    const void* base[9] = {r.meshChildren, r.meshTriangles, r.meshNormals, r.sample, r.walkCertTriangle,
+                           r.walkCertPoint, r.walkNode, r.walkItem, r.walkList};
+    uint64_t size[9] = {16ull * c.library16[0], 16ull * c.library16[1], 16ull * c.library16[2],
+                        16ull * c.library16[3], 8ull * kept, 16ull * kept, 16ull * kept, 8ull * kept, 4ull * kept};
+    uint32_t chunk = gtid();
+    for (int k = 0; k < 9; ++k) {
+        uint64_t bytes = size[k] & ~uint64_t(15);
+        uint64_t chunks = (bytes + CHUNK - 1) / CHUNK;
+        for (; chunk < chunks; chunk += gstride()) {
+            uint64_t offset = uint64_t(chunk) * CHUNK;
+            uint64_t left = bytes - offset;
+            uint32_t n = left < CHUNK ? uint32_t(left) : CHUNK;
+            const char* at = static_cast<const char*>(base[k]) + offset;
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(at), "r"(n) : "memory");
+        }
+        chunk -= uint32_t(chunks);
     }
 }
 // Emits one item's hits (the warp, lane per node slot of each 32-slot half).
@@ -1936,7 +2158,21 @@ static void collectWalk(const Params& P, cudaStream_t s) {
         launch_scan(r.survKeep, r.keepOffset, ScanCount{r.work + W_KEPT, c.survivorCapacity, 1, 0}, true,
                     r.work + W_SLOW, nullptr, r.scanPartials, s);
         k_slowList<<<g, 256, 0, s>>>(P);
-        k_nodeWalkSlow<<<g, 256, 0, s>>>(P);
+        if (c.shapes <= STAGE_MAX_SHAPES) {
+            size_t dynamic = STAGE_BYTES + 4 * (size_t(c.shapes) + 1);
+            // The opt-in shared-memory limit, set once per device.
+            static uint64_t attributed = 0;
+            int device = 0;
+            cudaGetDevice(&device);
+            if (device < 64 && !((attributed >> device) & 1u)) {
+                cudaFuncSetAttribute(k_nodeWalkStaged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(STAGE_BYTES + 4 * (STAGE_MAX_SHAPES + 1)));
+                attributed |= uint64_t(1) << device;
+            }
+            k_nodeWalkStaged<<<smCount(), STAGE_THREADS, dynamic, s>>>(P);
+        } else {
+            k_nodeWalkSlow<<<g, 256, 0, s>>>(P);
+        }
     } else {
         k_nodeWalk<<<grid(c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
     }
@@ -1988,6 +2224,9 @@ int launch_contacts(const std::string_view& name, const Params& P, uint32_t coun
     else if (name == "collect") contacts(P, s);
     else if (name == "collectCull") collectCull(P, s);
     else if (name == "collectHead") collectHead(P, s);
+    else if (name == "prefetch") {
+        if (c.meshGeometry != 0) k_prefetch<<<grid(0, 2), 64, 0, s>>>(P);
+    }
     else if (name == "collectBuild") { cullBuild(P, s); collectFilter(P, s); }
     else if (name == "collectTail") collectTail(P, s);
     else if (name == "collectQuery") collectQuery(P, s);

@@ -307,7 +307,7 @@ class Engine:
             "walkKey": 4 * self.survivor_capacity, "walkBucketCount": 4 * (len(library.shapes) * WALK_BUCKETS + 1),
             "walkBucketOffset": 4 * (len(library.shapes) * WALK_BUCKETS + 1),
             "sdfLaneCounts": 4 * 32 * pc if spec.contact_geometry == "sdf" else 16,
-            "walkCertPoint": 16 * self.survivor_capacity, "walkCertTriangle": 4 * self.survivor_capacity,
+            "walkCertPoint": 16 * self.survivor_capacity, "walkCertTriangle": 8 * self.survivor_capacity,
             "walkNode": 16 * self.survivor_capacity, "walkItem": 8 * self.survivor_capacity,
             "wallCounts": 4 * walls, "wallOffsets": 4 * (walls + 1),
         }
