@@ -910,8 +910,11 @@ __global__ void __launch_bounds__(256) k_nodeWalk(const __grid_constant__ Params
 // point, so while 2 |p - p0| + slack < g, T is still the unique nearest
 // triangle at p and the walk would record it with the values closestTriangle
 // gives for it: the step evaluates T alone (with its partner or tie, where it
-// has one).  The slack, 1e-5 (1 + |p|_1), covers the FP32 rounding of the
-// distances.  A dormant slot is skipped: its node cannot touch the target
+// has one).  The slack, 4e-6 (1 + |p|_1), covers the FP32 rounding of the
+// distances: with e the largest difference between a computed triangle
+// distance and the exact one (a few units in the last place of |p|, about
+// 3e-7 (1 + |p|) here), the other triangles stay strictly farther while
+// 2 |p - p0| + 4e = g; the slack is above 4e.  A dormant slot is skipped: its node cannot touch the target
 // before the stored results are built again.  The other slots are flagged
 // (survKeep, unused by a stored list while it is walked), listed in slot
 // order -- the walk-bucket order, so that a warp's walks stay coherent -- and
@@ -934,7 +937,7 @@ __global__ void __launch_bounds__(256) k_nodeWalkKnown(const __grid_constant__ P
                    tc = __ldg(&r.meshTriangles[base + 2]);
             float4 cp = r.walkCertPoint[t];
             WalkNode w = walkNode(r, t);
-            float slack = __fmul_rn(1e-5f, __fadd_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(w.local.x), fabsf(w.local.y)),
+            float slack = __fmul_rn(4e-6f, __fadd_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(w.local.x), fabsf(w.local.y)),
                                                                     fabsf(w.local.z))));
             known = __fadd_rn(__fmul_rn(2.002f, length(w.local - xyz(cp))), slack) < cp.w;
             if (known) {
@@ -998,12 +1001,15 @@ __device__ __forceinline__ void certifySlot(const Res& r, const Config& c, uint3
 // A certifying walk for each listed slot, recording its new certificate.
 // Few walks (up to two per warp of the grid) run a warp each; more run a
 // lane each, in 32-slot runs of the list (coherent walks) dealt to the
-// blocks in turn, so that either way they spread over every SM.
-__global__ void __launch_bounds__(256) k_nodeWalkSlow(const __grid_constant__ Params P) {
+// blocks in turn, so that either way they spread over every SM.  Only a
+// list longer than `above` is walked here (k_nodeWalkStaged takes the
+// shorter ones; 0: every list).
+__global__ void __launch_bounds__(256) k_nodeWalkSlow(const __grid_constant__ Params P, uint32_t above) {
     const Res& r = P.r;
     const Config& c = P.c;
     if (r.control[0] != 0) return;
     uint32_t n = min(r.work[W_SLOW], c.survivorCapacity);
+    if (n <= above && above != 0) return;
     if (gtid() == 0) r.work[W_CERTIFIED] += min(r.work[W_KEPT], c.survivorCapacity) - n;
     float margin = __uint_as_float(r.work[W_FILTER_MARGIN]);
     float reach = __fadd_rn(__fmul_rn(2.01f, margin), 1e-4f);
@@ -1031,6 +1037,9 @@ constexpr uint32_t STAGE_THREADS = 512;
 constexpr uint32_t STAGE_BYTES = 192u << 10;
 constexpr uint32_t STAGE_MAX_SHAPES = 4096;
 constexpr uint32_t STAGE_CHUNK = 16u << 10;
+// The staged kernel runs one CTA per SM and takes lists of up to two walks
+// per warp of its grid; longer lists go to k_nodeWalkSlow (a lane per walk,
+// full occupancy), which hides the walks' load latency better there.
 __device__ __forceinline__ uint32_t smemAddress(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
@@ -1060,12 +1069,14 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1) k_nodeWalkStaged(const __gri
     __syncthreads();
     if (!liveFlag) return;  // block-uniform
     uint32_t n = min(r.work[W_SLOW], c.survivorCapacity);
+    if (n > 2u * gridDim.x * warps) return;  // a long list: k_nodeWalkSlow walks it
     if (blockIdx.x == 0 && tid == 0) r.work[W_CERTIFIED] += min(r.work[W_KEPT], c.survivorCapacity) - n;
     if (n == 0) return;
     float margin = __uint_as_float(r.work[W_FILTER_MARGIN]);
     float reach = __fadd_rn(__fmul_rn(2.01f, margin), 1e-4f);
-    bool warpMode = n <= 2u * gridDim.x * warps;
-    uint32_t per = warpMode ? 2u * warps : 4u * STAGE_THREADS;  // walks per unit
+    // Walks per unit: one or two per warp, so that the units spread over
+    // every CTA.
+    uint32_t per = n <= gridDim.x * warps ? warps : 2u * warps;
     // Units per shape, scanned into unitStart (exclusive; unitStart[shapes] = total).
     if (tid == 0) carry = 0;
     __syncthreads();
@@ -1150,13 +1161,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1) k_nodeWalkStaged(const __gri
         }
         const float4* children = fits ? stage : r.meshChildren;
         uint32_t base = fits ? nodes.x : 0u;
-        if (warpMode) {
-            for (uint32_t i = first + warpId; i < last; i += warps)
-                certifySlot<true>(r, c, r.walkKey[i], margin, reach, children, base);
-        } else {
-            for (uint32_t i = first + tid; i < last; i += STAGE_THREADS)
-                certifySlot<false>(r, c, r.walkKey[i], margin, reach, children, base);
-        }
+        for (uint32_t i = first + warpId; i < last; i += warps)
+            certifySlot<true>(r, c, r.walkKey[i], margin, reach, children, base);
     }
     if (stalled && tid == 0) {
         // A copy may still be landing: wait for it (bounded) before the
@@ -2170,8 +2176,9 @@ static void collectWalk(const Params& P, cudaStream_t s) {
                 attributed |= uint64_t(1) << device;
             }
             k_nodeWalkStaged<<<smCount(), STAGE_THREADS, dynamic, s>>>(P);
+            k_nodeWalkSlow<<<g, 256, 0, s>>>(P, 2u * smCount() * (STAGE_THREADS / 32));
         } else {
-            k_nodeWalkSlow<<<g, 256, 0, s>>>(P);
+            k_nodeWalkSlow<<<g, 256, 0, s>>>(P, 0u);
         }
     } else {
         k_nodeWalk<<<grid(c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
