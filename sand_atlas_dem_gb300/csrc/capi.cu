@@ -414,15 +414,47 @@ int sdg_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* 
 
 int sdg_scan_partials(void) { return 2 * SCAN_BLOCKS; }
 
-// Device-to-device copies of n buffers on `stream`, one cudaMemcpyAsync each
-// (the engine's transactional backup before a chunk and its restore).
+// Device-to-device copies of n buffers on `stream` (the engine's
+// transactional backup before a chunk and its restore): one kernel launch
+// per 64 buffers instead of one copy call each.  Each (buffer, block-row)
+// pair of the grid copies a strided share of its buffer, in 16-byte words
+// where both ends are 16-byte aligned, else byte by byte.
+struct CopyList {
+    uint64_t dst[64], src[64], bytes[64];
+    uint32_t n;
+};
+__global__ void k_copyBuffers(const __grid_constant__ CopyList L) {
+    uint32_t k = blockIdx.y;
+    if (k >= L.n) return;
+    uint64_t bytes = L.bytes[k];
+    char* d = reinterpret_cast<char*>(L.dst[k]);
+    const char* s = reinterpret_cast<const char*>(L.src[k]);
+    uint64_t stride = uint64_t(gridDim.x) * blockDim.x, t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    uint64_t words = ((L.dst[k] | L.src[k]) & 15u) == 0 ? bytes / 16 : 0;
+    for (uint64_t i = t; i < words; i += stride)
+        reinterpret_cast<uint4*>(d)[i] = reinterpret_cast<const uint4*>(s)[i];
+    for (uint64_t i = 16 * words + t; i < bytes; i += stride) d[i] = s[i];
+}
 int sdg_copy_buffers(void* const* dst, void* const* src, const uint64_t* bytes, uint32_t n, void* stream) {
     if (n && (!dst || !src || !bytes)) { g_error = "null copy arguments"; return 1; }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    for (uint32_t k = 0; k < n; ++k) {
-        if (!bytes[k]) continue;
-        if (int rc = record(cudaMemcpyAsync(dst[k], src[k], bytes[k], cudaMemcpyDeviceToDevice, s), "copy"))
-            return rc;
+    for (uint32_t k = 0; k < n;) {
+        CopyList L = {};
+        uint64_t largest = 0;
+        for (; k < n && L.n < 64; ++k) {
+            if (!bytes[k]) continue;
+            if (!dst[k] || !src[k]) { g_error = "null copy arguments"; return 1; }
+            L.dst[L.n] = reinterpret_cast<uint64_t>(dst[k]);
+            L.src[L.n] = reinterpret_cast<uint64_t>(src[k]);
+            L.bytes[L.n] = bytes[k];
+            largest = std::max(largest, bytes[k]);
+            ++L.n;
+        }
+        if (!L.n) continue;
+        // Enough blocks per buffer for the largest one (16 KB each), up to 64.
+        uint32_t rows = uint32_t(std::min<uint64_t>(64, std::max<uint64_t>(1, largest >> 14)));
+        k_copyBuffers<<<dim3(rows, L.n), 256, 0, s>>>(L);
+        if (int rc = record(cudaGetLastError(), "copy")) return rc;
     }
     return 0;
 }

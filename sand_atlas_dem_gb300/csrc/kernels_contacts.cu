@@ -79,7 +79,7 @@ __global__ void k_scanTop(ScanCount count, uint32_t* out, bool writeEnd, uint32_
     }
 }
 __global__ void k_scanApply(const uint32_t* in, uint32_t* out, ScanCount count, const uint32_t* gate,
-                            const uint32_t* partials) {
+                            const uint32_t* partials, uint32_t* list) {
     __shared__ uint32_t shared[32];
     __shared__ uint32_t tileTotal;
     if (gate && *gate == 0) return;
@@ -91,7 +91,10 @@ __global__ void k_scanApply(const uint32_t* in, uint32_t* out, ScanCount count, 
         uint32_t i = base + threadIdx.x;
         uint32_t v = i < end ? in[i] : 0;
         uint32_t inc = blockInclusive(v, shared);
-        if (i < end) out[i] = carry + inc - v;
+        if (i < end) {
+            out[i] = carry + inc - v;
+            if (list && v) list[carry + inc - v] = i;
+        }
         if (threadIdx.x == blockDim.x - 1) tileTotal = inc;
         __syncthreads();
         carry += tileTotal;
@@ -103,7 +106,17 @@ void launch_scan(const uint32_t* in, uint32_t* out, ScanCount count, bool writeE
                  const uint32_t* gate, uint32_t* partials, cudaStream_t s) {
     k_scanReduce<<<SCAN_BLOCKS, 256, 0, s>>>(in, count, gate, partials);
     k_scanTop<<<1, 1024, 0, s>>>(count, out, writeEnd, totalDst, gate, partials, SCAN_BLOCKS);
-    k_scanApply<<<SCAN_BLOCKS, 256, 0, s>>>(in, out, count, gate, partials);
+    k_scanApply<<<SCAN_BLOCKS, 256, 0, s>>>(in, out, count, gate, partials, nullptr);
+}
+
+// The step's scans (r.scanPartials); with `list`, the apply pass also lists
+// each index whose value is nonzero at its scanned offset (stream compaction
+// in index order).
+void launch_step_scan(const Res& r, const uint32_t* in, uint32_t* out, ScanCount count, bool writeEnd,
+                      uint32_t* totalDst, const uint32_t* gate, cudaStream_t s, uint32_t* list = nullptr) {
+    k_scanReduce<<<SCAN_BLOCKS, 256, 0, s>>>(in, count, gate, r.scanPartials);
+    k_scanTop<<<1, 1024, 0, s>>>(count, out, writeEnd, totalDst, gate, r.scanPartials, SCAN_BLOCKS);
+    k_scanApply<<<SCAN_BLOCKS, 256, 0, s>>>(in, out, count, gate, r.scanPartials, list);
 }
 
 // ------------------------------------------------------------ neighbours
@@ -951,15 +964,6 @@ __global__ void __launch_bounds__(256) k_nodeWalkKnown(const __grid_constant__ P
         }
         r.survKeep[t] = known ? 0u : 1u;
     }
-}
-// The flagged slots in slot order (into walkKey, unused between builds).
-__global__ void k_slowList(const __grid_constant__ Params P) {
-    const Res& r = P.r;
-    const Config& c = P.c;
-    if (r.control[0] != 0) return;
-    uint32_t n = min(r.work[W_KEPT], c.survivorCapacity);
-    for (uint32_t t = gtid(); t < n; t += gstride())
-        if (r.survKeep[t]) r.walkKey[r.keepOffset[t]] = t;
 }
 // Dormant slots.  Until the next build, the motion check of k_pairSetup
 // bounds chord_i r_i + |d branch| + chord_j r_j by m s_j (chord: of a
@@ -2076,13 +2080,13 @@ static void neighbours(const Params& P, cudaStream_t s) {
     k_binsFill<<<blocks(c.N, T), T, 0, s>>>(P);
     k_binsSort<<<min(c.binCount, 152u * 16u), 128, 2 * c.binCapacity * sizeof(uint32_t), s>>>(P);
     k_pairsCount<<<blocks(c.N, 128), 128, 0, s>>>(P);
-    launch_scan(r.pairCounts, r.pairOffsets, ScanCount{nullptr, 0, 0, c.N}, false, r.control + 1, r.control + 4,
-                r.scanPartials, s);
+    launch_step_scan(r, r.pairCounts, r.pairOffsets, ScanCount{nullptr, 0, 0, c.N}, false, r.control + 1, r.control + 4,
+                s);
     k_pairsEmit<<<blocks(c.N, 128), 128, 0, s>>>(P);
     k_byJReset<<<blocks(c.N + 1, T), T, 0, s>>>(P);
     k_byJCount<<<PERSISTENT, T, 0, s>>>(P);
-    launch_scan(r.byJCounts, r.byJOffsets, ScanCount{nullptr, 0, 0, c.N}, true, nullptr, r.control + 4,
-                r.scanPartials, s);
+    launch_step_scan(r, r.byJCounts, r.byJOffsets, ScanCount{nullptr, 0, 0, c.N}, true, nullptr, r.control + 4,
+                s);
     k_byJFill<<<PERSISTENT, T, 0, s>>>(P);
     k_byJSort<<<blocks(c.N, T), T, 0, s>>>(P);
 }
@@ -2097,8 +2101,8 @@ static void collectHead(const Params& P, cudaStream_t s) {
     k_pairSetup<<<grid(c.cullBlocksPerSM, 8), T, 0, s>>>(P);
     if (c.meshGeometry == 0) {
         k_sdfCount<<<grid(c.queryBlocksPerSM, 8), T, 0, s>>>(P);
-        launch_scan(r.contactCounts, r.contactOffsets, ScanCount{r.control + 1, c.pairCapacity, 1, 0}, false,
-                    r.control + 2, nullptr, r.scanPartials, s);
+        launch_step_scan(r, r.contactCounts, r.contactOffsets, ScanCount{r.control + 1, c.pairCapacity, 1, 0}, false,
+                    r.control + 2, nullptr, s);
     }
 }
 // Root masks, leaf cull and the (directed pair, leaf) item list: steps that
@@ -2110,8 +2114,8 @@ static void cullBuild(const Params& P, cudaStream_t s) {
     uint32_t T = 256, g = grid(c.cullBlocksPerSM, 8);
     k_pairMasks<<<g, T, 0, s>>>(P);
     k_leafCull<<<g, T, 0, s>>>(P);
-    launch_scan(r.dpairLeafCount, r.dpairCandOffset, ScanCount{r.control + 1, c.pairCapacity, 2, 0}, true,
-                r.work + W_CANDIDATES, r.work + W_FILTER, r.scanPartials, s);
+    launch_step_scan(r, r.dpairLeafCount, r.dpairCandOffset, ScanCount{r.control + 1, c.pairCapacity, 2, 0}, true,
+                r.work + W_CANDIDATES, r.work + W_FILTER, s);
     k_leafEmit<<<g, T, 0, s>>>(P);
 }
 // Pair set-up, leaf cull and the (directed pair, leaf) item list; with the
@@ -2127,8 +2131,8 @@ static void collectFilter(const Params& P, cudaStream_t s) {
     if (c.meshGeometry == 0) return;
     uint32_t warps = c.queryWarps == 4 ? 4 : 8;
     k_nodeFilter<<<grid(c.queryBlocksPerSM, 8), 32 * warps, 0, s>>>(P);
-    launch_scan(r.candSurvCount, r.candSurvOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0},
-                true, r.work + W_SURVIVORS, r.work + W_FILTER, r.scanPartials, s);
+    launch_step_scan(r, r.candSurvCount, r.candSurvOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0},
+                true, r.work + W_SURVIVORS, r.work + W_FILTER, s);
     k_survivorList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
     k_survivorPrefilter<<<grid(c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
     if (c.cullerEnabled) {
@@ -2145,11 +2149,11 @@ static void collectFilter(const Params& P, cudaStream_t s) {
         k_cullSurvivors<<<grid(c.queryBlocksPerSM, 2), 256, 8 * CULLER_TILE_WORDS * sizeof(uint32_t), s>>>(P);
     }
     if (c.filterMargin > 0.0f && c.cullerEnabled == 0)
-        launch_scan(r.walkBucketCount, r.walkBucketOffset, ScanCount{nullptr, 0, 0, c.shapes * WALK_BUCKETS}, true,
-                    r.work + W_KEPT, r.work + W_FILTER, r.scanPartials, s);
+        launch_step_scan(r, r.walkBucketCount, r.walkBucketOffset, ScanCount{nullptr, 0, 0, c.shapes * WALK_BUCKETS}, true,
+                    r.work + W_KEPT, r.work + W_FILTER, s);
     else
-        launch_scan(r.survKeep, r.keepOffset, ScanCount{r.work + W_SURVIVORS, c.survivorCapacity, 1, 0}, true,
-                    r.work + W_KEPT, nullptr, r.scanPartials, s);
+        launch_step_scan(r, r.survKeep, r.keepOffset, ScanCount{r.work + W_SURVIVORS, c.survivorCapacity, 1, 0}, true,
+                    r.work + W_KEPT, nullptr, s);
     k_walkList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
 }
 // The exact queries.
@@ -2161,9 +2165,10 @@ static void collectWalk(const Params& P, cudaStream_t s) {
     } else if (c.filterMargin > 0.0f && c.cullerEnabled == 0) {
         uint32_t g = grid(c.walkBlocksPerSM, 8);
         k_nodeWalkKnown<<<g, 256, 0, s>>>(P);
-        launch_scan(r.survKeep, r.keepOffset, ScanCount{r.work + W_KEPT, c.survivorCapacity, 1, 0}, true,
-                    r.work + W_SLOW, nullptr, r.scanPartials, s);
-        k_slowList<<<g, 256, 0, s>>>(P);
+        // The flags' scan also lists the flagged slots in slot order (the
+        // walk-bucket order) into walkKey.
+        launch_step_scan(r, r.survKeep, r.keepOffset, ScanCount{r.work + W_KEPT, c.survivorCapacity, 1, 0}, true,
+                         r.work + W_SLOW, nullptr, s, r.walkKey);
         if (c.shapes <= STAGE_MAX_SHAPES) {
             size_t dynamic = STAGE_BYTES + 4 * (size_t(c.shapes) + 1);
             // The opt-in shared-memory limit, set once per device.
@@ -2193,8 +2198,8 @@ static void collectEmit(const Params& P, cudaStream_t s) {
     const Res& r = P.r;
     const Config& c = P.c;
     if (c.meshGeometry == 0) return;
-    launch_scan(r.candHitCount, r.candHitOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0}, true,
-                r.control + 2, nullptr, r.scanPartials, s);
+    launch_step_scan(r, r.candHitCount, r.candHitOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0}, true,
+                r.control + 2, nullptr, s);
     uint32_t g = grid(c.contactBlocksPerSM, 8);
     k_nodeEmit<<<g, 256, 0, s>>>(P);
     k_contactStart<<<g, 256, 0, s>>>(P);
@@ -2206,8 +2211,7 @@ static void collectWalls(const Params& P, cudaStream_t s) {
     if (c.wallCount == 0) return;
     uint32_t items = c.N * c.wallCount, g = min(blocks(items, 8), grid(0, 8));
     k_wallCount<<<g, 256, 0, s>>>(P);
-    launch_scan(r.wallCounts, r.wallOffsets, ScanCount{nullptr, 0, 0, items}, true, nullptr, nullptr, r.scanPartials,
-                s);
+    launch_step_scan(r, r.wallCounts, r.wallOffsets, ScanCount{nullptr, 0, 0, items}, true, nullptr, nullptr, s);
     k_wallEmit<<<g, 256, 0, s>>>(P);
 }
 static void contacts(const Params& P, cudaStream_t s) {
