@@ -533,7 +533,7 @@ def run_gb300(args, cpu=True):
     }
     if not args.no_plain and not e.sdf:  # the SDF geometry has no filters to compare
         line["plain_gpu_path"] = plain_comparison(w, args, flush)
-    if args.culler:
+    if not args.no_culler and not e.sdf:
         line["learned_culler"] = culler_comparison(w, args, flush)
     if "run_steps" in w.config and cpu and not args.no_cpu_baseline:
         line["full_run"] = full_run(w, args)
@@ -665,6 +665,7 @@ def culler_comparison(w, args, flush):
                          node_query_ms=phases["node_filter"] + phases["node_query"],
                          tested=int(stats[0]), culled=int(stats[1]), state=e.state())
     result = dict(steps=steps, training_s=round(train_s, 1), margins_mean=float(np.mean(c.margins)),
+                  cell_margins_mean=float(np.mean(c.cell_margins)), loss_over_weight=c.over,
                   validation_cull_rate=c.cull_rate())
     for grid in ("", "_no_grid"):
         p, q = out["plain" + grid], out["culled" + grid]
@@ -753,7 +754,9 @@ def main():
     p.add_argument("--cpu-threads", type=int, default=os.cpu_count() or 1)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--prepare-only", action="store_true")
-    p.add_argument("--culler", action="store_true", help="also train the learned culler and compare")
+    p.add_argument("--no-culler", action="store_true",
+                   help="skip the learned-culler comparison (training the per-shape networks and timing the "
+                        "culled steps)")
     p.add_argument("--no-graph", action="store_true",
                    help="launch each step's kernels one by one instead of replaying the captured graph "
                         "(for per-kernel profilers, which do not list the kernels of conditional graph nodes; "

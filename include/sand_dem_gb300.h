@@ -206,10 +206,12 @@ int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes
  * trained on exact signed distances.  sdg_culler_param_count() floats per
  * shape.  sample: shell candidates labelled by the exact BVH distance;
  * compact: keep accepted candidates in index order; train_step: one Adam
- * step on every shape (forward/backward kernels); gradients: forward and
- * backward only; round: BF16 hidden weights for inference; eval: FP32
+ * step on every shape (forward/backward kernels; squared error with an
+ * over-prediction at an inside point weighted by `over`); gradients: forward
+ * and backward only; round: BF16 hidden weights for inference; eval: FP32
  * evaluation with BF16 hidden weights; tile_eval: the run-time tensor-core
- * evaluation; inside_max: per-shape largest prediction at inside points
+ * evaluation (tcgen05, 128-point tiles; NaN where a tensor-core wait gave
+ * up); inside_max: per-shape largest prediction at inside points
  * (the calibrated margin, as an ordered integer); surface: points on each
  * shape's surface (shape s owns packed triangles [tri_start[s],
  * tri_start[s+1])), label 0, for the margin's boundary term.
@@ -223,11 +225,11 @@ int sdg_culler_surface(const void* triangles, const void* tri_start, uint32_t sh
 int sdg_culler_compact(const void* points, const void* accept, const void* offsets, uint32_t shapes,
                        uint32_t count, uint32_t capacity, void* out, void* stream);
 int sdg_culler_train_step(void* params, const void* points, uint32_t shapes, uint32_t points_per_shape,
-                          uint32_t batch, uint32_t step, uint32_t seed, float scale, float lr, void* grads,
-                          void* m, void* v, void* scratch, float* loss_out, void* stream);
+                          uint32_t batch, uint32_t step, uint32_t seed, float scale, float over, float lr,
+                          void* grads, void* m, void* v, void* scratch, float* loss_out, void* stream);
 int sdg_culler_gradients(const void* params, const void* points, uint32_t shapes, uint32_t points_per_shape,
-                         uint32_t batch, uint32_t step, uint32_t seed, float scale, void* grads, void* scratch,
-                         void* stream);
+                         uint32_t batch, uint32_t step, uint32_t seed, float scale, float over, void* grads,
+                         void* scratch, void* stream);
 int sdg_culler_round(const void* params, void* w1_bf16, uint32_t shapes, void* stream);
 int sdg_culler_eval(const void* params, const void* w1_bf16, const void* points, uint32_t shapes, uint32_t count,
                     void* out, void* stream);
@@ -235,6 +237,14 @@ int sdg_culler_tile_eval(const void* params, const void* w1_bf16, const void* po
                          uint32_t count, void* out, void* stream);
 int sdg_culler_inside_max(const void* points, const void* predictions, uint32_t shapes, uint32_t count,
                           void* keys, void* stream);
+/* Cells per shape of the culler's margin grid (8^3 over the shape's root
+ * box); the engine's cullerMargin buffer holds per shape the whole-shape
+ * margin then one margin per cell.  inside_max_cells: per (shape, cell) the
+ * ordered-integer maximum prediction at inside points and their count. */
+int sdg_culler_margin_cells(void);
+int sdg_culler_inside_max_cells(const void* points, const void* predictions, uint32_t shapes, uint32_t count,
+                                const void* roots, const void* mesh_min, const void* mesh_max, void* keys,
+                                void* counts, void* stream);
 
 /*
  * Kernel launches of a captured step that skips both conditional bodies (0

@@ -2,7 +2,8 @@
 
 float64 numpy forward and backward of the per-shape network the GPU trains
 (``sand_atlas_dem_gb300/csrc/culler.cu``): h0 = sin(W0 p + b0),
-h1 = relu(W1 h0 + b1), y = w2 . h1 + b2, loss = mean((y - phi/scale)^2).
+h1 = relu(W1 h0 + b1), y = w2 . h1 + b2, loss = mean(w (y - phi/scale)^2)
+with w = ``over`` where the target is inside (phi <= 0) and y exceeds it, else 1.
 Used to check the GPU gradients (there is no reference counterpart).
 """
 
@@ -12,7 +13,7 @@ H = 64
 W0, B0, W1, B1, W2, B2 = 0, 192, 256, 256 + 4096, 256 + 4096 + 64, 256 + 4096 + 128
 
 
-def forward_backward(params, points, scale):
+def forward_backward(params, points, scale, over=1.0):
     """Loss and gradient (same flat layout as ``params``) for one batch."""
     p = np.asarray(params, np.float64)
     x = np.asarray(points[:, :3], np.float64)
@@ -30,8 +31,9 @@ def forward_backward(params, points, scale):
     y = h1 @ w2 + b2
     n = len(x)
     err = y - t
-    loss = np.mean(err**2)
-    dy = 2 * err / n
+    weight = np.where((t <= 0) & (err > 0), over, 1.0)
+    loss = np.mean(weight * err**2)
+    dy = 2 * weight * err / n
     grad = np.zeros_like(p)
     grad[W2:B2] = dy @ h1
     grad[B2] = dy.sum()

@@ -14,6 +14,7 @@
 // the exact query.
 //
 // All kernels are batched over shapes (blockIdx.y = shape).
+#include <algorithm>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include "culler.cuh"
@@ -96,6 +97,7 @@ struct TrainArgs {
     const float4* points;      // shapes x pointsPerShape (x, y, z, phi)
     uint32_t pointsPerShape, batch, step, seed;
     float scale;               // target = phi / scale
+    float over;                // weight of an over-prediction inside the shape (target <= 0)
     float* dA1;                // shapes x batch x H   (dL/da1)
     float* H0;                 // shapes x batch x H
     float* dZ0;                // shapes x batch x H   (dL/dz0)
@@ -138,8 +140,12 @@ __global__ void __launch_bounds__(128) k_trainPoints(TrainArgs a) {
     }
     float t = q.w / a.scale;
     float err = y - t;
-    a.loss[row] = err * err;
-    float dy = 2.f * err / float(a.batch);
+    // Asymmetric squared error: an over-prediction at a point inside the
+    // shape weighs `over` times as much (the calibrated margin is the largest
+    // prediction inside, so it is what pushes the margin up).
+    float weight = (t <= 0.f && err > 0.f) ? a.over : 1.f;
+    a.loss[row] = weight * err * err;
+    float dy = 2.f * weight * err / float(a.batch);
     a.dY[row] = dy;
     float dz[H];
     for (int k = 0; k < H; ++k) dz[k] = 0.f;
@@ -239,26 +245,24 @@ __global__ void k_roundWeights(const float* params, __nv_bfloat16* w1, uint32_t 
     w1[k] = __float2bfloat16(params[size_t(s) * Net::SIZE + Net::W1 + e]);
 }
 
-// The run-time culling function (tensor-core tile) on stored points: warp
-// per 64 points of shape blockIdx.y.
-__global__ void __launch_bounds__(256) k_cullerTileEval(const float* params, const uint32_t* w1, const float4* points,
-                                                         uint32_t count, float* out) {
-    __shared__ uint32_t tiles[8 * CULLER_TILE_WORDS];
-    uint32_t s = blockIdx.y, lane = threadIdx.x & 31u;
-    uint32_t* tile = tiles + (threadIdx.x >> 5) * CULLER_TILE_WORDS;
-    const float* p = params + size_t(s) * CULLER_PARAMS;
-    const uint32_t* w = w1 + size_t(s) * 2048;
-    uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t group = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); group * 64 < count; group += warps) {
-        uint32_t a = group * 64 + lane, b = a + 32;
-        float4 qa = a < count ? points[size_t(s) * count + a] : make_float4(0.f, 0.f, 0.f, 0.f);
-        float4 qb = b < count ? points[size_t(s) * count + b] : make_float4(0.f, 0.f, 0.f, 0.f);
-        float ya, yb;
-        cullerTile(p, w, xyz(qa), xyz(qb), tile, ya, yb);
-        if (a < count) out[size_t(s) * count + a] = ya;
-        if (b < count) out[size_t(s) * count + b] = yb;
-        __syncwarp();
+// The run-time culling function (tensor-core tile, culler.cuh) on stored
+// points: shape s owns points [s count, (s + 1) count); tiles of 128 rows of
+// that shape-sorted list, one CTA of 128 threads per tile in turn.  A tile
+// whose tensor-core wait gave up writes NaN predictions.
+__global__ void __launch_bounds__(128) k_cullerPredict(const float* params, const uint32_t* w1, const float4* points,
+                                                        uint32_t shapes, uint32_t count, float* out) {
+    __shared__ CullerShared sh;
+    cullerBegin(sh);
+    uint32_t phase = 0, total = shapes * count, tiles = (total + CULLER_ROWS - 1) / CULLER_ROWS;
+    for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        uint32_t i = t * CULLER_ROWS + threadIdx.x;
+        float4 q = i < total ? points[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float y;
+        bool ok = cullerTile(sh, params, w1, i < total ? i / count : EMPTY, xyz(q), phase, y);
+        if (i < total) out[i] = ok ? y : __int_as_float(0x7fc00000);
+        if (!ok) break;
     }
+    cullerEnd(sh, phase);
 }
 __device__ __forceinline__ uint32_t orderedKey(float f) {
     uint32_t b = __float_as_uint(f);
@@ -277,22 +281,61 @@ __global__ void k_insideMax(const float4* points, const float* y, uint32_t count
     if ((threadIdx.x & 31u) == 0 && best) atomicMax(&keys[s], best);
 }
 
+// Per (shape, cell of the 8^3 grid over the shape's root box): the largest
+// prediction over points with phi <= 0, and how many there were.
+__global__ void k_insideMaxCells(const float4* points, const float* y, uint32_t count, const uint4* roots,
+                                 const float4* meshMin, const float4* meshMax, uint32_t* keys, uint32_t* counts) {
+    uint32_t s = blockIdx.y;
+    uint32_t root = roots[s].x;
+    float4 low = meshMin[root], high = meshMax[root];
+    const uint32_t cells = CULLER_MARGINS - 1;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        size_t at = size_t(s) * count + k;
+        float4 q = points[at];
+        if (q.w > 0.0f) continue;
+        uint32_t cell = cullerCell(low, high, xyz(q));
+        atomicMax(&keys[s * cells + cell], orderedKey(y[at]));
+        atomicAdd(&counts[s * cells + cell], 1u);
+    }
+}
+
 }  // namespace sdg
 
 using namespace sdg;
 
 extern "C" {
 
+int sdg_culler_margin_cells(void) { return CULLER_MARGINS - 1; }
+
+// Per (shape, cell): ordered-integer maximum of the predictions at inside
+// points and their count (keys and counts zeroed first, shapes x
+// sdg_culler_margin_cells() words each); roots, mesh_min, mesh_max: the
+// packed library's meshRoots, meshMin, meshMax.
+int sdg_culler_inside_max_cells(const void* points, const void* predictions, uint32_t shapes, uint32_t count,
+                                const void* roots, const void* mesh_min, const void* mesh_max, void* keys,
+                                void* counts, void* stream) {
+    dim3 grid((count + 255) / 256 < 256 ? (count + 255) / 256 : 256, shapes);
+    k_insideMaxCells<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float4*>(points), static_cast<const float*>(predictions), count,
+        static_cast<const uint4*>(roots), static_cast<const float4*>(mesh_min), static_cast<const float4*>(mesh_max),
+        static_cast<uint32_t*>(keys), static_cast<uint32_t*>(counts));
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
 int sdg_culler_param_count(void) { return Net::SIZE; }
 
 // Run-time culling predictions for stored points (shapes x count).
 int sdg_culler_tile_eval(const void* params, const void* w1_bf16, const void* points, uint32_t shapes,
                          uint32_t count, void* out, void* stream) {
-    uint32_t groups = (count + 63) / 64;
-    dim3 grid((groups + 7) / 8 < 1024 ? (groups + 7) / 8 : 1024, shapes);
-    k_cullerTileEval<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        static_cast<const float*>(params), static_cast<const uint32_t*>(w1_bf16), static_cast<const float4*>(points),
-        count, static_cast<float*>(out));
+    uint32_t tiles = (shapes * count + CULLER_ROWS - 1) / CULLER_ROWS;
+    int device = 0, sms = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    uint32_t grid = std::max(1u, std::min(tiles, 2u * uint32_t(sms)));
+    if (tiles)
+        k_cullerPredict<<<grid, CULLER_ROWS, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const float*>(params), static_cast<const uint32_t*>(w1_bf16),
+            static_cast<const float4*>(points), shapes, count, static_cast<float*>(out));
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
@@ -341,13 +384,13 @@ int sdg_culler_compact(const void* points, const void* accept, const void* offse
 // `scratch` holds 4*batch*64 + 3*batch floats per shape; `grads`, `m`, `v`
 // are shapes*param_count floats.
 int sdg_culler_train_step(void* params, const void* points, uint32_t shapes, uint32_t points_per_shape,
-                          uint32_t batch, uint32_t step, uint32_t seed, float scale, float lr, void* grads,
-                          void* m, void* v, void* scratch, float* loss_out, void* stream) {
+                          uint32_t batch, uint32_t step, uint32_t seed, float scale, float over, float lr,
+                          void* grads, void* m, void* v, void* scratch, float* loss_out, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     float* f = static_cast<float*>(scratch);
     size_t rows = size_t(shapes) * batch;
     TrainArgs a{static_cast<const float*>(params), static_cast<const float4*>(points), points_per_shape, batch,
-                step, seed, scale, f, f + rows * H, f + 2 * rows * H, f + 4 * rows * H, f + 3 * rows * H,
+                step, seed, scale, over, f, f + rows * H, f + 2 * rows * H, f + 4 * rows * H, f + 3 * rows * H,
                 f + 4 * rows * H + rows, reinterpret_cast<uint32_t*>(f + 4 * rows * H + 2 * rows)};
     k_trainPoints<<<dim3((batch + 127) / 128, shapes), 128, 0, s>>>(a);
     k_trainGrads<<<dim3((Net::SIZE + 127) / 128, shapes), 128, 0, s>>>(a, static_cast<float*>(grads));
@@ -361,13 +404,13 @@ int sdg_culler_train_step(void* params, const void* points, uint32_t shapes, uin
 // Forward and backward only (no update): per-parameter gradients of the mean
 // squared error for the batch of `step` (the gradient check entry).
 int sdg_culler_gradients(const void* params, const void* points, uint32_t shapes, uint32_t points_per_shape,
-                         uint32_t batch, uint32_t step, uint32_t seed, float scale, void* grads, void* scratch,
-                         void* stream) {
+                         uint32_t batch, uint32_t step, uint32_t seed, float scale, float over, void* grads,
+                         void* scratch, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     float* f = static_cast<float*>(scratch);
     size_t rows = size_t(shapes) * batch;
     TrainArgs a{static_cast<const float*>(params), static_cast<const float4*>(points), points_per_shape, batch,
-                step, seed, scale, f, f + rows * H, f + 2 * rows * H, f + 4 * rows * H, f + 3 * rows * H,
+                step, seed, scale, over, f, f + rows * H, f + 2 * rows * H, f + 4 * rows * H, f + 3 * rows * H,
                 f + 4 * rows * H + rows, reinterpret_cast<uint32_t*>(f + 4 * rows * H + 2 * rows)};
     k_trainPoints<<<dim3((batch + 127) / 128, shapes), 128, 0, s>>>(a);
     k_trainGrads<<<dim3((Net::SIZE + 127) / 128, shapes), 128, 0, s>>>(a, static_cast<float*>(grads));

@@ -117,7 +117,7 @@ struct Res {
     const uint4* specimenBins;        // specimens: bin grid x, y, z and first bin
     const float* cullerParams;        // shapes x CULLER_PARAMS: FP32 network parameters
     const uint32_t* cullerW1;         // shapes x 64 x 64 BF16 hidden weights (packed in pairs)
-    const float* cullerMargin;        // shapes: skip a node when the prediction exceeds this
+    const float* cullerMargin;        // shapes x (1 + 8^3): skip a node when the prediction exceeds its cell's
     uint32_t* cullerStats;            // 2 counters: nodes evaluated, nodes culled
     uint2* candSurvMask;              // candidateCapacity: 64-bit mask of the item's surviving nodes
     uint32_t* candSurvOffset;         // candidateCapacity+1: first survivor of each item
@@ -175,6 +175,7 @@ constexpr int W_CERTIFIED = 15;     // exact queries answered by a certificate (
 constexpr int W_WALL_BASE = 16;     // first plane contact: the grain-grain contact total
 constexpr int W_REBUILDS = 17;      // steps that rebuilt the neighbour list (counter)
 constexpr int W_DORMANT = 18;       // dormant slots in the stored exact-query list
+constexpr int W_CULL_ROWS = 19;     // kept survivors in the culler's shape-sorted list
 
 struct Params {
     Config c;

@@ -768,47 +768,94 @@ __global__ void k_distanceGrid(const __grid_constant__ Params P) {
         r.distanceGrid[t] = __fsub_rn(__fsub_rn(phi, reach), slack);
     }
 }
-// Learned culler over the survivor list: 64 survivors per warp iteration
-// (two per lane), one tensor-core tile per distinct target shape among them.
-// Clears keep[s] when the target's network places a kept survivor s beyond
-// the shape's calibrated margin; the exact query decides every other one.
-__global__ void __launch_bounds__(256) k_cullSurvivors(const __grid_constant__ Params P) {
-    extern __shared__ uint32_t cullTiles[];
+// Learned culler over the kept survivors, on the tensor cores (culler.cuh).
+// The survivors are first sorted by target shape (a counting sort into
+// walkKey: per-shape counts, their scan, then placement -- the walk-bucket
+// arrays and walkKey serve the stored exact-query list only, which the
+// culler does not use), so that a 128-row tile holds one shape, or a few at
+// its ends.  The culler clears keep[s] when the target's network places a
+// kept survivor s beyond the shape's calibrated margin; the exact query
+// decides every other one.  The order of the sorted list within a shape is
+// immaterial: each row's prediction depends on its own point only.
+__device__ __forceinline__ uint32_t survivorTargetShape(const Res& r, const Config& c, uint32_t s) {
+    uint2 sv = r.survivors[s];
+    uint32_t d = r.candidates[sv.x].x;
+    uint2 ij = r.pairs[d >> 1];
+    uint32_t shape = r.shapeId[(d & 1) ? ij.x : ij.y];
+    return shape < c.shapes ? shape : EMPTY;
+}
+// Per-shape counts of the kept survivors (walkBucketCount[shape]; zero on
+// entry: the placement below takes each back to zero).
+__global__ void k_cullCount(const __grid_constant__ Params P) {
     const Res& r = P.r;
     const Config& c = P.c;
-    uint32_t* tile = cullTiles + (threadIdx.x >> 5) * CULLER_TILE_WORDS;
     uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
-    if (r.control[0] != 0) n = 0;
-    uint32_t groups = (n + 63) / 64;
-    for (uint32_t g = warpGlobal(); g < groups; g += warpStride()) {
-        uint32_t s0 = 64 * g + laneId(), s1 = s0 + WARP;
-        bool valid0 = s0 < n && r.survKeep[s0], valid1 = s1 < n && r.survKeep[s1];
-        f3 l0 = mk(0.f, 0.f, 0.f), l1 = l0;
-        uint32_t t0 = EMPTY, t1 = EMPTY;
-        if (valid0) { SurvivorNode v = survivorNode(r, s0); l0 = v.local; t0 = r.shapeId[v.dst]; }
-        if (valid1) { SurvivorNode v = survivorNode(r, s1); l1 = v.local; t1 = r.shapeId[v.dst]; }
-        bool pending0 = valid0, pending1 = valid1, cut0 = false, cut1 = false;
-        for (;;) {
-            uint32_t b0 = __ballot_sync(0xffffffffu, pending0), b1 = __ballot_sync(0xffffffffu, pending1);
-            if ((b0 | b1) == 0) break;
-            uint32_t target = b0 ? __shfl_sync(0xffffffffu, t0, __ffs(b0) - 1)
-                                 : __shfl_sync(0xffffffffu, t1, __ffs(b1) - 1);
-            bool in0 = pending0 && t0 == target, in1 = pending1 && t1 == target;
-            float y0, y1;
-            cullerTile(r.cullerParams + size_t(target) * CULLER_PARAMS, r.cullerW1 + size_t(target) * 2048,
-                       in0 ? l0 : mk(0.f, 0.f, 0.f), in1 ? l1 : mk(0.f, 0.f, 0.f), tile, y0, y1);
-            float margin = r.cullerMargin[target];
-            if (in0) { cut0 = y0 > margin; pending0 = false; }
-            if (in1) { cut1 = y1 > margin; pending1 = false; }
+    for (uint32_t s = gtid(); s < n; s += gstride()) {
+        uint32_t shape = r.survKeep[s] ? survivorTargetShape(r, c, s) : EMPTY;
+        uint32_t same = __match_any_sync(__activemask(), shape);
+        if (shape != EMPTY && laneId() == uint32_t(__ffs(same) - 1)) atomicAdd(&r.walkBucketCount[shape], __popc(same));
+    }
+}
+// Placement in shape order (walkKey); each count returns to zero.
+__global__ void k_cullPlace(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t n = min(r.work[W_SURVIVORS], c.survivorCapacity);
+    for (uint32_t s = gtid(); s < n; s += gstride()) {
+        uint32_t shape = r.survKeep[s] ? survivorTargetShape(r, c, s) : EMPTY;
+        uint32_t same = __match_any_sync(__activemask(), shape);
+        uint32_t leader = __ffs(same) - 1, base = 0;
+        if (shape != EMPTY && laneId() == leader) base = atomicSub(&r.walkBucketCount[shape], __popc(same));
+        base = __shfl_sync(same, base, leader);
+        if (shape != EMPTY) {
+            uint32_t rank = __popc(same & lanesBelow());
+            r.walkKey[r.walkBucketOffset[shape] + base - 1 - rank] = s;
         }
-        if (cut0) r.survKeep[s0] = 0u;
-        if (cut1) r.survKeep[s1] = 0u;
-        uint32_t tested = __popc(__ballot_sync(0xffffffffu, valid0)) + __popc(__ballot_sync(0xffffffffu, valid1));
-        uint32_t culled = __popc(__ballot_sync(0xffffffffu, cut0)) + __popc(__ballot_sync(0xffffffffu, cut1));
-        if (laneId() == 0) {
-            atomicAdd(&r.cullerStats[0], tested);
-            atomicAdd(&r.cullerStats[1], culled);
+    }
+}
+__global__ void __launch_bounds__(CULLER_ROWS) k_cullSurvivors(const __grid_constant__ Params P) {
+    __shared__ CullerShared sh;
+    __shared__ uint32_t live, tested, culled;
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (threadIdx.x == 0) {
+        live = r.control[0] == 0;
+        tested = culled = 0;
+    }
+    cullerBegin(sh);  // synchronizes
+    uint32_t phase = 0;
+    uint32_t n = live ? min(r.work[W_CULL_ROWS], c.survivorCapacity) : 0u;
+    uint32_t tiles = (n + CULLER_ROWS - 1) / CULLER_ROWS;
+    for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        uint32_t i = t * CULLER_ROWS + threadIdx.x, s = EMPTY, shape = EMPTY;
+        f3 local = mk(0.f, 0.f, 0.f);
+        float margin = 0.0f;
+        if (i < n) {
+            s = r.walkKey[i];
+            SurvivorNode v = survivorNode(r, s);
+            local = v.local;
+            shape = r.shapeId[v.dst];
+            uint32_t root = __ldg(&r.meshRoots[shape].x);
+            margin = r.cullerMargin[size_t(shape) * CULLER_MARGINS + 1 +
+                                    cullerCell(__ldg(&r.meshMin[root]), __ldg(&r.meshMax[root]), local)];
         }
+        float y;
+        if (!cullerTile(sh, r.cullerParams, r.cullerW1, shape, local, phase, y)) {
+            if (threadIdx.x == 0) fail(r, F_WAIT);
+            break;
+        }
+        if (shape != EMPTY) {
+            atomicAdd(&tested, 1u);
+            if (y > margin) {
+                r.survKeep[s] = 0u;
+                atomicAdd(&culled, 1u);
+            }
+        }
+    }
+    cullerEnd(sh, phase);  // synchronizes
+    if (threadIdx.x == 0 && tested) {
+        atomicAdd(&r.cullerStats[0], tested);
+        atomicAdd(&r.cullerStats[1], culled);
     }
 }
 // Survivors kept for the exact query (their survivor indices): in survivor
@@ -2136,17 +2183,12 @@ static void collectFilter(const Params& P, cudaStream_t s) {
     k_survivorList<<<grid(c.contactBlocksPerSM, 8), 256, 0, s>>>(P);
     k_survivorPrefilter<<<grid(c.walkBlocksPerSM, 8), 256, 0, s>>>(P);
     if (c.cullerEnabled) {
-        // The 73.7 KB tile area needs the opt-in shared-memory limit, set
-        // once per device (the attribute is per device and function).
-        static uint64_t attributed = 0;
-        int device = 0;
-        cudaGetDevice(&device);
-        if (device < 64 && !((attributed >> device) & 1u)) {
-            cudaFuncSetAttribute(k_cullSurvivors, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 int(8 * CULLER_TILE_WORDS * sizeof(uint32_t)));
-            attributed |= uint64_t(1) << device;
-        }
-        k_cullSurvivors<<<grid(c.queryBlocksPerSM, 2), 256, 8 * CULLER_TILE_WORDS * sizeof(uint32_t), s>>>(P);
+        uint32_t g = grid(c.contactBlocksPerSM, 8);
+        k_cullCount<<<g, 256, 0, s>>>(P);
+        launch_step_scan(r, r.walkBucketCount, r.walkBucketOffset, ScanCount{nullptr, 0, 0, c.shapes}, true,
+                         r.work + W_CULL_ROWS, nullptr, s);
+        k_cullPlace<<<g, 256, 0, s>>>(P);
+        k_cullSurvivors<<<grid(0, 4), CULLER_ROWS, 0, s>>>(P);  // 4 x 64 TMEM columns per SM
     }
     if (c.filterMargin > 0.0f && c.cullerEnabled == 0)
         launch_step_scan(r, r.walkBucketCount, r.walkBucketOffset, ScanCount{nullptr, 0, 0, c.shapes * WALK_BUCKETS}, true,

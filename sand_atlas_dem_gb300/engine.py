@@ -51,6 +51,7 @@ EXTENSION_ORDER = (
 DISTANCE_GRID = 48  # cells per axis of each shape's distance-bound grid (csrc GRID)
 WALK_BUCKETS = 24**3  # walk-order buckets per shape (csrc WALK_BUCKETS)
 CULLER_PARAMS = 3 * 64 + 64 + 64 * 64 + 64 + 64 + 4
+CULLER_MARGINS = 1 + 8**3  # per shape: whole-shape margin, then one per cell (csrc CULLER_MARGINS)
 BUFFER_ORDER = RESOURCE_ORDER + EXTENSION_ORDER
 # History side fields: (name bound as the side being written, name bound as committed).
 SIDE_FIELDS = (
@@ -302,7 +303,7 @@ class Engine:
             "distanceGrid": 4 * len(library.shapes) * DISTANCE_GRID**3, "distanceGridInfo": 16 * len(library.shapes),
             "distanceGridTriangle": 4 * len(library.shapes) * DISTANCE_GRID**3,
             "cullerParams": 4 * CULLER_PARAMS * len(library.shapes), "cullerW1": 2 * 4096 * len(library.shapes),
-            "cullerMargin": 4 * len(library.shapes), "cullerStats": 16,
+            "cullerMargin": 4 * CULLER_MARGINS * len(library.shapes), "cullerStats": 16,
             "filterRefRotation": 16 * n, "filterRefBranch": 16 * pc, "filterRefPairs": 8 * pc,
             "walkKey": 4 * self.survivor_capacity, "walkBucketCount": 4 * (len(library.shapes) * WALK_BUCKETS + 1),
             "walkBucketOffset": 4 * (len(library.shapes) * WALK_BUCKETS + 1),

@@ -102,15 +102,17 @@ def load():
     F = ct.c_float
     culler = {
         "sdg_culler_param_count": [],
+        "sdg_culler_margin_cells": [],
         "sdg_culler_sample": [P(V), P(ct.c_uint64), P(ct.c_double), U, U, U, U, F, U, V, V, V],
         "sdg_culler_compact": [V, V, V, U, U, U, V, V],
         "sdg_culler_surface": [V, V, U, U, U, V, V],
-        "sdg_culler_train_step": [V, V, U, U, U, U, U, F, F, V, V, V, V, V, V],
-        "sdg_culler_gradients": [V, V, U, U, U, U, U, F, V, V, V],
+        "sdg_culler_train_step": [V, V, U, U, U, U, U, F, F, F, V, V, V, V, V, V],
+        "sdg_culler_gradients": [V, V, U, U, U, U, U, F, F, V, V, V],
         "sdg_culler_round": [V, V, U, V],
         "sdg_culler_eval": [V, V, V, U, U, V, V],
         "sdg_culler_tile_eval": [V, V, V, U, U, V, V],
         "sdg_culler_inside_max": [V, V, U, U, V, V],
+        "sdg_culler_inside_max_cells": [V, V, U, U, V, V, V, V, V, V],
     }
     for name, args in culler.items():
         fn = getattr(lib, name)
@@ -157,6 +159,8 @@ EXPORTS = (
     "sdg_culler_eval",
     "sdg_culler_tile_eval",
     "sdg_culler_inside_max",
+    "sdg_culler_inside_max_cells",
+    "sdg_culler_margin_cells",
 )
 PHASES = ("drift", "neighbours", "pair_cull", "node_filter", "node_query", "contact_emit", "friction_and_history",
           "force_reduction", "final_kick")

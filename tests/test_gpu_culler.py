@@ -35,9 +35,31 @@ def test_gradients_match_cpu_oracle(gpu_library):
     params = c.params.cpu().numpy()
     pts = c.training_points.cpu().numpy().reshape(c.shapes, c.points, 4)
     for s in range(c.shapes):
-        loss, ref = forward_backward(params[s], pts[s][index[s]], c.shell)
+        loss, ref = forward_backward(params[s], pts[s][index[s]], c.shell, c.over)
         scale = np.abs(ref).max()
         np.testing.assert_allclose(grads[s], ref, rtol=2e-3, atol=2e-4 * scale)
+
+
+def test_tensor_core_tile_matches_fp32_rows(gpu_library):
+    """The tcgen05 tile (BF16 x BF16 -> FP32 in tensor memory, 128 rows a
+    tile, several shapes per tile) against the same network evaluated row by
+    row on CUDA cores with the same BF16 features and weights: only the
+    order of the FP32 accumulation differs (tolerance 1e-5 of the output
+    range)."""
+    library, spec, case = lattice_case(side=4)
+    e = build(Engine, library, spec, case)
+    c = small_culler(e, steps=50)
+    c.train()
+    import ctypes as ct
+    from sand_atlas_dem_gb300 import native
+    native.check(c.lib.sdg_culler_round(ct.c_void_p(c.params.data_ptr()), ct.c_void_p(c.w1.data_ptr()), c.shapes,
+                                        ct.c_void_p(c.stream.cuda_stream)))
+    # 1000 points a shape: tiles straddle shape boundaries.
+    pts = c.sample(1000, 99)
+    tile = c.predict(pts).cpu().numpy()
+    rows = c.evaluate(pts).cpu().numpy()
+    scale = np.abs(rows).max()
+    np.testing.assert_allclose(tile, rows, rtol=0, atol=1e-5 * scale)
 
 
 def test_training_reduces_loss_and_margin_covers_inside(gpu_library):
@@ -52,6 +74,12 @@ def test_training_reduces_loss_and_margin_covers_inside(gpu_library):
     y = pred.cpu().numpy().reshape(c.shapes, -1)
     inside = phi <= 0
     assert np.all(y[inside] <= np.repeat(margins[:, None], y.shape[1], axis=1)[inside])
+    # Each cell's margin covers the inside calibration points of the cell
+    # and never exceeds the whole shape's.
+    cells = c._cells(pts).view(c.shapes, -1).cpu().numpy()
+    cell_margin = np.take_along_axis(c.cell_margins, cells, axis=1)
+    assert np.all(y[inside] <= cell_margin[inside])
+    assert np.all(c.cell_margins <= margins[:, None])
     assert c.cull_rate() > 0.1
 
 
