@@ -191,6 +191,144 @@ __global__ void k_binsSort(const __grid_constant__ Params P) {
         __syncthreads();
     }
 }
+// ---- radix-sorted cell list (solver.slang:345-359 fills the bins serially,
+// in grain order; a stable sort of the grains by bin gives the same slots).
+// Keys are the flat bin indices (a grain that fails the checks gets
+// binCount, past every bin); an LSD radix sort of 8-bit digits (stable:
+// each pass keeps the order of equal digits) orders (bin, grain) pairs, and
+// each bin's run is then copied into the reference's fixed-capacity slots.
+// The scratch lives in byJPairs (pair ids by second grain), which the
+// neighbour build rewrites only after the pairs exist: keys and grains twice
+// (ping-pong) and the per-(digit, tile) counts.
+constexpr uint32_t RADIX = 256, RADIX_ITEMS = 8, RADIX_TILE = 256 * RADIX_ITEMS;
+struct RadixScratch {
+    uint32_t *keys[2], *vals[2], *counts;
+    uint32_t tiles;
+};
+__host__ __device__ __forceinline__ uint32_t radixTiles(uint32_t n) { return (n + RADIX_TILE - 1) / RADIX_TILE; }
+// Words of byJPairs the sort needs (the radix path runs only where they fit).
+__host__ __device__ __forceinline__ uint64_t radixWords(uint32_t n) {
+    return 4ull * n + uint64_t(RADIX) * radixTiles(n) + 1;
+}
+__host__ __device__ __forceinline__ RadixScratch radixScratch(const Res& r, const Config& c) {
+    uint32_t* base = r.byJPairs;
+    RadixScratch x;
+    x.keys[0] = base;
+    x.vals[0] = base + c.N;
+    x.keys[1] = base + 2 * size_t(c.N);
+    x.vals[1] = base + 3 * size_t(c.N);
+    x.counts = base + 4 * size_t(c.N);
+    x.tiles = radixTiles(c.N);
+    return x;
+}
+// Keys: the same checks and bin as k_binsFill.
+__global__ void k_binKeys(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t id = gtid();
+    if (id >= c.N || r.control[4] == 0) return;
+    RadixScratch x = radixScratch(r, c);
+    uint32_t key = c.binCount;
+    f3 p = xyz(r.position[id]), pl = xyz(r.positionRemainder[id]);
+    uint32_t sp = specimenOf(r, id);
+    float4 cell = r.cell[3 * sp];
+    bool ok = finite3(p) && finite3(pl);
+    if (!ok) fail(r, F_NONFINITE);
+    if (ok && c.periodic == 0) {
+        f3 box = xyz(cell);
+        if (__fadd_rn(p.x, pl.x) < 0 || __fadd_rn(p.y, pl.y) < 0 || __fadd_rn(p.z, pl.z) < 0 ||
+            __fadd_rn(__fsub_rn(p.x, box.x), pl.x) >= 0 || __fadd_rn(__fsub_rn(p.y, box.y), pl.y) >= 0 ||
+            __fadd_rn(__fsub_rn(p.z, box.z), pl.z) >= 0) {
+            fail(r, F_ESCAPE);
+            ok = false;
+        }
+    }
+    if (ok) {
+        uint32_t b[3];
+        uint4 sb = r.specimenBins[sp];
+        binIndex(r, id, sb, cell, b);
+        key = binFlat(sb, b);
+    }
+    x.keys[0][id] = key;
+    x.vals[0][id] = id;
+}
+// Digit counts of each tile: counts[digit * tiles + tile].
+__global__ void __launch_bounds__(256) k_radixCount(const __grid_constant__ Params P, uint32_t shift, uint32_t from) {
+    __shared__ uint32_t hist[RADIX];
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[4] == 0) return;
+    RadixScratch x = radixScratch(r, c);
+    hist[threadIdx.x] = 0;
+    __syncthreads();
+    uint32_t base = blockIdx.x * RADIX_TILE;
+    for (uint32_t k = threadIdx.x; k < RADIX_TILE && base + k < c.N; k += blockDim.x)
+        atomicAdd(&hist[(x.keys[from][base + k] >> shift) & (RADIX - 1)], 1u);
+    __syncthreads();
+    x.counts[threadIdx.x * x.tiles + blockIdx.x] = hist[threadIdx.x];
+}
+// Stable scatter of a tile: its elements in index order, 256 at a time; an
+// element's place is its digit's offset for the tile (the scanned counts),
+// plus the tile's earlier elements with that digit (a running count), plus
+// the earlier warps of this round with it, plus the lower lanes of its warp
+// with it (__match_any_sync).
+__global__ void __launch_bounds__(256) k_radixScatter(const __grid_constant__ Params P, uint32_t shift, uint32_t from) {
+    __shared__ uint32_t offset[RADIX], warpCount[8][RADIX];
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[4] == 0) return;
+    RadixScratch x = radixScratch(r, c);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    offset[threadIdx.x] = x.counts[threadIdx.x * x.tiles + blockIdx.x];
+#pragma unroll
+    for (uint32_t w = 0; w < 8; ++w) warpCount[w][threadIdx.x] = 0;
+    __syncthreads();
+    uint32_t base = blockIdx.x * RADIX_TILE;
+    for (uint32_t round = 0; round < RADIX_ITEMS; ++round) {
+        uint32_t i = base + round * 256 + threadIdx.x;
+        bool valid = i < c.N && round * 256 + threadIdx.x < RADIX_TILE;
+        uint32_t key = valid ? x.keys[from][i] : 0u, val = valid ? x.vals[from][i] : 0u;
+        uint32_t digit = valid ? (key >> shift) & (RADIX - 1) : RADIX;  // RADIX: no element
+        uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        uint32_t below = __popc(peers & lanesBelow());
+        if (valid && below == 0) warpCount[warp][digit] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t place = offset[digit] + below;
+            for (uint32_t w = 0; w < warp; ++w) place += warpCount[w][digit];
+            x.keys[from ^ 1u][place] = key;
+            x.vals[from ^ 1u][place] = val;
+        }
+        __syncthreads();
+        // This round's elements of each digit move its offset on.
+        uint32_t total = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < 8; ++w) {
+            total += warpCount[w][threadIdx.x];
+            warpCount[w][threadIdx.x] = 0;
+        }
+        offset[threadIdx.x] += total;
+        __syncthreads();
+    }
+}
+// Each bin's run of the sorted grains into its reference slots.
+__global__ void k_binsFromSorted(const __grid_constant__ Params P, uint32_t from) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[4] == 0) return;
+    RadixScratch x = radixScratch(r, c);
+    for (uint32_t k = gtid(); k < c.N; k += gstride()) {
+        uint32_t bin = x.keys[from][k];
+        if (bin >= c.binCount || (k > 0 && x.keys[from][k - 1] == bin)) continue;  // not the start of a run
+        uint32_t occ = 0;
+        while (k + occ < c.N && x.keys[from][k + occ] == bin) {
+            if (occ < c.binCapacity) r.binParticles[bin * c.binCapacity + occ] = x.vals[from][k + occ];
+            ++occ;
+        }
+        r.binCounts[bin] = occ;
+        if (occ > c.binCapacity) fail(r, F_BIN);
+    }
+}
 // solver.slang:360-384.  An FP32 minimum-image estimate rejects grains that
 // are clearly beyond range before the exact FP64 branch decides.
 __device__ uint32_t findPairs(const Res& r, const Config& c, uint32_t id, bool emit) {
@@ -258,6 +396,130 @@ __device__ uint32_t findPairs(const Res& r, const Config& c, uint32_t id, bool e
                 }
             }
     return count;
+}
+// The same search with a warp per grain and ballot compaction.  The grain's
+// stencil bins (the reference's x, y, z order) are taken 32 at a time, one
+// per lane with its occupancy; their slots form one candidate sequence in
+// the reference's order (bin, then slot), which the lanes test 32 at a time
+// (the FP32 estimate, then the exact FP64 branch).  A ballot of the passing
+// candidates counts them or, in the emit pass, gives each its place in
+// order: the pair list is the serial search's, pair for pair.
+template <bool Emit>
+__device__ __forceinline__ void findPairsWarp(const Res& r, const Config& c, uint32_t id) {
+    const uint32_t lane = laneId();
+    uint32_t sp = specimenOf(r, id);
+    uint4 sb = r.specimenBins[sp];
+    uint32_t bins[3] = {sb.x, sb.y, sb.z};
+    float4 cell = r.cell[3 * sp];
+    uint32_t b[3];
+    binIndex(r, id, sb, cell, b);
+    float cutoff = r.referenceCell[2 * sp + 1].w;
+    float box[3] = {cell.x, cell.y, cell.z};
+    int reach[3], low[3];
+    uint32_t width[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        reach[k] = int(ceilf(__fmul_rn(__fdiv_rn(cutoff, box[k]), float(bins[k]))));
+        low[k] = max(int(b[k]) - reach[k], 0);
+        int high = min(int(b[k]) + reach[k], int(bins[k]) - 1);
+        uint32_t w = uint32_t(2 * reach[k] + 1);
+        width[k] = c.periodic != 0 ? min(w, bins[k]) : uint32_t(high - low[k] + 1);
+    }
+    float4 pi = r.position[id], li = r.positionRemainder[id];
+    float ri = r.body[id].z;
+    uint32_t stencil = width[0] * width[1] * width[2];
+    uint32_t count = 0, base = Emit ? r.pairOffsets[id] : 0u;
+    for (uint32_t q0 = 0; q0 < stencil; q0 += 32) {
+        // Lane q: stencil bin q0 + q (x slowest, z fastest) and its occupancy.
+        uint32_t q = q0 + lane, bin = 0, occ = 0;
+        if (q < stencil) {
+            uint32_t z = q % width[2], y = (q / width[2]) % width[1], x = q / (width[2] * width[1]);
+            uint32_t cc[3];
+            if (c.periodic != 0) {
+                cc[0] = modIndex(int(b[0]) - reach[0] + int(x), bins[0]);
+                cc[1] = modIndex(int(b[1]) - reach[1] + int(y), bins[1]);
+                cc[2] = modIndex(int(b[2]) - reach[2] + int(z), bins[2]);
+            } else {
+                cc[0] = uint32_t(low[0] + int(x));
+                cc[1] = uint32_t(low[1] + int(y));
+                cc[2] = uint32_t(low[2] + int(z));
+            }
+            bin = binFlat(sb, cc);
+            occ = min(r.binCounts[bin], c.binCapacity);
+        }
+        uint32_t inclusive = occ;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, inclusive, o);
+            if (lane >= o) inclusive += t;
+        }
+        uint32_t total = __shfl_sync(0xffffffffu, inclusive, 31);
+        for (uint32_t c0 = 0; c0 < total; c0 += 32) {
+            uint32_t k = c0 + lane;
+            // The stencil bin holding candidate k: the first lane whose
+            // inclusive count exceeds k (every lane searches, past the end
+            // with the last candidate, so that each shuffle has the warp).
+            uint32_t kk = min(k, total - 1), lo = 0, hi = 31;
+#pragma unroll
+            for (uint32_t step = 0; step < 5; ++step) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (__shfl_sync(0xffffffffu, inclusive, mid) > kk) hi = mid; else lo = mid + 1;
+            }
+            uint32_t before = __shfl_sync(0xffffffffu, inclusive - occ, lo);
+            uint32_t at = __shfl_sync(0xffffffffu, bin, lo);
+            bool pass = false;
+            uint32_t j = 0;
+            if (k < total) {
+                j = r.binParticles[at * c.binCapacity + (k - before)];
+                if (j > id) {
+                    float range = __fadd_rn(__fadd_rn(ri, r.body[j].z), c.skin);
+                    float rr = __fmul_rn(range, range);
+                    bool near = true;
+                    if (c.sourceSurfaceNormal == 0) {
+                        float4 pj = r.position[j], lj = r.positionRemainder[j];
+                        float e[3] = {(pj.x - pi.x) + (lj.x - li.x), (pj.y - pi.y) + (lj.y - li.y),
+                                      (pj.z - pi.z) + (lj.z - li.z)};
+                        if (c.periodic != 0) {
+#pragma unroll
+                            for (int a = 0; a < 3; ++a) e[a] -= floorf(e[a] / box[a] + 0.5f) * box[a];
+                        }
+                        near = e[0] * e[0] + e[1] * e[1] + e[2] * e[2] <= 1.002f * rr;  // estimate: ~1e-6 relative
+                    }
+                    if (near) {
+                        f3 d = centerBranch64(r, c, id, j);
+                        float dd = dot(d, d);
+                        if (c.sourceSurfaceNormal != 0 && dd < 1e-12f) fail(r, F_COINCIDENT);
+                        else pass = dd <= rr;
+                    }
+                }
+            }
+            uint32_t ballot = __ballot_sync(0xffffffffu, pass);
+            if (Emit && pass) {
+                uint32_t index = base + count + __popc(ballot & lanesBelow());
+                if (index < c.pairCapacity) r.pairs[index] = make_uint2(id, j);
+                else fail(r, F_PAIR);
+            }
+            count += __popc(ballot);
+        }
+    }
+    if (!Emit && lane == 0) r.pairCounts[id] = count;
+}
+__global__ void __launch_bounds__(256) k_pairsCountWarp(const __grid_constant__ Params P) {
+    if (P.r.control[4] == 0) return;
+    for (uint32_t id = warpGlobal(); id < P.c.N; id += warpStride()) findPairsWarp<false>(P.r, P.c, id);
+}
+// solver.slang:388-392 (the pair total is written by the scan)
+__global__ void __launch_bounds__(256) k_pairsEmitWarp(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    if (r.control[4] == 0) return;
+    if (gtid() == 0) r.work[W_REBUILDS] += 1u;
+    for (uint32_t id = warpGlobal(); id < P.c.N; id += warpStride()) findPairsWarp<true>(r, P.c, id);
+    for (uint32_t id = gtid(); id < P.c.N; id += gstride()) {
+        r.referencePosition[id] = r.position[id];
+        r.referencePositionRemainder[id] = r.positionRemainder[id];
+        uint32_t sp = specimenOf(r, id);
+        r.referenceCell[2 * sp] = r.cell[3 * sp];
+    }
 }
 __global__ void k_pairsCount(const __grid_constant__ Params P) {
     uint32_t id = gtid();
@@ -2119,17 +2381,35 @@ static uint32_t smCount() {
 // Grid of `perSM` CTAs per SM (the tuned value, or `fallback` when 0).
 static inline uint32_t grid(uint32_t perSM, uint32_t fallback) { return smCount() * (perSM ? perSM : fallback); }
 
+// The neighbour build on rebuild steps (every kernel returns at once on the
+// others): the cell list by radix sort (or, where byJPairs is too small to
+// hold the sort's scratch, by atomic fill and a rank sort per bin), the pair
+// search with a warp per grain, then the pairs grouped by second grain.
 static void neighbours(const Params& P, cudaStream_t s) {
     const Res& r = P.r;
     const Config& c = P.c;
     uint32_t T = 256;
     k_binsClear<<<blocks(c.binCount, T), T, 0, s>>>(P);
-    k_binsFill<<<blocks(c.N, T), T, 0, s>>>(P);
-    k_binsSort<<<min(c.binCount, 152u * 16u), 128, 2 * c.binCapacity * sizeof(uint32_t), s>>>(P);
-    k_pairsCount<<<blocks(c.N, 128), 128, 0, s>>>(P);
+    if (uint64_t(c.pairCapacity) >= radixWords(c.N)) {
+        uint32_t tiles = radixTiles(c.N), from = 0, bits = 1;
+        while (bits < 32 && (uint64_t(1) << bits) <= c.binCount) ++bits;  // keys 0 .. binCount
+        k_binKeys<<<blocks(c.N, T), T, 0, s>>>(P);
+        RadixScratch x = radixScratch(r, c);
+        for (uint32_t shift = 0; shift < bits; shift += 8, from ^= 1u) {
+            k_radixCount<<<tiles, T, 0, s>>>(P, shift, from);
+            launch_step_scan(r, x.counts, x.counts, ScanCount{nullptr, 0, 0, RADIX * tiles}, false, nullptr,
+                             r.control + 4, s);
+            k_radixScatter<<<tiles, T, 0, s>>>(P, shift, from);
+        }
+        k_binsFromSorted<<<blocks(c.N, T), T, 0, s>>>(P, from);
+    } else {
+        k_binsFill<<<blocks(c.N, T), T, 0, s>>>(P);
+        k_binsSort<<<min(c.binCount, 152u * 16u), 128, 2 * c.binCapacity * sizeof(uint32_t), s>>>(P);
+    }
+    k_pairsCountWarp<<<PERSISTENT, T, 0, s>>>(P);
     launch_step_scan(r, r.pairCounts, r.pairOffsets, ScanCount{nullptr, 0, 0, c.N}, false, r.control + 1, r.control + 4,
                 s);
-    k_pairsEmit<<<blocks(c.N, 128), 128, 0, s>>>(P);
+    k_pairsEmitWarp<<<PERSISTENT, T, 0, s>>>(P);
     k_byJReset<<<blocks(c.N + 1, T), T, 0, s>>>(P);
     k_byJCount<<<PERSISTENT, T, 0, s>>>(P);
     launch_step_scan(r, r.byJCounts, r.byJOffsets, ScanCount{nullptr, 0, 0, c.N}, true, nullptr, r.control + 4,
