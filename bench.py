@@ -13,9 +13,15 @@ Workloads (``--workload``):
     compression at 0.5/s with rho 2650, kn 1e12, kt 5e11, mu 0.5, normal
     viscosity for damping ratio 0.3 and dt one ulp below the reference's
     conservative bound.
-``uneven-50k``: 50,653 grains from the uneven library (64 shapes, triangle
-    counts log-uniform 320..5,120, axis ratios U(0.6, 1)) on a jittered cubic
-    lattice at solid fraction 0.58, compressed at 0.5/s.
+``uneven-50k``: 50,000 grains from the uneven library (64 shapes, triangle
+    counts log-uniform 320..5,120, axis ratios U(0.6, 1)): a dense periodic
+    packing of 6,250 grains prepared like dense-10k's (affine compression and
+    frictionless force descent toward solid fraction 0.58; the record states
+    what was reached, sand_atlas_dem_gb300/data/packing-uneven-6250.npz),
+    repeated 2 x 2 x 2, compressed at 0.5/s.
+``lattice-50k``: 50,653 grains of the uneven library on a jittered cubic
+    lattice at solid fraction 0.58 (about 127 contacts per grain: an
+    overlapped stress case), compressed at 0.5/s.
 ``specimens-128``: 128 independent periodic specimens batched in one engine
     (one launch per phase, one graph per step), 512..4,096 grains each from
     the uneven library at solid fractions U(0.55, 0.60), each compressed at
@@ -74,9 +80,13 @@ WORKLOADS = {
     "dense-10k": dict(COMMON, workload="dense-periodic-10k-icosphere-f8", library="f8", grains=10_000,
                       triangles_per_grain=1280, nodes_per_grain=642, solid_fraction_target=0.58,
                       max_overlap_fraction=0.1, strain_rate_per_s=-0.5),
-    "uneven-50k": dict(COMMON, workload="lattice-periodic-50k-uneven", library="uneven", grains=37**3,
-                       triangles_per_grain="320..5120", solid_fraction=0.58, max_overlap_fraction=0.5,
-                       strain_rate_per_s=-0.5, packing="jittered cubic lattice"),
+    "uneven-50k": dict(COMMON, workload="dense-periodic-50k-uneven", library="uneven", grains=50_000,
+                       triangles_per_grain="320..5120", solid_fraction_target=0.58, max_overlap_fraction=0.1,
+                       strain_rate_per_s=-0.5,
+                       packing="force-descent packing of 6,250 grains (packing-uneven-6250.npz) tiled 2x2x2"),
+    "lattice-50k": dict(COMMON, workload="lattice-periodic-50k-uneven", library="uneven", grains=37**3,
+                        triangles_per_grain="320..5120", solid_fraction=0.58, max_overlap_fraction=0.5,
+                        strain_rate_per_s=-0.5, packing="jittered cubic lattice (overlapped stress case)"),
     "specimens-128": dict(COMMON, workload="128-specimens-uneven", library="uneven", specimens=128,
                           grains_per_specimen="512..4096", solid_fraction="U(0.55, 0.60)",
                           strain_rate_per_s="-U(0.1, 1.0) per specimen", max_overlap_fraction=0.5,
@@ -92,17 +102,19 @@ WORKLOADS = {
                            pairs_per_particle=8, contacts_per_particle=256, strain_rate_per_s=0.0),
 }
 DATA = ROOT / "sand_atlas_dem_gb300" / "data"
-# DRAM bytes (read + write) of one step's exact queries (k_nodeWalkKnown and
-# k_nodeWalkSlow) from an ncu capture of the same workload
+# DRAM bytes (read + write) of one reuse step's exact queries
+# (k_nodeWalkKnown and k_nodeWalkStaged; k_nodeWalkSlow returns at once on a
+# short list) from an ncu capture of the same workload
 # (profiles/walk-dense-10k.md); None where not captured.
-WALK_TRAFFIC = {"dense-10k": 74.51e6}
+WALK_TRAFFIC = {"dense-10k": 40.03e6 + 0.48e6 + 9.26e6}
 # work[] counters (csrc/dem_device.cuh): the stored node-filter results and
 # the neighbour-list rebuilds.
 W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS, W_CERTIFIED, W_REBUILDS, W_DORMANT = 8, 9, 10, 15, 17, 18
 # Steps of the long window timed after the headline steps: the length of the
 # workload's own run, so that the filter builds and neighbour rebuilds its
 # motion causes are inside it.
-WINDOW_STEPS = {"dense-10k": 10_000, "sparse-1k": 2_000, "uneven-50k": 2_000, "specimens-128": 2_000,
+WINDOW_STEPS = {"dense-10k": 10_000, "sparse-1k": 2_000, "uneven-50k": 2_000, "lattice-50k": 2_000,
+                "specimens-128": 2_000,
                 "walled-10k": 2_000, "sdf-spheres-1k": 2_000}
 
 
@@ -194,6 +206,18 @@ class Workload:
             self.rates = np.zeros((1, 3))
             self.planes = case["planes"]
         elif name == "uneven-50k":
+            # 50,000 grains: the committed 6,250-grain dense packing of the
+            # uneven library, repeated 2 x 2 x 2 (a periodic packing of the
+            # same solid fraction and contacts per grain).
+            from sand_atlas_dem_gb300.workloads import load_packing, tile_packing
+
+            pack = tile_packing(load_packing(DATA / "packing-uneven-6250.npz"))
+            self.specimens = [(pack["positions"], pack["cell"], pack["ids"], pack["scales"])]
+            self.rotations = pack["rotations"]
+            self.rates = np.full((1, 3), self.config["strain_rate_per_s"])
+            self.config.update(packing_meta=pack["meta"],
+                               solid_fraction=pack["meta"].get("achieved_solid_fraction"))
+        elif name == "lattice-50k":
             case = lattice_at(self.lib, round(self.config["grains"] ** (1 / 3)), self.config["solid_fraction"],
                               seed=5)
             self.specimens = [(case["positions"], case["cell"], case["ids"], case["scales"])]
@@ -208,7 +232,7 @@ class Workload:
         scales = np.concatenate([s[3] for s in self.specimens])
         # Lattices have at most 26 neighbours in range: 16 pairs per grain
         # leave room, and the engine grows on overflow.
-        pairs = {} if name in ("dense-10k", "sparse-1k") else dict(pairs_per_particle=16)
+        pairs = {} if name in ("dense-10k", "sparse-1k", "uneven-50k") else dict(pairs_per_particle=16)
         if name == "sdf-spheres-1k":
             from sand_atlas_dem_gb300.spec import Experiment
 
@@ -450,7 +474,8 @@ def run_gb300(args, cpu=True):
     dormant = filter_cache["dormant_slots"]
     step_bytes, query_bytes, walk_bytes = algorithmic_bytes(w.grains, pairs, contacts, items, nodes, survivors,
                                                             kept, 0, lib_bytes, dormant)
-    kernel_name = ("k_nodeWalkKnown + k_nodeWalkSlow (exact queries: certified triangles, then full BVH walks)"
+    kernel_name = ("k_nodeWalkKnown + k_nodeWalkStaged/k_nodeWalkSlow (exact queries: certified triangles, "
+                   "then full BVH walks)"
                    if e.filter_margin > 0 and e.culler is None else "k_nodeWalk (exact BVH queries, one thread per kept node)")
     group_name = "k_nodeFilter, k_survivorList, k_survivorPrefilter, k_walkList, k_nodeWalk + scans"
     if e.sdf:

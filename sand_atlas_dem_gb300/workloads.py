@@ -451,6 +451,24 @@ def load_packing(path):
                     scales=z["scales"], meta=json.loads(str(z["meta"])))
 
 
+def tile_packing(record, reps=(2, 2, 2)):
+    """A periodic packing repeated ``reps`` times along each axis: copies of
+    every grain (same shape, scale and orientation) shifted by whole cells,
+    in a cell ``reps`` times larger.  The result is a periodic packing of the
+    same solid fraction and the same contacts per grain, ``prod(reps)`` times
+    larger (grain k of copy (a, b, c) is grain ``k + n (a reps[1] reps[2] +
+    b reps[2] + c)``)."""
+    positions = np.asarray(record["positions"], float)
+    cell = np.asarray(record["cell"], float)
+    shifts = np.stack(np.meshgrid(*(np.arange(r) for r in reps), indexing="ij"), -1).reshape(-1, 3)
+    tiled = (positions[None, :, :] + (shifts * cell)[:, None, :]).reshape(-1, 3)
+    copies = len(shifts)
+    return dict(positions=tiled, cell=cell * np.asarray(reps, float),
+                rotations=np.tile(np.asarray(record["rotations"]), (copies, 1)),
+                ids=np.tile(np.asarray(record["ids"], np.uint32), copies),
+                scales=np.tile(np.asarray(record["scales"], float), copies), meta=dict(record.get("meta", {})))
+
+
 def solid_fraction(engine):
     volume = sum(engine.library.shapes[int(i)].volume * s**3 for i, s in zip(engine.ids, engine.scales))
     cell = engine.read("cell", np.float32, (3, 4))[0, :3].astype(float) * engine.length_unit
