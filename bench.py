@@ -663,23 +663,30 @@ def culler_comparison(w, args, flush):
     = exact contacts absent from the culled run; forces are compared bit for
     bit.
     """
+    import gc
+
+    import torch
+
     from sand_atlas_dem_gb300.culler import LearnedCuller
     from sand_atlas_dem_gb300.engine import Engine
 
     rate = w.rate()
     reference_filters = dict(distance_grid=False, filter_margin=0.0)
-    engines = {"plain": w.engine(Engine), "culled": w.engine(Engine),
-               "plain_no_grid": w.engine(Engine, **reference_filters),
-               "culled_no_grid": w.engine(Engine, **reference_filters)}
+    configs = {"plain": {}, "culled": {}, "plain_no_grid": reference_filters, "culled_no_grid": reference_filters}
+    # One engine at a time (besides the one the culler samples its shapes
+    # through): a batched workload's engines take tens of GB each.
     t = time.perf_counter()
-    c = LearnedCuller(engines["culled"], points=1 << 20, steps=2000, batch=8192)
+    trainer = w.engine(Engine, **reference_filters)
+    c = LearnedCuller(trainer, points=1 << 20, steps=2000, batch=8192)
     c.train()
-    c.attach(engines["culled"])
-    c.attach(engines["culled_no_grid"])
+    c.calibrate()
     train_s = time.perf_counter() - t
     out = {}
     steps = min(args.steps, 50)
-    for name, e in engines.items():
+    for name, settings in configs.items():
+        e = w.engine(Engine, **settings)
+        if name.startswith("culled"):
+            c.attach(e)
         e.advance(max(3, args.warmup), rate=rate)
         set_rates(e, w)
         e.buffers["cullerStats"].copy_from_numpy(np.zeros(4, np.uint32))
@@ -689,6 +696,9 @@ def culler_comparison(w, args, flush):
         out[name] = dict(value=w.grains * steps / (sum(ms) / 1e3), ms_per_step=sum(ms) / steps,
                          node_query_ms=phases["node_filter"] + phases["node_query"],
                          tested=int(stats[0]), culled=int(stats[1]), state=e.state())
+        del e
+        gc.collect()
+        torch.cuda.empty_cache()
     result = dict(steps=steps, training_s=round(train_s, 1), margins_mean=float(np.mean(c.margins)),
                   cell_margins_mean=float(np.mean(c.cell_margins)), loss_over_weight=c.over,
                   validation_cull_rate=c.cull_rate())

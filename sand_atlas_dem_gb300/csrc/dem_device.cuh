@@ -820,7 +820,7 @@ __device__ __forceinline__ uint32_t gridSeed(const Res& r, uint32_t shape, f3 lo
 // Whether the exact-query list itself is stored with the filter results
 // (built with grown tests and ordered by target shape and coarse cell).  Not
 // with the learned culler, whose calibrated decision is taken every step.
-__device__ __forceinline__ bool storedKeep(const Config& c) { return c.filterMargin > 0.0f && c.cullerEnabled == 0; }
+__host__ __device__ __forceinline__ bool storedKeep(const Config& c) { return c.filterMargin > 0.0f && c.cullerEnabled == 0; }
 // Margin the filter results are built with on this step (0 without them).
 __device__ __forceinline__ float buildMargin(const Res& r, const Config& c) {
     return c.filterMargin > 0.0f ? __uint_as_float(r.work[W_FILTER_NEXT]) : 0.0f;

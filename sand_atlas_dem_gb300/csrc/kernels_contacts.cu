@@ -1571,8 +1571,39 @@ __global__ void __launch_bounds__(256) k_nodeEmit(const __grid_constant__ Params
         }
     }
 }
+// The same contact records from a stored exact-query list, a thread per
+// stored slot instead of a warp per item: a slot whose node hit (its bit in
+// its item's hit mask) writes its record at its item's offset plus the
+// number of the item's hits at lower node slots -- the canonical place
+// k_nodeEmit gives it -- from the slot's own node record (source, target,
+// directed pair, packed sample) and its hit scratch.  Dormant slots never
+// hit.  The item masks are cleared by k_clearHits afterwards (a slot cannot
+// clear its item's mask while the item's other hits still read it).
+__global__ void k_clearHits(const __grid_constant__ Params P);
+__global__ void __launch_bounds__(256) k_emitSlots(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    if (r.control[0] != 0) return;
+    uint32_t n = min(r.work[W_KEPT], c.survivorCapacity);
+    for (uint32_t t = gtid(); t < n; t += gstride()) {
+        if (r.walkCertTriangle[t].x == DORMANT) continue;
+        uint2 it = r.walkItem[t];
+        uint2 m = r.candHitMask[it.x];
+        uint32_t word = it.y < WARP ? m.x : m.y, bit = 1u << (it.y & 31u);
+        if (!(word & bit)) continue;
+        uint32_t rank = (it.y < WARP ? 0u : __popc(m.x)) + __popc(word & (bit - 1u));
+        uint32_t slot = r.candHitOffset[it.x] + rank, from = r.walkList[t];
+        if (slot >= c.contactCapacity || from >= c.survivorCapacity) { fail(r, F_CONTACT); continue; }
+        uint4 rec = r.walkNode[t];
+        uint32_t node = rec.w - __ldg(&r.sampleInfo[r.shapeId[rec.x]].x);
+        r.meta[slot] = make_uint4(rec.x, rec.y, node, 0);
+        r.pointDepth[slot] = r.hitScratch[2 * from];
+        r.normalArea[slot] = r.hitScratch[2 * from + 1];
+        r.contactPair[slot] = rec.z >> 1;
+    }
+}
 // Per pair: first contact of the pair on the side being written, and counts.
-__global__ void k_contactStart(const __grid_constant__ Params P) {
+__device__ __forceinline__ void contactStart(const Params& P) {
     const Res& r = P.r;
     const Config& c = P.c;
     uint32_t n = activePairs(r, c);
@@ -1590,6 +1621,20 @@ __global__ void k_contactStart(const __grid_constant__ Params P) {
             r.contactCounts[p] = end - start;
         }
     }
+}
+__global__ void k_contactStart(const __grid_constant__ Params P) { contactStart(P); }
+// Hit masks and counts of every item back to zero for the next step (also
+// after a failed step, whose walks may have set bits), and the per-pair
+// contact starts (k_contactStart) in the same launch.
+__global__ void k_clearHits(const __grid_constant__ Params P) {
+    const Res& r = P.r;
+    const Config& c = P.c;
+    uint32_t n = min(r.work[W_CANDIDATES], c.candidateCapacity);
+    for (uint32_t i = gtid(); i < n; i += gstride()) {
+        r.candHitMask[i] = make_uint2(0u, 0u);
+        r.candHitCount[i] = 0;
+    }
+    contactStart(P);
 }
 
 // ------------------------------------------------------------ SDF geometry
@@ -2523,8 +2568,13 @@ static void collectEmit(const Params& P, cudaStream_t s) {
     launch_step_scan(r, r.candHitCount, r.candHitOffset, ScanCount{r.work + W_CANDIDATES, c.candidateCapacity, 1, 0}, true,
                 r.control + 2, nullptr, s);
     uint32_t g = grid(c.contactBlocksPerSM, 8);
-    k_nodeEmit<<<g, 256, 0, s>>>(P);
-    k_contactStart<<<g, 256, 0, s>>>(P);
+    if (storedKeep(c)) {
+        k_emitSlots<<<g, 256, 0, s>>>(P);
+        k_clearHits<<<g, 256, 0, s>>>(P);  // and the per-pair contact starts
+    } else {
+        k_nodeEmit<<<g, 256, 0, s>>>(P);
+        k_contactStart<<<g, 256, 0, s>>>(P);
+    }
 }
 // Plane contacts after the grain-grain ones: counts, their scan, records.
 static void collectWalls(const Params& P, cudaStream_t s) {
