@@ -191,6 +191,19 @@ int sdg_engine_advance(void* engine, void* const* buffers, const uint64_t* bytes
                        uint32_t nvalues, uint32_t steps, uint32_t use_graph, void* stream);
 
 /*
+ * Engine.diagnostics (src/sand_atlas_dem/gpu.py:746-891) in one call: the
+ * diagnostic rows (solver.slang:922-947) and fabric rows with their 256-wide
+ * tree reductions (diagnostic.slang:3-28) through two device scratch buffers
+ * of scratch_bytes each (at least ceil(max(N, pairCapacity) / 256) x 8 rows x
+ * 16 bytes), then 272 bytes copied to `host` (pinned): the 8 reduced
+ * diagnostic rows, the 2 reduced fabric rows, the first 3 cell rows and the
+ * 16 control words.  The caller waits on the stream before reading `host`.
+ * Replaces the reference's per-reduction dispatches and reads.
+ */
+int sdg_engine_diagnostics(void* const* buffers, const uint64_t* bytes, const double* values, uint32_t nvalues,
+                           void* scratch_a, void* scratch_b, uint64_t scratch_bytes, void* host, void* stream);
+
+/*
  * One committed step with CUDA events between phases; writes SDG_PHASES
  * device milliseconds: drift, neighbours, pair cull, node filter (with the
  * survivor list and the learned culler), exact node queries, contact emit,

@@ -384,6 +384,49 @@ int sdg_engine_profile(void* engine, void* const* buffers, const uint64_t* bytes
     return rc ? rc : record(cudaGetLastError(), "profile");
 }
 
+// Engine.diagnostics in one call: the per-grain diagnostic rows and the
+// per-pair fabric rows with their 256-wide tree reductions
+// (diagnostic.slang:3-28; the same levels as sdg_reduce_rows), ping-ponged
+// through two scratch buffers, then the final 8 + 2 rows, the first three
+// cell rows and the 16 control words copied to `host` (pinned, 272 bytes:
+// 8 rows, 2 rows, 3 rows, 16 words).  The caller waits on the stream.
+static int reduceLevels(const float4* input, uint32_t n, uint32_t rows, int maxRow, float4* a, float4* b,
+                        uint64_t scratchBytes, const float4** result, cudaStream_t s) {
+    const float4* src = input;
+    float4* out = a;
+    while (n > 1) {
+        uint32_t groups = (n + 255) / 256;
+        if (uint64_t(groups) * rows * 16 > scratchBytes) { g_error = "diagnostics scratch too small"; return 1; }
+        launch_reduce_rows(src, out, n, rows, maxRow, s);
+        src = out;
+        out = out == a ? b : a;
+        n = groups;
+    }
+    *result = src;
+    return 0;
+}
+int sdg_engine_diagnostics(void* const* buffers, const uint64_t* bytes, const double* values, uint32_t nvalues,
+                           void* scratch_a, void* scratch_b, uint64_t scratch_bytes, void* host, void* stream) {
+    if (!scratch_a || !scratch_b || !host) { g_error = "null diagnostics argument"; return 1; }
+    Params P;
+    if (int rc = unpack(buffers, bytes, values, nvalues, P)) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const Config& c = P.c;
+    auto* a = static_cast<float4*>(scratch_a);
+    auto* b = static_cast<float4*>(scratch_b);
+    char* out = static_cast<char*>(host);
+    const float4* rows = nullptr;
+    launch_state("diagnosticRows", P, c.N, s);
+    if (int rc = reduceLevels(P.r.diagnosticRows, c.N, 8, 4, a, b, scratch_bytes, &rows, s)) return rc;
+    cudaMemcpyAsync(out, rows, 8 * 16, cudaMemcpyDeviceToHost, s);
+    launch_state("fabricRows", P, c.pairCapacity, s);
+    if (int rc = reduceLevels(P.r.fabricRows, c.pairCapacity, 2, -1, a, b, scratch_bytes, &rows, s)) return rc;
+    cudaMemcpyAsync(out + 128, rows, 2 * 16, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(out + 160, P.r.cell, 3 * 16, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(out + 208, P.r.control, 16 * 4, cudaMemcpyDeviceToHost, s);
+    return record(cudaGetLastError(), "diagnostics");
+}
+
 int sdg_reduce_rows(const void* input, void* output, uint32_t n, uint32_t rows, int32_t max_row, void* stream) {
     if (!input || !output || rows == 0) { g_error = "bad reduction arguments"; return 1; }
     launch_reduce_rows(static_cast<const float4*>(input), static_cast<float4*>(output), n, rows, max_row,

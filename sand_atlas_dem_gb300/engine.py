@@ -255,6 +255,7 @@ class Engine:
         # strain-rate rows last written into the cell.
         self._device_version = 0
         self._ctrl_cache = None
+        self._diagnostic_scratch = None
         self._rates = None
         # Host<->device bytes moved by this engine's own reads and uploads.
         self.h2d_bytes = self.d2h_bytes = 0
@@ -717,6 +718,26 @@ class Engine:
         self.active = 1
         self.step = step
 
+    def _diagnostic_rows(self, config):
+        """The reduced diagnostic and fabric rows, the cell rows and the control
+        words (``sdg_engine_diagnostics``)."""
+        if self._diagnostic_scratch is None:
+            size = 16 * 8 * ((max(self.n, self.pair_capacity) + 255) // 256)
+            self._diagnostic_scratch = (DeviceBuffer(self, size), DeviceBuffer(self, size), size)
+        a, b, size = self._diagnostic_scratch
+        self._touch()
+        ptrs, sizes = self._arrays(self.active)
+        values, nv = self._values(config)
+        host = self._staging[:272]
+        native.check(self.lib.sdg_engine_diagnostics(ptrs, sizes, values, nv, ct.c_void_p(a.ptr()),
+                                                     ct.c_void_p(b.ptr()), size, ct.c_void_p(host.data_ptr()),
+                                                     ct.c_void_p(self.stream.cuda_stream)))
+        self.stream.synchronize()
+        raw = host.numpy().copy()
+        self.d2h_bytes += 272
+        return (raw[:128].view(np.float32), raw[128:160].view(np.float32), raw[160:208].view(np.float32),
+                raw[208:272].view(np.uint32))
+
     def _reduce(self, name, rows, max_row, read=True):
         """Reference 256-wide tree reduction to one row set (``diagnostic.slang:3-28``);
         with ``read=False`` the device buffer holding the rows is returned."""
@@ -773,19 +794,24 @@ class Engine:
     def diagnostics(self):
         """Stress, energies, contact counts, fabric and wall rows (``gpu.py:746-891``)."""
         c = self.config()
-        self.dispatch("diagnosticRows", self.n, c)
-        rows = self._reduce("diagnosticRows", 8, 4, read=False)
-        self.dispatch("fabricRows", self.pair_capacity, c)
-        fabric_rows = self._reduce("fabricRows", 2, -1, read=False)
-        reads = [(rows, 16 * 8, np.float32), (fabric_rows, 16 * 2, np.float32),
-                 (self.buffers["cell"], 16 * 3, np.float32), (self.buffers["control"], 4 * 16, np.uint32)]
         w = self.wall_count
         if w:
+            self.dispatch("diagnosticRows", self.n, c)
+            rows = self._reduce("diagnosticRows", 8, 4, read=False)
+            self.dispatch("fabricRows", self.pair_capacity, c)
+            fabric_rows = self._reduce("fabricRows", 2, -1, read=False)
+            reads = [(rows, 16 * 8, np.float32), (fabric_rows, 16 * 2, np.float32),
+                     (self.buffers["cell"], 16 * 3, np.float32), (self.buffers["control"], 4 * 16, np.uint32)]
             reads += [(self._reduce_walls(), 48 * w, np.float32), (self.buffers["wallPlane"], 16 * w, np.float32),
                       (self.buffers["wallRemainder"], 16 * w, np.float32),
                       (self.buffers["wallVelocity"], 16 * w, np.float32)]
-        # One wait for all the small reads.
-        data, fabric_data, cell, ctrl, *wall_reads = read_batch(self, reads)
+            # One wait for all the small reads.
+            data, fabric_data, cell, ctrl, *wall_reads = read_batch(self, reads)
+        else:
+            # Without planes: the rows, their reductions and the reads in one
+            # native call and one wait.
+            data, fabric_data, cell, ctrl = self._diagnostic_rows(c)
+            wall_reads = []
         data, fabric_data, cell = data.reshape(8, 4), fabric_data.reshape(2, 4), cell.reshape(3, 4)
         ctrl = self._checked(ctrl)
         active_pairs = round(float(fabric_data[1, 2]))

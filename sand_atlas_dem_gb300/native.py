@@ -93,6 +93,9 @@ def load():
                                        ct.c_void_p]
     lib.sdg_exclusive_scan.restype = ct.c_int
     lib.sdg_scan_partials.restype = ct.c_int
+    lib.sdg_engine_diagnostics.argtypes = [P(ct.c_void_p), P(ct.c_uint64), P(ct.c_double), ct.c_uint32,
+                                           ct.c_void_p, ct.c_void_p, ct.c_uint64, ct.c_void_p, ct.c_void_p]
+    lib.sdg_engine_diagnostics.restype = ct.c_int
     lib.sdg_copy_buffers.argtypes = [P(ct.c_void_p), P(ct.c_void_p), P(ct.c_uint64), ct.c_uint32, ct.c_void_p]
     lib.sdg_copy_buffers.restype = ct.c_int
     lib.sdg_exclusive_scan_static.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_uint32, ct.c_void_p, ct.c_void_p]
@@ -143,6 +146,7 @@ EXPORTS = (
     "sdg_engine_destroy",
     "sdg_engine_advance",
     "sdg_engine_profile",
+    "sdg_engine_diagnostics",
     "sdg_engine_kernels_per_step",
     "sdg_engine_branch_kernels",
     "sdg_exclusive_scan",
