@@ -467,12 +467,16 @@ __device__ __forceinline__ bool sameResult(const Res& r, f3 q, uint32_t normal, 
 // diverging warp each.
 // `children`/`nodeBase`: where the walk reads node n's record --
 // children + 4 (n - nodeBase): the library's meshChildren (base 0) or the
-// shape's records staged in shared memory (base: its first node).
+// shape's records staged in shared memory (base: its first node); and
+// `triangles`/`triangleBase` likewise for triangle t's three vertices,
+// triangles + 3 (t - triangleBase).
 template <bool Warp>
 __device__ __forceinline__ float4 meshDistanceCertifiedT(const Res& r, uint32_t shape, f3 p, uint32_t seed,
                                                          float reach, uint32_t& triangle, uint32_t& tie, float& gap,
-                                                         const float4* children, uint32_t nodeBase) {
+                                                         const float4* children, uint32_t nodeBase,
+                                                         const float4* triangles, uint32_t triangleBase) {
     uint32_t root = __ldg(&r.meshRoots[shape].x);
+    auto vertex = [&](uint32_t t, uint32_t k) { return xyz(triangles[3 * (t - triangleBase) + k]); };
     uint32_t pending[32];
     float pendingDistance[32];
     uint32_t top = 1;
@@ -481,8 +485,7 @@ __device__ __forceinline__ float4 meshDistanceCertifiedT(const Res& r, uint32_t 
     float cap = 1e30f;
     if (seed != 0xFFFFFFFFu) {
         uint32_t feature;
-        f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * seed])), xyz(__ldg(&r.meshTriangles[3 * seed + 1])),
-                               xyz(__ldg(&r.meshTriangles[3 * seed + 2])), feature);
+        f3 q = closestTriangle(p, vertex(seed, 0), vertex(seed, 1), vertex(seed, 2), feature);
         f3 dq = p - q;
         float root2 = __fadd_rn(__fsqrt_rn(dot(dq, dq)), reach);
         cap = nextafterf(__fmul_rn(__fmul_rn(root2, root2), 1.0000019073486328f), 1e30f);
@@ -537,8 +540,7 @@ __device__ __forceinline__ float4 meshDistanceCertifiedT(const Res& r, uint32_t 
                 f3 q = mk(0.f, 0.f, 0.f);
                 float distance = 0.f;
                 if (k0 + lane < count) {
-                    q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * t])), xyz(__ldg(&r.meshTriangles[3 * t + 1])),
-                                        xyz(__ldg(&r.meshTriangles[3 * t + 2])), feature);
+                    q = closestTriangle(p, vertex(t, 0), vertex(t, 1), vertex(t, 2), feature);
                     f3 dq = p - q;
                     distance = dot(dq, dq);
                 }
@@ -553,8 +555,7 @@ __device__ __forceinline__ float4 meshDistanceCertifiedT(const Res& r, uint32_t 
         } else {
             for (uint32_t k = 0; k < count; ++k) {
                 uint32_t t = first + k, feature;
-                f3 q = closestTriangle(p, xyz(__ldg(&r.meshTriangles[3 * t])), xyz(__ldg(&r.meshTriangles[3 * t + 1])),
-                                       xyz(__ldg(&r.meshTriangles[3 * t + 2])), feature);
+                f3 q = closestTriangle(p, vertex(t, 0), vertex(t, 1), vertex(t, 2), feature);
                 f3 dq = p - q;
                 take(node, t, q, feature, dot(dq, dq));
             }
@@ -567,7 +568,8 @@ __device__ __forceinline__ float4 meshDistanceCertifiedT(const Res& r, uint32_t 
 }
 __device__ __forceinline__ float4 meshDistanceCertified(const Res& r, uint32_t shape, f3 p, uint32_t seed, float reach,
                                                         uint32_t& triangle, uint32_t& tie, float& gap) {
-    return meshDistanceCertifiedT<false>(r, shape, p, seed, reach, triangle, tie, gap, r.meshChildren, 0u);
+    return meshDistanceCertifiedT<false>(r, shape, p, seed, reach, triangle, tie, gap, r.meshChildren, 0u,
+                                         r.meshTriangles, 0u);
 }
 // The walk's result when the certified triangle (and its same-leaf partner,
 // encoded as by meshDistanceCertified, and its tie of another leaf) are

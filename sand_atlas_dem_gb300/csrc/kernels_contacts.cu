@@ -329,75 +329,9 @@ __global__ void k_binsFromSorted(const __grid_constant__ Params P, uint32_t from
         if (occ > c.binCapacity) fail(r, F_BIN);
     }
 }
-// solver.slang:360-384.  An FP32 minimum-image estimate rejects grains that
-// are clearly beyond range before the exact FP64 branch decides.
-__device__ uint32_t findPairs(const Res& r, const Config& c, uint32_t id, bool emit) {
-    uint32_t sp = specimenOf(r, id);
-    uint4 sb = r.specimenBins[sp];
-    uint32_t bins[3] = {sb.x, sb.y, sb.z};
-    float4 cell = r.cell[3 * sp];
-    uint32_t b[3];
-    binIndex(r, id, sb, cell, b);
-    float cutoff = r.referenceCell[2 * sp + 1].w;
-    float box[3] = {cell.x, cell.y, cell.z};
-    int reach[3], low[3];
-    uint32_t width[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        reach[k] = int(ceilf(__fmul_rn(__fdiv_rn(cutoff, box[k]), float(bins[k]))));
-        low[k] = max(int(b[k]) - reach[k], 0);
-        int high = min(int(b[k]) + reach[k], int(bins[k]) - 1);
-        uint32_t w = uint32_t(2 * reach[k] + 1);
-        width[k] = c.periodic != 0 ? min(w, bins[k]) : uint32_t(high - low[k] + 1);
-    }
-    float4 pi = r.position[id], li = r.positionRemainder[id];
-    float ri = r.body[id].z;
-    uint32_t count = 0, base = emit ? r.pairOffsets[id] : 0;
-    for (uint32_t x = 0; x < width[0]; ++x)
-        for (uint32_t y = 0; y < width[1]; ++y)
-            for (uint32_t z = 0; z < width[2]; ++z) {
-                uint32_t cc[3];
-                if (c.periodic != 0) {
-                    cc[0] = modIndex(int(b[0]) - reach[0] + int(x), bins[0]);
-                    cc[1] = modIndex(int(b[1]) - reach[1] + int(y), bins[1]);
-                    cc[2] = modIndex(int(b[2]) - reach[2] + int(z), bins[2]);
-                } else {
-                    cc[0] = uint32_t(low[0] + int(x));
-                    cc[1] = uint32_t(low[1] + int(y));
-                    cc[2] = uint32_t(low[2] + int(z));
-                }
-                uint32_t bi = binFlat(sb, cc);
-                uint32_t occ = min(r.binCounts[bi], c.binCapacity);
-                for (uint32_t slot = 0; slot < occ; ++slot) {
-                    uint32_t j = r.binParticles[bi * c.binCapacity + slot];
-                    if (j <= id) continue;
-                    float range = __fadd_rn(__fadd_rn(ri, r.body[j].z), c.skin);
-                    float rr = __fmul_rn(range, range);
-                    if (c.sourceSurfaceNormal == 0) {
-                        float4 pj = r.position[j], lj = r.positionRemainder[j];
-                        float e[3] = {(pj.x - pi.x) + (lj.x - li.x), (pj.y - pi.y) + (lj.y - li.y), (pj.z - pi.z) + (lj.z - li.z)};
-                        if (c.periodic != 0) {
-#pragma unroll
-                            for (int k = 0; k < 3; ++k) e[k] -= floorf(e[k] / box[k] + 0.5f) * box[k];
-                        }
-                        float est = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
-                        if (est > 1.002f * rr) continue;  // estimate error is ~1e-6 relative
-                    }
-                    f3 d = centerBranch64(r, c, id, j);
-                    float dd = dot(d, d);
-                    if (c.sourceSurfaceNormal != 0 && dd < 1e-12f) { fail(r, F_COINCIDENT); continue; }
-                    if (dd > rr) continue;
-                    if (emit) {
-                        uint32_t index = base + count;
-                        if (index < c.pairCapacity) r.pairs[index] = make_uint2(id, j);
-                        else fail(r, F_PAIR);
-                    }
-                    count++;
-                }
-            }
-    return count;
-}
-// The same search with a warp per grain and ballot compaction.  The grain's
+// solver.slang:360-392: the pair search, a warp per grain with ballot
+// compaction.  An FP32 minimum-image estimate rejects grains that are clearly
+// beyond range before the exact FP64 branch decides.  The grain's
 // stencil bins (the reference's x, y, z order) are taken 32 at a time, one
 // per lane with its occupancy; their slots form one candidate sequence in
 // the reference's order (bin, then slot), which the lanes test 32 at a time
@@ -520,24 +454,6 @@ __global__ void __launch_bounds__(256) k_pairsEmitWarp(const __grid_constant__ P
         uint32_t sp = specimenOf(r, id);
         r.referenceCell[2 * sp] = r.cell[3 * sp];
     }
-}
-__global__ void k_pairsCount(const __grid_constant__ Params P) {
-    uint32_t id = gtid();
-    if (id < P.c.N && P.r.control[4] != 0) P.r.pairCounts[id] = findPairs(P.r, P.c, id, false);
-}
-// solver.slang:388-392 (the pair total is written by the scan)
-__global__ void k_pairsEmit(const __grid_constant__ Params P) {
-    const Res& r = P.r;
-    uint32_t id = gtid();
-    if (id >= P.c.N || r.control[4] == 0) return;
-    if (id == 0) r.work[W_REBUILDS] += 1u;
-    findPairs(r, P.c, id, true);
-    r.referencePosition[id] = r.position[id];
-    r.referencePositionRemainder[id] = r.positionRemainder[id];
-    // Every grain of a specimen stores the same row (referenceCell[0] in the
-    // reference, written by its thread 0).
-    uint32_t sp = specimenOf(r, id);
-    r.referenceCell[2 * sp] = r.cell[3 * sp];
 }
 // Pairs grouped by their second grain, ascending pair id per grain.
 __global__ void k_byJReset(const __grid_constant__ Params P) {
@@ -1286,12 +1202,13 @@ __global__ void __launch_bounds__(256) k_nodeWalkKnown(const __grid_constant__ P
 // One slot's certifying walk (by its warp when `Warp`; lane 0 records).
 template <bool Warp>
 __device__ __forceinline__ void certifySlot(const Res& r, const Config& c, uint32_t t, float margin, float reach,
-                                            const float4* children, uint32_t nodeBase) {
+                                            const float4* children, uint32_t nodeBase, const float4* triangles,
+                                            uint32_t triangleBase) {
     WalkNode w = walkNode(r, t);
     uint32_t shape = r.shapeId[w.rec.y], triangle, tie;
     float gap;
     float4 f = meshDistanceCertifiedT<Warp>(r, shape, w.local, gridSeed(r, shape, w.local), reach, triangle, tie, gap,
-                                            children, nodeBase);
+                                            children, nodeBase, triangles, triangleBase);
     if (Warp && laneId() != 0) return;
     float slack = __fmul_rn(2e-5f, __fadd_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(w.local.x), fabsf(w.local.y)),
                                                              fabsf(w.local.z))));
@@ -1329,10 +1246,10 @@ __global__ void __launch_bounds__(256) k_nodeWalkSlow(const __grid_constant__ Pa
     uint32_t warps = gridDim.x * (blockDim.x >> 5), warp = blockIdx.x + gridDim.x * (threadIdx.x >> 5);
     if (n <= 2 * warps) {
         for (uint32_t i = warp; i < n; i += warps)
-            certifySlot<true>(r, c, r.walkKey[i], margin, reach, r.meshChildren, 0u);
+            certifySlot<true>(r, c, r.walkKey[i], margin, reach, r.meshChildren, 0u, r.meshTriangles, 0u);
     } else {
         for (uint32_t i = 32 * warp + laneId(); i < n; i += 32 * warps)
-            certifySlot<false>(r, c, r.walkKey[i], margin, reach, r.meshChildren, 0u);
+            certifySlot<false>(r, c, r.walkKey[i], margin, reach, r.meshChildren, 0u, r.meshTriangles, 0u);
     }
 }
 // The same walks with each target shape's BVH node records staged in shared
@@ -1374,7 +1291,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1) k_nodeWalkStaged(const __gri
     float4* stage = reinterpret_cast<float4*>(stageMemory);
     uint32_t* unitStart = reinterpret_cast<uint32_t*>(stageMemory + STAGE_BYTES);  // shapes + 1
     __shared__ __align__(8) uint64_t barrier;
-    __shared__ uint32_t warpTotals[STAGE_THREADS / 32], carry, liveFlag;
+    __shared__ uint32_t warpTotals[STAGE_THREADS / 32], carry, liveFlag, triangleFirst, triangleEnd;
     const Res& r = P.r;
     const Config& c = P.c;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warpId = tid >> 5, warps = STAGE_THREADS / 32;
@@ -1431,8 +1348,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1) k_nodeWalkStaged(const __gri
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    uint32_t total = unitStart[c.shapes], phase = 0, staged = EMPTY;
-    bool stalled = false;
+    uint32_t total = unitStart[c.shapes], phase = 0, staged = EMPTY, stagedFirst = 0;
+    bool stalled = false, trianglesStaged = false;  // the same on every thread
     for (uint32_t u = blockIdx.x; u < total && !stalled; u += gridDim.x) {
         // The unit's shape: the last s with unitStart[s] <= u.
         uint32_t lo = 0, hi = c.shapes;
@@ -1449,6 +1366,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1) k_nodeWalkStaged(const __gri
         if (fits && staged != shape) {
             __syncthreads();  // every warp is done with the staged shape
             if (tid == 0) {
+                triangleFirst = EMPTY;
+                triangleEnd = 0;
                 // The async proxy overwrites what the generic proxy read.
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
@@ -1471,11 +1390,50 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1) k_nodeWalkStaged(const __gri
             // Every thread leaves together if any thread gave up.
             stalled = __syncthreads_or(stalled);
             if (stalled) break;
+            // The shape's triangles: the range its leaves reference (a
+            // reduction over the staged records), staged after the records
+            // when both fit.
+            for (uint32_t k = tid; k < nodes.y - nodes.x; k += STAGE_THREADS) {
+                float4 head = stage[4 * k];
+                if (__float_as_uint(head.w) == LEAF_MARK) {
+                    atomicMin(&triangleFirst, __float_as_uint(head.x));
+                    atomicMax(&triangleEnd, __float_as_uint(head.x) + __float_as_uint(head.y));
+                }
+            }
+            __syncthreads();
+            stagedFirst = triangleFirst;
+            uint32_t triangleBytes = triangleEnd > stagedFirst ? (triangleEnd - stagedFirst) * 48u : 0u;
+            trianglesStaged = triangleBytes != 0 && bytes + triangleBytes <= STAGE_BYTES;
+            if (trianglesStaged) {
+                if (tid == 0) {
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(triangleBytes)
+                                 : "memory");
+                    const char* from = reinterpret_cast<const char*>(r.meshTriangles + 3 * size_t(stagedFirst));
+                    uint32_t to = smemAddress(stage) + bytes;
+                    for (uint32_t off = 0; off < triangleBytes; off += STAGE_CHUNK) {
+                        uint32_t size = min(STAGE_CHUNK, triangleBytes - off);
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                            ::"r"(to + off), "l"(from + off), "r"(size), "r"(bar)
+                            : "memory");
+                    }
+                }
+                if (!mbarrierWait(bar, phase)) {
+                    fail(r, F_WAIT);
+                    stalled = true;
+                }
+                phase ^= 1u;
+                stalled = __syncthreads_or(stalled);
+                if (stalled) break;
+            }
         }
         const float4* children = fits ? stage : r.meshChildren;
         uint32_t base = fits ? nodes.x : 0u;
+        bool local = fits && trianglesStaged;
+        const float4* triangles = local ? stage + 4 * size_t(nodes.y - nodes.x) : r.meshTriangles;
+        uint32_t triangleBase = local ? stagedFirst : 0u;
         for (uint32_t i = first + warpId; i < last; i += warps)
-            certifySlot<true>(r, c, r.walkKey[i], margin, reach, children, base);
+            certifySlot<true>(r, c, r.walkKey[i], margin, reach, children, base, triangles, triangleBase);
     }
     if (stalled && tid == 0) {
         // A copy may still be landing: wait for it (bounded) before the
