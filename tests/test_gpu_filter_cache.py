@@ -16,7 +16,7 @@ from sand_atlas_dem_gb300.engine import Engine
 from tests.specimens import build, lattice_case
 
 pytestmark = pytest.mark.gpu
-W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS, W_CERTIFIED = 8, 9, 10, 15
+W_FILTER_MARGIN, W_FILTER_BUILDS, W_FILTER_STEPS, W_CERTIFIED, W_DORMANT = 8, 9, 10, 15, 18
 RATE = (-0.5, -0.5, -0.5)
 
 
@@ -66,10 +66,13 @@ def test_reused_results_are_bit_identical(gpu_library):
     assert steps == 27  # the initialization and 26 steps
     assert 1 <= builds <= 2, builds  # built at the start, reused since
     assert counters(plain) == (0, 27)
-    # Most exact queries of the reuse steps were answered by a walk certificate.
-    certified = int(stored.read("work", np.uint32, (64,))[W_CERTIFIED])
-    kept = int(stored.read("work", np.uint32, (64,))[3])
+    # Most exact queries of the reuse steps were answered by a walk
+    # certificate, and some stored slots were dormant (their nodes proven out
+    # of reach until the next build) -- with the state bit-identical.
+    work = stored.read("work", np.uint32, (64,))
+    certified, kept, dormant = int(work[W_CERTIFIED]), int(work[3]), int(work[W_DORMANT])
     assert certified > 5 * kept, (certified, kept)
+    assert 0 < dormant < kept, (dormant, kept)
 
 
 def test_motion_beyond_the_margin_rebuilds(gpu_library):

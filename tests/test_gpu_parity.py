@@ -165,3 +165,26 @@ def test_graph_branches_skip_only_idle_work(gpu_library):
     assert lib.sdg_engine_kernels_per_step(engines[0]._native) > 0
     assert lib.sdg_engine_branch_kernels(engines[0]._native, 0) >= 10
     assert lib.sdg_engine_branch_kernels(engines[0]._native, 1) >= 10
+
+
+@pytest.mark.parametrize("pairs_per_particle", [8, 32])
+def test_both_cell_list_paths_give_the_reference_pairs(gpu_library, pairs_per_particle):
+    """The neighbour build sorts the grains into bins by an LSD radix sort
+    whose scratch lives in the pair-by-second-grain array; where that array is
+    too small for it (8 pairs a grain here: 512 words against the sort's 513)
+    the atomic bin fill with a rank sort per bin runs instead.  Both give the
+    oracle's pair list, pair for pair and in order."""
+    from dataclasses import replace
+
+    library, spec, case = lattice_case(spacing=1.05)
+    spec = replace(spec, pairs_per_particle=pairs_per_particle)
+    o = build(OracleEngine, library, spec, case)
+    g = build(Engine, library, spec, case)
+    o.initialize()
+    g.initialize()
+    oc, gc = o.check_errors(), g.check_errors()
+    pairs = int(oc[1])
+    assert gc[1] == pairs > 0
+    np.testing.assert_array_equal(gpu_buffer(g, "pairs", np.uint32, pairs, 2), o.buffers["pairs"][:pairs])
+    n = spec.particles
+    np.testing.assert_array_equal(gpu_buffer(g, "pairOffsets", np.uint32, n, 1), o.buffers["pairOffsets"][:n].reshape(n, 1))
