@@ -270,8 +270,8 @@ __global__ void __launch_bounds__(256) k_radixCount(const __grid_constant__ Para
 // Stable scatter of a tile: its elements in index order, 256 at a time; an
 // element's place is its digit's offset for the tile (the scanned counts),
 // plus the tile's earlier elements with that digit (a running count), plus
-// the earlier warps of this round with it, plus the lower lanes of its warp
-// with it (__match_any_sync).
+// the earlier warps of the same 256 with it, plus the lower lanes of its
+// warp with it (__match_any_sync).
 __global__ void __launch_bounds__(256) k_radixScatter(const __grid_constant__ Params P, uint32_t shift, uint32_t from) {
     __shared__ uint32_t offset[RADIX], warpCount[8][RADIX];
     const Res& r = P.r;
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(256) k_radixScatter(const __grid_constant__ Pa
             x.vals[from ^ 1u][place] = val;
         }
         __syncthreads();
-        // This round's elements of each digit move its offset on.
+        // These 256 elements of each digit move its offset on.
         uint32_t total = 0;
 #pragma unroll
         for (uint32_t w = 0; w < 8; ++w) {
