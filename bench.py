@@ -777,6 +777,115 @@ def run_reference(args):
         "e2e": {"value": value, "unit": "grain-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
+# Mesh-packing workload (the reference's startup, mesh.pack_meshes): not a
+# timestep workload, so it has its own line.
+PACK_WORKLOAD = "pack-53"
+PACK_CONFIG = dict(workload="pack-53-shapes-1M-nodes", shapes=53, distinct_grains=8, triangles_per_shape=32_000,
+                   nodes_per_shape=1 << 20, leaf_nodes=64, leaf_triangles=4,
+                   note="the reference profiles its startup at 53 shape roots and 2.4 million cluster-tree nodes")
+
+
+def tree_bytes(counts, leaf, key_bytes):
+    """Algorithmic DRAM bytes of one tree build: every level reads the key
+    (and box) of each item still in a node, and the stable sort of an internal
+    node reads and writes each item's index (4 + 4 bytes)."""
+    from sand_atlas_dem_gb300.trees import tree_levels
+
+    return sum(in_nodes * key_bytes + internal * 8 for in_nodes, internal, _, _ in tree_levels(counts, leaf))
+
+
+def run_packing(args, reference=False):
+    """Packs the 53-shape library: on the GPU (trees built by
+    sdg_median_trees, host parts on a thread pool) against the reference's
+    recursion on the host (packing.host_median_trees, byte-identical to
+    mesh.pack_meshes), timed on a bounded sample of one shape."""
+    from sand_atlas_dem_gb300.packing import pack_library
+    from sand_atlas_dem_gb300.shapes import ShapeLibrary
+    from sand_atlas_dem_gb300.workloads import packing_library
+
+    t = time.perf_counter()
+    lib = packing_library()
+    log("packing library generated in", round(time.perf_counter() - t, 1), "s")
+    nodes = sum(len(s.samples) for s in lib.shapes)
+    triangles = sum(len(s.faces) for s in lib.shapes)
+    config = dict(PACK_CONFIG, nodes=nodes, triangles=triangles)
+    unit = "sample nodes/s"
+
+    def host_sample():
+        one = ShapeLibrary(lib.shapes[:1])
+        t0 = time.perf_counter()
+        pack_library(one, 1e-3)
+        dt = time.perf_counter() - t0
+        return {"value": len(one.shapes[0].samples) / dt, "unit": unit, "cores": 1, "kind": "port",
+                "sample": f"one shape ({len(one.shapes[0].samples)} nodes, {len(one.shapes[0].faces)} triangles) "
+                          f"packed by the reference's recursion on the host in {dt:.2f} s"}
+
+    if reference:
+        base = host_sample()
+        return {"metric": "mesh packing throughput", "value": base["value"], "unit": unit, "impl": "reference",
+                "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": True, "data": "synthetic",
+                "dtype": "f32", "config": config, "cpu_baseline": base,
+                "e2e": {"value": base["value"], "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+    import torch
+
+    from sand_atlas_dem_gb300.trees import device_median_trees, tree_launches
+
+    timing = {}
+
+    def trees(items, leaf):
+        t0 = {}
+        out = device_median_trees(items, leaf, timing=t0)
+        timing[leaf] = t0["device_ms"]
+        return out
+
+    for _ in range(max(1, args.warmup)):
+        pack_library(ShapeLibrary(lib.shapes[:2]), 1e-3, trees=trees)
+    runs, device = [], []
+    steps = max(1, min(args.steps, 5))
+    with ClockSampler() as clocks:
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            packed = pack_library(lib, 1e-3, trees=trees)
+            runs.append(time.perf_counter() - t0)
+            device.append((timing[64], timing[4]))
+    wall = float(np.median(runs))
+    cluster_ms = float(np.median([d[0] for d in device]))
+    bvh_ms = float(np.median([d[1] for d in device]))
+    counts_nodes = [len(s.samples) for s in lib.shapes]
+    counts_tri = [len(s.faces) for s in lib.shapes]
+    alg = tree_bytes(counts_nodes, 64, 16)
+    peak, peak_kind = peaks()
+    achieved = alg / (cluster_ms * 1e-3) / 1e9
+    line = {
+        "metric": "mesh packing throughput", "value": nodes / ((cluster_ms + bvh_ms) * 1e-3), "unit": unit,
+        "n_gpus": 1, "steps": steps, "warmup": max(1, args.warmup), "ms_per_step": 1e3 * wall,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config,
+        "value_note": "value: nodes / device time of both tree builds (cluster tree and triangle BVH); "
+                      "e2e: nodes / wall time of the whole pack_library call (host parts, copies, trees)",
+        "e2e": {"value": nodes / wall, "unit": unit,
+                "h2d_bytes_per_step": 16 * (nodes + 3 * triangles), "d2h_bytes_per_step": None},
+        "trees_device_ms": {"cluster_tree": cluster_ms, "triangle_bvh": bvh_ms},
+        "pack_wall_s": runs,
+        "roofline": {"bound": "hbm", "kernel": "cluster-tree build (all levels)", "achieved": achieved,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "algorithmic_bytes": alg, "traffic": None},
+        "layout_nodes": int(len(packed["meshClusterRanges"])), "layout_bvh_nodes": int(len(packed["meshLinks"])),
+        "clocks": clocks.summary(),
+        "gpu_launches": steps * (tree_launches(counts_nodes, 64) + tree_launches(counts_tri, 4)),
+    }
+    line["e2e"]["d2h_bytes_per_step"] = int(4 * nodes + 4 * triangles + 36 * (len(packed["meshClusterRanges"])
+                                                                            + len(packed["meshLinks"])))
+    if args.no_cpu_baseline:
+        line["cpu_baseline"] = None
+    else:
+        line["cpu_baseline"] = host_sample()
+        line["speedup_over_host"] = {"device_trees": line["value"] / line["cpu_baseline"]["value"],
+                                     "e2e": line["e2e"]["value"] / line["cpu_baseline"]["value"]}
+    return line
+
+
 
 def main():
     p = argparse.ArgumentParser()
@@ -784,7 +893,7 @@ def main():
     p.add_argument("--steps", type=int, default=500)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
-    p.add_argument("--workload", default="dense-10k", choices=tuple(WORKLOADS))
+    p.add_argument("--workload", default="dense-10k", choices=tuple(WORKLOADS) + (PACK_WORKLOAD,))
     p.add_argument("--grains", type=int, default=None, help="dense-10k only: grains of the packing record")
     p.add_argument("--cpu-threads", type=int, default=os.cpu_count() or 1)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -802,6 +911,10 @@ def main():
                    help="steps of the long amortized window (default: the workload's run length; 0 skips it)")
     args = p.parse_args()
     rank = int(os.environ.get("RANK", "0"))
+    if args.workload == PACK_WORKLOAD:
+        if rank == 0:
+            print(json.dumps(run_packing(args, reference=args.impl == "reference")), flush=True)
+        return
     if args.impl == "reference":
         if args.steps > 20:
             args.steps = 20  # a bounded CPU sample: each oracle step of 10k grains takes a fraction of a second

@@ -274,6 +274,35 @@ int sdg_engine_kernels_per_step(void* engine);
  */
 int sdg_engine_branch_kernels(void* engine, int branch);
 
+/*
+ * The two median-split trees of the packed mesh layout, built on the device
+ * for every shape at once.  Replaces the host recursions of the reference's
+ * mesh.pack_meshes (src/sand_atlas_dem/mesh.py:33-56, the source-node
+ * cluster tree, leaf = 64; mesh.py:164-201, the triangle BVH, leaf = 4),
+ * whose results it reproduces bit for bit.
+ *
+ * Items of shape s are counts[s] consecutive rows of `keys` (float x, y, z,
+ * unused; finite), the split coordinates: sample points, or triangle centres
+ * (mean of the three FP32 vertices, as the reference computes it).  `low` and
+ * `high` (same layout) are each item's box, whose union bounds a node (the
+ * triangles' vertex minimum and maximum); both null: the box is the point.
+ * `counts` is a HOST array of `shapes` nonzero counts, at most 2^30 items in
+ * all.  Outputs, in preorder with the shapes one after another: `order` (one
+ * word per item: the item row at each position, leaves in preorder),
+ * `records` (4 words per node: escape = index past the node's subtree, first
+ * position and count for a leaf or 0, 0 for an internal node, depth) and
+ * `node_low`/`node_high` (4 floats per node: the bounds moved one ulp
+ * outward, then 0).  Nodes of shape s: sdg_median_tree_nodes(counts[s],
+ * leaf).  Scratch: sdg_median_trees_scratch(counts, shapes, leaf) bytes of
+ * device memory.  The call returns when the trees are built (it waits on
+ * `stream`).  Return codes as above.
+ */
+uint32_t sdg_median_tree_nodes(uint32_t items, uint32_t leaf);
+uint64_t sdg_median_trees_scratch(const uint32_t* counts, uint32_t shapes, uint32_t leaf);
+int sdg_median_trees(const float* keys, const float* low, const float* high, const uint32_t* counts, uint32_t shapes,
+                     uint32_t leaf, uint32_t* order, uint32_t* records, float* node_low, float* node_high,
+                     void* scratch, uint64_t scratch_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

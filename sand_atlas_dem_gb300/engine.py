@@ -30,6 +30,7 @@ from .model import (
     f4,
 )
 from .spec import finite_array
+from .trees import device_median_trees
 
 # Launch shapes the autotuner sets (values after the extension values; 0 =
 # built-in default).  They never change results.
@@ -207,7 +208,7 @@ class Engine:
         phase: ``specimens`` is a sequence of (positions, cell, shape_ids,
         scales).  Per-specimen cell rates are set with ``advance(rate=...)``
         given one row per specimen."""
-        layout = HostLayout.batch(library, spec, specimens)
+        layout = HostLayout.batch(library, spec, specimens, trees=device_median_trees)
         return cls(library, spec, None, None, None, None, layout=layout, **kwargs)
 
     def __init__(self, library, spec, positions, cell, shape_ids, scales, *, metal=None, device=None,
@@ -220,7 +221,8 @@ class Engine:
         self.lib = native.load()
         if self.lib.sdg_buffer_count() != len(BUFFER_ORDER):
             raise RuntimeError("GB300 library buffer ABI mismatch")
-        self.layout = h = layout or HostLayout(library, spec, positions, cell, shape_ids, scales)
+        self.layout = h = layout or HostLayout(library, spec, positions, cell, shape_ids, scales,
+                                               trees=device_median_trees)
         self.specimens = h.specimens
         self.spec, self.library, self.n = spec, library, h.n
         self.viscous = spec.viscous
@@ -488,7 +490,8 @@ class Engine:
                 ]
                 replacement = Engine(
                     self.library, replace(old, **settings), None, None, None, None,
-                    layout=HostLayout.batch(self.library, replace(old, **settings), specimens),
+                    layout=HostLayout.batch(self.library, replace(old, **settings), specimens,
+                                            trees=device_median_trees),
                     device=self.device, use_graph=self.use_graph, distance_grid=self.distance_grid,
                     filter_margin=self.filter_margin,
                 )

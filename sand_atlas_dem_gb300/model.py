@@ -15,7 +15,7 @@ import math
 import numpy as np
 
 from .boundaries import box_extents
-from .packing import pack_library
+from .packing import host_median_trees, pack_library
 from .spec import finite_array
 
 ERRORS = {
@@ -122,7 +122,7 @@ class HostLayout:
     """
 
     @classmethod
-    def batch(cls, library, spec, specimens):
+    def batch(cls, library, spec, specimens, trees=host_median_trees):
         """``specimens``: sequence of (positions, cell, shape_ids, scales)."""
         specimens = list(specimens)
         if not specimens:
@@ -132,9 +132,13 @@ class HostLayout:
         scales = np.concatenate([np.asarray(s[3], float) for s in specimens])
         cells = np.array([finite_array(s[1], (3,), positive=True) for s in specimens])
         counts = [len(s[0]) for s in specimens]
-        return cls(library, spec, positions, cells[0], ids, scales, cells=cells, counts=counts)
+        return cls(library, spec, positions, cells[0], ids, scales, cells=cells, counts=counts, trees=trees)
 
-    def __init__(self, library, spec, positions, cell, shape_ids, scales, *, cells=None, counts=None):
+    def __init__(self, library, spec, positions, cell, shape_ids, scales, *, cells=None, counts=None,
+                 trees=host_median_trees):
+        # Builder of the packed layout's median-split trees (host recursion,
+        # or the GPU builder the engine passes); the bytes are the same.
+        self.trees = trees
         positions = finite_array(positions)
         cell = finite_array(cell, (3,), positive=True)
         if cells is None:
@@ -282,7 +286,7 @@ class HostLayout:
         l = self.length_unit
         if self.spec.contact_geometry == "sdf":
             return self._sdf_geometry()
-        data = pack_library(self.library, self.length_unit)
+        data = pack_library(self.library, self.length_unit, trees=self.trees)
         info, samples, offset = [], [], 0
         for s in self.library.shapes:
             info.append([offset, len(s.samples), 0, 0])

@@ -16,7 +16,7 @@ PACKAGE = Path(__file__).resolve().parent
 CSRC = PACKAGE / "csrc"
 LIBDIR = PACKAGE / "_lib"
 LIBRARY = LIBDIR / "libsanddem_gb300.so"
-SOURCES = ("kernels_state.cu", "kernels_contacts.cu", "capi.cu", "culler.cu", "scan_static.cu")
+SOURCES = ("kernels_state.cu", "kernels_contacts.cu", "capi.cu", "culler.cu", "scan_static.cu", "trees.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false keeps the reference's FP32 operation order (no contraction);
 # division and square root stay IEEE (no fast math).
@@ -121,6 +121,12 @@ def load():
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = ct.c_int
+    lib.sdg_median_tree_nodes.argtypes = [U, U]
+    lib.sdg_median_tree_nodes.restype = U
+    lib.sdg_median_trees_scratch.argtypes = [V, U, U]
+    lib.sdg_median_trees_scratch.restype = ct.c_uint64
+    lib.sdg_median_trees.argtypes = [V, V, V, V, U, U, V, V, V, V, V, ct.c_uint64, V]
+    lib.sdg_median_trees.restype = ct.c_int
     lib.sdg_engine_kernels_per_step.argtypes = [ct.c_void_p]
     lib.sdg_engine_kernels_per_step.restype = ct.c_int
     lib.sdg_engine_branch_kernels.argtypes = [ct.c_void_p, ct.c_int]
@@ -165,6 +171,9 @@ EXPORTS = (
     "sdg_culler_inside_max",
     "sdg_culler_inside_max_cells",
     "sdg_culler_margin_cells",
+    "sdg_median_tree_nodes",
+    "sdg_median_trees_scratch",
+    "sdg_median_trees",
 )
 PHASES = ("drift", "neighbours", "pair_cull", "node_filter", "node_query", "contact_emit", "friction_and_history",
           "force_reduction", "final_kick")

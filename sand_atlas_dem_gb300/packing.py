@@ -23,6 +23,9 @@ and ``meshChildren``, the triangle BVH re-laid as one record per node holding
 both children's bounds (see :func:`child_records`).
 """
 
+import os
+from concurrent.futures import ThreadPoolExecutor
+
 import numpy as np
 from scipy.sparse import coo_matrix
 from scipy.sparse.csgraph import connected_components
@@ -57,32 +60,50 @@ def _up(x):
     return np.nextafter(x, F32(np.inf))
 
 
-class _ClusterTree:
-    """Preorder median-split tree over FP32 node coordinates."""
+def host_median_trees(items, leaf):
+    """Median-split trees over every shape, by the reference's recursion
+    (``mesh.py:33-56`` with leaf 64, ``mesh.py:164-201`` with leaf 4): a node
+    over more than ``leaf`` items sorts them stably along the axis of largest
+    key extent and gives the first half to its left child; its bounds are the
+    items' boxes' FP32 minimum and maximum, one ulp outward.
 
-    def __init__(self, points, first_sample):
-        self.points = points
-        self.ranges, self.low, self.high, self.order = [], [], [], []
-        self.first_sample = first_sample
-        self._split(np.arange(len(points)))
+    ``items``: per shape ``(keys, low, high)``, FP32 (n, 3) arrays (``low`` and
+    ``high`` None: the boxes are the key points).  Returns ``order`` (per
+    position, the item's row within its shape; shapes one after another),
+    ``records`` (per preorder node: escape index, first position and count of
+    a leaf or 0, 0, depth) and the node bounds ``low``/``high`` (nodes, 4).
+    :func:`device_median_trees` (``trees.py``) builds the same on the GPU.
+    """
+    records, low_out, high_out, order = [], [], [], []
+    for keys, low, high in items:
+        keys = np.asarray(keys, F32)
+        low = keys if low is None else np.asarray(low, F32)
+        high = keys if high is None else np.asarray(high, F32)
 
-    def _split(self, ids):
-        node = len(self.ranges)
-        self.ranges.append([0, 0, 0, 0])
-        p = self.points[ids]
-        self.low.append([*_down(p.min(0)), 0])
-        self.high.append([*_up(p.max(0)), 0])
-        if len(ids) > 64:
-            axis = np.ptp(p, axis=0).argmax()
-            ordered = ids[np.argsort(p[:, axis], kind="stable")]
-            half = len(ordered) // 2
-            self._split(ordered[:half])
-            self._split(ordered[half:])
-        else:
-            self.ranges[node][0] = self.first_sample + len(self.order)
-            self.ranges[node][1] = len(ids)
-            self.order.extend(ids.tolist())
-        self.ranges[node][2] = len(self.ranges)
+        def split(ids, depth):
+            node = len(records)
+            records.append([0, 0, 0, depth])
+            low_out.append(_down(low[ids].min(0)))
+            high_out.append(_up(high[ids].max(0)))
+            if len(ids) > leaf:
+                k = keys[ids]
+                axis = np.ptp(k, axis=0).argmax()
+                ids = ids[np.argsort(k[:, axis], kind="stable")]
+                half = len(ids) // 2
+                split(ids[:half], depth + 1)
+                split(ids[half:], depth + 1)
+            else:
+                records[node][1] = len(order)
+                records[node][2] = len(ids)
+                order.extend(ids.tolist())
+            records[node][0] = len(records)
+
+        split(np.arange(len(keys)), 0)
+
+    def rows(a):
+        return np.pad(np.asarray(a, F32).reshape(-1, 3), ((0, 0), (0, 1)))
+
+    return np.asarray(order, np.uint32), np.asarray(records, np.uint32).reshape(-1, 4), rows(low_out), rows(high_out)
 
 
 def _frontier(ranges, base):
@@ -128,9 +149,13 @@ def _feature_normals(vertices, faces):
     vertex_normal = np.zeros_like(vertices)
     np.add.at(vertex_normal, faces.ravel(), (face_normal[:, None, :] * angle[:, :, None]).reshape(-1, 3))
     edges = faces[:, [[0, 1], [1, 2], [2, 0]]].reshape(-1, 2)
-    unique, inverse, count = np.unique(
-        np.sort(edges, axis=1), axis=0, return_inverse=True, return_counts=True
-    )
+    # Unique undirected edges in lexicographic (low, high) order, as
+    # np.unique(rows, axis=0) orders them, through one int64 key per edge.
+    ordered = np.sort(edges, axis=1)
+    stride = int(faces.max()) + 1
+    keys, inverse, count = np.unique(ordered[:, 0] * stride + ordered[:, 1], return_inverse=True,
+                                     return_counts=True)
+    unique = np.column_stack([keys // stride, keys % stride])
     if np.any(count != 2):
         raise ValueError("Mesh query requires exactly two faces per edge")
     direction = np.where(edges[:, 0] < edges[:, 1], 1, -1)
@@ -162,80 +187,92 @@ def _feature_normals(vertices, faces):
     return feature / length[:, :, None]
 
 
-class _TriangleTree:
-    """Preorder median-split BVH over FP32 triangles (<= 4 per leaf)."""
-
-    def __init__(self, tri, first_node, first_triangle):
-        self.tri = tri
-        self.first_node, self.first_triangle = first_node, first_triangle
-        self.low, self.high, self.links, self.order, self.depth = [], [], [], [], 0
-        self._build(np.arange(len(tri)), 0)
-
-    def _build(self, ids, depth):
-        node = len(self.links)
-        self.depth = max(self.depth, depth)
-        t = self.tri[ids]
-        self.low.append([*_down(t.min(axis=(0, 1))), 0])
-        self.high.append([*_up(t.max(axis=(0, 1))), 0])
-        self.links.append([0, 0, 0, 0])
-        if len(ids) <= 4:
-            self.links[node][1] = self.first_triangle + len(self.order)
-            self.links[node][2] = len(ids)
-            self.order.extend(ids.tolist())
-        else:
-            centres = t.mean(axis=1)
-            axis = np.ptp(centres, axis=0).argmax()
-            ids = ids[np.argsort(centres[:, axis], kind="stable")]
-            half = len(ids) // 2
-            self._build(ids[:half], depth + 1)
-            self._build(ids[half:], depth + 1)
-        self.links[node][0] = self.first_node + len(self.links)
+def _prepare(shape, length_unit):
+    """One shape's host-side parts: FP32 sample points, hull plane groups,
+    feature pseudonormals and FP32 triangles (``mesh.py:21-162``)."""
+    if shape.provenance.get("display_mesh_only"):
+        raise ValueError("Mesh query requires physical source triangles, not a display-only fixture mesh")
+    vertices = np.asarray(shape.vertices, float) / length_unit
+    faces = np.asarray(shape.faces, np.int64)
+    points = (np.asarray(shape.samples) / length_unit).astype(F32)
+    if len(points) == 0 or not np.all(np.isfinite(points)):
+        raise ValueError("Shape samples must be finite and nonempty")
+    hull = _hull_groups(vertices)
+    feature = _feature_normals(vertices, faces)
+    tri = vertices[faces].astype(F32)
+    if not np.all(np.isfinite(tri)):
+        raise ValueError("Shape vertices must be finite")
+    if np.any(np.linalg.norm(np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]), axis=1) == 0):
+        raise ValueError("Triangle degenerates in normalized FP32")
+    return points, hull, feature, tri
 
 
-def pack_library(library, length_unit):
-    """Pack every shape; returns uint32/float32 arrays keyed by buffer name."""
+def pack_library(library, length_unit, trees=host_median_trees):
+    """Pack every shape; returns uint32/float32 arrays keyed by buffer name.
+
+    ``trees`` builds the two median-split trees of all shapes at once
+    (:func:`host_median_trees`, or the GPU builder
+    ``trees.device_median_trees``; both give the same bytes).  Triangle
+    centres are the mean of the three FP32 vertices, computed per triangle
+    as the reference computes them per subset (``mesh.py:191``).
+    """
     out = {k: [] for k in UINT_ARRAYS + FLOAT_ARRAYS}
-    leaf_info, leaves, ranks = [], [], []
-    for shape in library.shapes:
-        if shape.provenance.get("display_mesh_only"):
-            raise ValueError(
-                "Mesh query requires physical source triangles, not a display-only fixture mesh"
-            )
-        vertices = np.asarray(shape.vertices, float) / length_unit
-        faces = np.asarray(shape.faces, np.int64)
-        points = (np.asarray(shape.samples) / length_unit).astype(F32)
-        base = len(out["meshClusterRanges"])
-        tree = _ClusterTree(points, len(out["meshSampleIndices"]))
-        ranges = tree.ranges
-        out["meshClusterInfo"].append([base, len(ranges), 0, 0])
-        out["meshFrontier"].extend(_frontier(ranges, base))
-        # Stored escape links are absolute cluster indices.
-        out["meshClusterRanges"].extend([[r[0], r[1], base + r[2], 0] for r in ranges])
-        out["meshClusterMin"].extend(tree.low)
-        out["meshClusterMax"].extend(tree.high)
-        out["meshSampleIndices"].extend(tree.order)
-        shape_leaves = [base + n for n, r in enumerate(ranges) if r[1] > 0]
-        leaf_info.append([len(leaves), len(shape_leaves), 0, 0])
-        leaves.extend(shape_leaves)
-        rank = np.empty(len(points), np.uint32)
-        rank[np.asarray(tree.order, np.int64)] = np.arange(len(points), dtype=np.uint32)
-        ranks.append(rank)
-        for subset in _hull_groups(vertices):
+    # The per-shape host work (hull, pseudonormals, manifold checks) is
+    # independent between shapes: prepared on a thread pool, kept in order.
+    with ThreadPoolExecutor(max_workers=min(len(library.shapes), os.cpu_count() or 1)) as pool:
+        prepared = list(pool.map(lambda shape: _prepare(shape, length_unit), library.shapes))
+    sample_items, triangle_items, tris, features = [], [], [], []
+    for points, hull, feature, tri in prepared:
+        sample_items.append((points, None, None))
+        for subset in hull:
             out["meshHullInfo"].append([len(out["meshPlanes"]), len(subset), 0, 0])
             out["meshPlanes"].extend(subset)
-        feature = _feature_normals(vertices, faces)
-        tri = vertices[faces].astype(F32)
-        if np.any(np.linalg.norm(np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]), axis=1) == 0):
-            raise ValueError("Triangle degenerates in normalized FP32")
-        bvh = _TriangleTree(tri, len(out["meshLinks"]), len(out["meshTriangles"]) // 3)
-        if bvh.depth > 30:
+        features.append(feature)
+        tris.append(tri)
+        triangle_items.append((tri.mean(axis=1), tri.min(axis=1), tri.max(axis=1)))
+
+    sample_order, cluster, cluster_low, cluster_high = trees(sample_items, 64)
+    tri_order, links, tri_low, tri_high = trees(triangle_items, 4)
+
+    leaf_info, leaves, ranks = [], [], []
+    node, item = 0, 0
+    for points, _, _ in sample_items:
+        n = len(points)
+        count = int(cluster[node, 0]) - node  # the root's escape link
+        ranges = cluster[node:node + count]
+        out["meshClusterInfo"].append([node, count, 0, 0])
+        # (first, count, escape) with the escape link local to the shape.
+        local = np.column_stack([ranges[:, 1], ranges[:, 2], ranges[:, 0] - node]).astype(np.int64)
+        out["meshFrontier"].extend(_frontier(local, node))
+        shape_leaves = node + np.flatnonzero(ranges[:, 2] > 0)
+        leaf_info.append([len(leaves), len(shape_leaves), 0, 0])
+        leaves.extend(shape_leaves.tolist())
+        rank = np.empty(n, np.uint32)
+        rank[sample_order[item:item + n].astype(np.int64)] = np.arange(n, dtype=np.uint32)
+        ranks.append(rank)
+        node += count
+        item += n
+    out["meshClusterRanges"] = np.column_stack(
+        [cluster[:, 1], cluster[:, 2], cluster[:, 0], np.zeros(len(cluster), np.uint32)])
+    out["meshClusterMin"] = cluster_low
+    out["meshClusterMax"] = cluster_high
+    out["meshSampleIndices"] = sample_order
+
+    node, item = 0, 0
+    for tri, feature in zip(tris, features):
+        count = int(links[node, 0]) - node
+        depth = int(links[node:node + count, 3].max())
+        if depth > 30:
             raise ValueError("Mesh hierarchy exceeds GPU traversal stack depth")
-        out["meshRoots"].append([bvh.first_node, bvh.first_node + len(bvh.links), bvh.depth, 0])
-        out["meshMin"].extend(bvh.low)
-        out["meshMax"].extend(bvh.high)
-        out["meshLinks"].extend(bvh.links)
-        out["meshTriangles"].extend(tri[bvh.order].reshape(-1, 3))
-        out["meshNormals"].extend(feature[bvh.order].reshape(-1, 3))
+        out["meshRoots"].append([node, node + count, depth, 0])
+        rows = tri_order[item:item + len(tri)].astype(np.int64)
+        out["meshTriangles"].append(tri[rows].reshape(-1, 3))
+        out["meshNormals"].append(feature[rows].reshape(-1, 3))
+        node += count
+        item += len(tri)
+    out["meshLinks"] = np.column_stack([links[:, :3], np.zeros(len(links), np.uint32)])
+    out["meshMin"] = tri_low
+    out["meshMax"] = tri_high
 
     def f4(a):
         a = np.asarray(a, F32).reshape(-1, 3)
@@ -243,12 +280,12 @@ def pack_library(library, length_unit):
 
     packed = {}
     for name in UINT_ARRAYS:
-        packed[name] = np.asarray(out[name], np.uint32)
+        packed[name] = np.ascontiguousarray(np.asarray(out[name], np.uint32))
     for name in FLOAT_ARRAYS:
         if name in ("meshTriangles", "meshNormals"):
-            packed[name] = f4(out[name])
+            packed[name] = f4(np.concatenate(out[name]))
         else:
-            packed[name] = np.asarray(out[name], F32)
+            packed[name] = np.ascontiguousarray(np.asarray(out[name], F32))
     packed["meshLeafInfo"] = np.asarray(leaf_info, np.uint32)
     packed["meshLeaves"] = np.asarray(leaves, np.uint32)
     packed["meshSampleRank"] = np.concatenate(ranks).astype(np.uint32)

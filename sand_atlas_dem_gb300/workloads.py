@@ -532,3 +532,22 @@ def main(argv=None):
 
 if __name__ == "__main__":
     main()
+
+
+def packing_library(shapes=53, distinct=8, frequency=40, nodes=1 << 20, seed=3000):
+    """The mesh-packing workload: ``shapes`` rough grains (perturbed
+    icospheres of ``frequency``, 20 x frequency^2 triangles) with ``nodes``
+    surface sample nodes each, built from ``distinct`` seeded grains repeated
+    under their own ids (packing cost does not depend on which grain repeats).
+    53 shapes of about a million nodes is the size of the startup whose
+    host packing the reference profiles (``docs/RUNTIME_PROFILING.md:62-65``:
+    53 shape roots, 2.4 million cluster-tree nodes)."""
+    from dataclasses import replace
+
+    from .shapes import ShapeLibrary, perturbed_grain
+
+    rng = np.random.default_rng(seed)
+    base = [perturbed_grain(frequency, seed=seed + k, nodes=nodes, axes=rng.uniform(0.6, 1.0, 3))
+            for k in range(min(distinct, shapes))]
+    return ShapeLibrary([replace(base[k % len(base)], id=f"{base[k % len(base)].id}-copy{k}")
+                         for k in range(shapes)])

@@ -106,3 +106,30 @@ def test_plane_configurations_are_checked_before_any_launch(library):
     # 3 x planes x grains rows must fit the 32-bit row index.
     rc, message = dispatch(dict(config, periodic=0.0, N=float(1 << 30)), extra, large)
     assert rc == 1 and b"2^32" in message
+
+
+@pytest.mark.parametrize("leaf", [4, 64])
+def test_tree_node_counts_match_the_recursion(leaf):
+    """``sdg_median_tree_nodes`` (host arithmetic, no device call) against the
+    node count of the reference recursion on the same item count."""
+    import numpy as np
+
+    from sand_atlas_dem_gb300.packing import host_median_trees
+
+    lib = native.load()
+    rng = np.random.default_rng(leaf)
+    for n in (1, leaf, leaf + 1, 2 * leaf + 1, 257, 1000, 4099):
+        _, records, _, _ = host_median_trees([(rng.normal(size=(n, 3)).astype(np.float32), None, None)], leaf)
+        assert lib.sdg_median_tree_nodes(n, leaf) == len(records) == records[0, 0]
+    assert lib.sdg_median_tree_nodes(0, leaf) == 0
+
+
+def test_tree_scratch_rejects_empty_shapes():
+    import numpy as np
+
+    lib = native.load()
+    counts = np.array([10, 0, 5], np.uint32)
+    assert lib.sdg_median_trees_scratch(counts.ctypes.data_as(ct.c_void_p), 3, 64) == 0
+    assert b"no items" in lib.sdg_last_error()
+    counts = np.array([10, 3000], np.uint32)
+    assert lib.sdg_median_trees_scratch(counts.ctypes.data_as(ct.c_void_p), 2, 64) > 0

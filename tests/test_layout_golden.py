@@ -34,6 +34,19 @@ def test_packing_matches_reference_bytes():
             assert ours[name].tobytes() == ref[name].tobytes(), name
 
 
+def test_tree_arrays_match_reference_bytes():
+    """``golden/packing_trees.npz``: the reference's trees over 3,000 sample
+    nodes and 2,880 triangles, and over coordinates with many ties and signed
+    zeros (the stable sort's order decides the node keys' leaves)."""
+    from tests.golden.make_golden import stored_tree_shapes
+
+    ours = pack_library(ShapeLibrary(stored_tree_shapes()), 1e-3)
+    with np.load(GOLDEN / "packing_trees.npz") as ref:
+        for name in (f for f in ref.files if f.startswith("mesh")):
+            assert ours[name].dtype == ref[name].dtype and ours[name].shape == ref[name].shape, name
+            assert ours[name].tobytes() == ref[name].tobytes(), name
+
+
 def test_leaf_tables_cover_every_node_once():
     packed = pack_library(ShapeLibrary(shapes()), 1e-3)
     ranges = packed["meshClusterRanges"]
