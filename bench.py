@@ -804,11 +804,11 @@ def run_packing(args, reference=False):
     from sand_atlas_dem_gb300.workloads import packing_library
 
     t = time.perf_counter()
-    lib = packing_library()
+    lib = packing_library(shapes=args.pack_shapes)
     log("packing library generated in", round(time.perf_counter() - t, 1), "s")
     nodes = sum(len(s.samples) for s in lib.shapes)
     triangles = sum(len(s.faces) for s in lib.shapes)
-    config = dict(PACK_CONFIG, nodes=nodes, triangles=triangles)
+    config = dict(PACK_CONFIG, shapes=len(lib.shapes), nodes=nodes, triangles=triangles)
     unit = "sample nodes/s"
 
     def host_sample():
@@ -836,7 +836,7 @@ def run_packing(args, reference=False):
     def trees(items, leaf):
         t0 = {}
         out = device_median_trees(items, leaf, timing=t0)
-        timing[leaf] = t0["device_ms"]
+        timing[leaf] = t0
         return out
 
     for _ in range(max(1, args.warmup)):
@@ -848,7 +848,17 @@ def run_packing(args, reference=False):
             t0 = time.perf_counter()
             packed = pack_library(lib, 1e-3, trees=trees)
             runs.append(time.perf_counter() - t0)
-            device.append((timing[64], timing[4]))
+            device.append((timing[64]["device_ms"], timing[4]["device_ms"],
+                           timing[64]["wall_ms"] + timing[4]["wall_ms"]))
+    # The per-shape host stage alone (hull, pseudonormals, checks; thread pool).
+    from concurrent.futures import ThreadPoolExecutor
+
+    from sand_atlas_dem_gb300.packing import _prepare
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=min(len(lib.shapes), os.cpu_count() or 1)) as pool:
+        list(pool.map(lambda shape: _prepare(shape, 1e-3), lib.shapes))
+    prepare_s = time.perf_counter() - t0
     wall = float(np.median(runs))
     cluster_ms = float(np.median([d[0] for d in device]))
     bvh_ms = float(np.median([d[1] for d in device]))
@@ -868,6 +878,9 @@ def run_packing(args, reference=False):
                 "h2d_bytes_per_step": 16 * (nodes + 3 * triangles), "d2h_bytes_per_step": None},
         "trees_device_ms": {"cluster_tree": cluster_ms, "triangle_bvh": bvh_ms},
         "pack_wall_s": runs,
+        "pack_parts_s": {"shape_preparation": prepare_s,
+                         "tree_builder_calls": float(np.median([d[2] for d in device])) / 1e3,
+                         "host_threads": os.cpu_count()},
         "roofline": {"bound": "hbm", "kernel": "cluster-tree build (all levels)", "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes": alg, "traffic": None},
@@ -907,6 +920,8 @@ def main():
                         "the neighbour-build and filter-build kernels then launch and return at once on the "
                         "steps that skip them)")
     p.add_argument("--no-plain", action="store_true", help="skip the plain-path comparison")
+    p.add_argument("--pack-shapes", type=int, default=53,
+                   help="pack-53 only: shapes of the packing library (53 = the reference's profiled startup)")
     p.add_argument("--window", type=int, default=None,
                    help="steps of the long amortized window (default: the workload's run length; 0 skips it)")
     args = p.parse_args()

@@ -288,7 +288,8 @@ int sdg_engine_branch_kernels(void* engine, int branch);
  * triangles' vertex minimum and maximum); both null: the box is the point.
  * `counts` is a HOST array of `shapes` nonzero counts, at most 2^30 items in
  * all.  Outputs, in preorder with the shapes one after another: `order` (one
- * word per item: the item row at each position, leaves in preorder),
+ * word per item position: the row, within its shape, of the item placed
+ * there; leaves in preorder),
  * `records` (4 words per node: escape = index past the node's subtree, first
  * position and count for a leaf or 0, 0 for an internal node, depth) and
  * `node_low`/`node_high` (4 floats per node: the bounds moved one ulp

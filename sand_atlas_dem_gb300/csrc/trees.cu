@@ -99,6 +99,20 @@ __global__ void k_treeIota(uint32_t* order, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) order[i] = i;
 }
 
+// Turns each position's item index into its row within its shape: the
+// shape is the last whose first item is at or before the position (items
+// never leave their shape).
+__global__ void k_treeLocal(uint32_t* order, uint32_t n, const uint32_t* firsts, uint32_t shapes) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = shapes - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) / 2;
+            if (firsts[mid] <= p) lo = mid; else hi = mid - 1;
+        }
+        order[p] -= firsts[lo];
+    }
+}
+
 // Partial extents of one piece of one node: key minimum and maximum, box
 // minimum and maximum (12 floats).  Warp w handles piece w % parts of entry
 // w / parts.  `low`/`high` null: the boxes are the keys (single points).
@@ -119,15 +133,28 @@ __global__ void __launch_bounds__(256) k_treeReduce(const Entry* level, uint32_t
         a[c] = a[6 + c] = INFINITY;
         a[3 + c] = a[9 + c] = -INFINITY;
     }
-    for (uint32_t p = begin + lane; p < end; p += 32) {
-        const uint32_t id = order[p];
-        const float4 k = keys[id];
-        const float4 l = low ? low[id] : k;
-        const float4 h = high ? high[id] : k;
-        a[0] = fminf(a[0], k.x); a[1] = fminf(a[1], k.y); a[2] = fminf(a[2], k.z);
-        a[3] = fmaxf(a[3], k.x); a[4] = fmaxf(a[4], k.y); a[5] = fmaxf(a[5], k.z);
-        a[6] = fminf(a[6], l.x); a[7] = fminf(a[7], l.y); a[8] = fminf(a[8], l.z);
-        a[9] = fmaxf(a[9], h.x); a[10] = fmaxf(a[10], h.y); a[11] = fmaxf(a[11], h.z);
+    // Four items a lane per round: their index loads, then their key (and
+    // box) gathers, issued back to back.
+    for (uint32_t base = begin + lane; base < end; base += 128) {
+        uint32_t id[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) id[u] = base + 32 * u < end ? order[base + 32 * u] : 0xffffffffu;
+        float4 k[4], l[4], h[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (id[u] == 0xffffffffu) continue;
+            k[u] = keys[id[u]];
+            l[u] = low ? low[id[u]] : k[u];
+            h[u] = high ? high[id[u]] : k[u];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (id[u] == 0xffffffffu) continue;
+            a[0] = fminf(a[0], k[u].x); a[1] = fminf(a[1], k[u].y); a[2] = fminf(a[2], k[u].z);
+            a[3] = fmaxf(a[3], k[u].x); a[4] = fmaxf(a[4], k[u].y); a[5] = fmaxf(a[5], k[u].z);
+            a[6] = fminf(a[6], l[u].x); a[7] = fminf(a[7], l[u].y); a[8] = fminf(a[8], l[u].z);
+            a[9] = fmaxf(a[9], h[u].x); a[10] = fmaxf(a[10], h[u].y); a[11] = fmaxf(a[11], h[u].z);
+        }
     }
 #pragma unroll
     for (int off = 16; off; off >>= 1) {
@@ -231,16 +258,22 @@ __global__ void __launch_bounds__(256) k_treeCount(const Entry* large, uint32_t 
     hist[threadIdx.x] = 0;
     __syncthreads();
     const uint32_t shift = 8 * pass;
-    for (uint32_t p = begin + threadIdx.x; p < end; p += 256) {
-        uint32_t k;
+    // A thread's (at most) 8 items: loads first, then the histogram.
+    uint32_t k[TILE / 256];
+#pragma unroll
+    for (int j = 0; j < int(TILE / 256); ++j) {
+        const uint32_t p = begin + j * 256 + threadIdx.x;
+        if (p >= end) continue;
         if (pass == 0) {
-            k = sortable(component(keys[order[p]], e.axis));
-            key0[p] = k;
+            k[j] = sortable(component(keys[order[p]], e.axis));
+            key0[p] = k[j];
         } else {
-            k = keySrc[p];
+            k[j] = keySrc[p];
         }
-        atomicAdd(&hist[(k >> shift) & (RADIX - 1)], 1u);
     }
+#pragma unroll
+    for (int j = 0; j < int(TILE / 256); ++j)
+        if (begin + j * 256 + threadIdx.x < end) atomicAdd(&hist[(k[j] >> shift) & (RADIX - 1)], 1u);
     __syncthreads();
     counts[uint64_t(blockIdx.x) * RADIX + threadIdx.x] = hist[threadIdx.x];
 }
@@ -274,48 +307,75 @@ __global__ void __launch_bounds__(256) k_treeOffsets(const Entry* large, uint32_
     }
 }
 
-// Stable scatter of a tile: its items in index order, 256 at a time; an
-// item's place is its digit's running place for the tile, plus the earlier
-// warps' items of that digit among these 256, plus the lower lanes of its
-// warp with that digit (__match_any_sync).
+// Lanes of the warp whose digit equals this lane's: one ballot per digit
+// bit, plus one on validity (invalid lanes match only each other).
+__device__ __forceinline__ uint32_t sameDigit(uint32_t digit, bool valid) {
+    uint32_t peers = __ballot_sync(0xffffffffu, valid);
+    if (!valid) peers = ~peers;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const bool bit = (digit >> b) & 1u;
+        const uint32_t set = __ballot_sync(0xffffffffu, bit);
+        peers &= bit ? set : ~set;
+    }
+    return peers;
+}
+
+// Stable scatter of a tile.  Warp w holds the tile's items w*256 .. w*256+255
+// (8 a lane, loaded first, kept in registers) and ranks them among its own
+// items of the same digit: earlier sub-rounds through its shared histogram,
+// lower lanes of the same sub-round through the digit match.  A prefix over
+// the warps of each digit's count, from the tile's place for that digit, then
+// gives each warp its first place per digit.
 __global__ void __launch_bounds__(256) k_treeScatter(const Entry* large, uint32_t tiles, uint32_t pass,
                                                      const uint32_t* counts, const uint32_t* keySrc,
                                                      const uint32_t* orderSrc, uint32_t* keyDst, uint32_t* orderDst) {
-    __shared__ uint32_t offset[RADIX], warpCount[8][RADIX];
+    __shared__ uint32_t hist[8][RADIX];
     const Entry e = large[blockIdx.x / tiles];
     const uint32_t tile = blockIdx.x % tiles;
     if (uint64_t(tile) * TILE >= e.count) return;
     const uint32_t begin = e.start + tile * TILE, end = e.start + min(e.count, (tile + 1) * TILE);
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    offset[threadIdx.x] = counts[uint64_t(blockIdx.x) * RADIX + threadIdx.x];
+    const uint32_t first = begin + warp * 256 + lane;
+    uint32_t key[8], id[8], rank[8];
 #pragma unroll
-    for (int w = 0; w < 8; ++w) warpCount[w][threadIdx.x] = 0;
+    for (int j = 0; j < 8; ++j) {
+        const uint32_t p = first + j * 32;
+        key[j] = p < end ? keySrc[p] : 0u;
+        id[j] = p < end ? orderSrc[p] : 0u;
+    }
+#pragma unroll
+    for (int w = 0; w < 8; ++w) hist[w][threadIdx.x] = 0;
     __syncthreads();
     const uint32_t shift = 8 * pass;
-    for (uint32_t base = begin; base < end; base += 256) {
-        const uint32_t p = base + threadIdx.x;
-        const bool valid = p < end;
-        const uint32_t k = valid ? keySrc[p] : 0u;
-        const uint32_t digit = valid ? (k >> shift) & (RADIX - 1) : RADIX;
-        const uint32_t peers = __match_any_sync(0xffffffffu, digit);
-        const uint32_t below = __popc(peers & ((1u << lane) - 1u));
-        if (valid && below == 0) warpCount[warp][digit] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            uint32_t place = offset[digit] + below;
-            for (uint32_t w = 0; w < warp; ++w) place += warpCount[w][digit];
-            keyDst[place] = k;
-            orderDst[place] = orderSrc[p];
-        }
-        __syncthreads();
-        uint32_t moved = 0;
 #pragma unroll
-        for (int w = 0; w < 8; ++w) {
-            moved += warpCount[w][threadIdx.x];
-            warpCount[w][threadIdx.x] = 0;
+    for (int j = 0; j < 8; ++j) {
+        const bool valid = first + j * 32 < end;
+        const uint32_t digit = (key[j] >> shift) & (RADIX - 1);
+        const uint32_t peers = sameDigit(digit, valid);
+        const uint32_t below = __popc(peers & ((1u << lane) - 1u));
+        const uint32_t before = valid ? hist[warp][digit] : 0u;
+        __syncwarp();
+        if (valid && below == 0) hist[warp][digit] = before + __popc(peers);
+        __syncwarp();
+        rank[j] = before + below;
+    }
+    __syncthreads();
+    uint32_t run = counts[uint64_t(blockIdx.x) * RADIX + threadIdx.x];
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+        const uint32_t c = hist[w][threadIdx.x];
+        hist[w][threadIdx.x] = run;
+        run += c;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (first + j * 32 < end) {
+            const uint32_t place = hist[warp][(key[j] >> shift) & (RADIX - 1)] + rank[j];
+            keyDst[place] = key[j];
+            orderDst[place] = id[j];
         }
-        offset[threadIdx.x] += moved;
-        __syncthreads();
     }
 }
 
@@ -358,12 +418,12 @@ static std::vector<LevelPlan> plan(const uint32_t* counts, uint32_t shapes, uint
 }
 
 struct Scratch {
-    uint64_t lists, large, small, partial, counts, keys, order, counters, total;
+    uint64_t lists, large, small, partial, counts, keys, order, counters, firsts, total;
 };
 
 static uint64_t align256(uint64_t x) { return (x + 255) & ~uint64_t(255); }
 
-static Scratch layout(const std::vector<LevelPlan>& levels, uint64_t items) {
+static Scratch layout(const std::vector<LevelPlan>& levels, uint64_t items, uint32_t shapes) {
     uint64_t entries = 1, large = 1, small = 1, partial = 1, counts = 1;
     for (const LevelPlan& L : levels) {
         entries = std::max(entries, L.entries);
@@ -382,6 +442,7 @@ static Scratch layout(const std::vector<LevelPlan>& levels, uint64_t items) {
     s.keys = at; at += align256(2 * items * sizeof(uint32_t));
     s.order = at; at += align256(items * sizeof(uint32_t));
     s.counters = at; at += align256(MAX_LEVELS * 4 * sizeof(uint32_t));
+    s.firsts = at; at += align256(uint64_t(shapes) * sizeof(uint32_t));
     s.total = at;
     return s;
 }
@@ -421,7 +482,7 @@ extern "C" uint32_t sdg_median_tree_nodes(uint32_t items, uint32_t leaf) {
 extern "C" uint64_t sdg_median_trees_scratch(const uint32_t* counts, uint32_t shapes, uint32_t leaf) {
     uint64_t items, nodes;
     if (check(counts, shapes, leaf, items, nodes)) return 0;
-    return layout(plan(counts, shapes, leaf), items).total;
+    return layout(plan(counts, shapes, leaf), items, shapes).total;
 }
 
 extern "C" int sdg_median_trees(const float* keys, const float* low, const float* high, const uint32_t* counts,
@@ -438,7 +499,7 @@ extern "C" int sdg_median_trees(const float* keys, const float* low, const float
         set_last_error("median trees: more than 64 levels");
         return 1;
     }
-    const Scratch sl = layout(levels, items);
+    const Scratch sl = layout(levels, items, shapes);
     if (scratchBytes < sl.total) {
         set_last_error("median trees: scratch smaller than sdg_median_trees_scratch()");
         return 1;
@@ -455,19 +516,24 @@ extern "C" int sdg_median_trees(const float* keys, const float* low, const float
     uint32_t* keyBuf[2] = {reinterpret_cast<uint32_t*>(base + sl.keys), reinterpret_cast<uint32_t*>(base + sl.keys) + items};
     uint32_t* orderBuf[2] = {order, reinterpret_cast<uint32_t*>(base + sl.order)};
     uint32_t* counters = reinterpret_cast<uint32_t*>(base + sl.counters);
+    uint32_t* firsts = reinterpret_cast<uint32_t*>(base + sl.firsts);
     const float4* k4 = reinterpret_cast<const float4*>(keys);
     const float4* l4 = reinterpret_cast<const float4*>(low);
     const float4* h4 = reinterpret_cast<const float4*>(high);
 
     // Level 0: each shape's root over its items, in item order.
     std::vector<Entry> roots(shapes);
+    std::vector<uint32_t> first(shapes);
     uint32_t item = 0, node = 0;
     for (uint32_t sh = 0; sh < shapes; ++sh) {
         roots[sh] = Entry{node, item, counts[sh], 0};
+        first[sh] = item;
         item += counts[sh];
         node += treeNodes(counts[sh], leaf);
     }
     cudaError_t err = cudaMemcpyAsync(lists[0], roots.data(), shapes * sizeof(Entry), cudaMemcpyHostToDevice, s);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(firsts, first.data(), shapes * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
     if (err == cudaSuccess) err = cudaMemsetAsync(counters, 0, MAX_LEVELS * 4 * sizeof(uint32_t), s);
     k_treeIota<<<uint32_t(std::min<uint64_t>((items + 255) / 256, 4096)), 256, 0, s>>>(order, uint32_t(items));
     if (err != cudaSuccess) {
@@ -501,6 +567,8 @@ extern "C" int sdg_median_trees(const float* keys, const float* low, const float
             }
         }
     }
+    k_treeLocal<<<uint32_t(std::min<uint64_t>((items + 255) / 256, 4096)), 256, 0, s>>>(order, uint32_t(items), firsts,
+                                                                                      shapes);
     err = cudaGetLastError();
     if (err == cudaSuccess) err = cudaStreamSynchronize(s);
     if (err != cudaSuccess) {

@@ -189,7 +189,10 @@ def _feature_normals(vertices, faces):
 
 def _prepare(shape, length_unit):
     """One shape's host-side parts: FP32 sample points, hull plane groups,
-    feature pseudonormals and FP32 triangles (``mesh.py:21-162``)."""
+    feature pseudonormals, FP32 triangles (``mesh.py:21-162``) and the
+    triangles' split keys and boxes: centres as the reference computes them
+    (``mesh.py:191``, the mean of the three FP32 vertices) and the vertices'
+    minimum and maximum."""
     if shape.provenance.get("display_mesh_only"):
         raise ValueError("Mesh query requires physical source triangles, not a display-only fixture mesh")
     vertices = np.asarray(shape.vertices, float) / length_unit
@@ -204,7 +207,9 @@ def _prepare(shape, length_unit):
         raise ValueError("Shape vertices must be finite")
     if np.any(np.linalg.norm(np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]), axis=1) == 0):
         raise ValueError("Triangle degenerates in normalized FP32")
-    return points, hull, feature, tri
+    low = np.minimum(np.minimum(tri[:, 0], tri[:, 1]), tri[:, 2])
+    high = np.maximum(np.maximum(tri[:, 0], tri[:, 1]), tri[:, 2])
+    return points, hull, feature, tri, (tri.mean(axis=1), low, high)
 
 
 def pack_library(library, length_unit, trees=host_median_trees):
@@ -221,20 +226,24 @@ def pack_library(library, length_unit, trees=host_median_trees):
     # independent between shapes: prepared on a thread pool, kept in order.
     with ThreadPoolExecutor(max_workers=min(len(library.shapes), os.cpu_count() or 1)) as pool:
         prepared = list(pool.map(lambda shape: _prepare(shape, length_unit), library.shapes))
-    sample_items, triangle_items, tris, features = [], [], [], []
-    for points, hull, feature, tri in prepared:
+    sample_items, triangle_items, tris, features, planes = [], [], [], [], []
+    plane_count = 0
+    for points, hull, feature, tri, boxed in prepared:
         sample_items.append((points, None, None))
         for subset in hull:
-            out["meshHullInfo"].append([len(out["meshPlanes"]), len(subset), 0, 0])
-            out["meshPlanes"].extend(subset)
+            out["meshHullInfo"].append([plane_count, len(subset), 0, 0])
+            planes.append(subset)
+            plane_count += len(subset)
         features.append(feature)
         tris.append(tri)
-        triangle_items.append((tri.mean(axis=1), tri.min(axis=1), tri.max(axis=1)))
+        triangle_items.append(boxed)
+    out["meshPlanes"] = np.concatenate(planes).astype(F32).reshape(-1, 4)
 
     sample_order, cluster, cluster_low, cluster_high = trees(sample_items, 64)
     tri_order, links, tri_low, tri_high = trees(triangle_items, 4)
 
-    leaf_info, leaves, ranks = [], [], []
+    leaf_info, leaves, leaf_total = [], [], 0
+    ranks = np.empty(len(sample_order), np.uint32)
     node, item = 0, 0
     for points, _, _ in sample_items:
         n = len(points)
@@ -245,11 +254,10 @@ def pack_library(library, length_unit, trees=host_median_trees):
         local = np.column_stack([ranges[:, 1], ranges[:, 2], ranges[:, 0] - node]).astype(np.int64)
         out["meshFrontier"].extend(_frontier(local, node))
         shape_leaves = node + np.flatnonzero(ranges[:, 2] > 0)
-        leaf_info.append([len(leaves), len(shape_leaves), 0, 0])
-        leaves.extend(shape_leaves.tolist())
-        rank = np.empty(n, np.uint32)
-        rank[sample_order[item:item + n].astype(np.int64)] = np.arange(n, dtype=np.uint32)
-        ranks.append(rank)
+        leaf_info.append([leaf_total, len(shape_leaves), 0, 0])
+        leaves.append(shape_leaves)
+        leaf_total += len(shape_leaves)
+        ranks[item + sample_order[item:item + n].astype(np.int64)] = np.arange(n, dtype=np.uint32)
         node += count
         item += n
     out["meshClusterRanges"] = np.column_stack(
@@ -287,8 +295,8 @@ def pack_library(library, length_unit, trees=host_median_trees):
         else:
             packed[name] = np.ascontiguousarray(np.asarray(out[name], F32))
     packed["meshLeafInfo"] = np.asarray(leaf_info, np.uint32)
-    packed["meshLeaves"] = np.asarray(leaves, np.uint32)
-    packed["meshSampleRank"] = np.concatenate(ranks).astype(np.uint32)
+    packed["meshLeaves"] = np.concatenate(leaves).astype(np.uint32)
+    packed["meshSampleRank"] = ranks
     packed["meshChildren"] = child_records(packed["meshLinks"], packed["meshMin"], packed["meshMax"])
     return packed
 

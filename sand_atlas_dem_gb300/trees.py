@@ -10,6 +10,7 @@ raises when the CUDA library or device is missing).
 """
 
 import ctypes as ct
+import time
 
 import numpy as np
 
@@ -25,7 +26,8 @@ def device_median_trees(items, leaf, *, timing=None):
     ``low``/``high`` both None (boxes are the key points) or both given for
     every shape.  Returns ``(order, records, low, high)`` as
     ``packing.host_median_trees`` does.  ``timing`` (a dict) receives the
-    device time of the build in milliseconds (CUDA events on the stream)."""
+    device time of the build (``device_ms``, CUDA events on the stream) and
+    the wall time of the whole call with its copies (``wall_ms``)."""
     import torch
 
     if not torch.cuda.is_available():
@@ -39,13 +41,18 @@ def device_median_trees(items, leaf, *, timing=None):
         raise ValueError("Every shape needs at least one item")
     n = int(counts.sum(dtype=np.uint64))
     device = torch.device("cuda", torch.cuda.current_device())
+    wall = time.perf_counter()
+    firsts = np.cumsum(counts, dtype=np.int64) - counts
 
     def rows(arrays):
-        a = np.zeros((n, 4), np.float32)
-        a[:, :3] = np.concatenate([np.asarray(x, np.float32).reshape(-1, 3) for x in arrays])
-        if not np.all(np.isfinite(a)):
-            raise ValueError("Item coordinates must be finite")
-        return torch.from_numpy(a).to(device)
+        # Each shape's (n, 3) rows go straight into one padded device array.
+        out = torch.zeros((n, 4), dtype=torch.float32, device=device)
+        for first, x in zip(firsts, arrays):
+            x = np.ascontiguousarray(x, np.float32).reshape(-1, 3)
+            if not np.all(np.isfinite(x)):
+                raise ValueError("Item coordinates must be finite")
+            out[first:first + len(x), :3] = torch.from_numpy(x).to(device, non_blocking=False)
+        return out
 
     keys = rows([k for k, _, _ in items])
     low = rows([lo for _, lo, _ in items]) if boxes else None
@@ -72,10 +79,10 @@ def device_median_trees(items, leaf, *, timing=None):
         end.record(stream)
         end.synchronize()
         timing["device_ms"] = start.elapsed_time(end)
-    first = np.repeat(np.cumsum(counts, dtype=np.int64) - counts, counts)
-    local = (order.cpu().numpy().view(np.uint32).astype(np.int64) - first).astype(np.uint32)
-    return (local, records.cpu().numpy().view(np.uint32), node_low.cpu().numpy(), node_high.cpu().numpy())
-
+    out = (order.cpu().numpy().view(np.uint32), records.cpu().numpy().view(np.uint32), node_low.cpu().numpy(), node_high.cpu().numpy())
+    if timing is not None:
+        timing["wall_ms"] = 1e3 * (time.perf_counter() - wall)
+    return out
 
 def tree_levels(counts, leaf, small=256):
     """Per level of the trees over shapes of ``counts`` items: items in the
@@ -105,4 +112,4 @@ def tree_levels(counts, leaf, small=256):
 
 def tree_launches(counts, leaf):
     """Kernel launches of one ``sdg_median_trees`` call."""
-    return 1 + sum(2 + (small > 0) + 12 * (large > 0) for _, _, small, large in tree_levels(counts, leaf))
+    return 2 + sum(2 + (small > 0) + 12 * (large > 0) for _, _, small, large in tree_levels(counts, leaf))
