@@ -224,6 +224,8 @@ def pack_library(library, length_unit, trees=host_median_trees):
     out = {k: [] for k in UINT_ARRAYS + FLOAT_ARRAYS}
     # The per-shape host work (hull, pseudonormals, manifold checks) is
     # independent between shapes: prepared on a thread pool, kept in order.
+    if not library.shapes:
+        raise ValueError("Shape library is empty")
     with ThreadPoolExecutor(max_workers=min(len(library.shapes), os.cpu_count() or 1)) as pool:
         prepared = list(pool.map(lambda shape: _prepare(shape, length_unit), library.shapes))
     sample_items, triangle_items, tris, features, planes = [], [], [], [], []
@@ -282,16 +284,22 @@ def pack_library(library, length_unit, trees=host_median_trees):
     out["meshMin"] = tri_low
     out["meshMax"] = tri_high
 
-    def f4(a):
-        a = np.asarray(a, F32).reshape(-1, 3)
-        return np.pad(a, ((0, 0), (0, 1)))
+    def f4(parts):
+        # (x, y, z, 0) rows, written straight into the padded array.
+        rows = sum(len(p) for p in parts)
+        a = np.zeros((rows, 4), F32)
+        at = 0
+        for p in parts:
+            a[at:at + len(p), :3] = p
+            at += len(p)
+        return a
 
     packed = {}
     for name in UINT_ARRAYS:
         packed[name] = np.ascontiguousarray(np.asarray(out[name], np.uint32))
     for name in FLOAT_ARRAYS:
         if name in ("meshTriangles", "meshNormals"):
-            packed[name] = f4(np.concatenate(out[name]))
+            packed[name] = f4(out[name])
         else:
             packed[name] = np.ascontiguousarray(np.asarray(out[name], F32))
     packed["meshLeafInfo"] = np.asarray(leaf_info, np.uint32)
