@@ -325,12 +325,16 @@ __device__ __forceinline__ uint32_t sameDigit(uint32_t digit, bool valid) {
 // (8 a lane, loaded first, kept in registers) and ranks them among its own
 // items of the same digit: earlier sub-rounds through its shared histogram,
 // lower lanes of the same sub-round through the digit match.  A prefix over
-// the warps of each digit's count, from the tile's place for that digit, then
-// gives each warp its first place per digit.
+// the warps of each digit's count gives each warp its first rank per digit
+// within the tile.  The items are then staged in shared memory in digit
+// order and written out from there, so that consecutive threads write
+// consecutive places of a digit's run (coalesced stores).
 __global__ void __launch_bounds__(256) k_treeScatter(const Entry* large, uint32_t tiles, uint32_t pass,
                                                      const uint32_t* counts, const uint32_t* keySrc,
                                                      const uint32_t* orderSrc, uint32_t* keyDst, uint32_t* orderDst) {
     __shared__ uint32_t hist[8][RADIX];
+    __shared__ uint32_t tileBase[RADIX], localBase[RADIX], warpTotal[8];
+    __shared__ uint32_t stagedKey[TILE], stagedId[TILE];
     const Entry e = large[blockIdx.x / tiles];
     const uint32_t tile = blockIdx.x % tiles;
     if (uint64_t(tile) * TILE >= e.count) return;
@@ -361,21 +365,45 @@ __global__ void __launch_bounds__(256) k_treeScatter(const Entry* large, uint32_
         rank[j] = before + below;
     }
     __syncthreads();
-    uint32_t run = counts[uint64_t(blockIdx.x) * RADIX + threadIdx.x];
+    // Thread d: the warps' first ranks for digit d, the tile's count of it,
+    // and (block scan) where digit d starts among the tile's items.
+    uint32_t total = 0;
 #pragma unroll
     for (int w = 0; w < 8; ++w) {
         const uint32_t c = hist[w][threadIdx.x];
-        hist[w][threadIdx.x] = run;
-        run += c;
+        hist[w][threadIdx.x] = total;
+        total += c;
     }
+    uint32_t incl = total;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += o;
+    }
+    if (lane == 31) warpTotal[warp] = incl;
+    tileBase[threadIdx.x] = counts[uint64_t(blockIdx.x) * RADIX + threadIdx.x];
+    __syncthreads();
+    uint32_t before = 0;
+    for (uint32_t w = 0; w < warp; ++w) before += warpTotal[w];
+    localBase[threadIdx.x] = before + incl - total;
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         if (first + j * 32 < end) {
-            const uint32_t place = hist[warp][(key[j] >> shift) & (RADIX - 1)] + rank[j];
-            keyDst[place] = key[j];
-            orderDst[place] = id[j];
+            const uint32_t digit = (key[j] >> shift) & (RADIX - 1);
+            const uint32_t at = localBase[digit] + hist[warp][digit] + rank[j];
+            stagedKey[at] = key[j];
+            stagedId[at] = id[j];
         }
+    }
+    __syncthreads();
+    const uint32_t n = end - begin;
+    for (uint32_t q = threadIdx.x; q < n; q += 256) {
+        const uint32_t k = stagedKey[q];
+        const uint32_t digit = (k >> shift) & (RADIX - 1);
+        const uint32_t place = tileBase[digit] + (q - localBase[digit]);
+        keyDst[place] = k;
+        orderDst[place] = stagedId[q];
     }
 }
 
