@@ -133,3 +133,37 @@ def test_tree_scratch_rejects_empty_shapes():
     assert b"no items" in lib.sdg_last_error()
     counts = np.array([10, 3000], np.uint32)
     assert lib.sdg_median_trees_scratch(counts.ctypes.data_as(ct.c_void_p), 2, 64) > 0
+
+
+@pytest.mark.parametrize("leaf", [4, 64])
+def test_tree_level_plan_matches_the_recursion(leaf):
+    """``trees.tree_levels`` (items per level, in internal nodes, small and
+    large internal nodes) against the depths and sizes of the host recursion's
+    nodes, for several shapes at once."""
+    import numpy as np
+
+    from sand_atlas_dem_gb300.packing import host_median_trees
+    from sand_atlas_dem_gb300.trees import tree_launches, tree_levels
+
+    rng = np.random.default_rng(leaf + 1)
+    counts = [1, leaf + 1, 300, 2049, 5000]
+    items = [(rng.normal(size=(n, 3)).astype(np.float32), None, None) for n in counts]
+    _, records, _, _ = host_median_trees(items, leaf)
+    sizes = np.zeros(len(records), np.int64)
+    # A node's item count: the leaves' counts summed over its subtree.
+    for node in range(len(records) - 1, -1, -1):
+        escape = int(records[node, 0])
+        sizes[node] = records[node, 2] if records[node, 2] else sizes[node + 1] + sizes[int(records[node + 1, 0])]
+        assert escape > node
+    expected = {}
+    for node, size in enumerate(sizes):
+        d = int(records[node, 3])
+        level = expected.setdefault(d, [0, 0, 0, 0])
+        level[0] += size
+        if size > leaf:
+            level[1] += size
+            level[2 if size <= 256 else 3] += 1
+    assert [tuple(expected[d]) for d in sorted(expected)] == tree_levels(counts, leaf)
+    # Iota and local-row kernels, then per level: reduce, nodes, and the small
+    # sort and four radix passes (count, offsets, scatter) where present.
+    assert tree_launches(counts, leaf) >= 2 + 2 * len(expected)
