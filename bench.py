@@ -888,7 +888,8 @@ def run_packing(args, reference=False):
         "clocks": clocks.summary(),
         "gpu_launches": steps * (tree_launches(counts_nodes, 64) + tree_launches(counts_tri, 4)),
     }
-    line["e2e"]["d2h_bytes_per_step"] = int(4 * nodes + 4 * triangles + 36 * (len(packed["meshClusterRanges"])
+    # Per item its row (4 B); per tree node its record and two bound rows (48 B).
+    line["e2e"]["d2h_bytes_per_step"] = int(4 * nodes + 4 * triangles + 48 * (len(packed["meshClusterRanges"])
                                                                             + len(packed["meshLinks"])))
     if args.no_cpu_baseline:
         line["cpu_baseline"] = None
