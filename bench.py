@@ -746,8 +746,24 @@ def cpu_baseline(w, args, budget_s=15.0, max_steps=200):
             grains += e.n
         steps += 1
     what = "the whole workload" if len(w.specimens) == 1 else f"specimens 0-7 ({grains // steps} grains)"
-    return {"value": grains / seconds, "unit": "grain-steps/s", "cores": threads, "kind": "port",
+    line = {"value": grains / seconds, "unit": "grain-steps/s", "cores": threads, "kind": "port",
             "sample": f"{steps} full steps of {what}, {seconds:.2f} s"}
+    if threads > 1:
+        # The same oracle on one worker (the reference CPU backend's serial
+        # collector), a shorter sample: at least one step of each specimen.
+        del engines
+        one = [(w.engine(OracleEngine, chosen, threads=1), chosen) for chosen in cpu_sample(w)]
+        grains1, seconds1, steps1 = 0, 0.0, 0
+        while steps1 < 1 or (seconds1 < budget_s / 3 and steps1 < max_steps):
+            for e, chosen in one:
+                t = time.perf_counter()
+                e.advance(1, rate=w.rate(chosen))
+                seconds1 += time.perf_counter() - t
+                grains1 += e.n
+            steps1 += 1
+        line["single_worker"] = {"value": grains1 / seconds1, "unit": "grain-steps/s", "cores": 1,
+                                 "sample": f"{steps1} full steps of {what}, {seconds1:.2f} s"}
+    return line
 
 
 def run_reference(args):
