@@ -167,3 +167,27 @@ def test_tree_level_plan_matches_the_recursion(leaf):
     # Iota and local-row kernels, then per level: reduce, nodes, and the small
     # sort and four radix passes (count, offsets, scatter) where present.
     assert tree_launches(counts, leaf) >= 2 + 2 * len(expected)
+
+
+def test_tree_builder_rejects_bad_arguments_before_any_device_call():
+    """``sdg_median_trees`` checks its arguments on the host and returns 1
+    with a message, launching nothing: empty shapes, more than 2^30 items,
+    null buffers, boxes given for only one side, scratch too small."""
+    import numpy as np
+
+    lib = native.load()
+    P = ct.c_void_p
+    fake = P(256)  # never dereferenced: every call below fails its checks first
+
+    def call(counts, leaf=64, keys=fake, low=None, high=None, order=fake, scratch=fake, size=1 << 40):
+        c = np.asarray(counts, np.uint32)
+        return lib.sdg_median_trees(keys, low, high, c.ctypes.data_as(P), len(c), leaf, order, fake, fake, fake,
+                                    scratch, size, None)
+
+    assert call([5, 0]) == 1 and b"no items" in lib.sdg_last_error()
+    assert call([1 << 29, 1 << 29, 1]) == 1 and b"2^30" in lib.sdg_last_error()
+    assert call([10], leaf=0) == 1
+    assert call([10], keys=None) == 1 and b"null" in lib.sdg_last_error()
+    assert call([10], low=fake) == 1 and b"both" in lib.sdg_last_error()
+    assert call([10], order=None) == 1
+    assert call([10], size=16) == 1 and b"scratch" in lib.sdg_last_error()
