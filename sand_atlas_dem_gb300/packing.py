@@ -244,64 +244,65 @@ def pack_library(library, length_unit, trees=host_median_trees):
     sample_order, cluster, cluster_low, cluster_high = trees(sample_items, 64)
     tri_order, links, tri_low, tri_high = trees(triangle_items, 4)
 
-    leaf_info, leaves, leaf_total = [], [], 0
+    # Per shape: its first cluster, sample, BVH node and triangle (serial,
+    # through the roots' escape links), then the per-shape assembly on the
+    # thread pool, each shape writing its own slices.
+    starts, node, item, bvh, tri_item = [], 0, 0, 0, 0
+    for (points, _, _), tri in zip(sample_items, tris):
+        starts.append((node, item, bvh, tri_item))
+        node = int(cluster[node, 0])
+        bvh = int(links[bvh, 0])
+        item += len(points)
+        tri_item += len(tri)
     ranks = np.empty(len(sample_order), np.uint32)
-    node, item = 0, 0
-    for points, _, _ in sample_items:
-        n = len(points)
+    triangles = np.zeros((3 * tri_item, 4), F32)
+    normals = np.zeros((7 * tri_item, 4), F32)
+
+    def assemble(k):
+        node, item, bvh, tri_item = starts[k]
+        n = len(sample_items[k][0])
         count = int(cluster[node, 0]) - node  # the root's escape link
         ranges = cluster[node:node + count]
-        out["meshClusterInfo"].append([node, count, 0, 0])
         # (first, count, escape) with the escape link local to the shape.
         local = np.column_stack([ranges[:, 1], ranges[:, 2], ranges[:, 0] - node]).astype(np.int64)
-        out["meshFrontier"].extend(_frontier(local, node))
+        frontier = _frontier(local, node)
         shape_leaves = node + np.flatnonzero(ranges[:, 2] > 0)
+        ranks[item + sample_order[item:item + n].astype(np.int64)] = np.arange(n, dtype=np.uint32)
+        tri, feature = tris[k], features[k]
+        nodes = int(links[bvh, 0]) - bvh
+        depth = int(links[bvh:bvh + nodes, 3].max())
+        rows = tri_order[tri_item:tri_item + len(tri)].astype(np.int64)
+        triangles[3 * tri_item:3 * (tri_item + len(tri)), :3] = tri[rows].reshape(-1, 3)
+        normals[7 * tri_item:7 * (tri_item + len(tri)), :3] = feature[rows].reshape(-1, 3)
+        return count, frontier, shape_leaves, nodes, depth
+
+    with ThreadPoolExecutor(max_workers=min(len(library.shapes), os.cpu_count() or 1)) as pool:
+        assembled = list(pool.map(assemble, range(len(sample_items))))
+    leaf_info, leaves, leaf_total = [], [], 0
+    for (node, _, bvh, _), (count, frontier, shape_leaves, nodes, depth) in zip(starts, assembled):
+        out["meshClusterInfo"].append([node, count, 0, 0])
+        out["meshFrontier"].extend(frontier)
         leaf_info.append([leaf_total, len(shape_leaves), 0, 0])
         leaves.append(shape_leaves)
         leaf_total += len(shape_leaves)
-        ranks[item + sample_order[item:item + n].astype(np.int64)] = np.arange(n, dtype=np.uint32)
-        node += count
-        item += n
+        if depth > 30:
+            raise ValueError("Mesh hierarchy exceeds GPU traversal stack depth")
+        out["meshRoots"].append([bvh, bvh + nodes, depth, 0])
     out["meshClusterRanges"] = np.column_stack(
         [cluster[:, 1], cluster[:, 2], cluster[:, 0], np.zeros(len(cluster), np.uint32)])
     out["meshClusterMin"] = cluster_low
     out["meshClusterMax"] = cluster_high
     out["meshSampleIndices"] = sample_order
-
-    node, item = 0, 0
-    for tri, feature in zip(tris, features):
-        count = int(links[node, 0]) - node
-        depth = int(links[node:node + count, 3].max())
-        if depth > 30:
-            raise ValueError("Mesh hierarchy exceeds GPU traversal stack depth")
-        out["meshRoots"].append([node, node + count, depth, 0])
-        rows = tri_order[item:item + len(tri)].astype(np.int64)
-        out["meshTriangles"].append(tri[rows].reshape(-1, 3))
-        out["meshNormals"].append(feature[rows].reshape(-1, 3))
-        node += count
-        item += len(tri)
     out["meshLinks"] = np.column_stack([links[:, :3], np.zeros(len(links), np.uint32)])
     out["meshMin"] = tri_low
     out["meshMax"] = tri_high
 
-    def f4(parts):
-        # (x, y, z, 0) rows, written straight into the padded array.
-        rows = sum(len(p) for p in parts)
-        a = np.zeros((rows, 4), F32)
-        at = 0
-        for p in parts:
-            a[at:at + len(p), :3] = p
-            at += len(p)
-        return a
-
     packed = {}
     for name in UINT_ARRAYS:
         packed[name] = np.ascontiguousarray(np.asarray(out[name], np.uint32))
+    out["meshTriangles"], out["meshNormals"] = triangles, normals
     for name in FLOAT_ARRAYS:
-        if name in ("meshTriangles", "meshNormals"):
-            packed[name] = f4(out[name])
-        else:
-            packed[name] = np.ascontiguousarray(np.asarray(out[name], F32))
+        packed[name] = np.ascontiguousarray(np.asarray(out[name], F32))
     packed["meshLeafInfo"] = np.asarray(leaf_info, np.uint32)
     packed["meshLeaves"] = np.concatenate(leaves).astype(np.uint32)
     packed["meshSampleRank"] = ranks
