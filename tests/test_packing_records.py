@@ -50,3 +50,20 @@ def test_tiled_packing_repeats_every_grain_by_whole_cells():
         # in a neighbouring copy: compare the separations modulo the small cell.
         d -= np.round(d / record["cell"]) * record["cell"]
         assert np.allclose(d, d0)
+
+
+def test_edge_key_unique_orders_as_row_unique():
+    """The packer takes the unique undirected edges through one int64 key
+    per edge (low * stride + high); it must give the rows, inverse and counts
+    np.unique(rows, axis=0) gives (``mesh.py:115-121``)."""
+    rng = np.random.default_rng(17)
+    for vertices in (5, 300, 70_000):
+        edges = np.sort(rng.integers(0, vertices, (4_000, 2)), axis=1)
+        stride = int(edges.max()) + 1
+        keys, inverse, count = np.unique(edges[:, 0] * stride + edges[:, 1], return_inverse=True,
+                                         return_counts=True)
+        rows = np.column_stack([keys // stride, keys % stride])
+        ref_rows, ref_inverse, ref_count = np.unique(edges, axis=0, return_inverse=True, return_counts=True)
+        assert np.array_equal(rows, ref_rows)
+        assert np.array_equal(inverse.ravel(), ref_inverse.ravel())
+        assert np.array_equal(count, ref_count)
