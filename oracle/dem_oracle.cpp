@@ -1095,6 +1095,30 @@ PlaneResponse planeViscousResponse(vec3 normal, real signedDistance, real area, 
     value.slipLoss = f4(slip, mx(0.0f, -dot(ft, trial - slip)));
     return value;
 }
+// solver.slang:723-740: the grain-grain law of one directed node contact from
+// its transported elastic slip: the trial slip over the step, the normal
+// response (half weight: each pair contact is counted from both grains), the
+// tangential traction and its Coulomb cap.
+struct GrainLaw { vec4 slipLoss, forceEnergy; real normalLossPower; bool sliding; };
+GrainLaw grainLaw(vec3 n, real depth, real area, vec3 rv, vec3 elastic, real kn, real kt, real mu, real viscosity,
+                  real dt) {
+    GrainLaw value{{0, 0, 0, 0}, {0, 0, 0, 0}, 0, false};
+    elastic = elastic + (rv - n * dot(rv, n)) * dt;
+    vec3 trial = elastic;
+    NormalResponse response = normalResponse(depth, area, dot(rv, n), kn, viscosity, 0.5f);
+    real fn = response.force;
+    value.normalLossPower = response.lossPower;
+    vec3 ft = -0.5f * kt * area * elastic;
+    real magnitude = length(ft);
+    if (magnitude > mu * fn && magnitude > 0) {
+        ft = ft * (mu * fn / magnitude);
+        elastic = -ft / (0.5f * kt * area);
+        value.sliding = true;
+    }
+    value.slipLoss = f4(elastic, mx(0.0f, -dot(ft, trial - elastic)));
+    value.forceEnergy = f4(fn * n + ft, 0.25f * area * (kn * depth * depth + kt * dot(elastic, elastic)));
+    return value;
+}
 // solver.slang:697-701
 void clearContactStorage(R& r, uint32_t id) {
     if (id < r.c.hashSize) r.hash[id] = EMPTY;
@@ -1151,24 +1175,15 @@ void resolveContacts(R& r, uint32_t id) {
     vec3 translation = xyz(r.velocity[i]) - xyz(r.velocity[j]);
     if (viscosity > 0) translation = xyz(r.forceVelocity[i]) - xyz(r.forceVelocity[j]);
     vec3 rv = translation - xyz(r.cell[1]) * branch + cross(wi, arm) - cross(wj, arm - branch);
-    elastic = elastic + (rv - n * dot(rv, n)) * r.c.dt;
-    vec3 trial = elastic;
     real area = r.normalArea[id].w, depth = r.pointDepth[id].w;
-    NormalResponse response = normalResponse(depth, area, dot(rv, n), r.c.kn, viscosity, 0.5f);
-    real fn = response.force;
-    r.normalLossPower[id] = response.lossPower;
-    vec3 ft = -0.5f * r.c.kt * area * elastic;
-    real magnitude = length(ft);
-    if (magnitude > r.c.mu * fn && magnitude > 0) {
-        ft = ft * (r.c.mu * fn / magnitude);
-        elastic = -ft / (0.5f * r.c.kt * area);
-        r.control[6]++;
-    }
-    r.slip[id] = f4(elastic, mx(0.0f, -dot(ft, trial - elastic)));
-    vec4 cf = f4(fn * n + ft, 0.25f * area * (r.c.kn * depth * depth + r.c.kt * dot(elastic, elastic)));
+    GrainLaw law = grainLaw(n, depth, area, rv, elastic, r.c.kn, r.c.kt, r.c.mu, viscosity, r.c.dt);
+    r.normalLossPower[id] = law.normalLossPower;
+    if (law.sliding) r.control[6]++;
+    r.slip[id] = law.slipLoss;
+    vec4 cf = law.forceEnergy;
     r.contactForce[id] = cf;
     if (!std::isfinite(cf.x) || !std::isfinite(cf.y) || !std::isfinite(cf.z) || !std::isfinite(cf.w) ||
-        !std::isfinite(response.lossPower)) { fail(r, 512); return; }
+        !std::isfinite(law.normalLossPower)) { fail(r, 512); return; }
     uint32_t oldHead = r.heads[i];
     r.heads[i] = 2 * id;
     r.next[2 * id] = oldHead;
@@ -1393,6 +1408,27 @@ extern "C" int oracle_dispatch(const char* name, uint32_t count, void** buffers,
             slipLoss[id] = value.slipLoss;
             torqueActive[id] = f4(cross(xyz(point), xyz(value.forceEnergy)), phi < 0 ? 1.0f : 0.0f);
         }
+    } else if (k == "grainLawProbe") {  // grainLaw per contact: N; kn, kt, mu, viscosity, dt
+        real kn = real(r.uni[1]), kt = real(r.uni[2]), mu = real(r.uni[3]), viscosity = real(r.uni[4]);
+        real dt = real(r.uni[5]);
+        vec4* normalDepth = static_cast<vec4*>(r.extra[0]);
+        vec4* slipArea = static_cast<vec4*>(r.extra[1]);
+        vec4* velocity = static_cast<vec4*>(r.extra[2]);
+        vec4* forceEnergy = static_cast<vec4*>(r.extra[3]);
+        vec4* slipLoss = static_cast<vec4*>(r.extra[4]);
+        for (uint32_t id = 0; id < count; ++id) {
+            GrainLaw v = grainLaw(xyz(normalDepth[id]), normalDepth[id].w, slipArea[id].w, xyz(velocity[id]),
+                                  xyz(slipArea[id]), kn, kt, mu, viscosity, dt);
+            forceEnergy[id] = v.forceEnergy;
+            slipLoss[id] = v.slipLoss;
+        }
+    } else if (k == "transportProbe") {  // transported per contact: slip and spin, old normal, new normal
+        vec4* slipSpin = static_cast<vec4*>(r.extra[0]);
+        vec4* oldNormal = static_cast<vec4*>(r.extra[1]);
+        vec4* newNormal = static_cast<vec4*>(r.extra[2]);
+        vec4* result = static_cast<vec4*>(r.extra[3]);
+        for (uint32_t id = 0; id < count; ++id)
+            result[id] = f4(transported(xyz(slipSpin[id]), xyz(oldNormal[id]), xyz(newNormal[id]), slipSpin[id].w), 0);
     } else if (k == "normalProbe") {  // normal.slang:166-174: stiffness, viscosity, weight
         real stiffness = real(r.uni[1]), viscosity = real(r.uni[2]), weight = real(r.uni[3]);
         vec4* input = static_cast<vec4*>(r.extra[0]);
