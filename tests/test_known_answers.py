@@ -200,3 +200,46 @@ def test_contact_capacity_growth_is_explicit_and_replays(make):
     e.advance(1)
     assert e.state()["contacts"] > capacity
     assert e.contact_capacity >= e.state()["contacts"] and e.capacity_retries
+
+
+def _normal_probe(data, stiffness, viscosity, weight, precision="fp32"):
+    """The oracle's normalResponse (normal.slang:2-11) through its
+    normalProbe entry point (normal.slang:166-174): rows (depth, area, normal
+    velocity, 0) -> (force, loss power, 0, 0)."""
+    from oracle.engine import OracleEngine
+    from sand_atlas_dem_gb300.shapes import ShapeLibrary, box_shape
+    from sand_atlas_dem_gb300.spec import Experiment
+
+    real = np.float64 if precision == "fp64" else np.float32
+    e = OracleEngine(ShapeLibrary([box_shape([1e-3] * 3)]), Experiment(particles=2, contact_geometry="mesh",
+                                                                       timestep=1e-9),
+                     [[0.005] * 3, [0.015] * 3], [0.03] * 3, [0, 0], [1.0, 1.0], precision=precision)
+    source = np.ascontiguousarray(np.asarray(data, real))
+    out = np.zeros((len(source), 4), real)
+    e.dispatch("normalProbe", len(source), e.config(), extra=(source, out),
+               uniforms=(len(source), stiffness, viscosity, weight))
+    return out
+
+
+@pytest.mark.parametrize("weight", [0.5, 1.0])
+@pytest.mark.parametrize("viscosity", [0.0, 3.0])
+def test_normal_operator_compression_unload_clamp_inactive(weight, viscosity):
+    """The reference's hand-evaluated table (tests/test_normal_viscosity.py:37-71):
+    stiffness 8, area 2, depth 0.25 under compression, at rest, unloading
+    unclipped and clipped, then separation and exact contact."""
+    data = [[0.25, 2, v, 0] for v in (-2, 0, 0.25, 2)] + [[-0.1, 2, -2, 0], [0, 2, -2, 0]]
+    expected = np.array([[4, 0], [4, 0], [4, 0], [4, 0], [0, 0], [0, 0]] if viscosity == 0
+                        else [[16, 24], [4, 0], [2.5, 0.375], [0, 8], [0, 0], [0, 0]]) * weight
+    actual = _normal_probe(data, 8, viscosity, weight)[:, :2]
+    assert np.allclose(actual, expected, rtol=2e-6, atol=1e-7)
+    assert (actual >= 0).all()
+
+
+def test_compiled_normal_probe():
+    """The reference's CPU normal probe case (tests/test_cpu_solver.py:685-708):
+    kn 1e12, viscosity 1e6, weight 1/2."""
+    values = np.array([[1e-7, 1e-8, -0.01, 0], [1e-7, 1e-8, 0.2, 0], [-1e-7, 1e-8, 0, 0]], np.float32)
+    fn = np.where(values[:, 0] > 0,
+                  np.maximum(0, 0.5 * 1e12 * values[:, 1] * values[:, 0] - 0.5 * 1e6 * values[:, 1] * values[:, 2]),
+                  0)
+    np.testing.assert_allclose(_normal_probe(values, 1e12, 1e6, 0.5)[:, 0], fn, rtol=2e-5, atol=1e-9)
